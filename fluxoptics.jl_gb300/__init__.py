@@ -1,0 +1,29 @@
+"""GB300-native scalar-propagation hot path of FluxOptics.jl.
+
+Import name: ``fluxoptics_gb300`` (loaded from this directory by
+``__graft_entry__.load_package``).  Device arrays are CUDA tensors; every
+operation runs through libfluxoptics_gb300 (hand-written sm_103a kernels) and
+fails loudly when the library cannot be loaded.
+"""
+
+from . import _capi
+from ._capi import FluxOpticsError
+from .build import build as build_library
+from .components import (AS_BPM, ASProp, Backward, FieldProbe, Forward, Mask, OpticalSystem, Phase, RSProp,
+                         ScalarSource, backpropagate_, function_to_array, propagate, propagate_, reverse,
+                         spatial_vectors)
+from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
+from .metrics import SquaredIntensityDifference, withgradient
+from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
+from .optimisers import ClampProx, Fista, NoDescent, ProxRule, TVProx, make_rules, setup, update_
+
+load_library = _capi.load
+
+__all__ = [
+    "AS_BPM", "ASProp", "Backward", "ClampProx", "FieldProbe", "Fista", "FluxOpticsError", "Forward", "Mask",
+    "NoDescent", "OpticalSystem", "Phase", "ProxRule", "RSProp", "ScalarField", "ScalarSource",
+    "SquaredIntensityDifference", "TVProx", "backpropagate_", "build_library", "coupling_efficiency",
+    "function_to_array", "gaussian", "hermite_gaussian", "hermite_gaussian_groups", "intensity",
+    "load_library", "make_rules", "normalize_power_", "power", "propagate", "propagate_", "reverse",
+    "setup", "spatial_vectors", "update_", "withgradient",
+]

@@ -1,0 +1,120 @@
+"""ctypes binding of libfluxoptics_gb300 (the C ABI declared in include/fluxoptics_gb300.h)."""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+FO_OK = 0
+FO_FORWARD = 1
+FO_BACKWARD = -1
+FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN = 0, 1, 2, 3
+
+ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
+               5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
+
+
+class FluxOpticsError(RuntimeError):
+    """Raised when a C-ABI call returns a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class fo_mod(C.Structure):
+    _fields_ = [("kind", C.c_int), ("param", C.c_void_p), ("saved", C.c_void_p),
+                ("grad", C.c_void_p), ("scale", C.c_double)]
+
+
+_vp = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_ll = C.c_longlong
+_pd = C.POINTER(C.c_double)
+_pi = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "fo_version": (_i, []),
+    "fo_last_error": (C.c_char_p, []),
+    "fo_stream_synchronize": (_i, [_vp]),
+    "fo_asprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i]),
+    "fo_rsprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _i]),
+    "fo_prop_destroy": (_i, [_vp]),
+    "fo_prop_info": (_i, [_vp, _pi, _pi, C.POINTER(C.c_size_t)]),
+    "fo_propagate": (_i, [_vp, _vp, _i, _vp]),
+    "fo_phase_forward": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "fo_phase_backward": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "fo_mask_forward": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "fo_mask_backward": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "fo_chain_create": (_i, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
+    "fo_chain_destroy": (_i, [_vp]),
+    "fo_chain_forward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp]),
+    "fo_chain_backward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _vp]),
+    "fo_bpm_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i, _d, _i]),
+    "fo_bpm_destroy": (_i, [_vp]),
+    "fo_bpm_info": (_i, [_vp, _pi, C.POINTER(C.c_size_t)]),
+    "fo_bpm_forward": (_i, [_vp, _vp, _vp, _i, _i, _vp]),
+    "fo_bpm_backward": (_i, [_vp, _vp, _vp, _vp, _i, _vp]),
+    "fo_sid_create": (_i, [C.POINTER(_vp), _i, _i, _i, _i, _pi]),
+    "fo_sid_destroy": (_i, [_vp]),
+    "fo_sid_forward": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "fo_sid_backward": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "fo_fista_step": (_i, [_vp, _vp, _vp, _vp, _ll, _d, _vp, _vp]),
+    "fo_clamp": (_i, [_vp, _ll, _d, _d, _vp]),
+    "fo_tv_create": (_i, [C.POINTER(_vp), _i, _i, _d, _i, _i, _d]),
+    "fo_tv_destroy": (_i, [_vp]),
+    "fo_tv_apply": (_i, [_vp, _vp, _vp]),
+    "fo_graph_begin": (_i, [_vp]),
+    "fo_graph_end": (_i, [_vp, C.POINTER(_vp)]),
+    "fo_graph_launch": (_i, [_vp, _vp]),
+    "fo_graph_destroy": (_i, [_vp]),
+}
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Load the shared library (building it first when missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if build_if_missing and (_build.is_stale() or not os.path.exists(path)):
+        _build.build()
+    if not os.path.exists(path):
+        raise FluxOpticsError(6, f"{path} is missing; run build() first")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != FO_OK:
+        msg = _LIB.fo_last_error().decode() if _LIB is not None else ""
+        raise FluxOpticsError(rc, msg)
+
+
+def call(name, *args):
+    lib = load()
+    check(getattr(lib, name)(*args))
+
+
+def dvec(values):
+    arr = (C.c_double * len(values))(*[float(v) for v in values])
+    return arr
+
+
+def ivec(values):
+    return (C.c_int * len(values))(*[int(v) for v in values])

@@ -1,0 +1,624 @@
+"""Optical components of the hot path and the fused system executor.
+
+Mirrors the reference's component API (src/optical_components/OpticalComponents.jl,
+freespace_propagators/*, modulators/phasemask.jl, modulators/mask.jl,
+bulk_propagators/bpm.jl, sources/scalar_source.jl, system/optical_system.jl):
+``propagate_`` is Julia's ``propagate!``, ``backpropagate_with_gradient_`` is
+``backpropagate_with_gradient!``, and ``a | b`` builds an ``OpticalSystem`` like
+``a |> b``.  Every component executes on the GPU through libfluxoptics_gb300;
+there is no CPU fallback.
+
+When a system runs, maximal runs ``[mod] prop [mod] prop ... [mod]`` on one grid
+are executed as one fused chain (fo_chain_*): the inverse row transform of each
+propagator, the modulation after it and the next forward row transform share one
+pass over the field, which is the GPU counterpart of the reference's merge rules
+that cancel adjacent ift/ft pairs (system/merge_rules.jl:45-52).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+
+import numpy as np
+import torch
+
+from . import _capi
+from ._capi import FO_BACKWARD, FO_FORWARD, fo_mod
+from .fields import ScalarField, per_field
+
+Forward = FO_FORWARD
+Backward = FO_BACKWARD
+
+
+def reverse(direction):
+    return -direction
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def spatial_vectors(ns, ds, offset=None):
+    """Centred grid vectors (src/GridUtils.jl:56-60), Julia order (x, y)."""
+    if offset is None:
+        offset = (0.0,) * len(ns)
+    return tuple((np.arange(n) - (n - 1) / 2.0) * d - c for n, d, c in zip(ns, ds, offset))
+
+
+def function_to_array(f, ns, ds):
+    """Evaluate f(x, y) on the spatial grid; returns an (ny, nx) array
+    (OpticalComponents.jl:927-935)."""
+    x, y = spatial_vectors(ns, ds)
+    xv = x[None, :]
+    yv = y[:, None]
+    out = np.vectorize(f, otypes=[np.complex128])(np.broadcast_to(xv, (len(y), len(x))),
+                                                  np.broadcast_to(yv, (len(y), len(x))))
+    return out
+
+
+class Component:
+    """Base of all pipe components."""
+
+    trainable = False
+    buffered = False
+
+    def propagate_(self, u: ScalarField, direction=Forward):
+        raise NotImplementedError
+
+    def propagate(self, u: ScalarField, direction=Forward):
+        return self.propagate_(u.copy(), direction)
+
+    def backpropagate_(self, dv: ScalarField, direction=Forward):
+        raise NotImplementedError
+
+    def params(self):
+        """Trainable arrays, the reference's ``trainable(p)``."""
+        return {}
+
+    def __or__(self, other):
+        return OpticalSystem(None, [self]) | other
+
+    def istrainable(self):
+        return self.trainable
+
+    def isbuffered(self):
+        return self.trainable and self.buffered
+
+
+# ---------------------------------------------------------------------------
+# Propagators
+# ---------------------------------------------------------------------------
+
+class _Propagator(Component):
+    kind = None
+
+    def __init__(self, u: ScalarField, z, ds=None):
+        self.z = float(z)
+        self.ds = tuple(float(d) for d in (ds if ds is not None else u.ds))
+        self._plans = {}
+        self.plan_for(u)
+
+    def _create(self, u, lam):
+        raise NotImplementedError
+
+    def plan_for(self, u: ScalarField):
+        lam = tuple(float(v) for v in u.lambdas_per_field())
+        key = (u.nx, u.ny, u.batch, lam)
+        p = self._plans.get(key)
+        if p is None:
+            p = self._create(u, lam)
+            self._plans[key] = p
+        return p
+
+    def layout(self, u: ScalarField):
+        h = self.plan_for(u)
+        fx, fy = C.c_int(), C.c_int()
+        _capi.call("fo_prop_info", h, C.byref(fx), C.byref(fy), None)
+        return (self.kind, u.nx, u.ny, u.batch, fx.value, fy.value)
+
+    def propagate_(self, u, direction=Forward):
+        _capi.call("fo_propagate", self.plan_for(u), _ptr(u.electric), int(direction), _stream())
+        return u
+
+    def backpropagate_(self, dv, direction=Forward):
+        # backpropagate! = propagate!(reverse(direction)) (freespace.jl:61-63)
+        return self.propagate_(dv, reverse(direction))
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is None:
+            return
+        for h in getattr(self, "_plans", {}).values():
+            lib.fo_prop_destroy(h)
+
+
+class ASProp(_Propagator):
+    """Angular-spectrum propagation (angular_spectrum.jl:193-234)."""
+
+    kind = "AS"
+
+    def __init__(self, u, z, ds=None, n0=1.0, use_cache=True, double_precision_kernel=True,
+                 filter=None, paraxial=False, track_tilts=False):
+        if filter is not None or paraxial or track_tilts:
+            raise NotImplementedError("filtered / paraxial / tilt-tracking ASProp is not in the GB300 path")
+        self.n0 = float(n0)
+        super().__init__(u, z, ds)
+
+    def _create(self, u, lam):
+        h = C.c_void_p()
+        _capi.call("fo_asprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                   _capi.dvec(lam), len(lam), self.z, self.n0, 0)
+        return h
+
+
+def rs_valid_distance(nx, ny, dx, dy, lam):
+    """rayleigh_sommerfeld.jl:29-36."""
+    if dx < lam / 2 and dy < lam / 2:
+        return 0.0
+    zx = 0.0 if dx < lam / 2 else (nx * dx / 2) * math.sqrt(4 * dx ** 2 / lam ** 2 - 1)
+    zy = 0.0 if dy < lam / 2 else (ny * dy / 2) * math.sqrt(4 * dy ** 2 / lam ** 2 - 1)
+    return max(zx, zy)
+
+
+class RSProp(_Propagator):
+    """Rayleigh-Sommerfeld propagation as a zero-padded FFT convolution
+    (rayleigh_sommerfeld.jl:128-169)."""
+
+    kind = "RS"
+
+    def __init__(self, u, z, ds=None, use_cache=True, double_precision_kernel=True, track_tilts=False):
+        if track_tilts:
+            raise NotImplementedError("tilt tracking is not in the GB300 path")
+        dsv = tuple(ds) if ds is not None else u.ds
+        zc = rs_valid_distance(u.nx, u.ny, dsv[0], dsv[1], float(np.min(u.lambdas_per_field())))
+        if abs(z) < zc:
+            warnings.warn(f"RSProp: propagation distance z={z} is below critical distance zc={zc}. "
+                          "Numerical artifacts expected.")
+        super().__init__(u, z, ds)
+
+    def _create(self, u, lam):
+        h = C.c_void_p()
+        _capi.call("fo_rsprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                   _capi.dvec(lam), len(lam), self.z, 0)
+        return h
+
+
+# ---------------------------------------------------------------------------
+# Modulators
+# ---------------------------------------------------------------------------
+
+class _Modulator(Component):
+    mod_kind = None
+    pname = None
+
+    def _alloc_buffers(self, u):
+        if self.trainable and self.buffered:
+            self.grad_buffer = torch.empty_like(self.param)
+            self.saved_buffer = torch.empty_like(u.electric)
+        else:
+            self.grad_buffer = None
+            self.saved_buffer = None
+
+    @property
+    def param(self):
+        return getattr(self, self.pname)
+
+    def params(self):
+        return {self.pname: self.param} if self.trainable else {}
+
+    def get_data(self):
+        return self.param
+
+    def fo_mod(self, saved=None, grad=None):
+        return fo_mod(self.mod_kind, self.param.data_ptr(), saved.data_ptr() if saved is not None else None,
+                      grad.data_ptr() if grad is not None else None, 1.0)
+
+    def alloc_saved_buffer(self, u):
+        return torch.empty_like(u.electric)
+
+    def get_saved_buffer(self, u):
+        if self.saved_buffer is not None and self.saved_buffer.shape == u.electric.shape:
+            return self.saved_buffer
+        return self.alloc_saved_buffer(u)
+
+    def alloc_gradient(self):
+        return torch.empty_like(self.param)
+
+    def get_gradient_buffer(self):
+        return self.grad_buffer if self.grad_buffer is not None else self.alloc_gradient()
+
+
+class Phase(_Modulator):
+    """u -> u * cis(s*phi) (modulators/phasemask.jl:38-150)."""
+
+    mod_kind = _capi.FO_MOD_PHASE
+    pname = "phi"
+
+    def __init__(self, u, f=None, ds=None, trainable=False, buffered=False):
+        ds = tuple(ds) if ds is not None else u.ds
+        if f is None:
+            arr = np.zeros((u.ny, u.nx))
+        elif callable(f):
+            arr = np.real(function_to_array(f, (u.nx, u.ny), ds))
+        else:
+            arr = f.detach().cpu().numpy() if isinstance(f, torch.Tensor) else np.asarray(f)
+            if arr.shape != (u.ny, u.nx):
+                raise ValueError(f"phase array must have shape (ny, nx) = {(u.ny, u.nx)}")
+        self.phi = torch.as_tensor(np.asarray(arr, dtype=np.float32)).cuda().contiguous()
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+        self._alloc_buffers(u)
+
+    def propagate_(self, u, direction=Forward):
+        _capi.call("fo_phase_forward", _ptr(u.electric), _ptr(self.phi), None, u.nx, u.ny, u.batch,
+                   int(direction), _stream())
+        return u
+
+    def propagate_and_save_(self, u, saved, direction=Forward):
+        _capi.call("fo_phase_forward", _ptr(u.electric), _ptr(self.phi), _ptr(saved), u.nx, u.ny,
+                   u.batch, int(direction), _stream())
+        return u
+
+    def backpropagate_(self, dv, direction=Forward):
+        _capi.call("fo_phase_backward", _ptr(dv.electric), _ptr(self.phi), None, None, dv.nx, dv.ny,
+                   dv.batch, int(direction), _stream())
+        return dv
+
+    def backpropagate_with_gradient_(self, dv, saved, grad, direction=Forward):
+        _capi.call("fo_phase_backward", _ptr(dv.electric), _ptr(self.phi), _ptr(saved), _ptr(grad),
+                   dv.nx, dv.ny, dv.batch, int(direction), _stream())
+        return dv, {"phi": grad}
+
+
+class Mask(_Modulator):
+    """u -> u * m (conj(m) backward) (modulators/mask.jl:39-142)."""
+
+    mod_kind = _capi.FO_MOD_MASK
+    pname = "m"
+
+    def __init__(self, u, f=None, ds=None, trainable=False, buffered=False):
+        ds = tuple(ds) if ds is not None else u.ds
+        if f is None:
+            arr = np.ones((u.ny, u.nx), dtype=np.complex128)
+        elif callable(f):
+            arr = function_to_array(f, (u.nx, u.ny), ds)
+        else:
+            arr = f.detach().cpu().numpy() if isinstance(f, torch.Tensor) else np.asarray(f)
+            if arr.shape != (u.ny, u.nx):
+                raise ValueError(f"mask array must have shape (ny, nx) = {(u.ny, u.nx)}")
+        self.m = torch.as_tensor(np.asarray(arr, dtype=np.complex64)).cuda().contiguous()
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+        self._alloc_buffers(u)
+
+    def propagate_(self, u, direction=Forward):
+        _capi.call("fo_mask_forward", _ptr(u.electric), _ptr(self.m), None, u.nx, u.ny, u.batch,
+                   int(direction), _stream())
+        return u
+
+    def propagate_and_save_(self, u, saved, direction=Forward):
+        _capi.call("fo_mask_forward", _ptr(u.electric), _ptr(self.m), _ptr(saved), u.nx, u.ny, u.batch,
+                   int(direction), _stream())
+        return u
+
+    def backpropagate_(self, dv, direction=Forward):
+        _capi.call("fo_mask_backward", _ptr(dv.electric), _ptr(self.m), None, None, dv.nx, dv.ny,
+                   dv.batch, int(direction), _stream())
+        return dv
+
+    def backpropagate_with_gradient_(self, dv, saved, grad, direction=Forward):
+        _capi.call("fo_mask_backward", _ptr(dv.electric), _ptr(self.m), _ptr(saved), _ptr(grad), dv.nx,
+                   dv.ny, dv.batch, int(direction), _stream())
+        return dv, {"m": grad}
+
+
+# ---------------------------------------------------------------------------
+# AS_BPM
+# ---------------------------------------------------------------------------
+
+class AS_BPM(Component):
+    """Split-step beam propagation with angular-spectrum steps (bpm.jl:130-142).
+
+    ``dn0`` has shape (n_slices, ny, nx) -- the C view of the reference's
+    (nx, ny, n_slices) array.  The adjoint keeps every ``checkpoint_every``-th
+    slice input and recomputes the rest (0: round(sqrt(n_slices)); 1: keep all)."""
+
+    def __init__(self, u, thickness, n0, dn0, use_cache=True, paraxial=False, trainable=False,
+                 buffered=False, aperture=None, double_precision_kernel=True, checkpoint_every=0):
+        if paraxial:
+            raise NotImplementedError("paraxial AS_BPM is not in the GB300 path")
+        dn = dn0.detach().cpu().numpy() if isinstance(dn0, torch.Tensor) else np.asarray(dn0)
+        if dn.ndim != 3 or dn.shape[1:] != (u.ny, u.nx):
+            raise ValueError("dn0 must have shape (n_slices, ny, nx)")
+        if dn.shape[0] < 2:
+            raise ValueError("AS_BPM needs at least 2 slices")
+        self.dn = torch.as_tensor(np.asarray(dn, dtype=np.float32)).cuda().contiguous()
+        self.thickness = float(thickness)
+        self.n0 = float(n0)
+        self.n_slices = dn.shape[0]
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+        self.checkpoint_every = int(checkpoint_every)
+        self.ds = u.ds
+        self._bpms = {}
+        self.grad_buffer = torch.empty_like(self.dn) if (self.trainable and self.buffered) else None
+        self.handle(u)
+
+    def handle(self, u):
+        lam = tuple(float(v) for v in u.lambdas_per_field())
+        key = (u.nx, u.ny, u.batch, lam)
+        h = self._bpms.get(key)
+        if h is None:
+            h = C.c_void_p()
+            _capi.call("fo_bpm_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                       _capi.dvec(lam), len(lam), self.thickness, self.n0, self.n_slices,
+                       self.checkpoint_every, 1.0, 0)
+            self._bpms[key] = h
+        return h
+
+    def params(self):
+        return {"dn": self.dn} if self.trainable else {}
+
+    def get_data(self):
+        return self.dn
+
+    def propagate_(self, u, direction=Forward):
+        _capi.call("fo_bpm_forward", self.handle(u), _ptr(u.electric), _ptr(self.dn), int(direction), 0,
+                   _stream())
+        return u
+
+    def propagate_and_save_(self, u, saved=None, direction=Forward):
+        _capi.call("fo_bpm_forward", self.handle(u), _ptr(u.electric), _ptr(self.dn), int(direction), 1,
+                   _stream())
+        return u
+
+    def backpropagate_with_gradient_(self, dv, saved, grad, direction=Forward):
+        _capi.call("fo_bpm_backward", self.handle(dv), _ptr(dv.electric), _ptr(self.dn), _ptr(grad),
+                   int(direction), _stream())
+        return dv, {"dn": grad}
+
+    def get_gradient_buffer(self):
+        return self.grad_buffer if self.grad_buffer is not None else torch.empty_like(self.dn)
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is None:
+            return
+        for h in getattr(self, "_bpms", {}).values():
+            lib.fo_bpm_destroy(h)
+
+
+# ---------------------------------------------------------------------------
+# Source and system
+# ---------------------------------------------------------------------------
+
+class ScalarSource:
+    """Holds the input field (sources/scalar_source.jl:39-106)."""
+
+    def __init__(self, u: ScalarField, trainable=False, buffered=False):
+        self.u0 = u.copy()
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+
+    def propagate(self):
+        return self.u0.copy()
+
+    def params(self):
+        return {"u0": self.u0.electric} if self.trainable else {}
+
+    def get_source(self):
+        return self.u0
+
+    def __or__(self, other):
+        return OpticalSystem(self, []) | other
+
+
+class FieldProbe(Component):
+    """Records the field where it sits (system/field_probe.jl:31-43)."""
+
+    def propagate_(self, u, direction=Forward):
+        return u
+
+
+def _is_mod(c):
+    return isinstance(c, (Phase, Mask))
+
+
+def _is_prop(c):
+    return isinstance(c, _Propagator)
+
+
+class _Chain:
+    def __init__(self, props, mods):
+        self.props = props
+        self.mods = mods  # len(props) + 1, entries None or modulators
+
+
+class OpticalSystem:
+    """Source + pipe components (system/optical_system.jl:60-214)."""
+
+    def __init__(self, source, components, direction=Forward, inplace=True, merge_components=True):
+        self.source = source
+        self.components = list(components)
+        self.direction = direction
+        self.inplace = inplace
+        self.merge_components = merge_components
+        self._chains = {}
+
+    def __or__(self, other):
+        if isinstance(other, OpticalSystem):
+            if other.source is not None:
+                raise ValueError("the right-hand system must not have a source")
+            return OpticalSystem(self.source, self.components + other.components, self.direction)
+        if isinstance(other, Component):
+            return OpticalSystem(self.source, self.components + [other], self.direction)
+        raise TypeError(f"cannot pipe {type(other)}")
+
+    def __len__(self):
+        return len(self.components)
+
+    def get_components(self):
+        return list(self.components)
+
+    # -- planning ---------------------------------------------------------------
+    def segments(self, u: ScalarField):
+        """Split the components into fused chains and single components."""
+        comps = self.components
+        segs = []
+        i, n = 0, len(comps)
+        fuse = self.merge_components
+        while i < n:
+            if fuse and (_is_mod(comps[i]) or _is_prop(comps[i])):
+                j = i
+                mods = [None]
+                props = []
+                lay = None
+                if _is_mod(comps[j]):
+                    mods[0] = comps[j]
+                    j += 1
+                while j < n and _is_prop(comps[j]):
+                    lj = comps[j].layout(u)
+                    if lay is not None and lj != lay:
+                        break
+                    lay = lj
+                    props.append(comps[j])
+                    mods.append(None)
+                    j += 1
+                    if j < n and _is_mod(comps[j]):
+                        mods[-1] = comps[j]
+                        j += 1
+                if props:
+                    segs.append(_Chain(props, mods))
+                    i = j
+                    continue
+            segs.append(comps[i])
+            i += 1
+        return segs
+
+    def _chain_handle(self, ch: _Chain, u: ScalarField):
+        plans = tuple(p.plan_for(u).value for p in ch.props)
+        h = self._chains.get(plans)
+        if h is None:
+            h = C.c_void_p()
+            arr = (C.c_void_p * len(plans))(*plans)
+            _capi.call("fo_chain_create", C.byref(h), len(plans), arr)
+            self._chains[plans] = h
+        return h
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is None:
+            return
+        for h in getattr(self, "_chains", {}).values():
+            lib.fo_chain_destroy(h)
+
+    # -- execution ----------------------------------------------------------------
+    def forward(self, u: ScalarField, tape=None):
+        """Runs the system in place on u.  With a tape, trainable components save
+        their inputs and the tape records what the adjoint sweep needs."""
+        d = self.direction
+        for seg in self.segments(u):
+            if isinstance(seg, _Chain):
+                mods = (fo_mod * len(seg.mods))()
+                saved = []
+                for k, m in enumerate(seg.mods):
+                    if m is None:
+                        mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0)
+                        saved.append(None)
+                        continue
+                    sv = m.get_saved_buffer(u) if (tape is not None and m.trainable) else None
+                    mods[k] = m.fo_mod(saved=sv)
+                    saved.append(sv)
+                _capi.call("fo_chain_forward", self._chain_handle(seg, u), _ptr(u.electric), mods, int(d),
+                           _stream())
+                if tape is not None:
+                    tape.append((seg, saved))
+            else:
+                c = seg
+                if tape is not None and c.trainable and isinstance(c, _Modulator):
+                    sv = c.get_saved_buffer(u)
+                    c.propagate_and_save_(u, sv, d)
+                    tape.append((c, sv))
+                elif tape is not None and c.trainable and isinstance(c, AS_BPM):
+                    c.propagate_and_save_(u, None, d)
+                    tape.append((c, None))
+                else:
+                    c.propagate_(u, d)
+                    if tape is not None:
+                        tape.append((c, None))
+        return u
+
+    def backward(self, du: ScalarField, tape, seed=None):
+        """Adjoint sweep over a tape; returns {component: {name: grad}}."""
+        d = self.direction
+        grads = {}
+        first = True
+        for seg, saved in reversed(tape):
+            if isinstance(seg, _Chain):
+                mods = (fo_mod * len(seg.mods))()
+                for k, m in enumerate(seg.mods):
+                    if m is None:
+                        mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0)
+                        continue
+                    g = m.get_gradient_buffer() if m.trainable else None
+                    mods[k] = m.fo_mod(saved=saved[k], grad=g)
+                    if g is not None:
+                        grads[m] = {m.pname: g}
+                if first and seed is not None:
+                    sid, u_out = seed
+                    _capi.call("fo_chain_backward", self._chain_handle(seg, du), _ptr(du.electric), mods,
+                               int(d), sid.handle, _ptr(u_out.electric), _stream())
+                else:
+                    if first and seed is not None:
+                        pass
+                    _capi.call("fo_chain_backward", self._chain_handle(seg, du), _ptr(du.electric), mods,
+                               int(d), None, None, _stream())
+            else:
+                if first and seed is not None:
+                    sid, u_out = seed
+                    sid.backpropagate_into(u_out, du)
+                c = seg
+                if c.trainable and hasattr(c, "backpropagate_with_gradient_"):
+                    g = c.get_gradient_buffer()
+                    _, gd = c.backpropagate_with_gradient_(du, saved, g, d)
+                    grads[c] = gd
+                elif _is_prop(c) or _is_mod(c):
+                    c.backpropagate_(du, d)
+                elif isinstance(c, AS_BPM):
+                    c.backpropagate_with_gradient_(du, None, None, d)
+                elif isinstance(c, FieldProbe):
+                    pass
+                else:
+                    raise NotImplementedError(f"no adjoint for {type(c).__name__}")
+            first = False
+        if first and seed is not None:  # empty system
+            sid, u_out = seed
+            sid.backpropagate_into(u_out, du)
+        return grads
+
+    def __call__(self, x=None):
+        if (x is None) == (self.source is None):
+            raise ValueError("give exactly one of a source or an input field")
+        u = self.source.propagate() if x is None else x.copy()
+        self.forward(u)
+        return {"out": u, "probes": {}}
+
+
+def propagate(u, p, direction=Forward):
+    """Out-of-place propagate (the reference's ``propagate``)."""
+    return p.propagate(u, direction)
+
+
+def propagate_(u, p, direction=Forward):
+    """In-place propagate (the reference's ``propagate!``)."""
+    return p.propagate_(u, direction)
+
+
+def backpropagate_(dv, p, direction=Forward):
+    return p.backpropagate_(dv, direction)

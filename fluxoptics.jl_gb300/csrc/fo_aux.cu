@@ -1,0 +1,479 @@
+// Elementwise and reduction kernels around the propagation passes: transfer
+// functions (FP64), standalone modulators, the SquaredIntensityDifference metric,
+// the Fista step, ClampProx and the TVProx dual iteration.
+#include "fo_aux.h"
+#include "fo_fft.cuh"
+
+namespace fo {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(long long n, int threads = kThreads) {
+  long long g = (n + threads - 1) / threads;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+__device__ __forceinline__ float2 cis_f(float a) {
+  float s, c;
+  sincosf(a, &s, &c);
+  return make_float2(c, s);
+}
+
+// fftfreq(n, d)[k]: k/(n d) for k < ceil(n/2), (k-n)/(n d) otherwise.
+__device__ __forceinline__ double fftfreq_d(int k, int n, double d) {
+  const int h = (n + 1) / 2;
+  return (double)(k < h ? k : k - n) / ((double)n * d);
+}
+
+// ---------------------------------------------------------------------------
+// Transfer functions
+// ---------------------------------------------------------------------------
+
+// H[ky][kx] = cis(2 pi |z| sqrt(n0^2/lambda^2 - fx^2 - fy^2)) * scale, conj for z < 0;
+// evanescent: exp(-2 pi |z| sqrt(fx^2 + fy^2 - n0^2/lambda^2)).
+__global__ void as_h_kernel(float2* H, int fx_n, int fy_n, double dx, double dy, double f2,
+                            double z, double scale) {
+  const long long n = (long long)fx_n * fy_n;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(q % fx_n), ky = (int)(q / fx_n);
+    const double fx = fftfreq_d(kx, fx_n, dx), fy = fftfreq_d(ky, fy_n, dy);
+    const double arg = f2 - fx * fx - fy * fy;
+    const double za = fabs(z);
+    double re, im;
+    if (arg >= 0.0) {
+      const double ph = 2.0 * M_PI * za * sqrt(arg);
+      sincos(ph, &im, &re);
+    } else {
+      re = exp(-2.0 * M_PI * za * sqrt(-arg));
+      im = 0.0;
+    }
+    if (z < 0.0) im = -im;
+    H[q] = make_float2((float)(re * scale), (float)(im * scale));
+  }
+}
+
+// Rayleigh-Sommerfeld impulse response on the circular (py x px) offset grid:
+// offsets 0..n-1 at the start and -(n-1)..-1 at the end of each axis, zero between.
+__global__ void rs_h_spatial_kernel(float2* h, int nx, int ny, int px, int py, double dx, double dy,
+                                    double lambda, double z, double scale) {
+  const long long n = (long long)px * py;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(q % px), iy = (int)(q / px);
+    int ox, oy;
+    bool ok = true;
+    if (ix < nx) ox = ix; else if (ix > px - nx) ox = ix - px; else { ox = 0; ok = false; }
+    if (iy < ny) oy = iy; else if (iy > py - ny) oy = iy - py; else { oy = 0; ok = false; }
+    float2 out = make_float2(0.f, 0.f);
+    if (ok) {
+      const double x = ox * dx, y = oy * dy, za = fabs(z);
+      const double k = 2.0 * M_PI / lambda;
+      const double r = sqrt(x * x + y * y + za * za);
+      const double nrm = dx * dy / (2.0 * M_PI);
+      double s, c;
+      sincos(k * r, &s, &c);
+      // nrm * cis(k r)/r * (z/r) * (1/r - i k)
+      const double a = nrm * za / (r * r);
+      const double br = 1.0 / r, bi = -k;
+      double re = a * (c * br - s * bi);
+      double im = a * (c * bi + s * br);
+      if (z < 0.0) im = -im;
+      out = make_float2((float)(re * scale), (float)(im * scale));
+    }
+    h[q] = out;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Standalone modulators
+// ---------------------------------------------------------------------------
+
+__global__ void phase_fwd_kernel(float2* u, const float* phi, float2* saved, long long npix, int batch,
+                                 float s) {
+  const long long n = npix * batch;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float2 x = u[q];
+    if (saved) saved[q] = x;
+    u[q] = cmul(x, cis_f(s * phi[q % npix]));
+  }
+}
+
+__global__ void phase_bwd_kernel(float2* dv, const float* phi, const float2* saved, float* dphi,
+                                 long long npix, int batch, float s) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    const float2 w = cis_f(-s * phi[p]);
+    float acc = 0.f;
+    for (int b = 0; b < batch; ++b) {
+      const long long q = (long long)b * npix + p;
+      const float2 du = cmul(dv[q], w);
+      dv[q] = du;
+      if (dphi) {
+        const float2 u = saved[q];
+        acc += du.y * u.x - du.x * u.y;
+      }
+    }
+    if (dphi) dphi[p] = s * acc;
+  }
+}
+
+__global__ void mask_fwd_kernel(float2* u, const float2* m, float2* saved, long long npix, int batch,
+                                int conj_m) {
+  const long long n = npix * batch;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float2 x = u[q];
+    if (saved) saved[q] = x;
+    float2 mm = m[q % npix];
+    if (conj_m) mm = cconj(mm);
+    u[q] = cmul(x, mm);
+  }
+}
+
+__global__ void mask_bwd_kernel(float2* dv, const float2* m, const float2* saved, float2* dm,
+                                long long npix, int batch, float s) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    float2 mm = m[p];
+    if (s > 0.f) mm = cconj(mm);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int b = 0; b < batch; ++b) {
+      const long long q = (long long)b * npix + p;
+      const float2 d = dv[q];
+      if (dm) {
+        float2 g = cmul(d, cconj(saved[q]));
+        if (s < 0.f) g = cconj(g);
+        acc = cadd(acc, g);
+      }
+      dv[q] = cmul(d, mm);
+    }
+    if (dm) dm[p] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SquaredIntensityDifference
+// ---------------------------------------------------------------------------
+
+template <int BS>
+__device__ float block_sum(float v, float* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  float r = 0.f;
+  if (threadIdx.x < 32) {
+    r = (threadIdx.x < BS / 32) ? red[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+// One thread per pixel; fields visited target by target in the order of `order`
+// (offsets[t]..offsets[t+1]).  Writes resid[t][p] = I_t - target_t and per-block
+// partial sums of resid^2 (partials[block * T + t]).
+__global__ void sid_fwd_kernel(const float2* u, const float* target, const int* order,
+                               const int* offsets, int T, long long npix, float* resid,
+                               float* partials) {
+  __shared__ float red[kThreads / 32];
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool ok = p < npix;
+  for (int t = 0; t < T; ++t) {
+    float r2 = 0.f;
+    if (ok) {
+      float inten = 0.f;
+      for (int f = offsets[t]; f < offsets[t + 1]; ++f) {
+        const float2 x = u[(long long)order[f] * npix + p];
+        inten = fmaf(x.x, x.x, fmaf(x.y, x.y, inten));
+      }
+      const float r = inten - target[(long long)t * npix + p];
+      resid[(long long)t * npix + p] = r;
+      r2 = r * r;
+    }
+    const float bs = block_sum<kThreads>(r2, red);
+    if (threadIdx.x == 0) partials[(long long)blockIdx.x * T + t] = bs;
+  }
+}
+
+// loss[t] = sum over blocks of partials[block][t], fixed order, one CTA per t.
+__global__ void sid_finalize_kernel(const float* partials, int nblocks, int T, float* loss) {
+  __shared__ float red[kThreads / 32];
+  const int t = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[(long long)b * T + t];
+  const float s = block_sum<kThreads>((float)acc, red);
+  if (threadIdx.x == 0) loss[t] = s;
+}
+
+__global__ void sid_bwd_kernel(const float2* u, const float* resid, const int* tidx, const float* dc,
+                               long long npix, int batch, float2* du) {
+  const long long n = npix * batch;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(q / npix);
+    const long long p = q % npix;
+    const int t = tidx[b];
+    const float k = 4.f * (dc ? dc[t] : 1.f) * resid[(long long)t * npix + p];
+    du[q] = cscale(u[q], k);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fista / Clamp
+// ---------------------------------------------------------------------------
+
+__global__ void fista_kernel(float* x, float* xk, float* newdx, const float* dx, long long n, float e,
+                             const double* t_state) {
+  const double t = *t_state;
+  const double tn = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
+  const float beta = (float)((t - 1.0) / tn);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float xv = x[q];
+    const float nd = e * dx[q] - beta * (xv - xk[q]);
+    if (newdx) newdx[q] = nd;
+    xk[q] = xv;
+    x[q] = xv - nd;
+  }
+}
+
+__global__ void fista_t_kernel(double* t_state) {
+  const double t = *t_state;
+  *t_state = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
+}
+
+__global__ void clamp_kernel(float* x, long long n, float lo, float hi) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    x[q] = fminf(fmaxf(x[q], lo), hi);
+}
+
+// ---------------------------------------------------------------------------
+// TVProx (2-D).  p holds two dual slices: p0 (differences along x) and p1 (along y).
+// The dual is used through a per-slice scale (the isotropic projection of the
+// previous iteration), applied on read.
+// ---------------------------------------------------------------------------
+
+struct TvState {  // device-resident scalars
+  double t;        // Fista t of the dual iteration
+  float beta;      // Fista beta of the next update
+  float scale[2];  // per-slice projection factor of the current dual
+};
+
+__global__ void tv_init_kernel(float* p, float* xk, long long n2, TvState* st) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n2;
+       q += (long long)gridDim.x * blockDim.x) {
+    p[q] = 0.f;
+    xk[q] = 0.f;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->t = 1.0;
+    const double tn = (1.0 + sqrt(5.0)) / 2.0;
+    st->beta = (float)((1.0 - 1.0) / tn);
+    st->scale[0] = 1.f;
+    st->scale[1] = 1.f;
+  }
+}
+
+// D^T of the reference (tv_prox.jl:43-59), on the scaled dual.
+__device__ __forceinline__ float tv_dt(const float* p0, const float* p1, float s0, float s1, int x, int y,
+                                       int nx) {
+  const long long q = (long long)y * nx + x;
+  if (y == 0) return -s1 * p1[q];
+  if (x == 0) return -s0 * p0[q];
+  return s0 * (p0[q - 1] - p0[q]) + s1 * (p1[q - nx] - p1[q]);
+}
+
+// y = lam * D^T(p) - y0
+__global__ void tv_dt_kernel(const float* p, const float* y0, float* yv, int nx, int ny, float lam,
+                             const TvState* st) {
+  const long long n = (long long)nx * ny;
+  const float s0 = st->scale[0], s1 = st->scale[1];
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(q % nx), y = (int)(q / nx);
+    yv[q] = lam * tv_dt(p, p + n, s0, s1, x, y, nx) - y0[q];
+  }
+}
+
+// dp = D(y); Fista on the (scaled) dual; per-block partial sums of p^2 per slice
+// (isotropic) or clamp to [-1, 1] (anisotropic).
+__global__ void tv_step_kernel(float* p, float* xk, const float* yv, int nx, int ny, float e,
+                               const TvState* st, int isotropic, float* partials) {
+  __shared__ float red[kThreads / 32];
+  const long long n = (long long)nx * ny;
+  const float beta = st->beta;
+  float ss[2] = {0.f, 0.f};
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(q % nx), y = (int)(q / nx);
+    const float yc = yv[q];
+    float d[2];
+    d[0] = (x < nx - 1) ? yv[q + 1] - yc : 0.f;
+    d[1] = (y < ny - 1) ? yv[q + nx] - yc : 0.f;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const long long qi = q + i * n;
+      const float pv = p[qi] * st->scale[i];
+      const float nd = e * d[i] - beta * (pv - xk[qi]);
+      xk[qi] = pv;
+      float pn = pv - nd;
+      if (!isotropic) pn = fminf(fmaxf(pn, -1.f), 1.f);
+      p[qi] = pn;
+      ss[i] = fmaf(pn, pn, ss[i]);
+    }
+  }
+  if (isotropic) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const float b = block_sum<kThreads>(ss[i], red);
+      if (threadIdx.x == 0) partials[blockIdx.x * 2 + i] = b;
+    }
+  }
+}
+
+// Per-slice norms -> projection scale; Fista t/beta for the next update.
+__global__ void tv_norm_kernel(const float* partials, int nblocks, int isotropic, TvState* st) {
+  __shared__ float red[kThreads / 32];
+  float sc[2] = {1.f, 1.f};
+  if (isotropic) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      double acc = 0.0;
+      for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[b * 2 + i];
+      const float s = block_sum<kThreads>((float)acc, red);
+      if (threadIdx.x == 0) {
+        const float nrm = sqrtf(s);
+        sc[i] = nrm > 1.f ? 1.f / nrm : 1.f;
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    st->scale[0] = sc[0];
+    st->scale[1] = sc[1];
+    const double t = (1.0 + sqrt(1.0 + 4.0 * st->t * st->t)) / 2.0;  // t after this update
+    const double tn = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
+    st->t = t;
+    st->beta = (float)((t - 1.0) / tn);
+  }
+}
+
+// y0 -= lam * D^T(p)
+__global__ void tv_final_kernel(const float* p, float* y0, int nx, int ny, float lam, const TvState* st) {
+  const long long n = (long long)nx * ny;
+  const float s0 = st->scale[0], s1 = st->scale[1];
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(q % nx), y = (int)(q / nx);
+    y0[q] -= lam * tv_dt(p, p + n, s0, s1, x, y, nx);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+
+static unsigned capped_grid(long long n) {
+  long long g = (n + kThreads - 1) / kThreads;
+  if (g > 152LL * 32) g = 152LL * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+cudaError_t launch_as_h(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
+                        double z, double scale, cudaStream_t s) {
+  const double lm = lambda / n0;
+  as_h_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(H, fx_n, fy_n, dx, dy,
+                                                                       1.0 / (lm * lm), z, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rs_h_spatial(float2* h, int nx, int ny, int px, int py, double dx, double dy,
+                                double lambda, double z, double scale, cudaStream_t s) {
+  rs_h_spatial_kernel<<<capped_grid((long long)px * py), kThreads, 0, s>>>(h, nx, ny, px, py, dx, dy,
+                                                                           lambda, z, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_phase_fwd(float2* u, const float* phi, float2* saved, long long npix, int batch,
+                             float s, cudaStream_t st) {
+  phase_fwd_kernel<<<capped_grid(npix * batch), kThreads, 0, st>>>(u, phi, saved, npix, batch, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_phase_bwd(float2* dv, const float* phi, const float2* saved, float* dphi,
+                             long long npix, int batch, float s, cudaStream_t st) {
+  phase_bwd_kernel<<<capped_grid(npix), kThreads, 0, st>>>(dv, phi, saved, dphi, npix, batch, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_fwd(float2* u, const float2* m, float2* saved, long long npix, int batch,
+                            int conj_m, cudaStream_t st) {
+  mask_fwd_kernel<<<capped_grid(npix * batch), kThreads, 0, st>>>(u, m, saved, npix, batch, conj_m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mask_bwd(float2* dv, const float2* m, const float2* saved, float2* dm,
+                            long long npix, int batch, float s, cudaStream_t st) {
+  mask_bwd_kernel<<<capped_grid(npix), kThreads, 0, st>>>(dv, m, saved, dm, npix, batch, s);
+  return cudaGetLastError();
+}
+
+int sid_partial_blocks(long long npix) { return (int)grid_for(npix); }
+
+cudaError_t launch_sid_fwd(const float2* u, const float* target, const int* order, const int* offsets,
+                           int T, long long npix, float* resid, float* partials, float* loss,
+                           cudaStream_t st) {
+  const int nb = sid_partial_blocks(npix);
+  sid_fwd_kernel<<<nb, kThreads, 0, st>>>(u, target, order, offsets, T, npix, resid, partials);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sid_finalize_kernel<<<T, kThreads, 0, st>>>(partials, nb, T, loss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sid_bwd(const float2* u, const float* resid, const int* tidx, const float* dc,
+                           long long npix, int batch, float2* du, cudaStream_t st) {
+  sid_bwd_kernel<<<capped_grid(npix * batch), kThreads, 0, st>>>(u, resid, tidx, dc, npix, batch, du);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fista(float* x, float* xk, float* newdx, const float* dx, long long n, float e,
+                         double* t_state, cudaStream_t st) {
+  fista_kernel<<<capped_grid(n), kThreads, 0, st>>>(x, xk, newdx, dx, n, e, t_state);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  fista_t_kernel<<<1, 1, 0, st>>>(t_state);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clamp(float* x, long long n, float lo, float hi, cudaStream_t st) {
+  clamp_kernel<<<capped_grid(n), kThreads, 0, st>>>(x, n, lo, hi);
+  return cudaGetLastError();
+}
+
+size_t tv_state_bytes() { return sizeof(TvState); }
+int tv_partial_blocks(long long n) { return (int)capped_grid(n); }
+
+cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nx,
+                      int ny, float lam, int n_iter, int isotropic, float e, cudaStream_t st) {
+  const long long n = (long long)nx * ny;
+  TvState* s = reinterpret_cast<TvState*>(state);
+  const unsigned g = capped_grid(n);
+  tv_init_kernel<<<capped_grid(2 * n), kThreads, 0, st>>>(p, xk, 2 * n, s);
+  for (int it = 0; it < n_iter; ++it) {
+    tv_dt_kernel<<<g, kThreads, 0, st>>>(p, x, yv, nx, ny, lam, s);
+    tv_step_kernel<<<g, kThreads, 0, st>>>(p, xk, yv, nx, ny, e, s, isotropic, partials);
+    tv_norm_kernel<<<1, kThreads, 0, st>>>(partials, (int)g, isotropic, s);
+  }
+  tv_final_kernel<<<g, kThreads, 0, st>>>(p, x, nx, ny, lam, s);
+  return cudaGetLastError();
+}
+
+}  // namespace fo

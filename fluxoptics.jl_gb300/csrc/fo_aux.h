@@ -1,0 +1,38 @@
+// Launchers of the elementwise / reduction kernels in fo_aux.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fo {
+
+cudaError_t launch_as_h(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
+                        double z, double scale, cudaStream_t s);
+cudaError_t launch_rs_h_spatial(float2* h, int nx, int ny, int px, int py, double dx, double dy,
+                                double lambda, double z, double scale, cudaStream_t s);
+
+cudaError_t launch_phase_fwd(float2* u, const float* phi, float2* saved, long long npix, int batch,
+                             float s, cudaStream_t st);
+cudaError_t launch_phase_bwd(float2* dv, const float* phi, const float2* saved, float* dphi,
+                             long long npix, int batch, float s, cudaStream_t st);
+cudaError_t launch_mask_fwd(float2* u, const float2* m, float2* saved, long long npix, int batch,
+                            int conj_m, cudaStream_t st);
+cudaError_t launch_mask_bwd(float2* dv, const float2* m, const float2* saved, float2* dm,
+                            long long npix, int batch, float s, cudaStream_t st);
+
+int sid_partial_blocks(long long npix);
+cudaError_t launch_sid_fwd(const float2* u, const float* target, const int* order, const int* offsets,
+                           int T, long long npix, float* resid, float* partials, float* loss,
+                           cudaStream_t st);
+cudaError_t launch_sid_bwd(const float2* u, const float* resid, const int* tidx, const float* dc,
+                           long long npix, int batch, float2* du, cudaStream_t st);
+
+cudaError_t launch_fista(float* x, float* xk, float* newdx, const float* dx, long long n, float e,
+                         double* t_state, cudaStream_t st);
+cudaError_t launch_clamp(float* x, long long n, float lo, float hi, cudaStream_t st);
+
+size_t tv_state_bytes();
+int tv_partial_blocks(long long n);
+cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nx,
+                      int ny, float lam, int n_iter, int isotropic, float e, cudaStream_t st);
+
+}  // namespace fo

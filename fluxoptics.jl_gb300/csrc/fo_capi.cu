@@ -1,0 +1,982 @@
+// C ABI of libfluxoptics_gb300: plans, the fused chain engine, AS_BPM with
+// checkpointed adjoint, the metric and the optimiser entry points.
+#include <math.h>
+
+#include <cmath>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/fluxoptics_gb300.h"
+#include "fo_aux.h"
+#include "fo_internal.h"
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+namespace fo {
+
+static thread_local std::string g_last_error;
+
+void set_error(int code, const std::string& msg) {
+  (void)code;
+  g_last_error = msg;
+}
+
+int fail(int code, const std::string& msg) {
+  set_error(code, msg);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(FO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+// ---------------------------------------------------------------------------
+// Twiddle tables exp(-2 pi i m / N), one per (device, N), built in FP64.
+// ---------------------------------------------------------------------------
+static std::mutex g_tw_mu;
+static std::map<std::pair<int, int>, float2*> g_tw;
+
+const float2* twiddles(int N, int* err) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *err = cuda_fail(e, "cudaGetDevice");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto it = g_tw.find({dev, N});
+  if (it != g_tw.end()) return it->second;
+  std::vector<float2> h(N);
+  for (int m = 0; m < N; ++m) {
+    // reduce m/N to [0, 1/8] octant-free form via sincos of the exact angle in FP64
+    const double a = -2.0 * M_PI * (double)m / (double)N;
+    h[m] = make_float2((float)cos(a), (float)sin(a));
+  }
+  float2* d = nullptr;
+  e = cudaMalloc(&d, sizeof(float2) * N);
+  if (e != cudaSuccess) {
+    *err = fail(FO_ERR_ALLOC, "cudaMalloc twiddles failed");
+    return nullptr;
+  }
+  e = cudaMemcpy(d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    *err = cuda_fail(e, "cudaMemcpy twiddles");
+    return nullptr;
+  }
+  g_tw[{dev, N}] = d;
+  return d;
+}
+
+}  // namespace fo
+
+using namespace fo;
+
+// ---------------------------------------------------------------------------
+// Small helpers
+// ---------------------------------------------------------------------------
+namespace {
+
+int next_pow2(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int check_dir(int d) {
+  if (d != FO_FORWARD && d != FO_BACKWARD) return fail(FO_ERR_ARG, "direction must be FO_FORWARD (1) or FO_BACKWARD (-1)");
+  return FO_OK;
+}
+
+template <typename T>
+int dalloc(T** p, size_t count, const char* what) {
+  *p = nullptr;
+  if (count == 0) return FO_OK;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(FO_ERR_ALLOC, std::string("cudaMalloc failed for ") + what + " (" +
+                                  std::to_string(sizeof(T) * count) + " bytes)");
+  }
+  return FO_OK;
+}
+
+#define FO_TRY(expr)             \
+  do {                           \
+    int _rc = (expr);            \
+    if (_rc != FO_OK) return _rc; \
+  } while (0)
+
+#define FO_LAUNCH(expr)                                   \
+  do {                                                    \
+    cudaError_t _e = (expr);                              \
+    if (_e != cudaSuccess) return cuda_fail(_e, #expr);   \
+  } while (0)
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Propagator plans
+// ---------------------------------------------------------------------------
+struct fo_prop_plan_s {
+  int kind = 0;  // 0 AS, 1 RS
+  int nx = 0, ny = 0, batch = 0;
+  int fx = 0, fy = 0;  // transform sizes
+  double dx = 0, dy = 0, z = 0, n0 = 1;
+  std::vector<double> lambdas;  // per field
+  int n_tables = 0;
+  float2* H = nullptr;          // n_tables x fy x fx, scaled by 1/(fx*fy)
+  int* h_index = nullptr;       // device, per field
+  float* inv_lambda = nullptr;  // device, per field
+  const float2* tw_x = nullptr;
+  const float2* tw_y = nullptr;
+  float2* scratch = nullptr;    // RS: batch x ny x fx
+  size_t ws_bytes = 0;
+};
+
+namespace {
+
+void plan_free(fo_prop_plan p) {
+  if (!p) return;
+  cudaFree(p->H);
+  cudaFree(p->h_index);
+  cudaFree(p->inv_lambda);
+  cudaFree(p->scratch);
+  delete p;
+}
+
+struct Layout {
+  int nx, ny, batch, fx, fy;
+  bool padded;
+};
+
+Layout layout_of(const fo_prop_plan_s* p) { return Layout{p->nx, p->ny, p->batch, p->fx, p->fy, p->kind == 1}; }
+
+bool same_layout(const Layout& a, const Layout& b) {
+  return a.nx == b.nx && a.ny == b.ny && a.batch == b.batch && a.fx == b.fx && a.fy == b.fy &&
+         a.padded == b.padded;
+}
+
+// Internal modulation description.
+struct Mod {
+  int kind = MOD_NONE;
+  const void* param = nullptr;
+  void* saved = nullptr;
+  void* grad = nullptr;
+  float scale = 1.f;
+};
+
+Mod mod_from(const fo_mod* m) {
+  Mod r;
+  if (!m) return r;
+  r.kind = m->kind;
+  r.param = m->param;
+  r.saved = m->saved;
+  r.grad = m->grad;
+  r.scale = (float)m->scale;
+  return r;
+}
+
+struct SeedArgs {
+  const float* resid = nullptr;
+  const int* tidx = nullptr;
+  const float* dc = nullptr;
+};
+
+int validate_mod(const Mod& m, bool backward) {
+  if (m.kind < MOD_NONE || m.kind > MOD_DN) return fail(FO_ERR_ARG, "unknown modulation kind");
+  if (m.kind != MOD_NONE && !m.param) return fail(FO_ERR_ARG, "modulation parameter pointer is NULL");
+  if (backward && m.kind != MOD_NONE && m.grad && !m.saved)
+    return fail(FO_ERR_ARG, "a gradient needs the saved forward input");
+  return FO_OK;
+}
+
+// One row pass.  `src`/`dst` are real-space (ld nx) or spectral (ld fx) arrays as
+// selected by the inv/fwd flags.
+int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bool fwd_after,
+             const Mod& mod, bool bwd, float s, const float* inv_lambda, const SeedArgs* seed,
+             const float2* tw, cudaStream_t st) {
+  RowPassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const long long real_bs = (long long)L.nx * L.ny, spec_bs = (long long)L.fx * L.ny;
+  a.src = src;
+  a.dst = dst;
+  a.src_bstride = inv_first ? spec_bs : real_bs;
+  a.src_ld = inv_first ? L.fx : L.nx;
+  a.dst_bstride = fwd_after ? spec_bs : real_bs;
+  a.dst_ld = fwd_after ? L.fx : L.nx;
+  a.nrows = L.ny;
+  a.n_valid = L.nx;
+  a.batch = L.batch;
+  const bool grad = bwd && mod.kind != MOD_NONE && mod.grad != nullptr;
+  a.fields_per_cta = grad ? L.batch : 1;
+  a.field_list = nullptr;
+  a.inv_first = inv_first;
+  a.fwd_after = fwd_after;
+  a.mod_kind = mod.kind;
+  a.mod_bwd = bwd;
+  a.mod_sign = s;
+  a.mod_param = mod.param;
+  a.param_ld = L.nx;
+  a.mod_scale = mod.scale;
+  a.inv_lambda = inv_lambda;
+  if (!bwd) {
+    a.save = reinterpret_cast<float2*>(mod.saved);
+    a.save_bstride = real_bs;
+    a.save_ld = L.nx;
+  } else {
+    a.saved = reinterpret_cast<const float2*>(mod.saved);
+    a.saved_bstride = real_bs;
+    a.saved_ld = L.nx;
+    a.grad = mod.grad;
+  }
+  if (seed) {
+    a.seed = 1;
+    a.resid = seed->resid;
+    a.resid_tstride = real_bs;
+    a.resid_ld = L.nx;
+    a.tidx = seed->tidx;
+    a.dc = seed->dc;
+  }
+  FO_LAUNCH(launch_row_pass(L.fx, a, tw, st));
+  return FO_OK;
+}
+
+int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st) {
+  ColPassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.buf = buf;
+  a.bstride = (long long)p->fx * p->ny;
+  a.ld = p->fx;
+  a.ncols = p->fx;
+  a.y_in = p->ny;
+  a.y_out = p->ny;
+  a.H = p->H;
+  a.h_stride = (long long)p->fx * p->fy;
+  a.h_index = p->h_index;
+  a.conj_h = conj_h;
+  a.fft_only = 0;
+  a.batch = p->batch;
+  FO_LAUNCH(launch_col_pass(p->fy, a, p->tw_y, st));
+  return FO_OK;
+}
+
+// Forward sweep: mods[0] -> props[0] -> ... -> props[K-1] -> mods[K], in place on u.
+int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, const Mod* mods, int s,
+                cudaStream_t st) {
+  const int K = (int)props.size();
+  const Layout L = layout_of(props[0]);
+  const float* il = props[0]->inv_lambda;
+  const float sf = (float)s;
+  FO_TRY(row_pass(L, u, buf, false, true, mods[0], false, sf, il, nullptr, props[0]->tw_x, st));
+  for (int k = 0; k < K; ++k) {
+    FO_TRY(col_pass(props[k], buf, s < 0, st));
+    if (k + 1 < K)
+      FO_TRY(row_pass(L, buf, buf, true, true, mods[k + 1], false, sf, il, nullptr, props[0]->tw_x, st));
+    else
+      FO_TRY(row_pass(L, buf, u, true, false, mods[K], false, sf, il, nullptr, props[0]->tw_x, st));
+  }
+  return FO_OK;
+}
+
+// Adjoint sweep in reverse order, in place on du (src0 is du, or the forward
+// output when the sweep is seeded by the metric).
+int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du, const float2* src0,
+                 const Mod* mods, int s, const SeedArgs* seed, cudaStream_t st) {
+  const int K = (int)props.size();
+  const Layout L = layout_of(props[0]);
+  const float* il = props[0]->inv_lambda;
+  const float sf = (float)s;
+  FO_TRY(row_pass(L, src0, buf, false, true, mods[K], true, sf, il, seed, props[0]->tw_x, st));
+  for (int k = K - 1; k >= 0; --k) {
+    FO_TRY(col_pass(props[k], buf, s > 0, st));
+    if (k > 0)
+      FO_TRY(row_pass(L, buf, buf, true, true, mods[k], true, sf, il, nullptr, props[0]->tw_x, st));
+    else
+      FO_TRY(row_pass(L, buf, du, true, false, mods[0], true, sf, il, nullptr, props[0]->tw_x, st));
+  }
+  return FO_OK;
+}
+
+int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx, double dy,
+              const double* lambdas, int n_lambdas, double z, double n0) {
+  if (!out) return fail(FO_ERR_ARG, "plan output pointer is NULL");
+  *out = nullptr;
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  if (!(dx > 0) || !(dy > 0)) return fail(FO_ERR_ARG, "dx and dy must be positive");
+  if (!lambdas || (n_lambdas != 1 && n_lambdas != batch))
+    return fail(FO_ERR_ARG, "lambdas must hold 1 or batch wavelengths");
+  for (int i = 0; i < n_lambdas; ++i)
+    if (!(lambdas[i] > 0)) return fail(FO_ERR_ARG, "wavelengths must be positive");
+  if (!std::isfinite(z)) return fail(FO_ERR_ARG, "z must be finite");
+  if (kind == 0 && !(n0 > 0)) return fail(FO_ERR_ARG, "n0 must be positive");
+  const int fx = kind == 0 ? nx : next_pow2(2 * nx - 1);
+  const int fy = kind == 0 ? ny : next_pow2(2 * ny - 1);
+  if (!fft_size_supported(fx) || !fft_size_supported(fy))
+    return fail(FO_ERR_SHAPE, "transform size " + std::to_string(fx) + " x " + std::to_string(fy) +
+                                  " is not supported (powers of two from 16 to 4096)");
+  fo_prop_plan p = new fo_prop_plan_s();
+  p->kind = kind;
+  p->nx = nx;
+  p->ny = ny;
+  p->batch = batch;
+  p->fx = fx;
+  p->fy = fy;
+  p->dx = dx;
+  p->dy = dy;
+  p->z = z;
+  p->n0 = n0;
+  p->lambdas.resize(batch);
+  for (int b = 0; b < batch; ++b) p->lambdas[b] = lambdas[n_lambdas == 1 ? 0 : b];
+  // distinct wavelengths -> one transfer function each
+  std::vector<double> uniq;
+  std::vector<int> hidx(batch);
+  for (int b = 0; b < batch; ++b) {
+    auto it = std::find(uniq.begin(), uniq.end(), p->lambdas[b]);
+    if (it == uniq.end()) {
+      hidx[b] = (int)uniq.size();
+      uniq.push_back(p->lambdas[b]);
+    } else {
+      hidx[b] = (int)(it - uniq.begin());
+    }
+  }
+  p->n_tables = (int)uniq.size();
+  int rc = FO_OK;
+  const size_t table = (size_t)fx * fy;
+  if ((rc = dalloc(&p->H, table * p->n_tables, "transfer functions")) != FO_OK ||
+      (rc = dalloc(&p->h_index, batch, "table index")) != FO_OK ||
+      (rc = dalloc(&p->inv_lambda, batch, "inverse wavelengths")) != FO_OK) {
+    plan_free(p);
+    return rc;
+  }
+  p->ws_bytes = sizeof(float2) * table * p->n_tables + (sizeof(int) + sizeof(float)) * batch;
+  if (kind == 1) {
+    if ((rc = dalloc(&p->scratch, (size_t)batch * ny * fx, "padded scratch")) != FO_OK) {
+      plan_free(p);
+      return rc;
+    }
+    p->ws_bytes += sizeof(float2) * (size_t)batch * ny * fx;
+  }
+  p->tw_x = twiddles(fx, &rc);
+  if (!p->tw_x) {
+    plan_free(p);
+    return rc;
+  }
+  p->tw_y = twiddles(fy, &rc);
+  if (!p->tw_y) {
+    plan_free(p);
+    return rc;
+  }
+  std::vector<float> il(batch);
+  for (int b = 0; b < batch; ++b) il[b] = (float)(1.0 / p->lambdas[b]);
+  cudaError_t e = cudaMemcpy(p->h_index, hidx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->inv_lambda, il.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    plan_free(p);
+    return cuda_fail(e, "cudaMemcpy plan tables");
+  }
+  const double scale = 1.0 / ((double)fx * (double)fy);
+  for (int i = 0; i < p->n_tables && e == cudaSuccess; ++i) {
+    float2* Hi = p->H + table * i;
+    if (kind == 0) {
+      e = launch_as_h(Hi, fx, fy, dx, dy, uniq[i], n0, z, scale, 0);
+    } else {
+      e = launch_rs_h_spatial(Hi, nx, ny, fx, fy, dx, dy, uniq[i], z, scale, 0);
+      if (e == cudaSuccess) {
+        // H_RS = FFT2(h): row transforms of all fy rows, then column transforms
+        Layout L{fx, fy, 1, fx, fy, false};
+        Mod none;
+        rc = row_pass(L, Hi, Hi, false, true, none, false, 1.f, nullptr, nullptr, p->tw_x, 0);
+        if (rc != FO_OK) {
+          plan_free(p);
+          return rc;
+        }
+        ColPassArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.buf = Hi;
+        a.bstride = (long long)table;
+        a.ld = fx;
+        a.ncols = fx;
+        a.y_in = fy;
+        a.y_out = fy;
+        a.fft_only = 1;
+        a.batch = 1;
+        e = launch_col_pass(fy, a, p->tw_y, 0);
+      }
+    }
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    plan_free(p);
+    return cuda_fail(e, "building transfer functions");
+  }
+  *out = p;
+  return FO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+FO_API int fo_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+FO_API const char* fo_last_error(void) { return g_last_error.c_str(); }
+
+FO_API int fo_stream_synchronize(void* stream) {
+  cudaError_t e = cudaStreamSynchronize(S(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  return FO_OK;
+}
+
+FO_API int fo_asprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
+                            const double* lambdas, int n_lambdas, double z, double n0, int flags) {
+  (void)flags;
+  return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0);
+}
+
+FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
+                            const double* lambdas, int n_lambdas, double z, int flags) {
+  (void)flags;
+  return make_plan(plan, 1, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, 1.0);
+}
+
+FO_API int fo_prop_destroy(fo_prop_plan plan) {
+  plan_free(plan);
+  return FO_OK;
+}
+
+FO_API int fo_prop_info(fo_prop_plan plan, int* fft_nx, int* fft_ny, size_t* workspace_bytes) {
+  if (!plan) return fail(FO_ERR_ARG, "plan is NULL");
+  if (fft_nx) *fft_nx = plan->fx;
+  if (fft_ny) *fft_ny = plan->fy;
+  if (workspace_bytes) *workspace_bytes = plan->ws_bytes;
+  return FO_OK;
+}
+
+FO_API int fo_propagate(fo_prop_plan plan, void* u, int direction, void* stream) {
+  if (!plan || !u) return fail(FO_ERR_ARG, "plan and u must not be NULL");
+  FO_TRY(check_dir(direction));
+  std::vector<fo_prop_plan> props{plan};
+  Mod mods[2];
+  float2* uu = reinterpret_cast<float2*>(u);
+  float2* buf = plan->kind == 1 ? plan->scratch : uu;
+  return run_forward(props, buf, uu, mods, direction, S(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Standalone modulators
+// ---------------------------------------------------------------------------
+
+FO_API int fo_phase_forward(void* u, const float* phi, void* u_saved, int nx, int ny, int batch,
+                            int direction, void* stream) {
+  if (!u || !phi) return fail(FO_ERR_ARG, "u and phi must not be NULL");
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  FO_TRY(check_dir(direction));
+  FO_LAUNCH(launch_phase_fwd(reinterpret_cast<float2*>(u), phi, reinterpret_cast<float2*>(u_saved),
+                             (long long)nx * ny, batch, (float)direction, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_phase_backward(void* dv, const float* phi, const void* u_saved, float* dphi, int nx,
+                             int ny, int batch, int direction, void* stream) {
+  if (!dv || !phi) return fail(FO_ERR_ARG, "dv and phi must not be NULL");
+  if (dphi && !u_saved) return fail(FO_ERR_ARG, "dphi needs u_saved");
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  FO_TRY(check_dir(direction));
+  FO_LAUNCH(launch_phase_bwd(reinterpret_cast<float2*>(dv), phi, reinterpret_cast<const float2*>(u_saved),
+                             dphi, (long long)nx * ny, batch, (float)direction, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_mask_forward(void* u, const void* m, void* u_saved, int nx, int ny, int batch,
+                           int direction, void* stream) {
+  if (!u || !m) return fail(FO_ERR_ARG, "u and m must not be NULL");
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  FO_TRY(check_dir(direction));
+  FO_LAUNCH(launch_mask_fwd(reinterpret_cast<float2*>(u), reinterpret_cast<const float2*>(m),
+                            reinterpret_cast<float2*>(u_saved), (long long)nx * ny, batch,
+                            direction < 0, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_mask_backward(void* dv, const void* m, const void* u_saved, void* dm, int nx, int ny,
+                            int batch, int direction, void* stream) {
+  if (!dv || !m) return fail(FO_ERR_ARG, "dv and m must not be NULL");
+  if (dm && !u_saved) return fail(FO_ERR_ARG, "dm needs u_saved");
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  FO_TRY(check_dir(direction));
+  FO_LAUNCH(launch_mask_bwd(reinterpret_cast<float2*>(dv), reinterpret_cast<const float2*>(m),
+                            reinterpret_cast<const float2*>(u_saved), reinterpret_cast<float2*>(dm),
+                            (long long)nx * ny, batch, (float)direction, S(stream)));
+  return FO_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Chains
+// ---------------------------------------------------------------------------
+struct fo_chain_s {
+  std::vector<fo_prop_plan> props;
+  float2* scratch = nullptr;  // padded layouts only
+};
+
+struct fo_sid_s {
+  int nx = 0, ny = 0, batch = 0, T = 0;
+  int* tidx = nullptr;     // device, per field
+  int* order = nullptr;    // device, fields grouped by target slice
+  int* offsets = nullptr;  // device, T+1
+  float* resid = nullptr;  // device, T x ny x nx
+  float* partials = nullptr;
+  float* ones = nullptr;   // device, T
+};
+
+extern "C" {
+
+FO_API int fo_chain_create(fo_chain* chain, int n_props, const fo_prop_plan* props) {
+  if (!chain) return fail(FO_ERR_ARG, "chain output pointer is NULL");
+  *chain = nullptr;
+  if (n_props < 1 || !props) return fail(FO_ERR_ARG, "a chain needs at least one propagator");
+  for (int k = 0; k < n_props; ++k)
+    if (!props[k]) return fail(FO_ERR_ARG, "propagator plan is NULL");
+  const Layout L = layout_of(props[0]);
+  for (int k = 1; k < n_props; ++k)
+    if (!same_layout(L, layout_of(props[k])))
+      return fail(FO_ERR_SHAPE, "all propagators of a chain must share grid, batch and padding");
+  fo_chain c = new fo_chain_s();
+  c->props.assign(props, props + n_props);
+  if (L.padded) {
+    int rc = dalloc(&c->scratch, (size_t)L.batch * L.ny * L.fx, "chain scratch");
+    if (rc != FO_OK) {
+      delete c;
+      return rc;
+    }
+  }
+  *chain = c;
+  return FO_OK;
+}
+
+FO_API int fo_chain_destroy(fo_chain chain) {
+  if (chain) {
+    cudaFree(chain->scratch);
+    delete chain;
+  }
+  return FO_OK;
+}
+
+FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int direction, void* stream) {
+  if (!chain || !u || !mods) return fail(FO_ERR_ARG, "chain, u and mods must not be NULL");
+  FO_TRY(check_dir(direction));
+  const int K = (int)chain->props.size();
+  std::vector<Mod> m(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    m[k] = mod_from(&mods[k]);
+    FO_TRY(validate_mod(m[k], false));
+  }
+  float2* uu = reinterpret_cast<float2*>(u);
+  float2* buf = chain->scratch ? chain->scratch : uu;
+  return run_forward(chain->props, buf, uu, m.data(), direction, S(stream));
+}
+
+FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,
+                             const void* u_out, void* stream) {
+  if (!chain || !du || !mods) return fail(FO_ERR_ARG, "chain, du and mods must not be NULL");
+  FO_TRY(check_dir(direction));
+  const int K = (int)chain->props.size();
+  std::vector<Mod> m(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    m[k] = mod_from(&mods[k]);
+    FO_TRY(validate_mod(m[k], true));
+  }
+  float2* d = reinterpret_cast<float2*>(du);
+  float2* buf = chain->scratch ? chain->scratch : d;
+  SeedArgs seed;
+  const float2* src0 = d;
+  if (sid) {
+    const Layout L = layout_of(chain->props[0]);
+    if (!u_out) return fail(FO_ERR_ARG, "a seeded sweep needs u_out");
+    if (sid->nx != L.nx || sid->ny != L.ny || sid->batch != L.batch)
+      return fail(FO_ERR_SHAPE, "metric and chain shapes differ");
+    seed.resid = sid->resid;
+    seed.tidx = sid->tidx;
+    seed.dc = sid->ones;
+    src0 = reinterpret_cast<const float2*>(u_out);
+  }
+  return run_backward(chain->props, buf, d, src0, m.data(), direction, sid ? &seed : nullptr, S(stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// AS_BPM
+// ---------------------------------------------------------------------------
+struct fo_bpm_s {
+  fo_prop_plan full = nullptr, half = nullptr;
+  int nx = 0, ny = 0, batch = 0, n_slices = 0, every = 1, n_ckpt = 0;
+  double kdz = 0;
+  float2* ckpt = nullptr;  // n_ckpt x batch x ny x nx
+  float2* seg = nullptr;   // every x batch x ny x nx (slot 0 unused)
+  float2* rbuf = nullptr;  // recompute field
+  size_t ws_bytes = 0;
+};
+
+extern "C" {
+
+FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
+                         const double* lambdas, int n_lambdas, double thickness, double n0,
+                         int n_slices, int checkpoint_every, double cos_correction, int flags) {
+  (void)flags;
+  if (!bpm) return fail(FO_ERR_ARG, "bpm output pointer is NULL");
+  *bpm = nullptr;
+  if (n_slices < 2) return fail(FO_ERR_SHAPE, "AS_BPM needs at least 2 slices");
+  if (!(thickness > 0) || !(cos_correction > 0)) return fail(FO_ERR_ARG, "thickness and cos_correction must be positive");
+  if (checkpoint_every < 0) return fail(FO_ERR_ARG, "checkpoint_every must be >= 0");
+  const double dz = thickness / n_slices;
+  fo_bpm b = new fo_bpm_s();
+  int rc = make_plan(&b->full, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz, n0);
+  if (rc == FO_OK) rc = make_plan(&b->half, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz / 2, n0);
+  if (rc != FO_OK) {
+    plan_free(b->full);
+    delete b;
+    return rc;
+  }
+  b->nx = nx;
+  b->ny = ny;
+  b->batch = batch;
+  b->n_slices = n_slices;
+  int every = checkpoint_every == 0 ? (int)lround(sqrt((double)n_slices)) : checkpoint_every;
+  every = std::max(1, std::min(every, n_slices));
+  b->every = every;
+  b->n_ckpt = (n_slices + every - 1) / every;
+  b->kdz = 2.0 * M_PI * dz / cos_correction;
+  const size_t field = (size_t)batch * ny * nx;
+  if ((rc = dalloc(&b->ckpt, field * b->n_ckpt, "BPM checkpoints")) != FO_OK ||
+      (every > 1 && (rc = dalloc(&b->seg, field * every, "BPM segment")) != FO_OK) ||
+      (every > 1 && (rc = dalloc(&b->rbuf, field, "BPM recompute field")) != FO_OK)) {
+    cudaFree(b->ckpt);
+    cudaFree(b->seg);
+    plan_free(b->full);
+    plan_free(b->half);
+    delete b;
+    return rc;
+  }
+  b->ws_bytes = sizeof(float2) * field * (b->n_ckpt + (every > 1 ? every + 1 : 0)) + b->full->ws_bytes +
+                b->half->ws_bytes;
+  *bpm = b;
+  return FO_OK;
+}
+
+FO_API int fo_bpm_destroy(fo_bpm b) {
+  if (!b) return FO_OK;
+  cudaFree(b->ckpt);
+  cudaFree(b->seg);
+  cudaFree(b->rbuf);
+  plan_free(b->full);
+  plan_free(b->half);
+  delete b;
+  return FO_OK;
+}
+
+FO_API int fo_bpm_info(fo_bpm b, int* checkpoint_every, size_t* workspace_bytes) {
+  if (!b) return fail(FO_ERR_ARG, "bpm is NULL");
+  if (checkpoint_every) *checkpoint_every = b->every;
+  if (workspace_bytes) *workspace_bytes = b->ws_bytes;
+  return FO_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+float2* bpm_slot(fo_bpm b, int k) {
+  const size_t field = (size_t)b->batch * b->ny * b->nx;
+  if (k % b->every == 0) return b->ckpt + field * (k / b->every);
+  return b->seg + field * (k % b->every);
+}
+
+Mod dn_mod(fo_bpm b, const float* dn, int k, void* saved, void* grad) {
+  Mod m;
+  m.kind = MOD_DN;
+  m.param = dn + (size_t)k * b->ny * b->nx;
+  m.saved = saved;
+  m.grad = grad;
+  m.scale = (float)b->kdz;
+  return m;
+}
+
+// Recompute the slice inputs of the segment that starts at checkpoint g.
+int bpm_recompute(fo_bpm b, const float* dn, int g, int s, cudaStream_t st) {
+  const int a = g * b->every;
+  const int e = std::min(b->n_slices, a + b->every);
+  const int K = e - a - 1;  // full steps between the first and the last slice of the segment
+  if (K <= 0) return FO_OK;
+  const size_t field = (size_t)b->batch * b->ny * b->nx;
+  FO_LAUNCH(cudaMemcpyAsync(b->rbuf, b->ckpt + field * g, sizeof(float2) * field, cudaMemcpyDeviceToDevice, st));
+  std::vector<fo_prop_plan> props(K, b->full);
+  std::vector<Mod> mods(K + 1);
+  mods[0] = dn_mod(b, dn, a, nullptr, nullptr);
+  for (int k = 1; k <= K; ++k) mods[k] = dn_mod(b, dn, a + k, bpm_slot(b, a + k), nullptr);
+  return run_forward(props, b->rbuf, b->rbuf, mods.data(), s, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+FO_API int fo_bpm_forward(fo_bpm b, void* u, const float* dn, int direction, int save, void* stream) {
+  if (!b || !u || !dn) return fail(FO_ERR_ARG, "bpm, u and dn must not be NULL");
+  FO_TRY(check_dir(direction));
+  cudaStream_t st = S(stream);
+  const int n = b->n_slices;
+  // props: half, full x (n-1), half; mods: none, dn_0 .. dn_{n-1}, none
+  std::vector<fo_prop_plan> props;
+  props.reserve(n + 1);
+  props.push_back(b->half);
+  for (int k = 0; k < n - 1; ++k) props.push_back(b->full);
+  props.push_back(b->half);
+  std::vector<Mod> mods(n + 2);
+  for (int k = 0; k < n; ++k) {
+    void* sv = (save && k % b->every == 0) ? (void*)bpm_slot(b, k) : nullptr;
+    mods[k + 1] = dn_mod(b, dn, k, sv, nullptr);
+  }
+  float2* uu = reinterpret_cast<float2*>(u);
+  return run_forward(props, uu, uu, mods.data(), direction, st);
+}
+
+FO_API int fo_bpm_backward(fo_bpm b, void* du, const float* dn, float* ddn, int direction, void* stream) {
+  if (!b || !du || !dn) return fail(FO_ERR_ARG, "bpm, du and dn must not be NULL");
+  FO_TRY(check_dir(direction));
+  cudaStream_t st = S(stream);
+  const int n = b->n_slices;
+  const int s = direction;
+  const float sf = (float)s;
+  float2* d = reinterpret_cast<float2*>(du);
+  const Layout L = layout_of(b->full);
+  const float* il = b->full->inv_lambda;
+  const float2* tw = b->full->tw_x;
+  Mod none;
+  FO_TRY(row_pass(L, d, d, false, true, none, true, sf, il, nullptr, tw, st));
+  FO_TRY(col_pass(b->half, d, s > 0, st));
+  for (int k = n - 1; k >= 0; --k) {
+    const int g = k / b->every;
+    const bool top = (k == n - 1) || ((k + 1) % b->every == 0);
+    if (top && b->every > 1) FO_TRY(bpm_recompute(b, dn, g, s, st));
+    Mod m = dn_mod(b, dn, k, bpm_slot(b, k), ddn ? (void*)(ddn + (size_t)k * b->ny * b->nx) : nullptr);
+    FO_TRY(row_pass(L, d, d, true, true, m, true, sf, il, nullptr, tw, st));
+    FO_TRY(col_pass(k > 0 ? b->full : b->half, d, s > 0, st));
+  }
+  return row_pass(L, d, d, true, false, none, true, sf, il, nullptr, tw, st);
+}
+
+// ---------------------------------------------------------------------------
+// SquaredIntensityDifference
+// ---------------------------------------------------------------------------
+
+FO_API int fo_sid_create(fo_sid* sid, int nx, int ny, int batch, int n_targets, const int* target_index) {
+  if (!sid) return fail(FO_ERR_ARG, "sid output pointer is NULL");
+  *sid = nullptr;
+  if (nx <= 0 || ny <= 0 || batch <= 0 || n_targets <= 0) return fail(FO_ERR_SHAPE, "sizes must be positive");
+  std::vector<int> tidx(batch);
+  for (int b = 0; b < batch; ++b) {
+    tidx[b] = target_index ? target_index[b] : b % n_targets;
+    if (tidx[b] < 0 || tidx[b] >= n_targets) return fail(FO_ERR_ARG, "target_index out of range");
+  }
+  std::vector<int> order, offsets(n_targets + 1, 0);
+  for (int t = 0; t < n_targets; ++t) {
+    offsets[t] = (int)order.size();
+    for (int b = 0; b < batch; ++b)
+      if (tidx[b] == t) order.push_back(b);
+  }
+  offsets[n_targets] = (int)order.size();
+  fo_sid m = new fo_sid_s();
+  m->nx = nx;
+  m->ny = ny;
+  m->batch = batch;
+  m->T = n_targets;
+  const long long npix = (long long)nx * ny;
+  int rc;
+  std::vector<float> ones(n_targets, 1.f);
+  if ((rc = dalloc(&m->tidx, batch, "metric index")) != FO_OK ||
+      (rc = dalloc(&m->order, batch, "metric order")) != FO_OK ||
+      (rc = dalloc(&m->offsets, n_targets + 1, "metric offsets")) != FO_OK ||
+      (rc = dalloc(&m->resid, (size_t)n_targets * npix, "metric residuals")) != FO_OK ||
+      (rc = dalloc(&m->partials, (size_t)sid_partial_blocks(npix) * n_targets, "metric partial sums")) != FO_OK ||
+      (rc = dalloc(&m->ones, n_targets, "metric ones")) != FO_OK) {
+    fo_sid_destroy(m);
+    return rc;
+  }
+  cudaError_t e = cudaMemcpy(m->tidx, tidx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->order, order.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->offsets, offsets.data(), sizeof(int) * (n_targets + 1), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->ones, ones.data(), sizeof(float) * n_targets, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    fo_sid_destroy(m);
+    return cuda_fail(e, "cudaMemcpy metric tables");
+  }
+  *sid = m;
+  return FO_OK;
+}
+
+FO_API int fo_sid_destroy(fo_sid m) {
+  if (!m) return FO_OK;
+  cudaFree(m->tidx);
+  cudaFree(m->order);
+  cudaFree(m->offsets);
+  cudaFree(m->resid);
+  cudaFree(m->partials);
+  cudaFree(m->ones);
+  delete m;
+  return FO_OK;
+}
+
+FO_API int fo_sid_forward(fo_sid m, const void* u, const float* target, float* loss, void* stream) {
+  if (!m || !u || !target || !loss) return fail(FO_ERR_ARG, "sid, u, target and loss must not be NULL");
+  FO_LAUNCH(launch_sid_fwd(reinterpret_cast<const float2*>(u), target, m->order, m->offsets, m->T,
+                           (long long)m->nx * m->ny, m->resid, m->partials, loss, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_sid_backward(fo_sid m, const void* u, const float* dc, void* du, void* stream) {
+  if (!m || !u || !du) return fail(FO_ERR_ARG, "sid, u and du must not be NULL");
+  FO_LAUNCH(launch_sid_bwd(reinterpret_cast<const float2*>(u), m->resid, m->tidx, dc ? dc : m->ones,
+                           (long long)m->nx * m->ny, m->batch, reinterpret_cast<float2*>(du), S(stream)));
+  return FO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Optimiser / prox
+// ---------------------------------------------------------------------------
+
+FO_API int fo_fista_step(float* x, float* xk, float* newdx, const float* dx, long long n, double eta,
+                         double* t_state, void* stream) {
+  if (!x || !xk || !dx || !t_state) return fail(FO_ERR_ARG, "x, xk, dx and t_state must not be NULL");
+  if (n <= 0) return fail(FO_ERR_SHAPE, "n must be positive");
+  FO_LAUNCH(launch_fista(x, xk, newdx, dx, n, (float)(eta * eta), t_state, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream) {
+  if (!x) return fail(FO_ERR_ARG, "x must not be NULL");
+  if (n <= 0) return fail(FO_ERR_SHAPE, "n must be positive");
+  if (!(lo <= hi)) return fail(FO_ERR_ARG, "lo must not exceed hi");
+  FO_LAUNCH(launch_clamp(x, n, (float)lo, (float)hi, S(stream)));
+  return FO_OK;
+}
+
+}  // extern "C"
+
+struct fo_tv_s {
+  int nx = 0, ny = 0, n_iter = 0, isotropic = 1;
+  double lambda = 0, eta = 0;
+  float *p = nullptr, *xk = nullptr, *y = nullptr, *partials = nullptr;
+  void* state = nullptr;
+};
+
+extern "C" {
+
+FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta) {
+  if (!tv) return fail(FO_ERR_ARG, "tv output pointer is NULL");
+  *tv = nullptr;
+  if (nx < 2 || ny < 2) return fail(FO_ERR_SHAPE, "TVProx needs at least 2 x 2 samples");
+  if (n_iter < 0) return fail(FO_ERR_ARG, "n_iter must be >= 0");
+  fo_tv t = new fo_tv_s();
+  t->nx = nx;
+  t->ny = ny;
+  t->n_iter = n_iter;
+  t->isotropic = isotropic ? 1 : 0;
+  t->lambda = lambda;
+  t->eta = eta;
+  const size_t n = (size_t)nx * ny;
+  int rc;
+  if ((rc = dalloc(&t->p, 2 * n, "TV dual")) != FO_OK || (rc = dalloc(&t->xk, 2 * n, "TV state")) != FO_OK ||
+      (rc = dalloc(&t->y, n, "TV primal")) != FO_OK ||
+      (rc = dalloc(&t->partials, (size_t)tv_partial_blocks((long long)n) * 2, "TV partials")) != FO_OK ||
+      (rc = dalloc(reinterpret_cast<char**>(&t->state), tv_state_bytes(), "TV scalars")) != FO_OK) {
+    fo_tv_destroy(t);
+    return rc;
+  }
+  *tv = t;
+  return FO_OK;
+}
+
+FO_API int fo_tv_destroy(fo_tv t) {
+  if (!t) return FO_OK;
+  cudaFree(t->p);
+  cudaFree(t->xk);
+  cudaFree(t->y);
+  cudaFree(t->partials);
+  cudaFree(t->state);
+  delete t;
+  return FO_OK;
+}
+
+FO_API int fo_tv_apply(fo_tv t, float* x, void* stream) {
+  if (!t || !x) return fail(FO_ERR_ARG, "tv and x must not be NULL");
+  const double lam = t->isotropic ? t->lambda : t->lambda / 100.0;
+  FO_LAUNCH(launch_tv(x, t->p, t->xk, t->y, t->partials, t->state, t->nx, t->ny, (float)lam, t->n_iter,
+                      t->isotropic, (float)(t->eta * t->eta), S(stream)));
+  return FO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CUDA graphs
+// ---------------------------------------------------------------------------
+
+}  // extern "C"
+
+struct fo_graph_s {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+FO_API int fo_graph_begin(void* stream) {
+  if (!stream) return fail(FO_ERR_ARG, "graph capture needs a non-default stream");
+  FO_LAUNCH(cudaStreamBeginCapture(S(stream), cudaStreamCaptureModeThreadLocal));
+  return FO_OK;
+}
+
+FO_API int fo_graph_end(void* stream, fo_graph* graph) {
+  if (!stream || !graph) return fail(FO_ERR_ARG, "stream and graph must not be NULL");
+  *graph = nullptr;
+  fo_graph g = new fo_graph_s();
+  cudaError_t e = cudaStreamEndCapture(S(stream), &g->graph);
+  if (e != cudaSuccess) {
+    delete g;
+    return cuda_fail(e, "cudaStreamEndCapture");
+  }
+  e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g->graph);
+    delete g;
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  *graph = g;
+  return FO_OK;
+}
+
+FO_API int fo_graph_launch(fo_graph g, void* stream) {
+  if (!g) return fail(FO_ERR_ARG, "graph is NULL");
+  FO_LAUNCH(cudaGraphLaunch(g->exec, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_graph_destroy(fo_graph g) {
+  if (!g) return FO_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+  return FO_OK;
+}
+
+}  // extern "C"

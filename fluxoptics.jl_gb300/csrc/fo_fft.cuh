@@ -1,0 +1,250 @@
+// Device-side complex FP32 FFT building blocks for the scalar-propagation passes.
+//
+// One FFT of length N (a power of two) is computed by T = N/E threads, each holding
+// E elements in registers.  The schedule is a Stockham auto-sort decomposition
+// (Govindaraju et al., "High performance discrete Fourier transforms on graphics
+// processors", SC'08): stage s with radix R and span Ns reads x[j + r*N/R], applies
+// the twiddles w_{Ns*R}^{r*(j mod Ns)}, runs an R-point DFT in registers and writes
+// to j/Ns*Ns*R + j mod Ns + r*Ns.  The first and the last stage use the same radix,
+// so the last stage leaves a thread holding exactly the positions that the first
+// stage of another transform reads: an inverse transform, a pointwise operation and
+// a forward transform chain in registers without touching shared memory in between.
+// Intermediate stages exchange through shared memory with one pad slot per 16
+// elements, which keeps both the strided writes and the unit-stride reads free of
+// bank conflicts for the radices used here.
+//
+// Only the forward (negative exponent) transform is written out; inverse
+// transforms use IFFT(x) = conj(FFT(conj(x))), with the 1/N factors folded into
+// the transfer functions by the host.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fo {
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+
+// Stage schedule for N = 2^nb with E = 2^e elements per thread: first and last
+// stage have radix E, the middle bits are split into chunks of at most e bits.
+template <int N, int E>
+struct Sched {
+  static constexpr int nb = ilog2c(N);
+  static constexpr int e = ilog2c(E);
+  static_assert((1 << nb) == N, "N must be a power of two");
+  static_assert((1 << e) == E, "E must be a power of two");
+  static_assert(nb == e || nb >= 2 * e, "N must be E or at least E*E");
+  static constexpr int rem = (nb == e) ? 0 : nb - 2 * e;
+  static constexpr int nmid = (rem + e - 1) / e;
+  static constexpr int S = (nb == e) ? 1 : 2 + nmid;
+  static constexpr int T = N / E;
+  __host__ __device__ static constexpr int bits(int s) {
+    return (S == 1) ? e
+           : (s == 0 || s == S - 1) ? e
+           : ((s - 1) < rem / e ? e : rem - (rem / e) * e);
+  }
+  __host__ __device__ static constexpr int span(int s) {  // Ns = product of radices before s
+    return s == 0 ? 1 : span(s - 1) << bits(s - 1);
+  }
+};
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// a * (-i)
+__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// cos/sin of 2*pi*k/16, k = 1..3 (exact decimal expansions of the algebraic values)
+#define FO_C16_1 0.92387953251128675613f
+#define FO_S16_1 0.38268343236508977173f
+#define FO_SQRT1_2 0.70710678118654752440f
+
+// In-place DFTs on a[o], a[o+1], ... (forward sign).  Outputs in natural order.
+template <int R>
+struct Dft;
+
+template <>
+struct Dft<1> {
+  template <int E>
+  __device__ __forceinline__ static void run(float2 (&)[E], int) {}
+};
+
+template <>
+struct Dft<2> {
+  template <int E>
+  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
+    float2 t = a[o];
+    a[o] = cadd(t, a[o + 1]);
+    a[o + 1] = csub(t, a[o + 1]);
+  }
+};
+
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  float2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
+  float2 t2 = cadd(a1, a3), t3 = cmul_mi(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+template <>
+struct Dft<4> {
+  template <int E>
+  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
+    dft4(a[o], a[o + 1], a[o + 2], a[o + 3]);
+  }
+};
+
+template <>
+struct Dft<8> {
+  template <int E>
+  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
+    // even/odd split: E = DFT4(a0,a2,a4,a6), O = DFT4(a1,a3,a5,a7)
+    float2 e0 = a[o], e1 = a[o + 2], e2 = a[o + 4], e3 = a[o + 6];
+    float2 d0 = a[o + 1], d1 = a[o + 3], d2 = a[o + 5], d3 = a[o + 7];
+    dft4(e0, e1, e2, e3);
+    dft4(d0, d1, d2, d3);
+    // w8^k * O[k]
+    d1 = make_float2(FO_SQRT1_2 * (d1.x + d1.y), FO_SQRT1_2 * (d1.y - d1.x));
+    d2 = cmul_mi(d2);
+    d3 = make_float2(FO_SQRT1_2 * (d3.y - d3.x), -FO_SQRT1_2 * (d3.x + d3.y));
+    a[o] = cadd(e0, d0);
+    a[o + 4] = csub(e0, d0);
+    a[o + 1] = cadd(e1, d1);
+    a[o + 5] = csub(e1, d1);
+    a[o + 2] = cadd(e2, d2);
+    a[o + 6] = csub(e2, d2);
+    a[o + 3] = cadd(e3, d3);
+    a[o + 7] = csub(e3, d3);
+  }
+};
+
+template <>
+struct Dft<16> {
+  template <int E>
+  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
+    // 16 = 4 x 4: n = 4*n1 + n2, k = k1 + 4*k2
+    float2 y[16];
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) {
+      float2 b0 = a[o + n2], b1 = a[o + 4 + n2], b2 = a[o + 8 + n2], b3 = a[o + 12 + n2];
+      dft4(b0, b1, b2, b3);  // over n1 -> k1
+      y[0 * 4 + n2] = b0;
+      y[1 * 4 + n2] = b1;
+      y[2 * 4 + n2] = b2;
+      y[3 * 4 + n2] = b3;
+    }
+    // twiddles w16^(n2*k1), n2,k1 in 1..3
+    const float2 w1 = make_float2(FO_C16_1, -FO_S16_1);
+    const float2 w2 = make_float2(FO_SQRT1_2, -FO_SQRT1_2);
+    const float2 w3 = make_float2(FO_S16_1, -FO_C16_1);
+    const float2 w6 = make_float2(-FO_SQRT1_2, -FO_SQRT1_2);
+    const float2 w9 = make_float2(-FO_C16_1, FO_S16_1);
+    y[1 * 4 + 1] = cmul(y[1 * 4 + 1], w1);
+    y[1 * 4 + 2] = cmul(y[1 * 4 + 2], w2);
+    y[1 * 4 + 3] = cmul(y[1 * 4 + 3], w3);
+    y[2 * 4 + 1] = cmul(y[2 * 4 + 1], w2);
+    y[2 * 4 + 2] = cmul_mi(y[2 * 4 + 2]);
+    y[2 * 4 + 3] = cmul(y[2 * 4 + 3], w6);
+    y[3 * 4 + 1] = cmul(y[3 * 4 + 1], w3);
+    y[3 * 4 + 2] = cmul(y[3 * 4 + 2], w6);
+    y[3 * 4 + 3] = cmul(y[3 * 4 + 3], w9);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      float2 b0 = y[k1 * 4 + 0], b1 = y[k1 * 4 + 1], b2 = y[k1 * 4 + 2], b3 = y[k1 * 4 + 3];
+      dft4(b0, b1, b2, b3);  // over n2 -> k2
+      a[o + k1] = b0;
+      a[o + k1 + 4] = b1;
+      a[o + k1 + 8] = b2;
+      a[o + k1 + 12] = b3;
+    }
+  }
+};
+
+// Shared-memory slot of element `pos` (one pad slot per 16 elements).
+__device__ __forceinline__ int spad(int pos) { return pos + (pos >> 4); }
+
+template <int N>
+struct SmemSize {
+  static constexpr int value = N + N / 16;  // float2 slots per transform
+};
+
+// Register i of thread t holds position t + i*(N/E) on entry to the first stage
+// and on exit from the last stage.
+template <int N, int E>
+__device__ __forceinline__ int reg_pos(int t, int i) { return t + i * (N / E); }
+
+// One Stockham stage s >= 1: registers <- smem, twiddle, DFT.
+template <int N, int E, int s, int PS>
+__device__ __forceinline__ void stage_from_smem(float2 (&v)[E], int t, const float2* __restrict__ tw,
+                                                const float2* sm) {
+  using SC = Sched<N, E>;
+  constexpr int R = 1 << SC::bits(s);
+  constexpr int Ns = SC::span(s);
+  constexpr int T = SC::T;
+  constexpr int NB = E / R;  // butterflies per thread
+#pragma unroll
+  for (int m = 0; m < NB; ++m) {
+    const int j = t + m * T;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[m * R + r] = sm[spad(j + r * (N / R)) * PS];
+    if constexpr (Ns > 1) {
+      const int k = j & (Ns - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        const float2 w = __ldg(tw + r * k * (N / (Ns * R)));
+        v[m * R + r] = cmul(v[m * R + r], w);
+      }
+    }
+    Dft<R>::run(v, m * R);
+  }
+}
+
+// Write the outputs of stage s (s < S-1) to smem at their Stockham destinations.
+template <int N, int E, int s, int PS>
+__device__ __forceinline__ void stage_to_smem(const float2 (&v)[E], int t, float2* sm) {
+  using SC = Sched<N, E>;
+  constexpr int R = 1 << SC::bits(s);
+  constexpr int Ns = SC::span(s);
+  constexpr int T = SC::T;
+  constexpr int NB = E / R;
+#pragma unroll
+  for (int m = 0; m < NB; ++m) {
+    const int j = t + m * T;
+    const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
+#pragma unroll
+    for (int r = 0; r < R; ++r) sm[spad(d + r * Ns) * PS] = v[m * R + r];
+  }
+}
+
+template <int N, int E, int s, int PS>
+__device__ __forceinline__ void stages_from(float2 (&v)[E], int t, const float2* __restrict__ tw,
+                                            float2* sm) {
+  using SC = Sched<N, E>;
+  if constexpr (s < SC::S) {
+    __syncthreads();  // earlier readers of this smem region are done
+    stage_to_smem<N, E, s - 1, PS>(v, t, sm);
+    __syncthreads();
+    stage_from_smem<N, E, s, PS>(v, t, tw, sm);
+    stages_from<N, E, s + 1, PS>(v, t, tw, sm);
+  }
+}
+
+// Forward FFT of the N elements spread over the T = N/E threads of one lane.  On
+// entry register i of thread t holds x[t + i*T]; on exit it holds X[t + i*T].
+// `sm` points at this lane's first smem slot and PS is the slot stride between
+// consecutive positions.  Every thread of the block must make the call (it holds
+// __syncthreads when the schedule has more than one stage).
+template <int N, int E, int PS>
+__device__ __forceinline__ void fft_forward(float2 (&v)[E], int t, const float2* __restrict__ tw,
+                                            float2* sm) {
+  Dft<E>::run(v, 0);  // stage 0: radix E, span 1, no twiddles
+  stages_from<N, E, 1, PS>(v, t, tw, sm);
+}
+
+}  // namespace fo

@@ -1,0 +1,94 @@
+// Internal declarations shared by the CUDA translation units of libfluxoptics_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace fo {
+
+// ---------------------------------------------------------------------------
+// Errors: every C-ABI entry point returns one of the FO_* status codes from
+// include/fluxoptics_gb300.h and leaves a message in a thread-local string.
+// ---------------------------------------------------------------------------
+void set_error(int code, const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define FO_CUDA_CHECK(expr)                         \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return fo::cuda_fail(_e, #expr); \
+  } while (0)
+
+// Modulation kinds applied in real space inside the row passes.
+enum ModKind : int { MOD_NONE = 0, MOD_PHASE = 1, MOD_MASK = 2, MOD_DN = 3 };
+
+// One row pass over `batch` fields: for every row y < nrows of every field,
+// load -> [inverse FFT along x] -> [seed] -> [modulation] -> [forward FFT along x] -> store.
+struct RowPassArgs {
+  const float2* src;
+  float2* dst;
+  long long src_bstride, dst_bstride;  // elements between consecutive fields
+  int src_ld, dst_ld;                  // elements between consecutive rows
+  int nrows;                           // rows processed per field
+  int n_valid;                         // real-space x extent (N for AS; n < N for padded RS)
+  int batch;                           // fields processed by the launch
+  int fields_per_cta;                  // fields looped over inside one CTA
+  const int* field_list;               // optional device list of field ids (null: identity)
+  int inv_first;                       // row holds a spectrum: inverse-transform it first
+  int fwd_after;                       // forward-transform the row before storing
+  // modulation
+  int mod_kind;
+  int mod_bwd;            // 0: forward modulation (+ optional save); 1: adjoint + gradient
+  float mod_sign;         // direction sign s
+  const void* mod_param;  // phase / dn: float; mask: float2; row stride param_ld
+  int param_ld;
+  float mod_scale;            // MOD_DN: kdz; the phase factor of field b is mod_scale * inv_lambda[b]
+  const float* inv_lambda;    // MOD_DN: per field id, 1 / lambda
+  float2* save;               // forward: modulation input written here (nullable)
+  long long save_bstride;
+  int save_ld;
+  const float2* saved;        // adjoint: saved modulation input
+  long long saved_bstride;
+  int saved_ld;
+  void* grad;                 // adjoint: gradient (float or float2), row stride param_ld (nullable)
+  // seed of the adjoint sweep: du = 4 * dc[t] * resid_t * u, t = tidx[field]
+  int seed;
+  const float* resid;
+  long long resid_tstride;
+  int resid_ld;
+  const int* tidx;
+  const float* dc;
+};
+
+// One column pass: forward FFT along y, multiply by the transfer function of the
+// field's wavelength (conjugated for the adjoint direction), inverse FFT along y.
+struct ColPassArgs {
+  float2* buf;
+  long long bstride;
+  int ld;                // row stride (elements)
+  int ncols;             // columns to process
+  int y_in, y_out;       // rows read (zero beyond) / rows written
+  const float2* H;       // transfer functions, one table of N x ncols per wavelength
+  long long h_stride;
+  const int* h_index;    // per field id: table index
+  int conj_h;
+  int fft_only;          // 1: store the forward transform along y (no H, no inverse)
+  int batch;
+  const int* field_list;
+};
+
+// Launchers (return cudaError_t from the launch).  N is the FFT length along the
+// transformed axis; supported: powers of two from 16 to 4096.
+bool fft_size_supported(int n);
+cudaError_t launch_row_pass(int N, const RowPassArgs& a, const float2* tw, cudaStream_t s);
+cudaError_t launch_col_pass(int N, const ColPassArgs& a, const float2* tw, cudaStream_t s);
+// Rows handled by one CTA of the row pass for length N (host-side grid sizing).
+int row_pass_rows_per_cta(int N);
+
+// Device twiddle table exp(-2 pi i m / N), m < N, for the current device (cached).
+const float2* twiddles(int N, int* err);
+
+}  // namespace fo

@@ -1,0 +1,127 @@
+"""ScalarField: the field container of the hot path.
+
+Mirrors ``ScalarField`` of FluxOptics.jl (src/Fields.jl:118-149).  Storage is a
+CUDA complex64 tensor; the Julia column-major array ``(nx, ny, d3, d4, ...)``
+is the C-ordered tensor ``(..., d4, d3, ny, nx)``, so the two share one memory
+layout: x fastest, then y, then the trailing dims in Julia order.  Wavelengths
+(and tilts) are given in Julia order over the trailing dims and broadcast like
+the reference's ``parse_lambdas`` (src/Fields.jl:18-38).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+
+def _as_device_field(data):
+    if isinstance(data, torch.Tensor):
+        t = data
+    else:
+        t = torch.as_tensor(np.asarray(data))
+    if not t.is_complex():
+        t = t.to(torch.complex64)
+    if t.dtype != torch.complex64:
+        t = t.to(torch.complex64)
+    if t.device.type != "cuda":
+        t = t.to("cuda")
+    return t.contiguous()
+
+
+def per_field(values, julia_batch_shape):
+    """Broadcast a scalar or a Julia-ordered array over the trailing dims and
+    return one float64 value per field, in memory (column-major) order."""
+    nb = int(np.prod(julia_batch_shape)) if len(julia_batch_shape) else 1
+    v = np.asarray(values, dtype=np.float64)
+    if v.ndim == 0:
+        return np.full(nb, float(v))
+    if len(julia_batch_shape) == 0:
+        if v.size != 1:
+            raise ValueError("per-field values given for a single field")
+        return v.reshape(1)
+    shape = tuple(v.shape) + (1,) * (len(julia_batch_shape) - v.ndim)
+    b = np.broadcast_to(v.reshape(shape, order="F"), tuple(julia_batch_shape))
+    return np.asarray(b).reshape(-1, order="F")
+
+
+class ScalarField:
+    """A batch of scalar fields on a regular grid.
+
+    ``data``: complex tensor/array of shape ``(..., ny, nx)``; ``ds = (dx, dy)``;
+    ``lambdas``: a wavelength or an array broadcast over the trailing dims
+    (Julia order); ``tilts``: must be zero (tilted kernels are not in this path)."""
+
+    def __init__(self, data, ds, lambdas, tilts=None):
+        self.electric = _as_device_field(data)
+        if self.electric.dim() < 2:
+            raise ValueError("a field needs two spatial dims")
+        self.ds = (float(ds[0]), float(ds[1]))
+        self.lambdas = lambdas
+        if tilts is not None and np.any(np.asarray(tilts, dtype=float) != 0):
+            raise NotImplementedError("tilted fields are not supported by the GB300 path")
+        self.tilts = (0.0, 0.0)
+
+    # -- shape -------------------------------------------------------------
+    @property
+    def nx(self):
+        return int(self.electric.shape[-1])
+
+    @property
+    def ny(self):
+        return int(self.electric.shape[-2])
+
+    @property
+    def julia_batch_shape(self):
+        return tuple(int(s) for s in reversed(self.electric.shape[:-2]))
+
+    @property
+    def batch(self):
+        return int(np.prod(self.julia_batch_shape)) if self.electric.dim() > 2 else 1
+
+    def size(self):
+        """Size in Julia order (nx, ny, trailing...)."""
+        return (self.nx, self.ny) + self.julia_batch_shape
+
+    def lambdas_per_field(self):
+        return per_field(self.lambdas, self.julia_batch_shape)
+
+    # -- helpers of the reference API -------------------------------------------
+    def copy(self):
+        return ScalarField(self.electric.clone(), self.ds, self.lambdas)
+
+    def similar(self):
+        return ScalarField(torch.empty_like(self.electric), self.ds, self.lambdas)
+
+    def set_field_data(self, data):
+        """New field sharing grid and wavelengths (src/Fields.jl:213-215)."""
+        return ScalarField(data, self.ds, self.lambdas)
+
+    def is_on_axis(self):
+        return True
+
+
+def power(u: ScalarField):
+    """sum |u|^2 dx dy per field (src/Fields.jl:843-846)."""
+    return (u.electric.abs() ** 2).sum(dim=(-2, -1)) * (u.ds[0] * u.ds[1])
+
+
+def normalize_power_(u: ScalarField, target_power=1.0):
+    """In-place normalisation (src/Fields.jl:889-892)."""
+    p = power(u)
+    u.electric.mul_(torch.sqrt(target_power / p)[..., None, None].to(u.electric.dtype))
+    return u
+
+
+def intensity(u: ScalarField):
+    """sum over the trailing dims of |u|^2 (src/Fields.jl:608-616)."""
+    i = u.electric.abs() ** 2
+    return i.reshape(-1, u.ny, u.nx).sum(0)
+
+
+def coupling_efficiency(u: ScalarField, v: ScalarField):
+    """|<u, v>|^2 / (|u|^2 |v|^2) per field (src/Fields.jl:748-756)."""
+    a = u.electric.reshape(-1, u.ny * u.nx)
+    b = v.electric.reshape(-1, v.ny * v.nx)
+    num = (a.conj() * b).sum(-1).abs() ** 2
+    den = (a.abs() ** 2).sum(-1) * (b.abs() ** 2).sum(-1)
+    return num / den

@@ -1,0 +1,142 @@
+"""Fista, ProxRule, ClampProx and TVProx on the GPU (src/OptimisersExt.jl,
+src/proximal_operators/*)."""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _capi
+from .components import OpticalSystem, _ptr, _stream
+
+
+class Fista:
+    """Fista(eta): the rule keeps eta^2 (OptimisersExt.jl:33-54)."""
+
+    def __init__(self, eta):
+        self.eta = float(eta)
+
+    def init(self, x):
+        return {"t": torch.ones(1, dtype=torch.float64, device=x.device), "xk": x.detach().clone(),
+                "newdx": torch.zeros_like(x)}
+
+    def apply_(self, state, x, dx):
+        if x.dtype != torch.float32:
+            raise NotImplementedError("Fista on the GPU path updates float32 parameters")
+        _capi.call("fo_fista_step", _ptr(x), _ptr(state["xk"]), _ptr(state["newdx"]), _ptr(dx), x.numel(),
+                   self.eta, _ptr(state["t"]), _stream())
+
+
+class NoDescent:
+    def init(self, x):
+        return {}
+
+    def apply_(self, state, x, dx):
+        pass
+
+
+class ClampProx:
+    """clamp(x, lo, hi) (proximal_operators/clamp_prox.jl:35-37)."""
+
+    def __init__(self, lo, hi):
+        self.lo, self.hi = float(lo), float(hi)
+
+    def init(self, x):
+        return None
+
+    def apply_(self, state, x):
+        _capi.call("fo_clamp", _ptr(x), x.numel(), self.lo, self.hi, _stream())
+
+
+class TVProx:
+    """TVProx(lambda, n_iter; isotropic, rule=Fista(eta)) (tv_prox.jl:94-195), 2-D."""
+
+    def __init__(self, lam, n_iter=50, isotropic=True, eta=None):
+        self.lam = float(lam)
+        self.n_iter = int(n_iter)
+        self.isotropic = bool(isotropic)
+        self.eta = float(eta if eta is not None else (0.25 if isotropic else 2.5))
+
+    def init(self, x):
+        if x.dim() != 2:
+            raise NotImplementedError("TVProx on the GPU path is 2-D")
+        h = C.c_void_p()
+        _capi.call("fo_tv_create", C.byref(h), x.shape[1], x.shape[0], self.lam, self.n_iter,
+                   int(self.isotropic), self.eta)
+        return _TvHandle(h)
+
+    def apply_(self, state, x):
+        _capi.call("fo_tv_apply", state.h, _ptr(x), _stream())
+
+
+class _TvHandle:
+    def __init__(self, h):
+        self.h = h
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is not None:
+            lib.fo_tv_destroy(self.h)
+
+
+class ProxRule:
+    """Rule step, then the proximal operator (OptimisersExt.jl:222-244)."""
+
+    def __init__(self, rule, prox):
+        self.rule = rule
+        self.prox = prox
+
+    def init(self, x):
+        return {"rule": self.rule.init(x), "prox": self.prox.init(x)}
+
+    def apply_(self, state, x, dx):
+        self.rule.apply_(state["rule"], x, dx)
+        self.prox.apply_(state["prox"], x)
+
+
+def make_rules(*pairs):
+    """{parameter data_ptr: rule} from (component-or-tensor, rule) pairs
+    (OptimisersExt.jl:195-214)."""
+    rules = {}
+    for obj, rule in pairs:
+        if isinstance(obj, torch.Tensor):
+            rules[obj.data_ptr()] = rule
+        else:
+            for t in obj.params().values():
+                rules[t.data_ptr()] = rule
+    return rules
+
+
+class OptState:
+    def __init__(self):
+        self.leaves = []  # (component, name, tensor, rule, state)
+
+
+def setup(rules, model_or_default=None, model=None):
+    """setup(rule, system) / setup(rules, system) / setup(rules, default_rule, system)."""
+    if model is None:
+        model, default = model_or_default, None
+    else:
+        default = model_or_default
+    if not isinstance(rules, dict):
+        default, rules = rules, {}
+    st = OptState()
+    comps = list(model.components)
+    if model.source is not None:
+        comps = [model.source] + comps
+    for c in comps:
+        for name, t in c.params().items():
+            rule = rules.get(t.data_ptr(), default if default is not None else NoDescent())
+            st.leaves.append((c, name, t, rule, rule.init(t)))
+    return st
+
+
+def update_(state: OptState, system: OpticalSystem, grads):
+    """Apply each rule to its parameter in place (Optimisers.update!)."""
+    for c, name, t, rule, s in state.leaves:
+        g = grads.get(c)
+        if g is None or name not in g:
+            continue
+        rule.apply_(s, t, g[name])
+    return state

@@ -1,0 +1,300 @@
+/*
+ * fluxoptics_gb300.h -- C ABI of the GB300-native scalar-propagation hot path of
+ * FluxOptics.jl (angular-spectrum and Rayleigh-Sommerfeld propagation, Phase and
+ * Mask modulation, the AS_BPM split-step march, their adjoints and gradients, the
+ * SquaredIntensityDifference metric, and the Fista / ClampProx / TVProx update).
+ *
+ * Conventions
+ *   - Every entry point returns FO_OK (0) or an FO_ERR_* code; fo_last_error()
+ *     returns the message of the last failure on the calling thread.
+ *   - Arrays are borrowed device pointers owned by the caller.  A batch of fields
+ *     is `batch` contiguous complex-float (re, im) planes of ny rows x nx columns,
+ *     x fastest: exactly the memory of a Julia CuArray{ComplexF32}(nx, ny, dims...)
+ *     with the trailing dims flattened into `batch`.
+ *   - `direction` is FO_FORWARD (+1) or FO_BACKWARD (-1), the reference's
+ *     sign(Forward) / sign(Backward) (src/optical_components/OpticalComponents.jl:97-98).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     stream-ordered and do not synchronise; none allocates device memory except
+ *     the *_create functions, so sequences of calls can be captured in a CUDA
+ *     graph (fo_graph_*).
+ *   - Plans (fo_prop_plan, fo_chain, fo_bpm, fo_sid, fo_tv) own their device
+ *     workspace and are destroyed with the matching *_destroy.
+ *   - Grid sizes of the propagators are powers of two from 16 to 4096 along
+ *     each axis (RSProp: the padded size, >= 2n-1, must be one).
+ */
+#ifndef FLUXOPTICS_GB300_H
+#define FLUXOPTICS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define FO_API __attribute__((visibility("default")))
+#else
+#define FO_API
+#endif
+
+#define FO_OK 0
+#define FO_ERR_ARG 1         /* null pointer / bad value */
+#define FO_ERR_SHAPE 2       /* unsupported or mismatched sizes */
+#define FO_ERR_ALLOC 3       /* device allocation failed */
+#define FO_ERR_CUDA 4        /* a CUDA call failed */
+#define FO_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+#define FO_ERR_UNSUPPORTED 6 /* feature not available in this build */
+
+#define FO_FORWARD 1
+#define FO_BACKWARD (-1)
+
+/* Modulation kinds (fo_mod.kind) */
+#define FO_MOD_NONE 0
+#define FO_MOD_PHASE 1 /* u *= cis(s*phi)        param: float[ny*nx]        */
+#define FO_MOD_MASK 2  /* u *= m (conj(m) if s<0) param: complex float[ny*nx] */
+#define FO_MOD_DN 3    /* u *= cis(s*scale/lambda_b*dn)  param: float[ny*nx]   */
+
+/* ---------------------------------------------------------------------- */
+/* Library                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Version as major*10000 + minor*100 + patch. */
+FO_API int fo_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+FO_API const char* fo_last_error(void);
+
+/* Blocks until all work on `stream` is done; reports device-side errors. */
+FO_API int fo_stream_synchronize(void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Free-space propagators                                                  */
+/* ---------------------------------------------------------------------- */
+
+typedef struct fo_prop_plan_s* fo_prop_plan;
+
+/*
+ * ASProp: u <- IFFT2(H . FFT2(u)) with the on-axis angular-spectrum transfer
+ * function H = cis(2 pi z sqrt(n0^2/lambda^2 - fx^2 - fy^2)) (complex sqrt, so
+ * evanescent waves decay), conj(H(-z)) for z < 0, conj(H) for the Backward
+ * direction.  H is evaluated in FP64 and stored as complex float, once per
+ * distinct wavelength.  `lambdas` holds one wavelength per field (n_lambdas ==
+ * batch) or one shared wavelength (n_lambdas == 1).
+ * Replaces: ASProp(u, ds, z; n0) -- src/optical_components/freespace_propagators/
+ * angular_spectrum.jl:1-12 (as_kernel), :78-146 (ASKernelProp), :193-234 (ASProp),
+ * with FourierWrapper (fourier/fourier_wrapper.jl:1-5) and compute_ft!/compute_ift!
+ * (src/FFTutils.jl:13-28; CUFFT plans in src/cuda/CUDAExt.jl:29-35).
+ */
+FO_API int fo_asprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
+                            const double* lambdas, int n_lambdas, double z, double n0, int flags);
+
+/*
+ * RSProp: zero-pad to (px, py) = the smallest powers of two >= (2nx-1, 2ny-1),
+ * FFT, multiply by H_RS = FFT of the Rayleigh-Sommerfeld impulse response
+ * h = dx dy/(2 pi) cis(k r)/r (z/r)(1/r - i k) sampled on the circular offset
+ * grid, inverse FFT, crop the top-left nx x ny block.  The circular convolution
+ * on >= 2n-1 points equals the reference's linear convolution on the cropped
+ * block.  Padding is never materialised.
+ * Replaces: RSProp(u, ds, z) -- src/optical_components/freespace_propagators/
+ * rayleigh_sommerfeld.jl:1-12 (rs_kernel), :38-91 (RSKernelProp), :128-169 (RSProp),
+ * convolution_kernel.jl:1-55 and utilities/pad_crop_operators.jl:291-356.
+ */
+FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
+                            const double* lambdas, int n_lambdas, double z, int flags);
+
+FO_API int fo_prop_destroy(fo_prop_plan plan);
+
+/* Padded transform sizes and the workspace the plan owns. */
+FO_API int fo_prop_info(fo_prop_plan plan, int* fft_nx, int* fft_ny, size_t* workspace_bytes);
+
+/*
+ * In-place propagation of u (batch x ny x nx complex float).  FO_BACKWARD applies
+ * the exact adjoint (conj(H)).
+ * Replaces: propagate!(u, p::ASProp|RSProp, dir) and backpropagate!
+ * (src/optical_components/freespace_propagators/freespace.jl:29-63,
+ * system/optical_sequence.jl:54-66).
+ */
+FO_API int fo_propagate(fo_prop_plan plan, void* u, int direction, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Modulators (any nx, ny)                                                 */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * u *= cis(s*phi), phi (ny x nx float) broadcast over the batch; when u_saved is
+ * not NULL the input is copied there first.
+ * Replaces: propagate!/propagate_and_save!(u, p::Phase, dir) --
+ * src/optical_components/modulators/phasemask.jl:90-113.
+ */
+FO_API int fo_phase_forward(void* u, const float* phi, void* u_saved, int nx, int ny, int batch,
+                            int direction, void* stream);
+
+/*
+ * dv <- cis(-s*phi) dv and, when dphi is not NULL,
+ * dphi = s * sum_batch Im(dv_new * conj(u_saved)).
+ * Replaces: backpropagate_with_gradient!(dv, u_saved, dp, p::Phase, dir) --
+ * phasemask.jl:96-98, :115-150, and compute_phase_gradient! for CuArray
+ * (src/cuda/optical_components.jl:1-44).
+ */
+FO_API int fo_phase_backward(void* dv, const float* phi, const void* u_saved, float* dphi, int nx,
+                             int ny, int batch, int direction, void* stream);
+
+/* u *= m (conj(m) for FO_BACKWARD); saves the input when u_saved is not NULL.
+ * Replaces: propagate!(u, p::Mask, dir; u_saved) -- modulators/mask.jl:241-261. */
+FO_API int fo_mask_forward(void* u, const void* m, void* u_saved, int nx, int ny, int batch,
+                           int direction, void* stream);
+
+/* dm = sum_batch conj_dir(dv * conj(u_saved)) (when dm is not NULL), then
+ * dv <- conj_dir(m, reverse(dir)) dv.
+ * Replaces: backpropagate_with_gradient!(dv, u_saved, dp, p::Mask, dir) -- mask.jl:263-291. */
+FO_API int fo_mask_backward(void* dv, const void* m, const void* u_saved, void* dm, int nx, int ny,
+                            int batch, int direction, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Fused chains: mod_0 -> prop_0 -> mod_1 -> ... -> prop_{K-1} -> mod_K     */
+/* ---------------------------------------------------------------------- */
+
+typedef struct {
+  int kind;          /* FO_MOD_* */
+  const void* param; /* phi / dn: float[ny*nx]; mask: complex float[ny*nx] */
+  void* saved;       /* forward: the modulation input is written here when not NULL
+                        (batch x ny x nx complex float); backward: the saved input */
+  void* grad;        /* backward: gradient written here when not NULL
+                        (phase / dn: float[ny*nx]; mask: complex float[ny*nx]) */
+  double scale;      /* FO_MOD_DN: kdz = 2 pi dz / cos(theta); unused otherwise */
+} fo_mod;
+
+typedef struct fo_chain_s* fo_chain;
+
+/*
+ * A chain of K propagators on one grid (all ASProp, or all RSProp with equal
+ * padding) and one batch, executed as 2K+1 fused passes: the inverse row
+ * transform of each propagator, the modulation after it and the forward row
+ * transform of the next propagator run in one pass.  The plans stay owned by the
+ * caller and must outlive the chain.
+ * Replaces: OpticalSystem / AbstractSequence propagation over a run of
+ * propagators and modulators (system/optical_sequence.jl:54-66,
+ * system/optical_system.jl:189-214, system/merge_rules.jl:45-52).
+ */
+FO_API int fo_chain_create(fo_chain* chain, int n_props, const fo_prop_plan* props);
+FO_API int fo_chain_destroy(fo_chain chain);
+
+/* Forward through the chain, in place on u; mods has n_props+1 entries. */
+FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int direction,
+                            void* stream);
+
+/*
+ * Adjoint sweep in reverse order, in place on du.  For every mod with a grad
+ * pointer the gradient is written (mods[k].saved must then hold the input saved
+ * by the forward sweep).  When `sid` is not NULL the sweep is seeded with the
+ * SquaredIntensityDifference pullback du = 4 dc_t (I_t - target_t) u_out computed
+ * by that metric's last fo_sid_forward call on `u_out`; du's content is then
+ * ignored.
+ * Replaces: the rrule pullbacks of propagate!/Trainable components
+ * (src/ChainRulesCoreExt.jl:21-111) chained through the system in reverse.
+ */
+typedef struct fo_sid_s* fo_sid;
+FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction,
+                             fo_sid sid, const void* u_out, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* AS_BPM                                                                  */
+/* ---------------------------------------------------------------------- */
+
+typedef struct fo_bpm_s* fo_bpm;
+
+/*
+ * Split-step march through n_slices slices of thickness/n_slices: half step,
+ * (n_slices-1) x [dn phase, full step], dn phase, half step, with the dn phase
+ * cis(s*kdz/lambda*dn_k), kdz = 2 pi dz / cos_correction.  The adjoint needs the
+ * slice inputs: every `checkpoint_every`-th one is kept by fo_bpm_forward(save=1)
+ * and the others are recomputed segment by segment (checkpoint_every = 1 keeps
+ * all, like the reference; 0 picks round(sqrt(n_slices))).
+ * Replaces: AS_BPM(u, thickness, n0, dn) and BPM propagate!/backpropagate! --
+ * src/optical_components/bulk_propagators/bpm.jl:1-74, :130-142, :235-321.
+ */
+FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
+                         const double* lambdas, int n_lambdas, double thickness, double n0,
+                         int n_slices, int checkpoint_every, double cos_correction, int flags);
+FO_API int fo_bpm_destroy(fo_bpm bpm);
+FO_API int fo_bpm_info(fo_bpm bpm, int* checkpoint_every, size_t* workspace_bytes);
+
+/* dn: n_slices x ny x nx float (slice-major).  In place on u. */
+FO_API int fo_bpm_forward(fo_bpm bpm, void* u, const float* dn, int direction, int save,
+                          void* stream);
+
+/* Adjoint in place on du; ddn (n_slices x ny x nx float) receives the gradient
+ * when not NULL.  Requires a preceding fo_bpm_forward(save=1) on the same input. */
+FO_API int fo_bpm_backward(fo_bpm bpm, void* du, const float* dn, float* ddn, int direction,
+                           void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* SquaredIntensityDifference                                              */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * I_t = sum of |u_b|^2 over the fields b with target_index[b] == t;
+ * loss_t = sum (I_t - target_t)^2.  target_index (host array, batch entries,
+ * values < n_targets) is copied into the metric.  NULL target_index maps field b
+ * to slice b % n_targets (the broadcast of an (nx, ny, T) target over
+ * (nx, ny, T, M) fields).
+ * Replaces: SquaredIntensityDifference -- src/metrics/squared_intensity_difference.jl:58-90.
+ */
+FO_API int fo_sid_create(fo_sid* sid, int nx, int ny, int batch, int n_targets,
+                         const int* target_index);
+FO_API int fo_sid_destroy(fo_sid sid);
+
+/* Computes the residuals I - target (kept in the metric for the pullback) and
+ * writes loss[n_targets] (device float). */
+FO_API int fo_sid_forward(fo_sid sid, const void* u, const float* target, float* loss,
+                          void* stream);
+
+/* du = 4 dc_t (I_t - target_t) u from the last fo_sid_forward on u; dc: device
+ * float[n_targets] (NULL: all ones). */
+FO_API int fo_sid_backward(fo_sid sid, const void* u, const float* dc, void* du, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Optimiser and proximal operators                                        */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * One Fista step on n floats: t' = (1+sqrt(1+4t^2))/2, beta = (t-1)/t',
+ * newdx = eta^2 dx - beta (x - xk), xk <- x, x -= newdx, t <- t'.  `eta` is the
+ * value given to Fista(eta) (the rule stores eta^2); t_state is a device double
+ * (initialise to 1), read and advanced on the stream, so the step can be
+ * replayed from a CUDA graph.
+ * Replaces: Fista -- src/OptimisersExt.jl:33-54 with Optimisers' subtract!.
+ */
+FO_API int fo_fista_step(float* x, float* xk, float* newdx, const float* dx, long long n,
+                         double eta, double* t_state, void* stream);
+
+/* x = clamp(x, lo, hi).  Replaces ClampProx (proximal_operators/clamp_prox.jl:35-37). */
+FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream);
+
+/*
+ * TVProx(lambda, n_iter; isotropic, rule = Fista(eta)) on an ny x nx float
+ * array, in place: n_iter dual Fista iterations with the reference's D / D^T
+ * boundary handling and per-slice normalisation.
+ * Replaces: TVProx -- src/proximal_operators/tv_prox.jl:1-195.
+ */
+typedef struct fo_tv_s* fo_tv;
+FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic,
+                        double eta);
+FO_API int fo_tv_destroy(fo_tv tv);
+FO_API int fo_tv_apply(fo_tv tv, float* x, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* CUDA graphs of whole iterations                                         */
+/* ---------------------------------------------------------------------- */
+
+typedef struct fo_graph_s* fo_graph;
+FO_API int fo_graph_begin(void* stream);
+FO_API int fo_graph_end(void* stream, fo_graph* graph);
+FO_API int fo_graph_launch(fo_graph graph, void* stream);
+FO_API int fo_graph_destroy(fo_graph graph);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUXOPTICS_GB300_H */

@@ -1,0 +1,516 @@
+"""FP64 CPU oracle for FluxOptics.jl's scalar-propagation hot path.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product path may import this module:
+only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
+``bench.py`` use it, and only as the checker / the timed CPU restatement.
+
+This is a numpy/scipy (pocketfft, complex128) restatement of the reference's
+algorithm.  The reference is Julia (FluxOptics.jl v0.1.0) and cannot be run in
+this environment (no Julia toolchain), so the restatement is pinned by the
+reference's own property and known-answer tests (AS/RS unitarity, AS energy
+conservation, SquaredIntensityDifference closed form, HG00 == Gaussian, Fista
+convergence, Phase angle checks), by the analytic paraxial Gaussian beam, and
+by central finite differences of every gradient.  No reference test fixes the
+values of a propagated field or a gradient, so field-level parity is
+"partially pinned" (properties + analytic beams), not golden-vector pinned.
+
+Array layout (matches the GPU path): a field batch is a C-ordered array of
+shape ``(..., ny, nx)``; the last axis is the reference's first (fastest,
+column-major) Julia dimension ``x``.  Trailing Julia dims (wavelengths x modes)
+become the leading numpy axes, flattened to ``B`` fields.
+
+Third-party arithmetic the reference relies on and which is restated here:
+FFTW.jl 1.9.0 / FFTW_jll 3.3.11 (unnormalised forward FFT, 1/N-normalised
+inverse, ``plan_fft!``/``plan_ifft!`` in ``src/FFTutils.jl:13-28``) and
+AbstractFFTs 1.5.0 ``fftfreq``.
+"""
+
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+import scipy.fft as sfft
+
+FORWARD = 1
+BACKWARD = -1
+
+_WORKERS = int(os.environ.get("FO_ORACLE_WORKERS", "1"))
+
+
+def set_workers(n: int) -> None:
+    """Number of pocketfft threads used by the oracle (the CPU baseline sets it)."""
+    global _WORKERS
+    _WORKERS = max(1, int(n))
+
+
+def fft2(u):
+    # src/FFTutils.jl:20-23 -- unnormalised forward transform over the two spatial dims
+    return sfft.fft2(u, axes=(-2, -1), workers=_WORKERS)
+
+
+def ifft2(u):
+    # src/FFTutils.jl:25-28 -- inverse transform with 1/(nx*ny)
+    return sfft.ifft2(u, axes=(-2, -1), workers=_WORKERS)
+
+
+# ---------------------------------------------------------------------------
+# Grids, modes, field utilities
+# ---------------------------------------------------------------------------
+
+def spatial_vectors(ns, ds, offset=None):
+    """Centred grid ``((0:n-1) - (n-1)/2)*d - c`` (src/GridUtils.jl:56-60).
+
+    ``ns``/``ds`` are given in Julia order (x first)."""
+    if offset is None:
+        offset = (0.0,) * len(ns)
+    return tuple((np.arange(n) - (n - 1) / 2.0) * d - c for n, d, c in zip(ns, ds, offset))
+
+
+def gaussian(w0, x, y):
+    """Gaussian(w0) at the waist: sqrt(2/pi)/w0 * exp(-(x^2+y^2)/w0^2).
+
+    src/modes/gaussian_modes.jl:22-24 (normalisation), :116-127 (eval), :216-233 (2-D).
+    Returns an array of shape (ny, nx)."""
+    c = math.sqrt(math.sqrt(2.0 / math.pi) / w0)
+    gx = c * np.exp(-(x / w0) ** 2)
+    gy = c * np.exp(-(y / w0) ** 2)
+    return (gy[:, None] * gx[None, :]).astype(np.complex128)
+
+
+def _hermite(n, x):
+    # physicists' Hermite polynomial (src/modes/gaussian_modes.jl:238-250)
+    h0 = np.ones_like(x)
+    if n == 0:
+        return h0
+    h1 = 2.0 * x
+    for k in range(1, n):
+        h0, h1 = h1, 2.0 * x * h1 - 2.0 * k * h0
+    return h1
+
+
+def hermite_gaussian(w0, m, n, x, y):
+    """HG_{m,n} at the waist (src/modes/gaussian_modes.jl:288-426)."""
+    def one(w, k, s):
+        c = math.sqrt(math.sqrt(2.0 / math.pi) / w) / math.sqrt(2.0 ** k * math.factorial(k))
+        return c * _hermite(k, math.sqrt(2.0) * s / w) * np.exp(-(s / w) ** 2)
+    return (one(w0, n, y)[:, None] * one(w0, m, x)[None, :]).astype(np.complex128)
+
+
+def hermite_gaussian_groups(n_groups):
+    """Mode orders (m, n) with m + n < n_groups, in the reference's order
+    (src/modes/gaussian_modes.jl:469-478)."""
+    out = []
+    for m in range(n_groups):
+        for n in range(n_groups - m):
+            out.append((m, n))
+    return out
+
+
+def power(u, ds):
+    """sum |u|^2 * prod(ds) per field (src/Fields.jl:843-846)."""
+    return np.sum(np.abs(u) ** 2, axis=(-2, -1)) * float(np.prod(ds))
+
+
+def normalize_power(u, ds, target=1.0):
+    """In-place power normalisation per field (src/Fields.jl:889-892)."""
+    p = power(u, ds)
+    u *= np.sqrt(target / p)[..., None, None]
+    return u
+
+
+def coupling_efficiency(u, v):
+    """|<u,v>|^2/(|u|^2 |v|^2) per field (src/Fields.jl:748-756)."""
+    num = np.abs(np.sum(np.conj(u) * v, axis=(-2, -1))) ** 2
+    den = np.sum(np.abs(u) ** 2, axis=(-2, -1)) * np.sum(np.abs(v) ** 2, axis=(-2, -1))
+    return num / den
+
+
+def rel_l2(a, b):
+    """Relative L2 error ||a-b|| / ||b|| (b is the reference)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+# ---------------------------------------------------------------------------
+# Transfer functions
+# ---------------------------------------------------------------------------
+
+def fftfreqs(nx, ny, dx, dy):
+    """Frequency vectors in FFT order (src/optical_components/freespace_propagators/
+    fourier_kernel.jl:17-18)."""
+    return np.fft.fftfreq(nx, dx), np.fft.fftfreq(ny, dy)
+
+
+def as_kernel(nx, ny, dx, dy, lam, z, n0=1.0):
+    """On-axis angular-spectrum transfer function, shape (ny, nx).
+
+    H = cis(2 pi z sqrt(complex(n0^2/lam^2) - fx^2 - fy^2)); for z < 0 the kernel
+    is conj(H(-z)), so evanescent waves decay both ways
+    (src/optical_components/freespace_propagators/angular_spectrum.jl:1-12)."""
+    fx, fy = fftfreqs(nx, ny, dx, dy)
+    lam_m = lam / n0
+    f2 = 1.0 / lam_m ** 2
+    arg = (f2 - fx[None, :] ** 2 - fy[:, None] ** 2).astype(np.complex128)
+    za = abs(z)
+    h = np.exp(1j * 2.0 * np.pi * za * np.sqrt(arg))
+    return h if z >= 0 else np.conj(h)
+
+
+def rs_kernel_spatial(n_x, n_y, dx, dy, lam, z, m_x=None, m_y=None):
+    """Rayleigh-Sommerfeld impulse response sampled on offsets in FFT order.
+
+    h = nrm * cis(k r)/r * (z/r) * (1/r - i k), nrm = dx*dy/(2 pi), k = 2 pi/lam
+    (rayleigh_sommerfeld.jl:1-12, :660).  Offsets are circshift((1-n):(n-1), n)*d
+    on a grid of length 2n-1 (convolution_kernel.jl:492); with ``m_x``/``m_y``
+    larger than 2n-1 the same samples are placed on an m-point circular grid
+    (0..n-1 at the start, -(n-1)..-1 at the end, zeros between)."""
+    def offsets(n, m):
+        if m is None:
+            m = 2 * n - 1
+        o = np.zeros(m)
+        valid = np.zeros(m, dtype=bool)
+        o[:n] = np.arange(n)
+        valid[:n] = True
+        o[m - (n - 1):] = np.arange(-(n - 1), 0)
+        valid[m - (n - 1):] = True
+        return o, valid
+    ox, vx = offsets(n_x, m_x)
+    oy, vy = offsets(n_y, m_y)
+    x = ox[None, :] * dx
+    y = oy[:, None] * dy
+    za = abs(z)
+    k = 2.0 * np.pi / lam
+    r = np.sqrt(x ** 2 + y ** 2 + za ** 2)
+    nrm = dx * dy / (2.0 * np.pi)
+    h = nrm * (np.exp(1j * k * r) / r) * (za / r) * (1.0 / r - 1j * k)
+    h = h * (vy[:, None] & vx[None, :])
+    return h if z >= 0 else np.conj(h)
+
+
+def rs_kernel(n_x, n_y, dx, dy, lam, z, m_x=None, m_y=None):
+    """FFT of the sampled RS kernel (convolution_kernel.jl:47-55, unnormalised fft!)."""
+    return fft2(rs_kernel_spatial(n_x, n_y, dx, dy, lam, z, m_x, m_y))
+
+
+def rs_valid_distance(nx, ny, dx, dy, lam):
+    """Critical distance below which RSProp warns (rayleigh_sommerfeld.jl:29-36)."""
+    if dx < lam / 2 and dy < lam / 2:
+        return 0.0
+    zx = 0.0 if dx < lam / 2 else (nx * dx / 2) * math.sqrt(4 * dx ** 2 / lam ** 2 - 1)
+    zy = 0.0 if dy < lam / 2 else (ny * dy / 2) * math.sqrt(4 * dy ** 2 / lam ** 2 - 1)
+    return max(zx, zy)
+
+
+def _lams(lambdas, nb):
+    lam = np.broadcast_to(np.asarray(lambdas, dtype=np.float64).ravel(), (nb,)) \
+        if np.ndim(lambdas) else np.full(nb, float(lambdas))
+    return np.asarray(lam)
+
+
+# ---------------------------------------------------------------------------
+# Free-space propagators
+# ---------------------------------------------------------------------------
+
+def asprop(u, dx, dy, lambdas, z, direction=FORWARD, n0=1.0):
+    """ASProp: u <- IFFT2(conj_direction(H) * FFT2(u)) per field.
+
+    Sequence (ft, ASKernelProp, ift) of angular_spectrum.jl:193-234; Backward
+    applies conj(H) (abstract_kernel.jl:36,45 with OpticalComponents.jl:919-925).
+    ``u`` has shape (..., ny, nx); ``lambdas`` is a scalar or one value per field."""
+    u = np.asarray(u, dtype=np.complex128)
+    shp = u.shape
+    ny, nx = shp[-2:]
+    v = u.reshape(-1, ny, nx)
+    lam = _lams(lambdas, v.shape[0])
+    out = np.empty_like(v)
+    cache = {}
+    for b in range(v.shape[0]):
+        key = float(lam[b])
+        if key not in cache:
+            cache[key] = as_kernel(nx, ny, dx, dy, key, z, n0)
+        h = cache[key] if direction == FORWARD else np.conj(cache[key])
+        out[b] = ifft2(fft2(v[b]) * h)
+    return out.reshape(shp)
+
+
+def rsprop(u, dx, dy, lambdas, z, direction=FORWARD, pad=None):
+    """RSProp: pad to (2n-1) (or ``pad``) at offset 0, FFT, * H_RS (conj for
+    Backward), IFFT, crop the top-left n x n (rayleigh_sommerfeld.jl:128-169,
+    pad_crop_operators.jl:1-16,61-79,291-356)."""
+    u = np.asarray(u, dtype=np.complex128)
+    shp = u.shape
+    ny, nx = shp[-2:]
+    v = u.reshape(-1, ny, nx)
+    mx = (2 * nx - 1) if pad is None else pad[0]
+    my = (2 * ny - 1) if pad is None else pad[1]
+    lam = _lams(lambdas, v.shape[0])
+    out = np.empty_like(v)
+    cache = {}
+    for b in range(v.shape[0]):
+        key = float(lam[b])
+        if key not in cache:
+            cache[key] = rs_kernel(nx, ny, dx, dy, key, z, mx, my)
+        h = cache[key] if direction == FORWARD else np.conj(cache[key])
+        up = np.zeros((my, mx), dtype=np.complex128)
+        up[:ny, :nx] = v[b]
+        out[b] = ifft2(fft2(up) * h)[:ny, :nx]
+    return out.reshape(shp)
+
+
+# ---------------------------------------------------------------------------
+# Modulators
+# ---------------------------------------------------------------------------
+
+def phase_forward(u, phi, direction=FORWARD):
+    """u * cis(s*phi), phi broadcast over the batch (phasemask.jl:90-94)."""
+    return np.asarray(u) * np.exp(1j * direction * np.asarray(phi, dtype=np.float64))
+
+
+def phase_backward(dv, phi, u_saved, direction=FORWARD):
+    """Adjoint of Phase with its gradient (phasemask.jl:96-98, :115-150).
+
+    du = cis(-s*phi) dv;  dphi = s * sum_batch Im(du * conj(u_saved))."""
+    du = np.asarray(dv) * np.exp(-1j * direction * np.asarray(phi, dtype=np.float64))
+    g = direction * np.imag(du * np.conj(u_saved))
+    dphi = g.reshape(-1, *g.shape[-2:]).sum(axis=0)
+    return du, dphi
+
+
+def mask_forward(u, m, direction=FORWARD):
+    """u * conj_direction(m) (mask.jl:241-248)."""
+    m = np.asarray(m, dtype=np.complex128)
+    return np.asarray(u) * (m if direction == FORWARD else np.conj(m))
+
+
+def mask_backward(dv, m, u_saved, direction=FORWARD):
+    """Adjoint of Mask with its gradient (mask.jl:263-291).
+
+    dm = sum_batch conj_direction(dv * conj(u_saved)), taken before
+    du = conj_direction(m, reverse(direction)) * dv."""
+    m = np.asarray(m, dtype=np.complex128)
+    g = np.asarray(dv) * np.conj(u_saved)
+    if direction == BACKWARD:
+        g = np.conj(g)
+    dm = g.reshape(-1, *g.shape[-2:]).sum(axis=0)
+    du = np.asarray(dv) * (np.conj(m) if direction == FORWARD else m)
+    return du, dm
+
+
+# ---------------------------------------------------------------------------
+# AS_BPM
+# ---------------------------------------------------------------------------
+
+def bpm_forward(u, dx, dy, lambdas, thickness, n0, dn, direction=FORWARD, save=False):
+    """Symmetric split-step AS_BPM march (bpm.jl:54-74, :130-142, :235-260).
+
+    dn has shape (n_slices, ny, nx).  dz = thickness/n_slices, props ASProp(dz; n0)
+    and ASProp(dz/2; n0), on-axis kdz = 2 pi dz.  Returns the output field and,
+    when ``save``, the list of slice inputs u_k (taken before the dn phase)."""
+    u = np.array(u, dtype=np.complex128)
+    shp = u.shape
+    ny, nx = shp[-2:]
+    v = u.reshape(-1, ny, nx)
+    lam = _lams(lambdas, v.shape[0])[:, None, None]
+    n_slices = dn.shape[0]
+    dz = thickness / n_slices
+    kdz = 2.0 * np.pi * dz
+    saves = []
+    v = asprop(v, dx, dy, lam.ravel(), dz / 2, direction, n0)
+    for k in range(n_slices - 1):
+        if save:
+            saves.append(v.copy())
+        v = v * np.exp(1j * direction * kdz / lam * dn[k][None])
+        v = asprop(v, dx, dy, lam.ravel(), dz, direction, n0)
+    if save:
+        saves.append(v.copy())
+    v = v * np.exp(1j * direction * kdz / lam * dn[-1][None])
+    v = asprop(v, dx, dy, lam.ravel(), dz / 2, direction, n0)
+    return v.reshape(shp), saves
+
+
+def bpm_backward(dv, dx, dy, lambdas, thickness, n0, dn, saves, direction=FORWARD):
+    """Adjoint march with the dn gradient (bpm.jl:275-321).
+
+    d_dn_k = s * kdz/lam * sum_batch Im(du * conj(u_k)), taken after the
+    conjugate dn phase of slice k."""
+    du = np.array(dv, dtype=np.complex128)
+    shp = du.shape
+    ny, nx = shp[-2:]
+    du = du.reshape(-1, ny, nx)
+    lam = _lams(lambdas, du.shape[0])[:, None, None]
+    n_slices = dn.shape[0]
+    dz = thickness / n_slices
+    kdz = 2.0 * np.pi * dz
+    rev = -direction
+    ddn = np.zeros_like(dn, dtype=np.float64)
+    du = asprop(du, dx, dy, lam.ravel(), dz / 2, rev, n0)
+    for k in range(n_slices - 1, 0, -1):
+        du = du * np.exp(1j * rev * kdz / lam * dn[k][None])
+        ddn[k] = (direction * kdz / lam * np.imag(du * np.conj(saves[k].reshape(du.shape)))).sum(0)
+        du = asprop(du, dx, dy, lam.ravel(), dz, rev, n0)
+    du = du * np.exp(1j * rev * kdz / lam * dn[0][None])
+    ddn[0] = (direction * kdz / lam * np.imag(du * np.conj(saves[0].reshape(du.shape)))).sum(0)
+    du = asprop(du, dx, dy, lam.ravel(), dz / 2, rev, n0)
+    return du.reshape(shp), ddn
+
+
+# ---------------------------------------------------------------------------
+# Metric
+# ---------------------------------------------------------------------------
+
+def sid_value(u, target, target_index=None):
+    """SquaredIntensityDifference (squared_intensity_difference.jl:58-83).
+
+    I_t = sum over the fields mapped to target slice t of |u|^2; returns the
+    per-slice losses c_t = sum (I_t - target_t)^2 and the residuals I - target.
+    ``u`` has shape (B, ny, nx), ``target`` (T, ny, nx) and ``target_index[b]``
+    gives the slice of field b (default: all fields to slice 0 when T == 1, else
+    b % T -- the broadcast of a (nx, ny, T) target over (nx, ny, T, M) fields)."""
+    u = np.asarray(u).reshape(-1, *np.shape(u)[-2:])
+    t = np.asarray(target, dtype=np.float64)
+    if t.ndim == 2:
+        t = t[None]
+    nb, nt = u.shape[0], t.shape[0]
+    if target_index is None:
+        target_index = np.arange(nb) % nt
+    inten = np.zeros_like(t)
+    for b in range(nb):
+        inten[target_index[b]] += np.abs(u[b]) ** 2
+    r = inten - t
+    return np.sum(r ** 2, axis=(-2, -1)), r
+
+
+def sid_backward(u, target, dc=1.0, target_index=None):
+    """du = 4 * dc * (I - target) * u (squared_intensity_difference.jl:85-90)."""
+    u2 = np.asarray(u).reshape(-1, *np.shape(u)[-2:])
+    _, r = sid_value(u2, target, target_index)
+    nt = r.shape[0]
+    if target_index is None:
+        target_index = np.arange(u2.shape[0]) % nt
+    dc = np.broadcast_to(np.asarray(dc, dtype=np.float64).ravel(), (nt,)) \
+        if np.ndim(dc) else np.full(nt, float(dc))
+    du = np.empty_like(u2)
+    for b in range(u2.shape[0]):
+        ti = target_index[b]
+        du[b] = 4.0 * dc[ti] * r[ti] * u2[b]
+    return du.reshape(np.shape(u))
+
+
+# ---------------------------------------------------------------------------
+# Optimiser and proximal operators
+# ---------------------------------------------------------------------------
+
+class FistaState:
+    """State (t_k, x_k, newdx) of Optimisers.init(::Fista) (OptimisersExt.jl:41-43)."""
+
+    def __init__(self, x):
+        self.t = 1.0
+        self.xk = np.array(x, dtype=np.float64, copy=True)
+        self.newdx = np.zeros_like(self.xk)
+
+
+def fista_apply(eta, state, x, dx):
+    """One Fista step, in place on x; the rule stores eta^2 (OptimisersExt.jl:33-54).
+
+    t' = (1+sqrt(1+4t^2))/2, beta = (t-1)/t', newdx = eta^2 dx - beta (x - x_k),
+    x_k <- x, then Optimisers subtracts newdx from x."""
+    e = eta * eta
+    tkn = (1.0 + math.sqrt(1.0 + 4.0 * state.t * state.t)) / 2.0
+    beta = (state.t - 1.0) / tkn
+    state.newdx = e * dx - beta * (x - state.xk)
+    state.xk = x.copy()
+    state.t = tkn
+    x -= state.newdx
+    return x
+
+
+def clamp_prox(x, lo, hi):
+    """ClampProx (clamp_prox.jl:35-37)."""
+    np.clip(x, lo, hi, out=x)
+    return x
+
+
+def positive_prox(x):
+    """PositiveProx (positive_prox.jl:1-12)."""
+    x[x < 0] = 0
+    return x
+
+
+def ista_prox(x, s, c=0.0):
+    """IstaProx soft threshold towards c (ista_prox.jl:1-19)."""
+    xc = x - c
+    out = np.where(np.abs(xc) <= s, c, np.where(xc > s, x - s, x + s))
+    x[...] = out
+    return x
+
+
+def _d(p_out, a):
+    # D! (tv_prox.jl:30-41): forward differences per dim, written into slice i
+    # over 1:n-1 along that dim; the last index along dim i is not written.
+    # numpy axis order: Julia dim 1 (x) is axis -1, dim 2 (y) is axis -2.
+    nd = a.ndim
+    for i in range(nd):
+        ax = nd - 1 - i
+        sl_hi = [slice(None)] * nd
+        sl_lo = [slice(None)] * nd
+        sl_hi[ax] = slice(1, None)
+        sl_lo[ax] = slice(0, -1)
+        p_out[i][tuple(sl_lo)] = a[tuple(sl_hi)] - a[tuple(sl_lo)]
+    return p_out
+
+
+def _dt(a, p):
+    # Dt! (tv_prox.jl:43-59), including the boundary overwrite A[1 along dim i] = -p_i[1]
+    nd = a.ndim
+    for i in range(nd):
+        ax = nd - 1 - i
+        hi = [slice(None)] * nd
+        lo = [slice(None)] * nd
+        hi[ax] = slice(1, None)
+        lo[ax] = slice(0, -1)
+        val = p[i][tuple(lo)] - p[i][tuple(hi)]
+        if i == 0:
+            a[tuple(hi)] = val
+        else:
+            a[tuple(hi)] += val
+    for i in range(nd):
+        ax = nd - 1 - i
+        first = [slice(None)] * nd
+        first[ax] = 0
+        a[tuple(first)] = -p[i][tuple(first)]
+    return a
+
+
+def tv_prox(y0, lam, n_iter=50, isotropic=True, eta=None):
+    """TVProx: dual FISTA on p (tv_prox.jl:94-195), in place on y0.
+
+    Default inner rule Fista(0.25) (isotropic) / Fista(2.5) (anisotropic); the
+    isotropic projection divides each dual slice by its global norm when > 1;
+    anisotropic uses lam/100 and clamps to [-1, 1]."""
+    y0 = np.asarray(y0)
+    if eta is None:
+        eta = 0.25 if isotropic else 2.5
+    nd = y0.ndim
+    lam_eff = lam if isotropic else lam / 100.0
+    p = np.zeros((nd,) + y0.shape)
+    dp = np.zeros_like(p)
+    y = np.zeros_like(y0, dtype=np.float64)
+    st = FistaState(p)
+    for _ in range(n_iter):
+        _dt(y, p)
+        y = lam_eff * y - y0
+        _d(dp, y)
+        fista_apply(eta, st, p, dp)
+        for i in range(nd):
+            if isotropic:
+                nrm = np.linalg.norm(p[i])
+                if nrm > 1:
+                    p[i] /= nrm
+            else:
+                np.clip(p[i], -1, 1, out=p[i])
+    _dt(y, p)
+    y0 -= lam_eff * y
+    return y0

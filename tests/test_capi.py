@@ -1,0 +1,81 @@
+"""The C-ABI library loads, exports every symbol of include/*.h, and rejects bad
+arguments before touching the GPU (CPU only: argument validation runs first)."""
+
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from __graft_entry__ import build, load_package
+    build()
+    pkg = load_package()
+    return pkg._capi
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = open(h).read()
+        names |= set(re.findall(r"FO_API\s+[\w\s\*]+?\b(fo_\w+)\s*\(", txt))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert "fo_asprop_create" in names and "fo_chain_backward" in names
+    assert len(names) >= 30
+
+
+def test_library_exports_every_declared_symbol(capi):
+    lib = capi.load()
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    # the ctypes table covers the header exactly
+    assert set(capi.SIGNATURES) == set(declared_symbols())
+
+
+def test_version(capi):
+    assert capi.load().fo_version() == 10000
+
+
+def _err(capi, rc):
+    assert rc != 0
+    return capi.load().fo_last_error().decode()
+
+
+def test_bad_shapes_are_rejected(capi):
+    lib = capi.load()
+    h = C.c_void_p()
+    lam = capi.dvec([1.064])
+    rc = lib.fo_asprop_create(C.byref(h), 0, 64, 1, 1.0, 1.0, lam, 1, 100.0, 1.0, 0)
+    assert rc == 2 and "positive" in _err(capi, rc)
+    rc = lib.fo_asprop_create(C.byref(h), 100, 64, 1, 1.0, 1.0, lam, 1, 100.0, 1.0, 0)
+    assert rc == 2 and "not supported" in _err(capi, rc)
+    rc = lib.fo_rsprop_create(C.byref(h), 4000, 64, 1, 1.0, 1.0, lam, 1, 100.0, 0)
+    assert rc == 2
+    rc = lib.fo_asprop_create(C.byref(h), 64, 64, 2, 1.0, 1.0, lam, 3, 100.0, 1.0, 0)
+    assert rc == 1 and "lambdas" in _err(capi, rc)
+    rc = lib.fo_asprop_create(C.byref(h), 64, 64, 1, -1.0, 1.0, lam, 1, 100.0, 1.0, 0)
+    assert rc == 1
+    rc = lib.fo_bpm_create(C.byref(h), 64, 64, 1, 1.0, 1.0, lam, 1, 10.0, 1.45, 1, 0, 1.0, 0)
+    assert rc == 2 and "2 slices" in _err(capi, rc)
+
+
+def test_bad_arguments_are_rejected(capi):
+    lib = capi.load()
+    assert lib.fo_propagate(None, None, 1, None) == 1
+    assert lib.fo_phase_forward(C.c_void_p(16), C.c_void_p(16), None, 8, 8, 1, 3, None) == 1
+    assert "direction" in lib.fo_last_error().decode()
+    assert lib.fo_phase_backward(C.c_void_p(16), C.c_void_p(16), None, C.c_void_p(16), 8, 8, 1, 1, None) == 1
+    assert lib.fo_clamp(C.c_void_p(16), 10, 1.0, 0.0, None) == 1
+    assert lib.fo_chain_create(C.byref(C.c_void_p()), 0, None) == 1
+    assert lib.fo_sid_create(C.byref(C.c_void_p()), 8, 8, 2, 2, capi.ivec([0, 5])) == 1
+    assert lib.fo_tv_create(C.byref(C.c_void_p()), 1, 8, 0.1, 10, 1, 0.25) == 2
+    assert lib.fo_fista_step(None, None, None, None, 10, 0.1, None, None) == 1

@@ -1,0 +1,373 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle.
+
+Tolerances (relative L2 against the FP64 oracle, inputs rounded to the GPU's
+float32 first): fields 1e-5, gradients 1e-4, losses 1e-4.
+"""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-5
+GRAD_TOL = 1e-4
+
+
+def c64(a):
+    return np.asarray(a).astype(np.complex64).astype(np.complex128)
+
+
+def f32(a):
+    return np.asarray(a).astype(np.float32).astype(np.float64)
+
+
+def npy(t):
+    return t.detach().cpu().numpy().astype(np.complex128 if t.is_complex() else np.float64)
+
+
+def rand_field(rng, shape):
+    return c64(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+
+
+# ---------------------------------------------------------------------------
+# Free-space propagators
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256, 512, 1024, 2048, 4096])
+def test_asprop_sizes(fo, orc, n):
+    rng = np.random.default_rng(n)
+    ds, lam, z = (1.0, 1.0), 1.064, 700.0
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(orc.gaussian(n / 8, x, y) * (1 + 0.2 * rng.standard_normal((n, n))))
+    u = fo.ScalarField(u0, ds, lam)
+    p = fo.ASProp(u, z)
+    for d in (fo.Forward, fo.Backward):
+        v = p.propagate(u, d)
+        ref = orc.asprop(u0, ds[0], ds[1], lam, z, d)
+        assert orc.rel_l2(npy(v.electric), ref) < FIELD_TOL
+
+
+@pytest.mark.parametrize("shape", [(64, 128), (256, 32), (16, 4096), (2048, 64)])
+def test_asprop_rectangular(fo, orc, shape):
+    ny, nx = shape
+    rng = np.random.default_rng(1)
+    u0 = rand_field(rng, (ny, nx))
+    u = fo.ScalarField(u0, (0.7, 1.3), 0.8)
+    v = fo.ASProp(u, 250.0).propagate(u)
+    assert orc.rel_l2(npy(v.electric), orc.asprop(u0, 0.7, 1.3, 0.8, 250.0)) < FIELD_TOL
+
+
+def test_asprop_batch_wavelengths_n0_negative_z(fo, orc):
+    rng = np.random.default_rng(2)
+    lams = np.array([0.640, 0.538, 0.455])
+    u0 = rand_field(rng, (4, 3, 128, 128))  # Julia (128, 128, 3, 4): lambda along dim 3
+    u = fo.ScalarField(u0, (0.5, 0.5), lams)
+    for z, n0 in ((5000.0, 1.0), (-800.0, 1.45)):
+        v = fo.ASProp(u, z, n0=n0).propagate(u)
+        ref = orc.asprop(u0.reshape(12, 128, 128), 0.5, 0.5, np.tile(lams, 4), z, 1, n0).reshape(u0.shape)
+        assert orc.rel_l2(npy(v.electric), ref) < FIELD_TOL
+
+
+def test_asprop_evanescent(fo, orc):
+    # ds < lambda/2: part of the spectrum is evanescent and must decay
+    rng = np.random.default_rng(3)
+    u0 = rand_field(rng, (64, 64))
+    u = fo.ScalarField(u0, (0.2, 0.2), 1.064)
+    for z in (3.0, -3.0):
+        v = fo.ASProp(u, z).propagate(u)
+        assert orc.rel_l2(npy(v.electric), orc.asprop(u0, 0.2, 0.2, 1.064, z)) < FIELD_TOL
+
+
+@pytest.mark.parametrize("n", [16, 40, 64, 250, 512])
+def test_rsprop(fo, orc, n):
+    rng = np.random.default_rng(n)
+    ds, lam, z = (1.0, 1.0), 1.064, 1500.0
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(orc.gaussian(n / 6, x, y) * (1 + 0.2 * rng.standard_normal((n, n))))
+    u = fo.ScalarField(u0, ds, lam)
+    p = fo.RSProp(u, z)
+    for d in (fo.Forward, fo.Backward):
+        v = p.propagate(u, d)
+        ref = orc.rsprop(u0, ds[0], ds[1], lam, z, d)  # the reference's 2n-1 padding
+        assert orc.rel_l2(npy(v.electric), ref) < FIELD_TOL
+
+
+def test_rsprop_rect_batch(fo, orc):
+    rng = np.random.default_rng(5)
+    u0 = rand_field(rng, (2, 48, 100))
+    u = fo.ScalarField(u0, (2.0, 1.5), [1.064, 0.532])
+    v = fo.RSProp(u, 900.0).propagate(u)
+    ref = orc.rsprop(u0, 2.0, 1.5, [1.064, 0.532], 900.0)
+    assert orc.rel_l2(npy(v.electric), ref) < FIELD_TOL
+
+
+# ---------------------------------------------------------------------------
+# Modulators
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("d", [1, -1])
+def test_phase_mask_standalone(fo, orc, d):
+    rng = np.random.default_rng(6)
+    ny, nx, B = 33, 47, 3
+    u0 = rand_field(rng, (B, ny, nx))
+    dv0 = rand_field(rng, (B, ny, nx))
+    phi = f32(rng.uniform(0, 2 * np.pi, (ny, nx)))
+    m = c64(rng.standard_normal((ny, nx)) + 1j * rng.standard_normal((ny, nx)))
+    u = fo.ScalarField(u0, (1.0, 1.0), 1.0)
+    ph = fo.Phase(u, phi, trainable=True)
+    mk = fo.Mask(u, m, trainable=True)
+    saved = torch.empty_like(u.electric)
+    v = u.copy()
+    ph.propagate_and_save_(v, saved, d)
+    assert orc.rel_l2(npy(v.electric), orc.phase_forward(u0, phi, d)) < FIELD_TOL
+    assert orc.rel_l2(npy(saved), u0) == 0.0
+    dv = fo.ScalarField(dv0, (1.0, 1.0), 1.0)
+    g = torch.empty_like(ph.phi)
+    ph.backpropagate_with_gradient_(dv, saved, g, d)
+    du_ref, g_ref = orc.phase_backward(dv0, phi, u0, d)
+    assert orc.rel_l2(npy(dv.electric), du_ref) < FIELD_TOL
+    assert orc.rel_l2(npy(g), g_ref) < GRAD_TOL
+    v = u.copy()
+    mk.propagate_and_save_(v, saved, d)
+    assert orc.rel_l2(npy(v.electric), orc.mask_forward(u0, m, d)) < FIELD_TOL
+    dv = fo.ScalarField(dv0, (1.0, 1.0), 1.0)
+    gm = torch.empty_like(mk.m)
+    mk.backpropagate_with_gradient_(dv, saved, gm, d)
+    du_ref, gm_ref = orc.mask_backward(dv0, m, u0, d)
+    assert orc.rel_l2(npy(dv.electric), du_ref) < FIELD_TOL
+    assert orc.rel_l2(npy(gm), gm_ref) < GRAD_TOL
+
+
+# ---------------------------------------------------------------------------
+# Fused chains with gradients
+# ---------------------------------------------------------------------------
+
+def _oracle_chain(orc, kind, u0, mods, ds, lams, zs, d):
+    """mods: list of (kind, param) or None, len(zs)+1; returns out, saves."""
+    def prop(v, z, dd):
+        if kind == "AS":
+            return orc.asprop(v, ds[0], ds[1], lams, z, dd)
+        return orc.rsprop(v, ds[0], ds[1], lams, z, dd)
+
+    def apply(v, m):
+        if m is None:
+            return v
+        return orc.phase_forward(v, m[1], d) if m[0] == "phase" else orc.mask_forward(v, m[1], d)
+
+    saves = []
+    v = u0
+    for k, z in enumerate(zs):
+        saves.append(v)
+        v = prop(apply(v, mods[k]), z, d)
+    saves.append(v)
+    return apply(v, mods[-1]), saves, prop
+
+
+@pytest.mark.parametrize("kind,d", [("AS", 1), ("RS", 1), ("AS", -1)])
+def test_chain_gradients(fo, orc, kind, d):
+    rng = np.random.default_rng(8)
+    n, B = 64, 2
+    ds, lams = (1.0, 1.0), np.array([1.064, 0.8])
+    zs = [300.0, 450.0, 200.0]
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(9.0, x, y)] * B) * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    phi0 = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    m1 = c64(0.5 + rng.uniform(0, 1, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+    phi3 = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    target = f32(np.abs(orc.gaussian(7.0, x - 5, y)) ** 2)
+
+    u = fo.ScalarField(u0, ds, lams)
+    P = fo.ASProp if kind == "AS" else fo.RSProp
+    c0 = fo.Phase(u, phi0, trainable=True)
+    c1 = fo.Mask(u, m1, trainable=True)
+    c3 = fo.Phase(u, phi3, trainable=True)
+    props = [P(u, z) for z in zs]
+    system = fo.OpticalSystem(fo.ScalarSource(u), [c0, props[0], c1, props[1], props[2], c3], direction=d)
+    segs = system.segments(u)
+    assert len(segs) == 1  # one fused chain
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+
+    mods = [("phase", phi0), ("mask", m1), None, ("phase", phi3)]
+    out, saves, prop = _oracle_chain(orc, kind, u0, mods, ds, lams, zs, d)
+    got = npy(system()["out"].electric)
+    assert orc.rel_l2(got, out) < FIELD_TOL
+    c_ref, _ = orc.sid_value(out, target)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    dv = orc.sid_backward(out, target)
+    dv, g3 = orc.phase_backward(dv, phi3, saves[3], d)
+    dv = prop(dv, zs[2], -d)
+    dv = prop(dv, zs[1], -d)
+    dv, g1 = orc.mask_backward(dv, m1, saves[1], d)
+    dv = prop(dv, zs[0], -d)
+    _, g0 = orc.phase_backward(dv, phi0, saves[0], d)
+    assert orc.rel_l2(npy(grads[c3]["phi"]), g3) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[c1]["m"]), g1) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[c0]["phi"]), g0) < GRAD_TOL
+
+
+# ---------------------------------------------------------------------------
+# AS_BPM
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("every", [1, 0, 3, 7])
+def test_bpm_forward_and_gradient(fo, orc, every):
+    rng = np.random.default_rng(9)
+    n, ns, B = 64, 20, 2
+    ds, lams, n0, L = (0.5, 0.5), np.array([1.064, 0.9]), 1.45, 40.0
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(6.0, x, y), orc.gaussian(5.0, x - 1, y)]))
+    dn = f32(3e-3 * rng.standard_normal((ns, n, n)))
+    target = f32(np.abs(orc.gaussian(5.0, x, y)) ** 2)
+    u = fo.ScalarField(u0, ds, lams)
+    bpm = fo.AS_BPM(u, L, n0, dn, trainable=True, checkpoint_every=every)
+    system = fo.ScalarSource(u) | bpm
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    out, saves = orc.bpm_forward(u0, ds[0], ds[1], lams, L, n0, dn, 1, save=True)
+    assert orc.rel_l2(npy(system()["out"].electric), out) < FIELD_TOL
+    _, g = orc.bpm_backward(orc.sid_backward(out, target), ds[0], ds[1], lams, L, n0, dn, saves, 1)
+    assert orc.rel_l2(npy(grads[bpm]["dn"]), g) < GRAD_TOL
+
+
+def test_bpm_backward_direction(fo, orc):
+    rng = np.random.default_rng(10)
+    n, ns = 32, 6
+    ds, lam, n0, L = (0.5, 0.5), 1.064, 1.45, 12.0
+    u0 = rand_field(rng, (n, n))
+    dv0 = rand_field(rng, (n, n))
+    dn = f32(5e-3 * rng.standard_normal((ns, n, n)))
+    u = fo.ScalarField(u0, ds, lam)
+    bpm = fo.AS_BPM(u, L, n0, dn, trainable=True, checkpoint_every=2)
+    v = u.copy()
+    bpm.propagate_and_save_(v, None, fo.Backward)
+    out, saves = orc.bpm_forward(u0, ds[0], ds[1], lam, L, n0, dn, -1, save=True)
+    assert orc.rel_l2(npy(v.electric), out) < FIELD_TOL
+    dv = fo.ScalarField(dv0, ds, lam)
+    g = torch.empty_like(bpm.dn)
+    bpm.backpropagate_with_gradient_(dv, None, g, fo.Backward)
+    du_ref, g_ref = orc.bpm_backward(dv0, ds[0], ds[1], lam, L, n0, dn, saves, -1)
+    assert orc.rel_l2(npy(dv.electric), du_ref) < FIELD_TOL
+    assert orc.rel_l2(npy(g), g_ref) < GRAD_TOL
+
+
+# ---------------------------------------------------------------------------
+# Metric and optimiser
+# ---------------------------------------------------------------------------
+
+def test_sid_multi_target(fo, orc):
+    rng = np.random.default_rng(12)
+    u0 = rand_field(rng, (2, 3, 40, 24))  # Julia (24, 40, 3, 2): target (24, 40, 3)
+    target = f32(rng.uniform(0, 4, (3, 40, 24)))
+    u = fo.ScalarField(u0, (1.0, 1.0), 1.0)
+    m = fo.SquaredIntensityDifference((u, target))
+    loss = npy(m(u))
+    ref, _ = orc.sid_value(u0.reshape(6, 40, 24), target)
+    assert np.max(np.abs(loss - ref) / np.abs(ref)) < 1e-4
+    du = m.backpropagate(u)
+    du_ref = orc.sid_backward(u0.reshape(6, 40, 24), target).reshape(u0.shape)
+    assert orc.rel_l2(npy(du.electric), du_ref) < 1e-5
+
+
+def test_fista_clamp_tv(fo, orc):
+    rng = np.random.default_rng(13)
+    x0 = f32(rng.standard_normal((37, 53)))
+    xs = torch.tensor(x0, dtype=torch.float32, device="cuda")
+    rule = fo.ProxRule(fo.Fista(0.3), fo.ClampProx(-0.5, 0.7))
+    st = rule.init(xs)
+    xo = x0.copy()
+    so = orc.FistaState(xo)
+    for it in range(5):
+        g = f32(rng.standard_normal(x0.shape))
+        rule.apply_(st, xs, torch.tensor(g, dtype=torch.float32, device="cuda"))
+        orc.fista_apply(0.3, so, xo, g)
+        orc.clamp_prox(xo, -0.5, 0.7)
+        assert orc.rel_l2(npy(xs), xo) < 1e-5
+    for iso in (True, False):
+        y0 = f32(rng.standard_normal((40, 30)))
+        yt = torch.tensor(y0, dtype=torch.float32, device="cuda")
+        tv = fo.TVProx(0.2, 25, isotropic=iso)
+        tv.apply_(tv.init(yt), yt)
+        ref = orc.tv_prox(y0.copy(), 0.2, 25, isotropic=iso)
+        assert orc.rel_l2(npy(yt), ref) < 1e-5
+
+
+# ---------------------------------------------------------------------------
+# Full-size properties (sizes where the FP64 oracle is too slow)
+# ---------------------------------------------------------------------------
+
+def test_fullsize_unitarity_and_power(fo):
+    torch.manual_seed(0)
+    n, B = 2048, 6
+    u0 = torch.randn(B, n, n, dtype=torch.complex64, device="cuda")
+    u = fo.ScalarField(u0, (0.5, 0.5), [0.640, 0.538, 0.455])
+    p = fo.ASProp(u, 5000.0)
+    v = p.propagate(u)
+    # power is conserved up to the evanescent part, which is empty at ds = 0.5 > lambda/2... check ratio
+    pw0 = (u0.abs() ** 2).sum(dim=(-2, -1))
+    pw1 = (v.electric.abs() ** 2).sum(dim=(-2, -1))
+    assert torch.all(pw1 <= pw0 * (1 + 1e-5))
+    w = p.propagate(v, fo.Backward)
+    # propagating the result back recovers the propagating part of the input exactly
+    v2 = p.propagate(w)
+    rel = torch.linalg.vector_norm(v2.electric - v.electric) / torch.linalg.vector_norm(v.electric)
+    assert rel.item() < 1e-5
+    # linearity
+    a = p.propagate(fo.ScalarField(u0 * (2 - 1j), (0.5, 0.5), [0.640, 0.538, 0.455]))
+    rel = torch.linalg.vector_norm(a.electric - v.electric * (2 - 1j)) / torch.linalg.vector_norm(a.electric)
+    assert rel.item() < 1e-6
+
+
+def test_graph_capture_replays_iteration(fo, orc):
+    rng = np.random.default_rng(14)
+    n = 128
+    u0 = rand_field(rng, (2, n, n))
+    u = fo.ScalarField(u0, (1.0, 1.0), [1.0, 0.7])
+    ph = fo.Phase(u, f32(rng.uniform(0, 6, (n, n))), trainable=True, buffered=True)
+    system = fo.ScalarSource(u) | ph | fo.ASProp(u, 300.0) | fo.Phase(u, f32(rng.uniform(0, 6, (n, n)))) \
+        | fo.ASProp(u, 100.0)
+    metric = fo.SquaredIntensityDifference((u, f32(rng.uniform(0, 1, (n, n)))))
+    opt = fo.setup(fo.Fista(0.01), system)
+    phi_start = ph.phi.clone()
+    losses_eager = []
+    for _ in range(3):
+        loss, g = fo.withgradient(metric, system)
+        fo.update_(opt, system, g)
+        losses_eager.append(float(loss))
+    phi_eager = ph.phi.clone()
+    # same iterations, captured once and replayed
+    ph.phi.copy_(phi_start)
+    opt = fo.setup(fo.Fista(0.01), system)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        lib = fo.load_library()
+        x = system.source.propagate()  # allocations happen outside the capture
+        tape = []
+        system.forward(x, tape)
+        torch.cuda.synchronize()
+        ph.phi.copy_(phi_start)
+        opt = fo.setup(fo.Fista(0.01), system)
+        torch.cuda.synchronize()
+        du = x.similar()
+        h = C.c_void_p()
+        assert lib.fo_graph_begin(C.c_void_p(s.cuda_stream)) == 0
+        x.electric.copy_(system.source.u0.electric)
+        tape = []
+        system.forward(x, tape)
+        loss_t = metric(x)
+        grads = system.backward(du, tape, seed=(metric, x))
+        fo.update_(opt, system, grads)
+        assert lib.fo_graph_end(C.c_void_p(s.cuda_stream), C.byref(h)) == 0
+        losses = []
+        for _ in range(3):
+            assert lib.fo_graph_launch(h, C.c_void_p(s.cuda_stream)) == 0
+            s.synchronize()
+            losses.append(float(loss_t.sum()))
+        lib.fo_graph_destroy(h)
+    torch.cuda.synchronize()
+    assert np.allclose(losses, losses_eager, rtol=1e-5)
+    assert torch.allclose(ph.phi, phi_eager, rtol=1e-5, atol=1e-6)

@@ -1,0 +1,290 @@
+"""Pins the FP64 oracle to the reference's own tests (CPU only).
+
+Each test restates a property or known answer from FluxOptics.jl's test suite
+(test/*.jl) or source (analytic beams), plus central finite differences of every
+hand-written adjoint.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from oracle import fluxoptics_oracle as orc
+
+
+def gauss_field(n, ds, w0):
+    x, y = orc.spatial_vectors((n, n), ds)
+    return orc.gaussian(w0, x, y)
+
+
+# --- test/optical_components_test.jl:85-112 -----------------------------------
+def test_as_rs_unitarity():
+    ds, lam, z = (1.0, 1.0), 1.064, 1000.0
+    u = gauss_field(128, ds, 20.0)
+    v = orc.asprop(u, ds[0], ds[1], lam, z)
+    w = orc.asprop(v, ds[0], ds[1], lam, z, orc.BACKWARD)
+    assert orc.coupling_efficiency(u, w) > 0.9999
+    v = orc.rsprop(u, ds[0], ds[1], lam, z)
+    w = orc.rsprop(v, ds[0], ds[1], lam, z, orc.BACKWARD)
+    assert orc.coupling_efficiency(u, w) > 0.999
+
+
+# --- test/optical_components_test.jl:114-133 ----------------------------------
+def test_as_energy_conservation():
+    ds = (0.5, 0.5)
+    u = gauss_field(128, ds, 15.0)
+    orc.normalize_power(u, ds, 1.0)
+    v = orc.asprop(u, ds[0], ds[1], 1.064, 500.0)
+    assert np.isclose(orc.power(v, ds), orc.power(u, ds), rtol=1e-6)
+
+
+# --- test/optical_components_test.jl:22-44 ------------------------------------
+def test_phase_angles():
+    n, ds = 64, (1.0, 1.0)
+    u = np.ones((n, n), dtype=complex)
+    r = orc.phase_forward(u, np.full((n, n), np.pi / 2))
+    assert np.allclose(np.angle(r), np.pi / 2)
+    x, y = orc.spatial_vectors((n, n), ds)
+    phi = x[None, :] + y[:, None]
+    r = orc.phase_forward(u, phi)
+    assert np.allclose(np.angle(r), np.angle(np.exp(1j * phi)))
+
+
+# --- test/optical_components_test.jl:46-65 ------------------------------------
+def test_mask_aperture():
+    n, ds = 64, (1.0, 1.0)
+    x, y = orc.spatial_vectors((n, n), ds)
+    m = ((x[None, :] ** 2 + y[:, None] ** 2) < 20.0 ** 2).astype(float)
+    r = orc.mask_forward(np.ones((n, n), dtype=complex), m)
+    c = n // 2 - 1  # Julia's center_idx = 32 (1-based)
+    assert abs(r[c, c]) == pytest.approx(1.0)
+    assert abs(r[0, 0]) < 0.1
+
+
+# --- test/metrics_test.jl:52-75 ------------------------------------------------
+def test_sid_closed_form():
+    n = 32
+    u = np.ones((n, n), dtype=complex)
+    c, _ = orc.sid_value(u, 2.0 * np.ones((n, n)))
+    assert c[0] == pytest.approx(n * n * 1.0 * 1.0, rel=1e-6)
+    c, _ = orc.sid_value(math.sqrt(2.0) * u, 2.0 * np.ones((n, n)))
+    assert c[0] < 1e-10
+
+
+# --- test/modes_test.jl:21-43 and the hermite_gaussian_groups doctest -------------
+def test_hermite_gauss_modes():
+    x, y = orc.spatial_vectors((129, 129), (1.0, 1.0))
+    assert np.max(np.abs(orc.hermite_gaussian(15.0, 0, 0, x, y) - orc.gaussian(15.0, x, y))) < 1e-10
+    hg10 = orc.hermite_gaussian(15.0, 1, 0, x, y)
+    assert abs(hg10[64, 64]) < 1e-10
+    hg20 = orc.hermite_gaussian(15.0, 2, 0, x, y)
+    assert abs(hg20[64, 69]) == pytest.approx(abs(hg20[64, 59]), abs=1e-10)
+    assert len(orc.hermite_gaussian_groups(3)) == 6
+    assert len(orc.hermite_gaussian_groups(4)) == 10
+    assert len(orc.hermite_gaussian_groups(5)) == 15
+    x, y = orc.spatial_vectors((64, 64), (2.0, 2.0))
+    for m, n in orc.hermite_gaussian_groups(3):
+        f = orc.hermite_gaussian(10.0, m, n, x, y)
+        assert abs(np.sum(np.abs(f) ** 2) * 4.0 - 1.0) < 1e-10
+
+
+# --- test/fields_test.jl:49-72 --------------------------------------------------
+def test_power_normalisation():
+    ds = (0.5, 0.5)
+    u = gauss_field(128, ds, 20.0)
+    orc.normalize_power(u, ds, 1.0)
+    assert orc.power(u, ds) == pytest.approx(1.0, rel=1e-6)
+    orc.normalize_power(u, ds, 2.5)
+    assert orc.power(u, ds) == pytest.approx(2.5, rel=1e-6)
+
+
+# --- test/optimisers_test.jl:50-66 ------------------------------------------------
+def test_fista_quadratic():
+    x = np.array([0.0])
+    st = orc.FistaState(x)
+    for _ in range(50):
+        g = np.array([2 * (x[0] - 3.0)])
+        orc.fista_apply(0.9, st, x, g)
+    assert x[0] == pytest.approx(3.0, abs=1e-3)
+
+
+# --- test/optimisers_test.jl:30-47 (IstaProx / ClampProx doctests) -----------------
+def test_pointwise_prox():
+    x = np.array([-1.0, -0.2, 0.0, 0.4, 1.5])
+    orc.ista_prox(x, 0.5)
+    assert np.allclose(x, [-0.5, 0.0, 0.0, 0.0, 1.0])
+    x = np.array([-0.5, 0.3, 1.2, 0.8])
+    orc.clamp_prox(x, 0.0, 1.0)
+    assert np.allclose(x, [0.0, 0.3, 1.0, 0.8])
+
+
+# --- analytic paraxial Gaussian beam (src/modes/gaussian_modes.jl:87-104) -----------
+def test_as_matches_paraxial_gaussian_beam():
+    n, ds, lam, w0, z = 512, (1.0, 1.0), 1.064, 30.0, 1500.0
+    x, y = orc.spatial_vectors((n, n), ds)
+    u = orc.gaussian(w0, x, y)
+    v = orc.asprop(u, ds[0], ds[1], lam, z)
+    k = 2 * np.pi / lam
+    zr = np.pi * w0 ** 2 / lam
+    q0, qz = -1j * zr, z - 1j * zr
+    r2 = x[None, :] ** 2 + y[:, None] ** 2
+    ana = (math.sqrt(2 / np.pi) / w0) * (q0 / qz) * np.exp(1j * k * r2 / (2 * qz)) * np.exp(1j * k * z)
+    assert orc.rel_l2(v, ana) < 1e-3
+
+
+# --- AS_BPM with dn = 0 is one ASProp over the thickness (bpm.jl:244-260) ------------
+def test_bpm_zero_dn_is_asprop():
+    n, ds, lam, n0, L = 64, (1.0, 1.0), 1.064, 1.5, 100.0
+    u = gauss_field(n, ds, 10.0)
+    dn = np.zeros((20, n, n))
+    v, _ = orc.bpm_forward(u, ds[0], ds[1], lam, L, n0, dn)
+    w = orc.asprop(u, ds[0], ds[1], lam, L, orc.FORWARD, n0)
+    assert orc.rel_l2(v, w) < 1e-12
+    assert v.shape == (n, n)
+
+
+# --- padding RSProp to a power of two >= 2n-1 is exact on the cropped block ----------
+def test_rs_pow2_padding_is_exact():
+    n, ds, lam, z = 40, (1.0, 1.0), 1.064, 300.0
+    rng = np.random.default_rng(1)
+    u = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    a = orc.rsprop(u, ds[0], ds[1], lam, z)
+    b = orc.rsprop(u, ds[0], ds[1], lam, z, pad=(128, 128))
+    assert orc.rel_l2(b, a) < 1e-12
+
+
+# --- adjoints against central finite differences ------------------------------------
+def _fd_check(loss, grad_dot, x, d, eps=1e-6):
+    fd = (loss(x + eps * d) - loss(x - eps * d)) / (2 * eps)
+    an = grad_dot(d)
+    assert abs(fd - an) <= 1e-6 * max(abs(an), 1e-12) + 1e-9, (fd, an)
+
+
+def _chain_setup(n=32, kind="as"):
+    ds, lam = (1.0, 1.0), 1.064
+    rng = np.random.default_rng(7)
+    u0 = gauss_field(n, ds, 6.0) * (1 + 0.1 * rng.standard_normal((n, n)))
+    phi1 = rng.uniform(0, 2 * np.pi, (n, n))
+    phi2 = rng.uniform(0, 2 * np.pi, (n, n))
+    target = np.abs(gauss_field(n, ds, 5.0)) ** 2
+    prop = (lambda u, d=orc.FORWARD: orc.asprop(u, ds[0], ds[1], lam, 150.0, d)) if kind == "as" else \
+        (lambda u, d=orc.FORWARD: orc.rsprop(u, ds[0], ds[1], lam, 150.0, d))
+    return u0, phi1, phi2, target, prop
+
+
+@pytest.mark.parametrize("kind", ["as", "rs"])
+def test_fd_phase_chain(kind):
+    u0, phi1, phi2, target, prop = _chain_setup(kind=kind)
+
+    def fwd(p1, p2):
+        v1 = prop(orc.phase_forward(u0, p1))
+        v2 = prop(orc.phase_forward(v1, p2))
+        return v1, v2
+
+    def loss(p1):
+        return orc.sid_value(fwd(p1, phi2)[1], target)[0].sum()
+
+    v1, v2 = fwd(phi1, phi2)
+    dv = prop(orc.sid_backward(v2, target), orc.BACKWARD)
+    dv, g2 = orc.phase_backward(dv, phi2, v1)
+    dv = prop(dv, orc.BACKWARD)
+    _, g1 = orc.phase_backward(dv, phi1, u0)
+    d = np.random.default_rng(3).standard_normal(phi1.shape)
+    _fd_check(loss, lambda dd: np.sum(g1 * dd), phi1, d)
+    loss2 = lambda p2: orc.sid_value(fwd(phi1, p2)[1], target)[0].sum()  # noqa: E731
+    _fd_check(loss2, lambda dd: np.sum(g2 * dd), phi2, d)
+
+
+@pytest.mark.parametrize("direction", [1, -1])
+def test_fd_mask(direction):
+    u0, _, _, target, prop = _chain_setup()
+    rng = np.random.default_rng(5)
+    m = rng.standard_normal(u0.shape) + 1j * rng.standard_normal(u0.shape)
+
+    def loss(mm):
+        return orc.sid_value(prop(orc.mask_forward(u0, mm, direction)), target)[0].sum()
+
+    v = prop(orc.mask_forward(u0, m, direction))
+    dv = prop(orc.sid_backward(v, target), orc.BACKWARD)
+    _, gm = orc.mask_backward(dv, m, u0, direction)
+    d = rng.standard_normal(m.shape) + 1j * rng.standard_normal(m.shape)
+    _fd_check(loss, lambda dd: np.real(np.sum(np.conj(gm) * dd)), m, d)
+
+
+@pytest.mark.parametrize("direction", [1, -1])
+def test_fd_bpm(direction):
+    n, ds, lam, n0, L = 32, (0.5, 0.5), 1.064, 1.45, 12.0
+    rng = np.random.default_rng(11)
+    u0 = gauss_field(n, ds, 4.0).astype(complex)
+    dn = 5e-3 * rng.standard_normal((6, n, n))
+    target = np.abs(gauss_field(n, ds, 3.0)) ** 2
+
+    def loss(d):
+        v, _ = orc.bpm_forward(u0, ds[0], ds[1], lam, L, n0, d, direction)
+        return orc.sid_value(v, target)[0].sum()
+
+    v, saves = orc.bpm_forward(u0, ds[0], ds[1], lam, L, n0, dn, direction, save=True)
+    _, g = orc.bpm_backward(orc.sid_backward(v, target), ds[0], ds[1], lam, L, n0, dn, saves, direction)
+    d = rng.standard_normal(dn.shape)
+    _fd_check(loss, lambda dd: np.sum(g * dd), dn, d, eps=1e-7)
+
+
+# --- TVProx against a loop-by-loop restatement of tv_prox.jl:1-59 ---------------------
+def _loop_tv(y0, lam, n_iter, eta=0.25):
+    ny, nx = y0.shape
+    y0 = y0.copy()
+    p = np.zeros((2, ny, nx))
+    dp = np.zeros_like(p)
+    xk = p.copy()
+    t = 1.0
+
+    def dt(p):
+        a = np.zeros((ny, nx))
+        for j in range(ny):
+            for i in range(1, nx):
+                a[j, i] = p[0, j, i - 1] - p[0, j, i]
+        for j in range(1, ny):
+            for i in range(nx):
+                a[j, i] += p[1, j - 1, i] - p[1, j, i]
+        for j in range(ny):
+            a[j, 0] = -p[0, j, 0]
+        for i in range(nx):
+            a[0, i] = -p[1, 0, i]
+        return a
+
+    for _ in range(n_iter):
+        y = lam * dt(p) - y0
+        for j in range(ny):
+            for i in range(nx - 1):
+                dp[0, j, i] = y[j, i + 1] - y[j, i]
+        for j in range(ny - 1):
+            for i in range(nx):
+                dp[1, j, i] = y[j + 1, i] - y[j, i]
+        tn = (1 + math.sqrt(1 + 4 * t * t)) / 2
+        beta = (t - 1) / tn
+        newdx = eta * eta * dp - beta * (p - xk)
+        xk = p.copy()
+        p = p - newdx
+        t = tn
+        for k in range(2):
+            nr = np.linalg.norm(p[k])
+            if nr > 1:
+                p[k] /= nr
+    return y0 - lam * dt(p)
+
+
+def test_tv_prox_matches_loops():
+    rng = np.random.default_rng(2)
+    y0 = rng.standard_normal((9, 11))
+    ref = _loop_tv(y0, 0.3, 7)
+    got = orc.tv_prox(y0.copy(), 0.3, 7)
+    assert np.max(np.abs(got - ref)) < 1e-12
+
+
+def test_tv_prox_smooths():
+    rng = np.random.default_rng(4)
+    x = np.outer(np.sin(0.1 * np.arange(64)), np.sin(0.1 * np.arange(64))) * 5 + rng.standard_normal((64, 64))
+    v0 = np.var(x)
+    orc.tv_prox(x, 0.1, 100)
+    assert np.var(x) < v0
