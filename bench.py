@@ -1,0 +1,477 @@
+"""Benchmark of the GB300 scalar-propagation hot path.
+
+Workload (default): the 2048 x 2048 multi-wavelength, multi-mode batch -- 48
+fields (3 wavelengths 0.640 / 0.538 / 0.455 um x 16 Hermite-Gauss modes, waist
+80 um, ds = 0.5 um), cascade Phase -> ASProp(5000 um) -> Phase -> ASProp ->
+Phase -> ASProp, SquaredIntensityDifference against a per-wavelength target,
+gradient with respect to the three masks and one Fista + ClampProx step,
+captured as one CUDA graph.  One step = one optimisation iteration =
+3 forward + 3 adjoint propagations of 48 fields = 288 propagations.
+
+Inputs are synthetic and seeded (the reference publishes no dataset for this
+path).  All fields live in HBM (1.5 GiB per field batch, > L2), so no L2 flush
+is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the FP64 CPU restatement of the reference path (the
+oracle; the Julia reference cannot run here) on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 2048
+DS = (0.5, 0.5)
+LAMBDAS = (0.640, 0.538, 0.455)
+N_MODES = 16
+W0 = 80.0
+Z = 5000.0
+N_MASKS = 3
+ETA = 2e-4
+SEED = 1234
+METRIC = "fwd+adjoint propagations/s"
+UNIT = "propagations/s"
+WORKLOAD = "2048x2048 x {fields} fields (3 lambdas x HG modes), 3 trainable phase masks, ASProp z=5000um, " \
+           "SquaredIntensityDifference, fwd+adjoint+Fista/ClampProx step in one CUDA graph"
+
+
+def hg_orders():
+    # hermite_gaussian_groups(w0, 5) gives the 15 modes with m+n <= 4; the 16th is HG(5,0)
+    orders = [(m, n) for m in range(5) for n in range(5 - m)]
+    return orders + [(5, 0)]
+
+
+def make_inputs(n=N):
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(SEED)
+    x = (np.arange(n) - (n - 1) / 2) * DS[0]
+    y = (np.arange(n) - (n - 1) / 2) * DS[1]
+
+    def hg(m, k):
+        def one(q, s):
+            c = (2 / math.pi) ** 0.25 / math.sqrt(W0) / math.sqrt(2.0 ** q * math.factorial(q))
+            h0 = np.ones_like(s)
+            if q > 0:
+                h1 = 2 * np.sqrt(2) * s / W0
+                hp = h0
+                for j in range(1, q):
+                    hp, h1 = h1, 2 * np.sqrt(2) * s / W0 * h1 - 2 * j * hp
+                h0 = h1
+            return c * h0 * np.exp(-(s / W0) ** 2)
+        return (one(k, y)[:, None] * one(m, x)[None, :]).astype(np.complex64)
+
+    modes = np.stack([hg(m, k) for (m, k) in hg_orders()[:N_MODES]])  # (modes, n, n)
+    fields = np.broadcast_to(modes[:, None], (N_MODES, len(LAMBDAS), n, n)).copy()  # Julia (n, n, 3, 16)
+    masks = []
+    for _ in range(N_MASKS):
+        w = gaussian_filter(rng.standard_normal((n, n)), 8.0)
+        masks.append((np.pi * w / np.max(np.abs(w))).astype(np.float32))
+    targets = []
+    for _ in LAMBDAS:
+        t = gaussian_filter(rng.standard_normal((n, n)), 32.0) ** 2
+        t *= N_MODES / (t.sum() * DS[0] * DS[1])
+        targets.append(t.astype(np.float32))
+    return fields, masks, np.stack(targets)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GB300 path
+# ---------------------------------------------------------------------------
+def build_system(fo, fields_np, masks_np, targets_np):
+    import torch
+    u0 = fo.ScalarField(torch.from_numpy(fields_np).cuda(), DS, np.array(LAMBDAS))
+    phases = [fo.Phase(u0, m, trainable=True, buffered=True) for m in masks_np]
+    prop = fo.ASProp(u0, Z)
+    comps = []
+    for ph in phases:
+        comps += [ph, prop]
+    system = fo.OpticalSystem(fo.ScalarSource(u0), comps)
+    metric = fo.SquaredIntensityDifference((u0, targets_np))
+    rule = fo.ProxRule(fo.Fista(ETA), fo.ClampProx(-np.pi, np.pi))
+    opt = fo.setup(rule, system)
+    return u0, system, metric, opt, phases
+
+
+def iteration(fo, system, metric, opt, x, du, src):
+    tape = []
+    system.forward(x, tape, src=src)
+    loss = metric(x)
+    grads = system.backward(du, tape, seed=(metric, x))
+    fo.update_(opt, system, grads)
+    return loss
+
+
+def algorithmic_bytes_per_step(n=N, batch=None):
+    batch = batch or N_MODES * len(LAMBDAS)
+    n2 = n * n
+    props = 2 * N_MASKS * batch * 16 * n2                 # read + write one c32 field per propagation
+    fwd_phase = N_MASKS * (4 * n2 + 8 * n2 * batch)       # mask read + saved input written
+    adj_phase = N_MASKS * (8 * n2 * batch + 4 * n2)       # saved input read + gradient written
+    h = 2 * N_MASKS * len(LAMBDAS) * 8 * n2               # one transfer function per wavelength per pass
+    fista = N_MASKS * 6 * 4 * n2                          # x, xk, dx read; x, xk, newdx written
+    return props + fwd_phase + adj_phase + h + fista
+
+
+def col_pass_bytes(n=N, batch=None):
+    batch = batch or N_MODES * len(LAMBDAS)
+    # one column pass over the batch: every field read and written once, one
+    # transfer-function table per wavelength
+    return batch * 16 * n * n + len(LAMBDAS) * 8 * n * n
+
+
+def run_gb300(args, rank, world):
+    import torch
+    from __graft_entry__ import build, load_package
+
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    build()
+    fo = load_package()
+    lib = fo.load_library()
+    fields_np, masks_np, targets_np = make_inputs()
+    u0, system, metric, opt, phases = build_system(fo, fields_np, masks_np, targets_np)
+    batch = u0.batch
+    props_per_step = 2 * N_MASKS * batch
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        src = system.source.u0
+        x = src.similar()
+        du = src.similar()
+        iteration(fo, system, metric, opt, x, du, src)   # creates every plan before the capture
+        torch.cuda.synchronize()
+        sp = C.c_void_p(stream.cuda_stream)
+        g = C.c_void_p()
+        fo._capi.check(lib.fo_graph_begin(sp))
+        loss_t = iteration(fo, system, metric, opt, x, du, src)
+        fo._capi.check(lib.fo_graph_end(sp, C.byref(g)))
+        nk = C.c_int()
+        fo._capi.check(lib.fo_graph_info(g, C.byref(nk)))
+        for _ in range(args.warmup):
+            fo._capi.check(lib.fo_graph_launch(g, sp))
+        stream.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                fo._capi.check(lib.fo_graph_launch(g, sp))
+            e1.record(stream)
+            stream.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dist.barrier()
+            ms = float(t.item())
+        final_loss = float(loss_t.sum())
+
+        # per-pass device times of the same iteration, eager, events around every pass
+        fo._capi.check(lib.fo_profile_begin())
+        for _ in range(2):
+            iteration(fo, system, metric, opt, x, du, src)
+        arr_ms = (C.c_double * 3)()
+        arr_n = (C.c_int * 3)()
+        fo._capi.check(lib.fo_profile_end(arr_ms, arr_n))
+        col_ms = arr_ms[2] / max(1, arr_n[2])
+        pass_ms = {"row_single": arr_ms[0] / max(1, arr_n[0]), "row_fused": arr_ms[1] / max(1, arr_n[1]),
+                   "col": col_ms}
+        pass_share = {k: arr_ms[i] / max(1e-9, sum(arr_ms)) for i, k in enumerate(pass_ms)}
+
+        # end to end through the public C ABI with host buffers: H2D of the 48 input
+        # fields from pinned memory, the captured iteration, D2H of the loss
+        host_in = torch.from_numpy(fields_np).pin_memory()
+        host_loss = torch.empty(len(LAMBDAS), dtype=torch.float32).pin_memory()
+        torch.cuda.synchronize()
+        e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e2_steps = max(1, min(args.steps, 5))
+        e2.record(stream)
+        for _ in range(e2_steps):
+            src.electric.copy_(host_in, non_blocking=True)
+            fo._capi.check(lib.fo_graph_launch(g, sp))
+            host_loss.copy_(metric.loss, non_blocking=True)
+        e3.record(stream)
+        stream.synchronize()
+        e2e_ms = e2.elapsed_time(e3) / e2_steps
+        fo._capi.check(lib.fo_graph_destroy(g))
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = col_pass_bytes() / (col_ms * 1e-3) / 1e9
+    traffic = read_traffic()
+    value = props_per_step * world / (ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c32 (fp32 complex; fp64 transfer-function phase)",
+        "data": "synthetic, seeded (HG modes, Gaussian-filtered random masks and targets)",
+        "config": {"workload": WORKLOAD.format(fields=batch), "grid": N, "fields": batch, "masks": N_MASKS,
+                   "props_per_step": props_per_step, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (1.5 GiB field batch), no flush"},
+        "algorithmic_gb_per_step": round(algorithmic_bytes_per_step() / 1e9, 3),
+        "algorithmic_gbs": round(algorithmic_bytes_per_step() / (ms * 1e-3) / 1e9, 1),
+        "roofline": {"bound": "hbm", "kernel": "col_pass_kernel<2048> (FFT_y * H * IFFT_y over 48 fields)",
+                     "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(achieved / hbm_peak, 4), "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": col_pass_bytes()},
+        "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()},
+        "pass_share": {k: round(v, 3) for k, v in pass_share.items()},
+        "gpu_launches": int(nk.value) * args.steps,
+        "gpu_launches_per_step": int(nk.value),
+        "e2e": {"value": round(props_per_step / (e2e_ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
+                "h2d_bytes_per_step": int(fields_np.nbytes), "d2h_bytes_per_step": int(host_loss.numel() * 4)},
+        "clocks": clk.summary(),
+        "final_loss": final_loss,
+    }
+    return line
+
+
+def read_traffic():
+    """DRAM bytes per column-pass launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "col_pass_2048x48_traffic.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_launch"):
+                return int(float(ln.split("=")[1]))
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# plain cuFFT + elementwise path (the reference's CUDA.jl launch sequence in torch)
+# ---------------------------------------------------------------------------
+def run_plain(steps=3, warmup=1):
+    import torch
+    fields_np, masks_np, targets_np = make_inputs()
+    dev = "cuda"
+    u0 = torch.from_numpy(fields_np).to(dev).reshape(-1, N, N)
+    B = u0.shape[0]
+    lam_f = np.tile(np.array(LAMBDAS), N_MODES)
+    fx = torch.fft.fftfreq(N, DS[0], dtype=torch.float64, device=dev)
+    fy = torch.fft.fftfreq(N, DS[1], dtype=torch.float64, device=dev)
+    H = {}
+    for lam in LAMBDAS:
+        arg = (1 / lam ** 2 - fx[None, :] ** 2 - fy[:, None] ** 2).to(torch.complex128)
+        H[lam] = torch.exp(1j * 2 * np.pi * Z * torch.sqrt(arg)).to(torch.complex64)
+    phis = [torch.from_numpy(m).to(dev) for m in masks_np]
+    xks = [p.clone() for p in phis]
+    ts = [1.0] * N_MASKS
+    target = torch.from_numpy(targets_np).to(dev)
+
+    def prop(u, conj):
+        u = torch.fft.fft2(u)
+        for b in range(B):                       # one multiply launch per trailing slice
+            h = H[lam_f[b]]
+            u[b] *= h.conj() if conj else h
+        return torch.fft.ifft2(u)
+
+    def step():
+        u = u0.clone()
+        saves = []
+        for k in range(N_MASKS):
+            saves.append(u.clone())
+            u = u * torch.exp(1j * phis[k])
+            u = prop(u, False)
+        inten = (u.abs() ** 2).reshape(N_MODES, len(LAMBDAS), N, N).sum(0)
+        r = inten - target
+        loss = (r ** 2).sum()
+        du = 4 * r.repeat(N_MODES, 1, 1) * u
+        for k in reversed(range(N_MASKS)):
+            du = prop(du, True)
+            du = du * torch.exp(-1j * phis[k])
+            g = torch.imag(du * saves[k].conj()).sum(0)
+            tn = (1 + np.sqrt(1 + 4 * ts[k] ** 2)) / 2
+            beta = (ts[k] - 1) / tn
+            newdx = ETA ** 2 * g - beta * (phis[k] - xks[k])
+            xks[k] = phis[k].clone()
+            phis[k] -= newdx
+            phis[k].clamp_(-np.pi, np.pi)
+            ts[k] = tn
+        return loss
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": round(2 * N_MASKS * B / (ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(ms, 3),
+            "impl": "torch.fft (cuFFT) + per-slice elementwise launches, the reference's CUDA.jl sequence"}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the FP64 oracle (restatement of the reference path)
+# ---------------------------------------------------------------------------
+def run_cpu_sample(budget_s=12.0, threads=None):
+    from oracle import fluxoptics_oracle as orc
+    threads = threads or os.cpu_count() or 1
+    orc.set_workers(threads)
+    fields_np, masks_np, targets_np = make_inputs()
+    u0 = fields_np[0, 0].astype(np.complex128)      # HG00 at lambda = 0.640 um
+    lam = LAMBDAS[0]
+    phis = [m.astype(np.float64) for m in masks_np]
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        v = u0
+        saves = []
+        for k in range(N_MASKS):
+            saves.append(v)
+            v = orc.asprop(orc.phase_forward(v, phis[k]), DS[0], DS[1], lam, Z)
+        dv = orc.sid_backward(v, targets_np[0])
+        for k in reversed(range(N_MASKS)):
+            dv = orc.asprop(dv, DS[0], DS[1], lam, Z, orc.BACKWARD)
+            dv, _ = orc.phase_backward(dv, phis[k], saves[k])
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or reps >= 50:
+            break
+    return {"value": round(2 * N_MASKS * reps / el, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{reps} x (1 of 48 fields, HG00 at 0.640 um, 2048^2) through the 3-mask chain, "
+                      f"forward + adjoint, FP64 numpy/scipy.fft with {threads} workers, {el:.1f} s"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain cuFFT comparison")
+    ap.add_argument("--modes", type=int, default=16,
+                    help="modes per wavelength (default 16; smaller values only for profiler captures)")
+    args = ap.parse_args()
+    global N_MODES
+    N_MODES = args.modes
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        run_cpu_sample(budget_s=0.0)  # warm-up: one repetition
+        samples = []
+        for _ in range(args.steps):
+            s = run_cpu_sample(budget_s=max(2.0, 60.0 / max(1, args.steps)))
+            samples.append(s)
+            vals.append(s["value"])
+        v = statistics.median(vals)
+        cpu = dict(samples[0])
+        cpu["value"] = v
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(2 * N_MASKS * 48 / v * 1e3, 1),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)",
+                "data": "synthetic, seeded", "config": {"workload": WORKLOAD.format(fields=48), "grid": N, "fields": 48},
+                "cpu_baseline": cpu,
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "Julia is absent on this box: the reference arm is the FP64 oracle restatement of the "
+                        "reference's CPU path (FFTW replaced by pocketfft), timed on a bounded sample"}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    line = run_gb300(args, rank, world)
+    if rank == 0:
+        if not args.no_plain:
+            line["plain_cufft"] = run_plain()
+            line["speedup_vs_plain_cufft"] = round(line["value"] / line["plain_cufft"]["value"] / world, 2)
+        if not args.no_cpu and world == 1:
+            line["cpu_baseline"] = run_cpu_sample()
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

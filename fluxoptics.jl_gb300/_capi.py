@@ -41,6 +41,8 @@ SIGNATURES = {
     "fo_version": (_i, []),
     "fo_last_error": (C.c_char_p, []),
     "fo_stream_synchronize": (_i, [_vp]),
+    "fo_profile_begin": (_i, []),
+    "fo_profile_end": (_i, [_pd, _pi]),
     "fo_asprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i]),
     "fo_rsprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _i]),
     "fo_prop_destroy": (_i, [_vp]),
@@ -53,6 +55,7 @@ SIGNATURES = {
     "fo_chain_create": (_i, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
     "fo_chain_destroy": (_i, [_vp]),
     "fo_chain_forward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp]),
+    "fo_chain_forward_from": (_i, [_vp, _vp, _vp, C.POINTER(fo_mod), _i, _vp]),
     "fo_chain_backward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _vp]),
     "fo_bpm_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i, _d, _i]),
     "fo_bpm_destroy": (_i, [_vp]),
@@ -71,6 +74,7 @@ SIGNATURES = {
     "fo_graph_begin": (_i, [_vp]),
     "fo_graph_end": (_i, [_vp, C.POINTER(_vp)]),
     "fo_graph_launch": (_i, [_vp, _vp]),
+    "fo_graph_info": (_i, [_vp, _pi]),
     "fo_graph_destroy": (_i, [_vp]),
 }
 

@@ -519,11 +519,16 @@ class OpticalSystem:
             lib.fo_chain_destroy(h)
 
     # -- execution ----------------------------------------------------------------
-    def forward(self, u: ScalarField, tape=None):
-        """Runs the system in place on u.  With a tape, trainable components save
-        their inputs and the tape records what the adjoint sweep needs."""
+    def forward(self, u: ScalarField, tape=None, src: ScalarField = None):
+        """Runs the system in place on u (or from ``src`` into u).  With a tape,
+        trainable components save their inputs and the tape records what the
+        adjoint sweep needs."""
         d = self.direction
-        for seg in self.segments(u):
+        for i, seg in enumerate(self.segments(u)):
+            from_src = src is not None and i == 0
+            if src is not None and i == 0 and not isinstance(seg, _Chain):
+                u.electric.copy_(src.electric)
+                from_src = False
             if isinstance(seg, _Chain):
                 mods = (fo_mod * len(seg.mods))()
                 saved = []
@@ -535,8 +540,12 @@ class OpticalSystem:
                     sv = m.get_saved_buffer(u) if (tape is not None and m.trainable) else None
                     mods[k] = m.fo_mod(saved=sv)
                     saved.append(sv)
-                _capi.call("fo_chain_forward", self._chain_handle(seg, u), _ptr(u.electric), mods, int(d),
-                           _stream())
+                if from_src:
+                    _capi.call("fo_chain_forward_from", self._chain_handle(seg, u), _ptr(src.electric),
+                               _ptr(u.electric), mods, int(d), _stream())
+                else:
+                    _capi.call("fo_chain_forward", self._chain_handle(seg, u), _ptr(u.electric), mods, int(d),
+                               _stream())
                 if tape is not None:
                     tape.append((seg, saved))
             else:
@@ -552,6 +561,8 @@ class OpticalSystem:
                     c.propagate_(u, d)
                     if tape is not None:
                         tape.append((c, None))
+        if src is not None and not self.components:
+            u.electric.copy_(src.electric)
         return u
 
     def backward(self, du: ScalarField, tape, seed=None):
@@ -605,8 +616,9 @@ class OpticalSystem:
     def __call__(self, x=None):
         if (x is None) == (self.source is None):
             raise ValueError("give exactly one of a source or an input field")
-        u = self.source.propagate() if x is None else x.copy()
-        self.forward(u)
+        src = self.source.u0 if x is None else x
+        u = src.similar()
+        self.forward(u, src=src)
         return {"out": u, "probes": {}}
 
 

@@ -135,6 +135,7 @@ struct fo_prop_plan_s {
   int n_tables = 0;
   float2* H = nullptr;          // n_tables x fy x fx, scaled by 1/(fx*fy)
   int* h_index = nullptr;       // device, per field
+  int* sorted_fields = nullptr; // device, fields ordered by transfer-function table
   float* inv_lambda = nullptr;  // device, per field
   const float2* tw_x = nullptr;
   const float2* tw_y = nullptr;
@@ -148,6 +149,7 @@ void plan_free(fo_prop_plan p) {
   if (!p) return;
   cudaFree(p->H);
   cudaFree(p->h_index);
+  cudaFree(p->sorted_fields);
   cudaFree(p->inv_lambda);
   cudaFree(p->scratch);
   delete p;
@@ -164,6 +166,33 @@ bool same_layout(const Layout& a, const Layout& b) {
   return a.nx == b.nx && a.ny == b.ny && a.batch == b.batch && a.fx == b.fx && a.fy == b.fy &&
          a.padded == b.padded;
 }
+
+// Optional per-pass timing of eager calls: CUDA events around every pass launch,
+// summed per pass kind (0 single row transform, 1 fused inverse+forward row
+// pass, 2 column pass) by fo_profile_end.
+struct ProfRec {
+  int kind;
+  cudaEvent_t a, b;
+};
+bool g_prof = false;
+std::vector<ProfRec> g_prof_recs;
+
+struct ProfScope {
+  int kind;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(int k, cudaStream_t s) : kind(k), st(s) {
+    if (!g_prof) return;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, st);
+  }
+  ~ProfScope() {
+    if (!a) return;
+    cudaEventRecord(b, st);
+    g_prof_recs.push_back({kind, a, b});
+  }
+};
 
 // Internal modulation description.
 struct Mod {
@@ -246,6 +275,7 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
     a.tidx = seed->tidx;
     a.dc = seed->dc;
   }
+  ProfScope prof(inv_first && fwd_after ? 1 : 0, st);
   FO_LAUNCH(launch_row_pass(L.fx, a, tw, st));
   return FO_OK;
 }
@@ -265,18 +295,20 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.conj_h = conj_h;
   a.fft_only = 0;
   a.batch = p->batch;
+  a.field_list = p->sorted_fields;
+  ProfScope prof(2, st);
   FO_LAUNCH(launch_col_pass(p->fy, a, p->tw_y, st));
   return FO_OK;
 }
 
 // Forward sweep: mods[0] -> props[0] -> ... -> props[K-1] -> mods[K], in place on u.
 int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, const Mod* mods, int s,
-                cudaStream_t st) {
+                cudaStream_t st, const float2* src = nullptr) {
   const int K = (int)props.size();
   const Layout L = layout_of(props[0]);
   const float* il = props[0]->inv_lambda;
   const float sf = (float)s;
-  FO_TRY(row_pass(L, u, buf, false, true, mods[0], false, sf, il, nullptr, props[0]->tw_x, st));
+  FO_TRY(row_pass(L, src ? src : u, buf, false, true, mods[0], false, sf, il, nullptr, props[0]->tw_x, st));
   for (int k = 0; k < K; ++k) {
     FO_TRY(col_pass(props[k], buf, s < 0, st));
     if (k + 1 < K)
@@ -353,6 +385,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   const size_t table = (size_t)fx * fy;
   if ((rc = dalloc(&p->H, table * p->n_tables, "transfer functions")) != FO_OK ||
       (rc = dalloc(&p->h_index, batch, "table index")) != FO_OK ||
+      (rc = dalloc(&p->sorted_fields, batch, "field order")) != FO_OK ||
       (rc = dalloc(&p->inv_lambda, batch, "inverse wavelengths")) != FO_OK) {
     plan_free(p);
     return rc;
@@ -377,7 +410,11 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   }
   std::vector<float> il(batch);
   for (int b = 0; b < batch; ++b) il[b] = (float)(1.0 / p->lambdas[b]);
+  std::vector<int> order(batch);
+  for (int b = 0; b < batch; ++b) order[b] = b;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hidx[a] < hidx[b]; });
   cudaError_t e = cudaMemcpy(p->h_index, hidx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->sorted_fields, order.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->inv_lambda, il.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     plan_free(p);
@@ -429,6 +466,34 @@ extern "C" {
 FO_API int fo_version(void) { return 1 * 10000 + 0 * 100 + 0; }
 
 FO_API const char* fo_last_error(void) { return g_last_error.c_str(); }
+
+FO_API int fo_profile_begin(void) {
+  g_prof = true;
+  return FO_OK;
+}
+
+FO_API int fo_profile_end(double* ms, int* launches) {
+  g_prof = false;
+  double acc[3] = {0, 0, 0};
+  int cnt[3] = {0, 0, 0};
+  int rc = FO_OK;
+  for (auto& r : g_prof_recs) {
+    float t = 0.f;
+    cudaError_t e = cudaEventSynchronize(r.b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.a, r.b);
+    if (e != cudaSuccess && rc == FO_OK) rc = cuda_fail(e, "cudaEventElapsedTime");
+    acc[r.kind] += t;
+    cnt[r.kind] += 1;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  g_prof_recs.clear();
+  for (int k = 0; k < 3; ++k) {
+    if (ms) ms[k] = acc[k];
+    if (launches) launches[k] = cnt[k];
+  }
+  return rc;
+}
 
 FO_API int fo_stream_synchronize(void* stream) {
   cudaError_t e = cudaStreamSynchronize(S(stream));
@@ -584,6 +649,22 @@ FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int dir
   float2* uu = reinterpret_cast<float2*>(u);
   float2* buf = chain->scratch ? chain->scratch : uu;
   return run_forward(chain->props, buf, uu, m.data(), direction, S(stream));
+}
+
+FO_API int fo_chain_forward_from(fo_chain chain, const void* u_in, void* u, const fo_mod* mods,
+                                 int direction, void* stream) {
+  if (!chain || !u_in || !u || !mods) return fail(FO_ERR_ARG, "chain, u_in, u and mods must not be NULL");
+  FO_TRY(check_dir(direction));
+  const int K = (int)chain->props.size();
+  std::vector<Mod> m(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    m[k] = mod_from(&mods[k]);
+    FO_TRY(validate_mod(m[k], false));
+  }
+  float2* uu = reinterpret_cast<float2*>(u);
+  float2* buf = chain->scratch ? chain->scratch : uu;
+  return run_forward(chain->props, buf, uu, m.data(), direction, S(stream),
+                     reinterpret_cast<const float2*>(u_in));
 }
 
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,
@@ -962,6 +1043,22 @@ FO_API int fo_graph_end(void* stream, fo_graph* graph) {
     return cuda_fail(e, "cudaGraphInstantiate");
   }
   *graph = g;
+  return FO_OK;
+}
+
+FO_API int fo_graph_info(fo_graph g, int* kernel_nodes) {
+  if (!g || !kernel_nodes) return fail(FO_ERR_ARG, "graph and kernel_nodes must not be NULL");
+  size_t n = 0;
+  FO_LAUNCH(cudaGraphGetNodes(g->graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  FO_LAUNCH(cudaGraphGetNodes(g->graph, nodes.data(), &n));
+  int k = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    FO_LAUNCH(cudaGraphNodeGetType(nd, &t));
+    if (t == cudaGraphNodeTypeKernel) ++k;
+  }
+  *kernel_nodes = k;
   return FO_OK;
 }
 

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(RowCfg<N>::ROWS*(N / RowCfg<N>::E))
 
   const int t = threadIdx.x % T;
   const int lane = threadIdx.x / T;
-  const int y = blockIdx.x * ROWS + lane;
+  const int y = blockIdx.y * ROWS + lane;
   const bool row_ok = y < a.nrows;
   float2* sm = smem + lane * SLOTS;
 
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(RowCfg<N>::ROWS*(N / RowCfg<N>::E))
 #pragma unroll
   for (int i = 0; i < GC; ++i) gacc_c[i] = make_float2(0.f, 0.f);
 
-  const int f0 = blockIdx.y * a.fields_per_cta;
+  const int f0 = blockIdx.x * a.fields_per_cta;
   const int f1 = min(a.batch, f0 + a.fields_per_cta);
   for (int f = f0; f < f1; ++f) {
     const int b = a.field_list ? a.field_list[f] : f;
@@ -223,9 +223,9 @@ __global__ void __launch_bounds__(ColCfg<N>::W*(N / ColCfg<N>::E))
 
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
-  const int col = blockIdx.x * W + c;
+  const int col = blockIdx.y * W + c;
   const bool col_ok = col < a.ncols;
-  const int f = blockIdx.y;
+  const int f = blockIdx.x;
   const int b = a.field_list ? a.field_list[f] : f;
   float2* buf = a.buf + (long long)b * a.bstride + col;
   const float2* H = a.fft_only ? nullptr : a.H + (long long)a.h_index[b] * a.h_stride + col;
@@ -292,7 +292,9 @@ template <int N>
 static cudaError_t row_launch(const RowPassArgs& a, const float2* tw, cudaStream_t s) {
   constexpr int ROWS = RowCfg<N>::ROWS;
   constexpr int threads = ROWS * (N / RowCfg<N>::E);
-  dim3 grid((a.nrows + ROWS - 1) / ROWS, (a.batch + a.fields_per_cta - 1) / a.fields_per_cta);
+  // fields vary fastest across the grid: CTAs that run together share the rows of
+  // the modulation parameters, which then stay in L2
+  dim3 grid((a.batch + a.fields_per_cta - 1) / a.fields_per_cta, (a.nrows + ROWS - 1) / ROWS);
   const bool grad = a.mod_bwd && a.grad != nullptr && a.mod_kind != MOD_NONE;
   if (!grad)
     row_pass_kernel<N, 0><<<grid, threads, 0, s>>>(a, tw);
@@ -315,7 +317,9 @@ static cudaError_t col_launch(const ColPassArgs& a, const float2* tw, cudaStream
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  dim3 grid((a.ncols + W - 1) / W, a.batch);
+  // fields (sorted by wavelength) vary fastest: the CTAs of one column tile run
+  // together and read the tile of their transfer function from L2
+  dim3 grid(a.batch, (a.ncols + W - 1) / W);
   col_pass_kernel<N><<<grid, threads, smem, s>>>(a, tw);
   return cudaGetLastError();
 }

@@ -59,9 +59,10 @@ def withgradient(metric: SquaredIntensityDifference, system: OpticalSystem, x=No
     """Loss sum_t c_t and the gradients of every trainable component, through
     the hand-written adjoint (the GPU counterpart of Zygote.withgradient over
     the reference's rrules, src/ChainRulesCoreExt.jl:21-111)."""
-    u = system.source.propagate() if x is None else x.copy()
+    src = system.source.u0 if x is None else x
+    u = src.similar()
     tape = []
-    system.forward(u, tape)
+    system.forward(u, tape, src=src)
     loss = metric(u)
     du = u.similar()
     grads = system.backward(du, tape, seed=(metric, u))

@@ -67,6 +67,14 @@ FO_API const char* fo_last_error(void);
 /* Blocks until all work on `stream` is done; reports device-side errors. */
 FO_API int fo_stream_synchronize(void* stream);
 
+/* Per-pass timing of the calls made between begin and end (eager calls only,
+ * not graph replays): CUDA events around every pass launch.  ms[3] / launches[3]
+ * receive the summed device time and the launch count of the single row
+ * transforms, the fused inverse+forward row passes and the column passes.
+ * No counterpart in the reference (it has no profiling hooks). */
+FO_API int fo_profile_begin(void);
+FO_API int fo_profile_end(double* ms, int* launches);
+
 /* ---------------------------------------------------------------------- */
 /* Free-space propagators                                                  */
 /* ---------------------------------------------------------------------- */
@@ -183,6 +191,12 @@ FO_API int fo_chain_destroy(fo_chain chain);
 FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int direction,
                             void* stream);
 
+/* As fo_chain_forward, but the input is read from u_in (left unchanged) and the
+ * result written to u: the source copy of the reference's system call
+ * (sources/scalar_source.jl:69-72) fused into the first pass. */
+FO_API int fo_chain_forward_from(fo_chain chain, const void* u_in, void* u, const fo_mod* mods,
+                                 int direction, void* stream);
+
 /*
  * Adjoint sweep in reverse order, in place on du.  For every mod with a grad
  * pointer the gradient is written (mods[k].saved must then hold the input saved
@@ -291,6 +305,8 @@ typedef struct fo_graph_s* fo_graph;
 FO_API int fo_graph_begin(void* stream);
 FO_API int fo_graph_end(void* stream, fo_graph* graph);
 FO_API int fo_graph_launch(fo_graph graph, void* stream);
+/* Number of kernel nodes in a captured graph. */
+FO_API int fo_graph_info(fo_graph graph, int* kernel_nodes);
 FO_API int fo_graph_destroy(fo_graph graph);
 
 #ifdef __cplusplus
