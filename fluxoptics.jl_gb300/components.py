@@ -97,6 +97,7 @@ class Component:
 
 class _Propagator(Component):
     kind = None
+    autotune = True  # time the launch shapes of the passes at plan creation (cached per grid)
 
     def __init__(self, u: ScalarField, z, ds=None):
         self.z = float(z)
@@ -153,7 +154,7 @@ class ASProp(_Propagator):
     def _create(self, u, lam):
         h = C.c_void_p()
         _capi.call("fo_asprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
-                   _capi.dvec(lam), len(lam), self.z, self.n0, 0)
+                   _capi.dvec(lam), len(lam), self.z, self.n0, int(self.autotune))
         return h
 
 
@@ -185,7 +186,7 @@ class RSProp(_Propagator):
     def _create(self, u, lam):
         h = C.c_void_p()
         _capi.call("fo_rsprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
-                   _capi.dvec(lam), len(lam), self.z, 0)
+                   _capi.dvec(lam), len(lam), self.z, int(self.autotune))
         return h
 
 
@@ -358,7 +359,7 @@ class AS_BPM(Component):
             h = C.c_void_p()
             _capi.call("fo_bpm_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
                        _capi.dvec(lam), len(lam), self.thickness, self.n0, self.n_slices,
-                       self.checkpoint_every, 1.0, 0)
+                       self.checkpoint_every, 1.0, 1)
             self._bpms[key] = h
         return h
 

@@ -5,7 +5,11 @@
 #include <cmath>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
+#include <tuple>
 #include <map>
 #include <mutex>
 #include <string>
@@ -136,6 +140,10 @@ struct fo_prop_plan_s {
   float2* H = nullptr;          // n_tables x fy x fx, scaled by 1/(fx*fy)
   int* h_index = nullptr;       // device, per field
   int* sorted_fields = nullptr; // device, fields ordered by transfer-function table
+  int* items = nullptr;         // device, n_items+1 offsets into sorted_fields (runs of one table)
+  int n_items = 0;
+  int row_v = 0, col_v = 0;     // launch-shape variants (autotuned or default)
+  bool row_pf = true, col_pf = true;
   float* inv_lambda = nullptr;  // device, per field
   const float2* tw_x = nullptr;
   const float2* tw_y = nullptr;
@@ -150,6 +158,7 @@ void plan_free(fo_prop_plan p) {
   cudaFree(p->H);
   cudaFree(p->h_index);
   cudaFree(p->sorted_fields);
+  cudaFree(p->items);
   cudaFree(p->inv_lambda);
   cudaFree(p->scratch);
   delete p;
@@ -158,9 +167,13 @@ void plan_free(fo_prop_plan p) {
 struct Layout {
   int nx, ny, batch, fx, fy;
   bool padded;
+  int row_v;
+  bool row_pf;
 };
 
-Layout layout_of(const fo_prop_plan_s* p) { return Layout{p->nx, p->ny, p->batch, p->fx, p->fy, p->kind == 1}; }
+Layout layout_of(const fo_prop_plan_s* p) {
+  return Layout{p->nx, p->ny, p->batch, p->fx, p->fy, p->kind == 1, p->row_v, p->row_pf};
+}
 
 bool same_layout(const Layout& a, const Layout& b) {
   return a.nx == b.nx && a.ny == b.ny && a.batch == b.batch && a.fx == b.fx && a.fy == b.fy &&
@@ -246,7 +259,7 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
   a.n_valid = L.nx;
   a.batch = L.batch;
   const bool grad = bwd && mod.kind != MOD_NONE && mod.grad != nullptr;
-  a.fields_per_cta = grad ? L.batch : 1;
+  a.fields_per_cta = grad ? L.batch : std::min(L.batch, 8);
   a.field_list = nullptr;
   a.inv_first = inv_first;
   a.fwd_after = fwd_after;
@@ -275,8 +288,11 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
     a.tidx = seed->tidx;
     a.dc = seed->dc;
   }
+  const int load_n = inv_first ? L.fx : L.nx;
+  const bool pf = L.row_pf && load_n == L.fx && row_prefetch_fits(L.fx, L.row_v) &&
+                  !(grad && mod.kind == MOD_MASK);
   ProfScope prof(inv_first && fwd_after ? 1 : 0, st);
-  FO_LAUNCH(launch_row_pass(L.fx, a, tw, st));
+  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, pf, a, tw, st));
   return FO_OK;
 }
 
@@ -296,8 +312,11 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.fft_only = 0;
   a.batch = p->batch;
   a.field_list = p->sorted_fields;
+  a.item_start = p->items;
+  a.n_items = p->n_items;
+  const bool pf = p->col_pf && col_prefetch_fits(p->fy, p->col_v);
   ProfScope prof(2, st);
-  FO_LAUNCH(launch_col_pass(p->fy, a, p->tw_y, st));
+  FO_LAUNCH(launch_col_pass(p->fy, p->col_v, pf, a, p->tw_y, st));
   return FO_OK;
 }
 
@@ -338,8 +357,144 @@ int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du
   return FO_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: times every launch-shape variant (with and without cp.async
+// staging) of the row and column passes on the plan's grid and keeps the
+// fastest.  Results are cached per (kind, fx, fy, ny, fields) for the process.
+// FO_ROW_VARIANT / FO_COL_VARIANT / FO_PREFETCH=0 override the choice.
+// ---------------------------------------------------------------------------
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, std::tuple<int, bool, int, bool>> g_tune;
+
+int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  return (v && *v) ? atoi(v) : dflt;
+}
+
+float time_launches(const std::function<cudaError_t()>& fn, int reps) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 1e30f;
+  if (fn() != cudaSuccess) best = -1.f;  // warm-up (and a launch-failure probe)
+  for (int r = 0; r < reps && best >= 0.f; ++r) {
+    cudaEventRecord(a, 0);
+    if (fn() != cudaSuccess) {
+      best = -1.f;
+      break;
+    }
+    cudaEventRecord(b, 0);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaGetLastError();
+  return best;
+}
+
+int autotune_plan(fo_prop_plan p) {
+  const int nb = std::min(p->batch, 8);
+  const auto key = std::make_tuple(p->kind, p->fx, p->fy, p->ny, nb);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      std::tie(p->row_v, p->row_pf, p->col_v, p->col_pf) = it->second;
+      return FO_OK;
+    }
+  }
+  float2* tmp = nullptr;
+  int* idx = nullptr;
+  FO_TRY(dalloc(&tmp, (size_t)nb * p->ny * p->fx, "autotune buffer"));
+  if (dalloc(&idx, 2 * (size_t)nb + 2, "autotune indices") != FO_OK) {
+    cudaFree(tmp);
+    return FO_ERR_ALLOC;
+  }
+  std::vector<int> hidx(2 * nb + 2, 0);
+  for (int i = 0; i < nb; ++i) hidx[i] = i;                     // field list
+  for (int i = 0; i <= (nb + 3) / 4; ++i) hidx[nb + i] = std::min(nb, 4 * i);  // runs of 4
+  const int n_items = (nb + 3) / 4;
+  cudaMemcpy(idx, hidx.data(), sizeof(int) * hidx.size(), cudaMemcpyHostToDevice);
+  cudaMemset(tmp, 0, sizeof(float2) * (size_t)nb * p->ny * p->fx);
+  float best = 1e30f;
+  int bv = 0;
+  bool bpf = false;
+  for (int v = 0; v < row_variant_count(p->fx); ++v) {
+    for (int pf = 0; pf < 2; ++pf) {
+      if (pf && !row_prefetch_fits(p->fx, v)) continue;
+      RowPassArgs a;
+      std::memset(&a, 0, sizeof(a));
+      a.src = tmp;
+      a.dst = tmp;
+      a.src_bstride = a.dst_bstride = (long long)p->fx * p->ny;
+      a.src_ld = a.dst_ld = p->fx;
+      a.nrows = p->ny;
+      a.n_valid = p->nx;
+      a.batch = nb;
+      a.fields_per_cta = nb;
+      a.inv_first = 1;
+      a.fwd_after = 1;
+      const float ms = time_launches([&] { return launch_row_pass(p->fx, v, pf != 0, a, p->tw_x, 0); }, 3);
+      if (ms >= 0.f && ms < best) {
+        best = ms;
+        bv = v;
+        bpf = pf != 0;
+      }
+    }
+  }
+  p->row_v = bv;
+  p->row_pf = bpf;
+  best = 1e30f;
+  bv = 0;
+  bpf = false;
+  for (int v = 0; v < col_variant_count(p->fy); ++v) {
+    for (int pf = 0; pf < 2; ++pf) {
+      if (pf && !col_prefetch_fits(p->fy, v)) continue;
+      ColPassArgs a;
+      std::memset(&a, 0, sizeof(a));
+      a.buf = tmp;
+      a.bstride = (long long)p->fx * p->ny;
+      a.ld = p->fx;
+      a.ncols = p->fx;
+      a.y_in = a.y_out = p->ny;
+      a.H = p->H;
+      a.h_stride = (long long)p->fx * p->fy;
+      a.h_index = p->h_index;
+      a.batch = nb;
+      a.field_list = idx;
+      a.item_start = idx + nb;
+      a.n_items = n_items;
+      const float ms = time_launches([&] { return launch_col_pass(p->fy, v, pf != 0, a, p->tw_y, 0); }, 3);
+      if (ms >= 0.f && ms < best) {
+        best = ms;
+        bv = v;
+        bpf = pf != 0;
+      }
+    }
+  }
+  p->col_v = bv;
+  p->col_pf = bpf;
+  cudaFree(tmp);
+  cudaFree(idx);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "autotuning");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = std::make_tuple(p->row_v, p->row_pf, p->col_v, p->col_pf);
+  return FO_OK;
+}
+
+void apply_overrides(fo_prop_plan p) {
+  const int rv = env_int("FO_ROW_VARIANT", -1), cv = env_int("FO_COL_VARIANT", -1);
+  if (rv >= 0 && rv < row_variant_count(p->fx)) p->row_v = rv;
+  if (cv >= 0 && cv < col_variant_count(p->fy)) p->col_v = cv;
+  if (env_int("FO_PREFETCH", 1) == 0) p->row_pf = p->col_pf = false;
+}
+
 int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx, double dy,
-              const double* lambdas, int n_lambdas, double z, double n0) {
+              const double* lambdas, int n_lambdas, double z, double n0, int flags) {
   if (!out) return fail(FO_ERR_ARG, "plan output pointer is NULL");
   *out = nullptr;
   if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
@@ -386,6 +541,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   if ((rc = dalloc(&p->H, table * p->n_tables, "transfer functions")) != FO_OK ||
       (rc = dalloc(&p->h_index, batch, "table index")) != FO_OK ||
       (rc = dalloc(&p->sorted_fields, batch, "field order")) != FO_OK ||
+      (rc = dalloc(&p->items, batch + 1, "field runs")) != FO_OK ||
       (rc = dalloc(&p->inv_lambda, batch, "inverse wavelengths")) != FO_OK) {
     plan_free(p);
     return rc;
@@ -413,8 +569,18 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   std::vector<int> order(batch);
   for (int b = 0; b < batch; ++b) order[b] = b;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hidx[a] < hidx[b]; });
+  // column-pass work items: runs of at most kFieldsPerItem fields sharing one table
+  const int kFieldsPerItem = 4;
+  std::vector<int> items{0};
+  for (int i = 1; i <= batch; ++i) {
+    if (i == batch || hidx[order[i]] != hidx[order[i - 1]] || i - items.back() >= kFieldsPerItem)
+      items.push_back(i);
+  }
+  p->n_items = (int)items.size() - 1;
   cudaError_t e = cudaMemcpy(p->h_index, hidx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->sorted_fields, order.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->items, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->inv_lambda, il.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     plan_free(p);
@@ -429,7 +595,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
       e = launch_rs_h_spatial(Hi, nx, ny, fx, fy, dx, dy, uniq[i], z, scale, 0);
       if (e == cudaSuccess) {
         // H_RS = FFT2(h): row transforms of all fy rows, then column transforms
-        Layout L{fx, fy, 1, fx, fy, false};
+        Layout L{fx, fy, 1, fx, fy, false, 0, false};
         Mod none;
         rc = row_pass(L, Hi, Hi, false, true, none, false, 1.f, nullptr, nullptr, p->tw_x, 0);
         if (rc != FO_OK) {
@@ -446,7 +612,8 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
         a.y_out = fy;
         a.fft_only = 1;
         a.batch = 1;
-        e = launch_col_pass(fy, a, p->tw_y, 0);
+        a.n_items = 1;
+        e = launch_col_pass(fy, 0, false, a, p->tw_y, 0);
       }
     }
   }
@@ -455,6 +622,21 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     plan_free(p);
     return cuda_fail(e, "building transfer functions");
   }
+  // FO_AUTOTUNE=0 / =1 in the environment forces the tuner off / on
+  const int tune_env = env_int("FO_AUTOTUNE", -1);
+  if (tune_env == 1 || (tune_env != 0 && (flags & FO_FLAG_AUTOTUNE))) {
+    rc = autotune_plan(p);
+    if (rc != FO_OK) {
+      plan_free(p);
+      return rc;
+    }
+  }
+  apply_overrides(p);
+  if (env_int("FO_VERBOSE", 0))
+    fprintf(stderr, "[fluxoptics_gb300] plan %s %dx%d (fft %dx%d) batch %d: row variant %d (E=%d, lanes=%d, pf=%d), col variant %d (E=%d, lanes=%d, pf=%d)\n",
+            kind == 0 ? "AS" : "RS", nx, ny, fx, fy, batch, p->row_v, row_variant(fx, p->row_v).E,
+            row_variant(fx, p->row_v).lanes, (int)p->row_pf, p->col_v, col_variant(fy, p->col_v).E,
+            col_variant(fy, p->col_v).lanes, (int)p->col_pf);
   *out = p;
   return FO_OK;
 }
@@ -503,14 +685,12 @@ FO_API int fo_stream_synchronize(void* stream) {
 
 FO_API int fo_asprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
                             const double* lambdas, int n_lambdas, double z, double n0, int flags) {
-  (void)flags;
-  return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0);
+  return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0, flags);
 }
 
 FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
                             const double* lambdas, int n_lambdas, double z, int flags) {
-  (void)flags;
-  return make_plan(plan, 1, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, 1.0);
+  return make_plan(plan, 1, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, 1.0, flags);
 }
 
 FO_API int fo_prop_destroy(fo_prop_plan plan) {
@@ -714,7 +894,6 @@ extern "C" {
 FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
                          const double* lambdas, int n_lambdas, double thickness, double n0,
                          int n_slices, int checkpoint_every, double cos_correction, int flags) {
-  (void)flags;
   if (!bpm) return fail(FO_ERR_ARG, "bpm output pointer is NULL");
   *bpm = nullptr;
   if (n_slices < 2) return fail(FO_ERR_SHAPE, "AS_BPM needs at least 2 slices");
@@ -722,8 +901,8 @@ FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, doub
   if (checkpoint_every < 0) return fail(FO_ERR_ARG, "checkpoint_every must be >= 0");
   const double dz = thickness / n_slices;
   fo_bpm b = new fo_bpm_s();
-  int rc = make_plan(&b->full, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz, n0);
-  if (rc == FO_OK) rc = make_plan(&b->half, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz / 2, n0);
+  int rc = make_plan(&b->full, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz, n0, flags);
+  if (rc == FO_OK) rc = make_plan(&b->half, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz / 2, n0, flags);
   if (rc != FO_OK) {
     plan_free(b->full);
     delete b;

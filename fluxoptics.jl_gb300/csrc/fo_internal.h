@@ -77,16 +77,29 @@ struct ColPassArgs {
   int conj_h;
   int fft_only;          // 1: store the forward transform along y (no H, no inverse)
   int batch;
-  const int* field_list;
+  const int* field_list;  // fields ordered so that each work item shares one table
+  const int* item_start;  // n_items+1 offsets into field_list (null: one field per item)
+  int n_items;
 };
 
-// Launchers (return cudaError_t from the launch).  N is the FFT length along the
-// transformed axis; supported: powers of two from 16 to 4096.
+// Launch-shape variants (fo_variants.h): E elements per thread, `lanes` rows or
+// columns per CTA.  N is the FFT length along the transformed axis; supported:
+// powers of two from 16 to 4096.  `pf` selects the cp.async-staged kernels.
+struct PassVariant {
+  int E;
+  int lanes;
+};
 bool fft_size_supported(int n);
-cudaError_t launch_row_pass(int N, const RowPassArgs& a, const float2* tw, cudaStream_t s);
-cudaError_t launch_col_pass(int N, const ColPassArgs& a, const float2* tw, cudaStream_t s);
-// Rows handled by one CTA of the row pass for length N (host-side grid sizing).
-int row_pass_rows_per_cta(int N);
+int row_variant_count(int N);
+int col_variant_count(int N);
+PassVariant row_variant(int N, int v);
+PassVariant col_variant(int N, int v);
+size_t row_smem_bytes(int N, int v, bool pf);
+size_t col_smem_bytes(int N, int v, bool pf);
+bool row_prefetch_fits(int N, int v);
+bool col_prefetch_fits(int N, int v);
+cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s);
+cudaError_t launch_col_pass(int N, int v, bool pf, const ColPassArgs& a, const float2* tw, cudaStream_t s);
 
 // Device twiddle table exp(-2 pi i m / N), m < N, for the current device (cached).
 const float2* twiddles(int N, int* err);

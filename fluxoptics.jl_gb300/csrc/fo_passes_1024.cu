@@ -1,0 +1,31 @@
+// Instantiations of the row / column passes for transform length 1024.
+#include "fo_passes.cuh"
+#include "fo_variants.h"
+
+namespace fo {
+
+cudaError_t row_launch_1024(int v, const RowPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
+  switch (v) {
+#define X(I, E, L) \
+  case I:          \
+    return row_launch_shape<1024, E, L>(a, tw, s, pf);
+    FO_ROW_VARIANTS_1024(X)
+#undef X
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t col_launch_1024(int v, const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
+  switch (v) {
+#define X(I, E, W) \
+  case I:          \
+    return col_launch_shape<1024, E, W>(a, tw, s, pf);
+    FO_COL_VARIANTS_1024(X)
+#undef X
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace fo

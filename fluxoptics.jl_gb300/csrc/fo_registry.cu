@@ -1,0 +1,100 @@
+// Dispatch of the row / column passes to their per-size launch-shape variants.
+#include "fo_fft.cuh"
+#include "fo_internal.h"
+#include "fo_variants.h"
+
+namespace fo {
+
+#define FO_DECL(NN)                                                                                  \
+  cudaError_t row_launch_##NN(int v, const RowPassArgs& a, const float2* tw, cudaStream_t s, bool pf); \
+  cudaError_t col_launch_##NN(int v, const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf);
+FO_FOR_EACH_N(FO_DECL)
+#undef FO_DECL
+
+namespace {
+
+struct Table {
+  int n = 0;
+  PassVariant v[8];
+};
+
+template <int N>
+Table row_table();
+template <int N>
+Table col_table();
+
+#define FO_TABLES(NN)                                             \
+  template <>                                                     \
+  Table row_table<NN>() {                                         \
+    Table t;                                                      \
+    FO_ROW_VARIANTS_##NN(FO_ADD) return t;                        \
+  }                                                               \
+  template <>                                                     \
+  Table col_table<NN>() {                                         \
+    Table t;                                                      \
+    FO_COL_VARIANTS_##NN(FO_ADD) return t;                        \
+  }
+#define FO_ADD(I, E, L) t.v[t.n++] = PassVariant{E, L};
+FO_FOR_EACH_N(FO_TABLES)
+#undef FO_ADD
+#undef FO_TABLES
+
+Table table_for(int N, bool row) {
+  switch (N) {
+#define FO_CASE(NN) \
+  case NN:          \
+    return row ? row_table<NN>() : col_table<NN>();
+    FO_FOR_EACH_N(FO_CASE)
+#undef FO_CASE
+    default:
+      return Table{};
+  }
+}
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+}  // namespace
+
+bool fft_size_supported(int n) { return table_for(n, true).n > 0; }
+
+int row_variant_count(int N) { return table_for(N, true).n; }
+int col_variant_count(int N) { return table_for(N, false).n; }
+PassVariant row_variant(int N, int v) { return table_for(N, true).v[v]; }
+PassVariant col_variant(int N, int v) { return table_for(N, false).v[v]; }
+
+size_t row_smem_bytes(int N, int v, bool pf) {
+  const PassVariant pv = row_variant(N, v);
+  return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);
+}
+size_t col_smem_bytes(int N, int v, bool pf) {
+  const PassVariant pv = col_variant(N, v);
+  return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);
+}
+bool row_prefetch_fits(int N, int v) { return row_smem_bytes(N, v, true) <= kMaxSmem; }
+bool col_prefetch_fits(int N, int v) { return col_smem_bytes(N, v, true) <= kMaxSmem; }
+
+cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s) {
+  switch (N) {
+#define FO_CASE(NN) \
+  case NN:          \
+    return row_launch_##NN(v, a, tw, s, pf);
+    FO_FOR_EACH_N(FO_CASE)
+#undef FO_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_col_pass(int N, int v, bool pf, const ColPassArgs& a, const float2* tw, cudaStream_t s) {
+  switch (N) {
+#define FO_CASE(NN) \
+  case NN:          \
+    return col_launch_##NN(v, a, tw, s, pf);
+    FO_FOR_EACH_N(FO_CASE)
+#undef FO_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace fo

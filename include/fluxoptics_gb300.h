@@ -48,6 +48,9 @@ extern "C" {
 #define FO_FORWARD 1
 #define FO_BACKWARD (-1)
 
+/* Plan flags */
+#define FO_FLAG_AUTOTUNE 1 /* time every launch shape of the passes and keep the fastest */
+
 /* Modulation kinds (fo_mod.kind) */
 #define FO_MOD_NONE 0
 #define FO_MOD_PHASE 1 /* u *= cis(s*phi)        param: float[ny*nx]        */

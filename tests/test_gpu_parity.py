@@ -303,8 +303,8 @@ def test_fista_clamp_tv(fo, orc):
 
 def test_fullsize_unitarity_and_power(fo):
     torch.manual_seed(0)
-    n, B = 2048, 6
-    u0 = torch.randn(B, n, n, dtype=torch.complex64, device="cuda")
+    n = 2048
+    u0 = torch.randn(2, 3, n, n, dtype=torch.complex64, device="cuda")  # Julia (n, n, 3, 2)
     u = fo.ScalarField(u0, (0.5, 0.5), [0.640, 0.538, 0.455])
     p = fo.ASProp(u, 5000.0)
     v = p.propagate(u)
