@@ -17,6 +17,7 @@
 
 #include "../../include/fluxoptics_gb300.h"
 #include "fo_aux.h"
+#include "fo_fft.cuh"
 #include "fo_internal.h"
 
 // ---------------------------------------------------------------------------
@@ -41,12 +42,13 @@ int cuda_fail(cudaError_t e, const char* what) {
 }
 
 // ---------------------------------------------------------------------------
-// Twiddle tables exp(-2 pi i m / N), one per (device, N), built in FP64.
+// Stage-major twiddle tables of the (N, E) schedule, one per (device, N, E),
+// built in FP64 and rounded once to float.
 // ---------------------------------------------------------------------------
 static std::mutex g_tw_mu;
-static std::map<std::pair<int, int>, float2*> g_tw;
+static std::map<std::tuple<int, int, int>, float2*> g_tw;
 
-const float2* twiddles(int N, int* err) {
+const float2* twiddles(int N, int E, int* err) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
@@ -54,27 +56,28 @@ const float2* twiddles(int N, int* err) {
     return nullptr;
   }
   std::lock_guard<std::mutex> lk(g_tw_mu);
-  auto it = g_tw.find({dev, N});
+  auto it = g_tw.find({dev, N, E});
   if (it != g_tw.end()) return it->second;
-  std::vector<float2> h(N);
-  for (int m = 0; m < N; ++m) {
-    // reduce m/N to [0, 1/8] octant-free form via sincos of the exact angle in FP64
-    const double a = -2.0 * M_PI * (double)m / (double)N;
-    h[m] = make_float2((float)cos(a), (float)sin(a));
-  }
+  const int n = std::max(1, stage_twiddle_count(N, E));
+  std::vector<float2> h(n, make_float2(1.f, 0.f));
+  for_each_stage_twiddle(N, E, [&](int idx, long long num, long long den) {
+    const long long m = num % den;  // exact reduction of the angle
+    const double a = -2.0 * M_PI * (double)m / (double)den;
+    h[idx] = make_float2((float)cos(a), (float)sin(a));
+  });
   float2* d = nullptr;
-  e = cudaMalloc(&d, sizeof(float2) * N);
+  e = cudaMalloc(&d, sizeof(float2) * n);
   if (e != cudaSuccess) {
     *err = fail(FO_ERR_ALLOC, "cudaMalloc twiddles failed");
     return nullptr;
   }
-  e = cudaMemcpy(d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice);
+  e = cudaMemcpy(d, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(d);
     *err = cuda_fail(e, "cudaMemcpy twiddles");
     return nullptr;
   }
-  g_tw[{dev, N}] = d;
+  g_tw[{dev, N, E}] = d;
   return d;
 }
 
@@ -396,7 +399,7 @@ float time_launches(const std::function<cudaError_t()>& fn, int reps) {
 }
 
 int autotune_plan(fo_prop_plan p) {
-  const int nb = std::min(p->batch, 8);
+  const int nb = std::min(p->batch, 16);
   const auto key = std::make_tuple(p->kind, p->fx, p->fy, p->ny, nb);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -415,8 +418,9 @@ int autotune_plan(fo_prop_plan p) {
   }
   std::vector<int> hidx(2 * nb + 2, 0);
   for (int i = 0; i < nb; ++i) hidx[i] = i;                     // field list
-  for (int i = 0; i <= (nb + 3) / 4; ++i) hidx[nb + i] = std::min(nb, 4 * i);  // runs of 4
-  const int n_items = (nb + 3) / 4;
+  hidx[nb] = 0;  // one run of nb fields
+  hidx[nb + 1] = nb;
+  const int n_items = 1;
   cudaMemcpy(idx, hidx.data(), sizeof(int) * hidx.size(), cudaMemcpyHostToDevice);
   cudaMemset(tmp, 0, sizeof(float2) * (size_t)nb * p->ny * p->fx);
   float best = 1e30f;
@@ -434,10 +438,16 @@ int autotune_plan(fo_prop_plan p) {
       a.nrows = p->ny;
       a.n_valid = p->nx;
       a.batch = nb;
-      a.fields_per_cta = nb;
+      a.fields_per_cta = std::min(nb, 8);
       a.inv_first = 1;
       a.fwd_after = 1;
-      const float ms = time_launches([&] { return launch_row_pass(p->fx, v, pf != 0, a, p->tw_x, 0); }, 3);
+      int trc = FO_OK;
+      const float2* tw = twiddles(p->fx, row_variant(p->fx, v).E, &trc);
+      if (!tw) continue;
+      const float ms = time_launches([&] { return launch_row_pass(p->fx, v, pf != 0, a, tw, 0); }, 3);
+      if (env_int("FO_VERBOSE", 0) > 1)
+        fprintf(stderr, "[fluxoptics_gb300] tune row N=%d v=%d (E=%d lanes=%d) pf=%d: %.4f ms\n", p->fx, v,
+                row_variant(p->fx, v).E, row_variant(p->fx, v).lanes, pf, ms);
       if (ms >= 0.f && ms < best) {
         best = ms;
         bv = v;
@@ -467,7 +477,13 @@ int autotune_plan(fo_prop_plan p) {
       a.field_list = idx;
       a.item_start = idx + nb;
       a.n_items = n_items;
-      const float ms = time_launches([&] { return launch_col_pass(p->fy, v, pf != 0, a, p->tw_y, 0); }, 3);
+      int trc = FO_OK;
+      const float2* tw = twiddles(p->fy, col_variant(p->fy, v).E, &trc);
+      if (!tw) continue;
+      const float ms = time_launches([&] { return launch_col_pass(p->fy, v, pf != 0, a, tw, 0); }, 3);
+      if (env_int("FO_VERBOSE", 0) > 1)
+        fprintf(stderr, "[fluxoptics_gb300] tune col N=%d v=%d (E=%d lanes=%d) pf=%d: %.4f ms\n", p->fy, v,
+                col_variant(p->fy, v).E, col_variant(p->fy, v).lanes, pf, ms);
       if (ms >= 0.f && ms < best) {
         best = ms;
         bv = v;
@@ -554,12 +570,12 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     }
     p->ws_bytes += sizeof(float2) * (size_t)batch * ny * fx;
   }
-  p->tw_x = twiddles(fx, &rc);
+  p->tw_x = twiddles(fx, row_variant(fx, 0).E, &rc);
   if (!p->tw_x) {
     plan_free(p);
     return rc;
   }
-  p->tw_y = twiddles(fy, &rc);
+  p->tw_y = twiddles(fy, col_variant(fy, 0).E, &rc);
   if (!p->tw_y) {
     plan_free(p);
     return rc;
@@ -570,7 +586,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   for (int b = 0; b < batch; ++b) order[b] = b;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hidx[a] < hidx[b]; });
   // column-pass work items: runs of at most kFieldsPerItem fields sharing one table
-  const int kFieldsPerItem = 4;
+  const int kFieldsPerItem = 16;
   std::vector<int> items{0};
   for (int i = 1; i <= batch; ++i) {
     if (i == batch || hidx[order[i]] != hidx[order[i - 1]] || i - items.back() >= kFieldsPerItem)
@@ -632,6 +648,12 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     }
   }
   apply_overrides(p);
+  p->tw_x = twiddles(fx, row_variant(fx, p->row_v).E, &rc);
+  p->tw_y = p->tw_x ? twiddles(fy, col_variant(fy, p->col_v).E, &rc) : nullptr;
+  if (!p->tw_x || !p->tw_y) {
+    plan_free(p);
+    return rc;
+  }
   if (env_int("FO_VERBOSE", 0))
     fprintf(stderr, "[fluxoptics_gb300] plan %s %dx%d (fft %dx%d) batch %d: row variant %d (E=%d, lanes=%d, pf=%d), col variant %d (E=%d, lanes=%d, pf=%d)\n",
             kind == 0 ? "AS" : "RS", nx, ny, fx, fy, batch, p->row_v, row_variant(fx, p->row_v).E,

@@ -46,7 +46,46 @@ struct Sched {
   __host__ __device__ static constexpr int span(int s) {  // Ns = product of radices before s
     return s == 0 ? 1 : span(s - 1) << bits(s - 1);
   }
+  // Offset of stage s's twiddle table (stages >= 1; table s holds R*Ns entries,
+  // entry r*Ns + k = exp(-2 pi i r k / (Ns R))).
+  __host__ __device__ static constexpr int twoff(int s) {
+    return s <= 1 ? 0 : twoff(s - 1) + (1 << bits(s - 1)) * span(s - 1);
+  }
+  static constexpr int twsize = twoff(S);
 };
+
+// Host-side copy of the schedule for runtime (N, E): fills the stage-major
+// twiddle tables of every stage s >= 1 (see Sched::twoff).  Returns the entry count.
+inline int stage_twiddle_count(int N, int E) {
+  int nb = ilog2c(N), e = ilog2c(E);
+  if (nb == e) return 0;
+  const int rem = nb - 2 * e, nmid = (rem + e - 1) / e, S = 2 + nmid;
+  int total = 0, span = 1;
+  for (int s = 0; s < S; ++s) {
+    const int b = (s == 0 || s == S - 1) ? e : ((s - 1) < rem / e ? e : rem - (rem / e) * e);
+    if (s >= 1) total += (1 << b) * span;
+    span <<= b;
+  }
+  return total;
+}
+
+template <typename F>
+inline void for_each_stage_twiddle(int N, int E, F f) {  // f(index, numerator, denominator)
+  int nb = ilog2c(N), e = ilog2c(E);
+  if (nb == e) return;
+  const int rem = nb - 2 * e, nmid = (rem + e - 1) / e, S = 2 + nmid;
+  int off = 0, span = 1;
+  for (int s = 0; s < S; ++s) {
+    const int b = (s == 0 || s == S - 1) ? e : ((s - 1) < rem / e ? e : rem - (rem / e) * e);
+    const int R = 1 << b;
+    if (s >= 1) {
+      for (int r = 0; r < R; ++r)
+        for (int k = 0; k < span; ++k) f(off + r * span + k, (long long)r * k, (long long)span * R);
+      off += R * span;
+    }
+    span <<= b;
+  }
+}
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -57,6 +96,30 @@ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y
 // a * (-i)
 __device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// Two independent complex values carried by one thread (two adjacent columns of
+// the column pass, or two rows of the row pass).  Every operation below applies
+// to both halves, so a thread runs two transforms with the same twiddles and
+// moves them through shared memory as one 16-byte access.
+struct __align__(16) cf2 {
+  float2 a, b;
+};
+__device__ __forceinline__ cf2 cadd(cf2 x, cf2 y) { return cf2{cadd(x.a, y.a), cadd(x.b, y.b)}; }
+__device__ __forceinline__ cf2 csub(cf2 x, cf2 y) { return cf2{csub(x.a, y.a), csub(x.b, y.b)}; }
+__device__ __forceinline__ cf2 cmul(cf2 x, float2 w) { return cf2{cmul(x.a, w), cmul(x.b, w)}; }
+__device__ __forceinline__ cf2 cmul_mi(cf2 x) { return cf2{cmul_mi(x.a), cmul_mi(x.b)}; }
+__device__ __forceinline__ cf2 cconj(cf2 x) { return cf2{cconj(x.a), cconj(x.b)}; }
+template <typename V>
+__device__ __forceinline__ V vzero();
+template <>
+__device__ __forceinline__ float2 vzero<float2>() { return make_float2(0.f, 0.f); }
+template <>
+__device__ __forceinline__ cf2 vzero<cf2>() { return cf2{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}; }
+// w8 multiplications used by the radix-8 butterfly
+__device__ __forceinline__ float2 mul_w8_1(float2 d) { return make_float2(0.70710678118654752440f * (d.x + d.y), 0.70710678118654752440f * (d.y - d.x)); }
+__device__ __forceinline__ float2 mul_w8_3(float2 d) { return make_float2(0.70710678118654752440f * (d.y - d.x), -0.70710678118654752440f * (d.x + d.y)); }
+__device__ __forceinline__ cf2 mul_w8_1(cf2 d) { return cf2{mul_w8_1(d.a), mul_w8_1(d.b)}; }
+__device__ __forceinline__ cf2 mul_w8_3(cf2 d) { return cf2{mul_w8_3(d.a), mul_w8_3(d.b)}; }
 
 // cos/sin of 2*pi*k/16, k = 1..3 (exact decimal expansions of the algebraic values)
 #define FO_C16_1 0.92387953251128675613f
@@ -69,23 +132,26 @@ struct Dft;
 
 template <>
 struct Dft<1> {
-  template <int E>
-  __device__ __forceinline__ static void run(float2 (&)[E], int) {}
+  __host__ __device__ static constexpr int out(int r) { return r; }
+  template <typename V, int E>
+  __device__ __forceinline__ static void run(V (&)[E], int) {}
 };
 
 template <>
 struct Dft<2> {
-  template <int E>
-  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
-    float2 t = a[o];
+  __host__ __device__ static constexpr int out(int r) { return r; }
+  template <typename V, int E>
+  __device__ __forceinline__ static void run(V (&a)[E], int o) {
+    V t = a[o];
     a[o] = cadd(t, a[o + 1]);
     a[o + 1] = csub(t, a[o + 1]);
   }
 };
 
-__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
-  float2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
-  float2 t2 = cadd(a1, a3), t3 = cmul_mi(csub(a1, a3));
+template <typename V>
+__device__ __forceinline__ void dft4(V& a0, V& a1, V& a2, V& a3) {
+  V t0 = cadd(a0, a2), t1 = csub(a0, a2);
+  V t2 = cadd(a1, a3), t3 = cmul_mi(csub(a1, a3));
   a0 = cadd(t0, t2);
   a2 = csub(t0, t2);
   a1 = cadd(t1, t3);
@@ -94,25 +160,27 @@ __device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2&
 
 template <>
 struct Dft<4> {
-  template <int E>
-  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
+  __host__ __device__ static constexpr int out(int r) { return r; }
+  template <typename V, int E>
+  __device__ __forceinline__ static void run(V (&a)[E], int o) {
     dft4(a[o], a[o + 1], a[o + 2], a[o + 3]);
   }
 };
 
 template <>
 struct Dft<8> {
-  template <int E>
-  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
+  __host__ __device__ static constexpr int out(int r) { return r; }
+  template <typename V, int E>
+  __device__ __forceinline__ static void run(V (&a)[E], int o) {
     // even/odd split: E = DFT4(a0,a2,a4,a6), O = DFT4(a1,a3,a5,a7)
-    float2 e0 = a[o], e1 = a[o + 2], e2 = a[o + 4], e3 = a[o + 6];
-    float2 d0 = a[o + 1], d1 = a[o + 3], d2 = a[o + 5], d3 = a[o + 7];
+    V e0 = a[o], e1 = a[o + 2], e2 = a[o + 4], e3 = a[o + 6];
+    V d0 = a[o + 1], d1 = a[o + 3], d2 = a[o + 5], d3 = a[o + 7];
     dft4(e0, e1, e2, e3);
     dft4(d0, d1, d2, d3);
     // w8^k * O[k]
-    d1 = make_float2(FO_SQRT1_2 * (d1.x + d1.y), FO_SQRT1_2 * (d1.y - d1.x));
+    d1 = mul_w8_1(d1);
     d2 = cmul_mi(d2);
-    d3 = make_float2(FO_SQRT1_2 * (d3.y - d3.x), -FO_SQRT1_2 * (d3.x + d3.y));
+    d3 = mul_w8_3(d3);
     a[o] = cadd(e0, d0);
     a[o + 4] = csub(e0, d0);
     a[o + 1] = cadd(e1, d1);
@@ -124,45 +192,33 @@ struct Dft<8> {
   }
 };
 
+// 16 = 4 x 4 in place: n = 4*n1 + n2, k = k1 + 4*k2.  Output X[r] is left in
+// register out(r) = 4*(r%4) + r/4 (a compile-time renaming, no data movement).
 template <>
 struct Dft<16> {
-  template <int E>
-  __device__ __forceinline__ static void run(float2 (&a)[E], int o) {
-    // 16 = 4 x 4: n = 4*n1 + n2, k = k1 + 4*k2
-    float2 y[16];
+  __host__ __device__ static constexpr int out(int r) { return 4 * (r % 4) + r / 4; }
+  template <typename V, int E>
+  __device__ __forceinline__ static void run(V (&a)[E], int o) {
 #pragma unroll
-    for (int n2 = 0; n2 < 4; ++n2) {
-      float2 b0 = a[o + n2], b1 = a[o + 4 + n2], b2 = a[o + 8 + n2], b3 = a[o + 12 + n2];
-      dft4(b0, b1, b2, b3);  // over n1 -> k1
-      y[0 * 4 + n2] = b0;
-      y[1 * 4 + n2] = b1;
-      y[2 * 4 + n2] = b2;
-      y[3 * 4 + n2] = b3;
-    }
-    // twiddles w16^(n2*k1), n2,k1 in 1..3
+    for (int n2 = 0; n2 < 4; ++n2) dft4(a[o + n2], a[o + 4 + n2], a[o + 8 + n2], a[o + 12 + n2]);
+    // a[o + n2 + 4*k1] = Y[k1][n2]; twiddles w16^(n2*k1)
     const float2 w1 = make_float2(FO_C16_1, -FO_S16_1);
     const float2 w2 = make_float2(FO_SQRT1_2, -FO_SQRT1_2);
     const float2 w3 = make_float2(FO_S16_1, -FO_C16_1);
     const float2 w6 = make_float2(-FO_SQRT1_2, -FO_SQRT1_2);
     const float2 w9 = make_float2(-FO_C16_1, FO_S16_1);
-    y[1 * 4 + 1] = cmul(y[1 * 4 + 1], w1);
-    y[1 * 4 + 2] = cmul(y[1 * 4 + 2], w2);
-    y[1 * 4 + 3] = cmul(y[1 * 4 + 3], w3);
-    y[2 * 4 + 1] = cmul(y[2 * 4 + 1], w2);
-    y[2 * 4 + 2] = cmul_mi(y[2 * 4 + 2]);
-    y[2 * 4 + 3] = cmul(y[2 * 4 + 3], w6);
-    y[3 * 4 + 1] = cmul(y[3 * 4 + 1], w3);
-    y[3 * 4 + 2] = cmul(y[3 * 4 + 2], w6);
-    y[3 * 4 + 3] = cmul(y[3 * 4 + 3], w9);
+    a[o + 1 + 4] = cmul(a[o + 1 + 4], w1);
+    a[o + 2 + 4] = cmul(a[o + 2 + 4], w2);
+    a[o + 3 + 4] = cmul(a[o + 3 + 4], w3);
+    a[o + 1 + 8] = cmul(a[o + 1 + 8], w2);
+    a[o + 2 + 8] = cmul_mi(a[o + 2 + 8]);
+    a[o + 3 + 8] = cmul(a[o + 3 + 8], w6);
+    a[o + 1 + 12] = cmul(a[o + 1 + 12], w3);
+    a[o + 2 + 12] = cmul(a[o + 2 + 12], w6);
+    a[o + 3 + 12] = cmul(a[o + 3 + 12], w9);
 #pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1) {
-      float2 b0 = y[k1 * 4 + 0], b1 = y[k1 * 4 + 1], b2 = y[k1 * 4 + 2], b3 = y[k1 * 4 + 3];
-      dft4(b0, b1, b2, b3);  // over n2 -> k2
-      a[o + k1] = b0;
-      a[o + k1 + 4] = b1;
-      a[o + k1 + 8] = b2;
-      a[o + k1 + 12] = b3;
-    }
+    for (int k1 = 0; k1 < 4; ++k1) dft4(a[o + 4 * k1], a[o + 4 * k1 + 1], a[o + 4 * k1 + 2], a[o + 4 * k1 + 3]);
+    // X[k1 + 4*k2] is now in a[o + 4*k1 + k2]
   }
 };
 
@@ -180,9 +236,9 @@ template <int N, int E>
 __device__ __forceinline__ int reg_pos(int t, int i) { return t + i * (N / E); }
 
 // One Stockham stage s >= 1: registers <- smem, twiddle, DFT.
-template <int N, int E, int s, int PS>
-__device__ __forceinline__ void stage_from_smem(float2 (&v)[E], int t, const float2* __restrict__ tw,
-                                                const float2* sm) {
+template <int N, int E, int s, int PS, typename V>
+__device__ __forceinline__ void stage_from_smem(V (&v)[E], int t, const float2* __restrict__ tw,
+                                                const V* sm) {
   using SC = Sched<N, E>;
   constexpr int R = 1 << SC::bits(s);
   constexpr int Ns = SC::span(s);
@@ -197,7 +253,7 @@ __device__ __forceinline__ void stage_from_smem(float2 (&v)[E], int t, const flo
       const int k = j & (Ns - 1);
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        const float2 w = __ldg(tw + r * k * (N / (Ns * R)));
+        const float2 w = tw[SC::twoff(s) + r * Ns + k];
         v[m * R + r] = cmul(v[m * R + r], w);
       }
     }
@@ -206,8 +262,8 @@ __device__ __forceinline__ void stage_from_smem(float2 (&v)[E], int t, const flo
 }
 
 // Write the outputs of stage s (s < S-1) to smem at their Stockham destinations.
-template <int N, int E, int s, int PS>
-__device__ __forceinline__ void stage_to_smem(const float2 (&v)[E], int t, float2* sm) {
+template <int N, int E, int s, int PS, typename V>
+__device__ __forceinline__ void stage_to_smem(const V (&v)[E], int t, V* sm) {
   using SC = Sched<N, E>;
   constexpr int R = 1 << SC::bits(s);
   constexpr int Ns = SC::span(s);
@@ -218,20 +274,29 @@ __device__ __forceinline__ void stage_to_smem(const float2 (&v)[E], int t, float
     const int j = t + m * T;
     const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
 #pragma unroll
-    for (int r = 0; r < R; ++r) sm[spad(d + r * Ns) * PS] = v[m * R + r];
+    for (int r = 0; r < R; ++r) sm[spad(d + r * Ns) * PS] = v[m * R + Dft<R>::out(r)];
   }
 }
 
-template <int N, int E, int s, int PS>
-__device__ __forceinline__ void stages_from(float2 (&v)[E], int t, const float2* __restrict__ tw,
-                                            float2* sm) {
+// Barrier among the threads of one transform: the whole CTA (bar_id 0) or the
+// bar_n threads of a named barrier (bar_id 1..15, bar_n a multiple of 32).
+__device__ __forceinline__ void fft_sync(int bar_id, int bar_n) {
+  if (bar_id == 0)
+    __syncthreads();
+  else
+    asm volatile("bar.sync %0, %1;\n" ::"r"(bar_id), "r"(bar_n) : "memory");
+}
+
+template <int N, int E, int s, int PS, typename V>
+__device__ __forceinline__ void stages_from(V (&v)[E], int t, const float2* __restrict__ tw, V* sm, int bar_id,
+                                            int bar_n) {
   using SC = Sched<N, E>;
   if constexpr (s < SC::S) {
-    __syncthreads();  // earlier readers of this smem region are done
+    fft_sync(bar_id, bar_n);  // earlier readers of this smem region are done
     stage_to_smem<N, E, s - 1, PS>(v, t, sm);
-    __syncthreads();
+    fft_sync(bar_id, bar_n);
     stage_from_smem<N, E, s, PS>(v, t, tw, sm);
-    stages_from<N, E, s + 1, PS>(v, t, tw, sm);
+    stages_from<N, E, s + 1, PS>(v, t, tw, sm, bar_id, bar_n);
   }
 }
 
@@ -240,11 +305,19 @@ __device__ __forceinline__ void stages_from(float2 (&v)[E], int t, const float2*
 // `sm` points at this lane's first smem slot and PS is the slot stride between
 // consecutive positions.  Every thread of the block must make the call (it holds
 // __syncthreads when the schedule has more than one stage).
-template <int N, int E, int PS>
-__device__ __forceinline__ void fft_forward(float2 (&v)[E], int t, const float2* __restrict__ tw,
-                                            float2* sm) {
+template <int N, int E, int PS, typename V>
+__device__ __forceinline__ void fft_forward(V (&v)[E], int t, const float2* __restrict__ tw, V* sm,
+                                            int bar_id = 0, int bar_n = 0) {
   Dft<E>::run(v, 0);  // stage 0: radix E, span 1, no twiddles
-  stages_from<N, E, 1, PS>(v, t, tw, sm);
+  stages_from<N, E, 1, PS>(v, t, tw, sm, bar_id, bar_n);
+  // the last stage has one butterfly of radix E per thread: register out(r) holds X[t + r*T]
+  if constexpr (Dft<E>::out(1) != 1) {
+    V w[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) w[r] = v[Dft<E>::out(r)];
+#pragma unroll
+    for (int r = 0; r < E; ++r) v[r] = w[r];
+  }
 }
 
 }  // namespace fo

@@ -88,6 +88,7 @@ struct ColPassArgs {
 struct PassVariant {
   int E;
   int lanes;
+  int P;  // transforms per thread (column pass: 2 = paired columns)
 };
 bool fft_size_supported(int n);
 int row_variant_count(int N);
@@ -101,7 +102,7 @@ bool col_prefetch_fits(int N, int v);
 cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s);
 cudaError_t launch_col_pass(int N, int v, bool pf, const ColPassArgs& a, const float2* tw, cudaStream_t s);
 
-// Device twiddle table exp(-2 pi i m / N), m < N, for the current device (cached).
-const float2* twiddles(int N, int* err);
+// Stage-major twiddle tables of the (N, E) schedule for the current device (cached).
+const float2* twiddles(int N, int E, int* err);
 
 }  // namespace fo

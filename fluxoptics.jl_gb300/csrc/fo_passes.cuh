@@ -23,10 +23,10 @@
 
 namespace fo {
 
-// Minimum resident CTAs per SM requested from the compiler: caps registers at 64
-// per thread for E <= 8 and at 128 for E = 16.
+// Minimum resident CTAs per SM requested from the compiler: caps registers near
+// 96 per thread for E <= 8 and at 128 for E = 16.
 __host__ __device__ constexpr int min_blocks(int threads, int E) {
-  return (65536 / (threads * (E <= 8 ? 64 : 128))) > 0 ? 65536 / (threads * (E <= 8 ? 64 : 128)) : 1;
+  return (65536 / (threads * (E <= 8 ? 96 : 128))) > 0 ? 65536 / (threads * (E <= 8 ? 96 : 128)) : 1;
 }
 
 __device__ __forceinline__ float2 cis_f(float a) {
@@ -235,55 +235,84 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 
 // --------------------------------------------------------------------------
 // Column pass: CTA (work item, column tile).  A work item is a run of fields
-// (from a.field_list) that share one transfer function; the H tile is loaded
-// once into registers.  PF stages the next field's tile with cp.async.
-// Shared memory: 2 * W * SLOTS float2 (PF) or W * SLOTS float2.
+// (from a.field_list) that share one transfer function.  HS stages the H tile of
+// the item in shared memory once; PF stages the next field's tile with 16-byte
+// cp.async copies while the current one is transformed.
+// Shared memory: (PF ? 2 : 1) * W * SLOTS float2 [+ N * W float2 when HS].
 // --------------------------------------------------------------------------
-template <int N, int E, int W, bool PF>
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+
+template <int N, int E, int W, bool PF, bool HS>
 __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     col_pass_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
+  static_assert(W % 2 == 0, "16-byte staging needs an even tile width");
   constexpr int T = N / E;
   constexpr int SLOTS = SmemSize<N>::value;
-  extern __shared__ float2 dsm[];
+  constexpr int THREADS = W * (N / E);
+  constexpr int CHUNKS = N * W / 2;  // 16-byte chunks of one tile
+  extern __shared__ float4 dsm4[];
+  float2* dsm = reinterpret_cast<float2*>(dsm4);
+  float2* st0 = dsm;
+  float2* st1 = dsm + W * SLOTS;
+  float2* hs = dsm + (PF ? 2 : 1) * W * SLOTS;
 
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
-  const int col = blockIdx.y * W + c;
+  const int col0 = blockIdx.y * W;
+  const int col = col0 + c;
   const bool col_ok = col < a.ncols;
   const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
   const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
-  float2* buf0 = dsm + c;
-  float2* buf1 = dsm + W * SLOTS + c;
   auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
+  const float2* Hg = a.fft_only ? nullptr : a.H + (long long)a.h_index[field_of(f0)] * a.h_stride + col0;
 
-  // one transfer function per work item, read through L1/L2 for every field
-  const float2* H = a.fft_only ? nullptr : a.H + (long long)a.h_index[field_of(f0)] * a.h_stride + col;
+  // tile (rows < y_in, columns col0 .. col0+W-1) -> padded smem, 16 bytes per copy
   auto prefetch = [&](int f, float2* dst) {
-    const float2* src = a.buf + (long long)field_of(f) * a.bstride + col;
+    const float2* src = a.buf + (long long)field_of(f) * a.bstride + col0;
 #pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const int p = t + i * T;
-      if (p < a.y_in) cp_async8(dst + spad(p) * W, src + (long long)p * a.ld);
+    for (int k = 0; k < CHUNKS / THREADS; ++k) {
+      const int q = threadIdx.x + k * THREADS;
+      const int row = q / (W / 2), cp = q % (W / 2);
+      if (row < a.y_in && col0 + 2 * cp < a.ncols)
+        cp_async16(dst + spad(row) * W + 2 * cp, src + (long long)row * a.ld + 2 * cp);
     }
   };
-  if constexpr (PF) {
-    if (col_ok && f0 < f1) prefetch(f0, buf0);
-    cp_async_commit();
+  if constexpr (HS) {
+    if (!a.fft_only) {
+#pragma unroll
+      for (int k = 0; k < CHUNKS / THREADS; ++k) {
+        const int q = threadIdx.x + k * THREADS;
+        const int row = q / (W / 2), cp = q % (W / 2);
+        if (col0 + 2 * cp < a.ncols) cp_async16(hs + row * W + 2 * cp, Hg + (long long)row * a.ncols + 2 * cp);
+      }
+    }
   }
+  if constexpr (PF) {
+    if (f0 < f1) prefetch(f0, st0);
+  }
+  cp_async_commit();
+  if constexpr (!PF) {
+    cp_async_wait<0>();
+    __syncthreads();
+  }
+
   for (int f = f0; f < f1; ++f) {
     float2* buf = a.buf + (long long)field_of(f) * a.bstride + col;
-    float2* cur = ((f - f0) & 1) ? buf1 : buf0;
+    float2* cur = ((f - f0) & 1) ? st1 : st0;
     float2 v[E];
     if constexpr (PF) {
-      float2* nxt = ((f - f0) & 1) ? buf0 : buf1;
-      if (col_ok && f + 1 < f1) prefetch(f + 1, nxt);
+      float2* nxt = ((f - f0) & 1) ? st0 : st1;
+      if (f + 1 < f1) prefetch(f + 1, nxt);
       cp_async_commit();
       cp_async_wait<1>();
       __syncthreads();
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        v[i] = (col_ok && p < a.y_in) ? cur[spad(p) * W] : make_float2(0.f, 0.f);
+        v[i] = (col_ok && p < a.y_in) ? cur[spad(p) * W + c] : make_float2(0.f, 0.f);
       }
     } else {
 #pragma unroll
@@ -292,7 +321,8 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
         v[i] = (col_ok && p < a.y_in) ? buf[(long long)p * a.ld] : make_float2(0.f, 0.f);
       }
     }
-    fft_forward<N, E, W>(v, t, tw, PF ? cur : buf0);
+    float2* ex = (PF ? cur : st0) + c;
+    fft_forward<N, E, W>(v, t, tw, ex);
     if (a.fft_only) {
       if (col_ok) {
 #pragma unroll
@@ -306,11 +336,15 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        float2 hv = col_ok ? __ldg(H + (long long)p * a.ncols) : make_float2(0.f, 0.f);
+        float2 hv;
+        if constexpr (HS)
+          hv = hs[p * W + c];
+        else
+          hv = col_ok ? Hg[(long long)p * a.ncols + c] : make_float2(0.f, 0.f);
         if (a.conj_h) hv = cconj(hv);
         v[i] = cconj(cmul(v[i], hv));
       }
-      fft_forward<N, E, W>(v, t, tw, PF ? cur : buf0);
+      fft_forward<N, E, W>(v, t, tw, ex);
       if (col_ok) {
 #pragma unroll
         for (int i = 0; i < E; ++i) {
@@ -318,6 +352,226 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
           if (p < a.y_out) buf[(long long)p * a.ld] = cconj(v[i]);
         }
       }
+    }
+    __syncthreads();  // `cur` is refilled by the prefetch of the next iteration
+  }
+}
+
+// --------------------------------------------------------------------------
+// Paired column pass: each thread carries two adjacent columns (cf2), so global,
+// shared-memory and twiddle accesses are shared by two independent transforms.
+// Same shared-memory layout as col_pass_kernel (a padded tile of W columns).
+// --------------------------------------------------------------------------
+template <int N, int E, int W, bool PF, bool HS>
+__global__ void __launch_bounds__((W / 2) * (N / E), min_blocks((W / 2) * (N / E), 2 * E))
+    col_pass2_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
+  static_assert(W % 2 == 0, "paired columns need an even tile width");
+  constexpr int T = N / E;
+  constexpr int SLOTS = SmemSize<N>::value;
+  constexpr int WP = W / 2;             // column pairs per tile
+  constexpr int THREADS = WP * (N / E);
+  constexpr int CHUNKS = N * WP;         // 16-byte chunks of one tile
+  extern __shared__ float4 dsm4[];
+  cf2* st0 = reinterpret_cast<cf2*>(dsm4);
+  cf2* st1 = st0 + WP * SLOTS;
+  cf2* hs = st0 + (PF ? 2 : 1) * WP * SLOTS;
+
+  const int cp = threadIdx.x % WP;
+  const int t = threadIdx.x / WP;
+  const int col0 = blockIdx.y * W;
+  const int col = col0 + 2 * cp;
+  const bool col_ok = col < a.ncols;
+  const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
+  const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
+  auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
+  const float2* Hg = a.fft_only ? nullptr : a.H + (long long)a.h_index[field_of(f0)] * a.h_stride + col0;
+
+  auto prefetch = [&](int f, cf2* dst) {
+    const float2* src = a.buf + (long long)field_of(f) * a.bstride + col0;
+#pragma unroll
+    for (int k = 0; k < CHUNKS / THREADS; ++k) {
+      const int q = threadIdx.x + k * THREADS;
+      const int row = q / WP, c2 = q % WP;
+      if (row < a.y_in && col0 + 2 * c2 < a.ncols)
+        cp_async16(dst + spad(row) * WP + c2, src + (long long)row * a.ld + 2 * c2);
+    }
+  };
+  if constexpr (HS) {
+    if (!a.fft_only) {
+#pragma unroll
+      for (int k = 0; k < CHUNKS / THREADS; ++k) {
+        const int q = threadIdx.x + k * THREADS;
+        const int row = q / WP, c2 = q % WP;
+        if (col0 + 2 * c2 < a.ncols) cp_async16(hs + row * WP + c2, Hg + (long long)row * a.ncols + 2 * c2);
+      }
+    }
+  }
+  if constexpr (PF) {
+    if (f0 < f1) prefetch(f0, st0);
+  }
+  cp_async_commit();
+  if constexpr (!PF) {
+    cp_async_wait<0>();
+    __syncthreads();
+  }
+
+  for (int f = f0; f < f1; ++f) {
+    cf2* buf = reinterpret_cast<cf2*>(a.buf + (long long)field_of(f) * a.bstride + col);
+    const long long ldp = a.ld / 2;  // row stride in cf2 units (ld is even)
+    cf2* cur = ((f - f0) & 1) ? st1 : st0;
+    cf2 v[E];
+    if constexpr (PF) {
+      cf2* nxt = ((f - f0) & 1) ? st0 : st1;
+      if (f + 1 < f1) prefetch(f + 1, nxt);
+      cp_async_commit();
+      cp_async_wait<1>();
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        v[i] = (col_ok && p < a.y_in) ? cur[spad(p) * WP + cp] : vzero<cf2>();
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        v[i] = (col_ok && p < a.y_in) ? buf[(long long)p * ldp] : vzero<cf2>();
+      }
+    }
+    cf2* ex = (PF ? cur : st0) + cp;
+    fft_forward<N, E, WP>(v, t, tw, ex);
+    if (a.fft_only) {
+      if (col_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          const int p = t + i * T;
+          if (p < a.y_out) buf[(long long)p * ldp] = v[i];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        cf2 hv;
+        if constexpr (HS) {
+          hv = hs[p * WP + cp];
+        } else {
+          hv = col_ok ? *reinterpret_cast<const cf2*>(Hg + (long long)p * a.ncols + 2 * cp) : vzero<cf2>();
+        }
+        if (a.conj_h) hv = cconj(hv);
+        v[i] = cf2{cconj(cmul(v[i].a, hv.a)), cconj(cmul(v[i].b, hv.b))};
+      }
+      fft_forward<N, E, WP>(v, t, tw, ex);
+      if (col_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          const int p = t + i * T;
+          if (p < a.y_out) buf[(long long)p * ldp] = cconj(v[i]);
+        }
+      }
+    }
+    __syncthreads();  // `cur` is refilled by the prefetch of the next iteration
+  }
+}
+
+// --------------------------------------------------------------------------
+// Lane-major column pass: the T threads of lane c transform column col0 + c and
+// synchronise among themselves only (named barrier c+1), like the row pass.
+// Tiles move between global and shared memory with a row-major copy mapping
+// (coalesced 32-byte row segments): cp.async in, shared-memory staging out.
+// Shared memory: 2 * W * LS float2 (LS = SLOTS + 4, conflict-free lane stride)
+// [+ W * (N + 4) float2 for the H tile when HS].
+// --------------------------------------------------------------------------
+template <int N>
+struct LaneStride {
+  static constexpr int value = SmemSize<N>::value + 4;
+};
+
+template <int N, int E, int W, bool HS>
+__global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
+    col_lane_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
+  constexpr int T = N / E;
+  static_assert(T % 32 == 0, "a lane must be whole warps");
+  constexpr int LS = LaneStride<N>::value;
+  constexpr int HLS = N + 4;
+  constexpr int THREADS = W * T;
+  extern __shared__ float4 dsm4[];
+  float2* st0 = reinterpret_cast<float2*>(dsm4);
+  float2* st1 = st0 + W * LS;
+  float2* hs = st0 + 2 * W * LS;
+
+  const int lane = threadIdx.x / T;
+  const int t = threadIdx.x % T;
+  const int col0 = blockIdx.y * W;
+  const bool lane_ok = col0 + lane < a.ncols;
+  const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
+  const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
+  auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
+  const float2* Hg = a.fft_only ? nullptr : a.H + (long long)a.h_index[field_of(f0)] * a.h_stride + col0;
+
+  auto prefetch = [&](int f, float2* dst) {
+    const float2* src = a.buf + (long long)field_of(f) * a.bstride + col0;
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int q = threadIdx.x + k * THREADS;
+      const int row = q / W, c = q % W;
+      if (row < a.y_in && col0 + c < a.ncols) cp_async8(dst + c * LS + spad(row), src + (long long)row * a.ld + c);
+    }
+  };
+  if constexpr (HS) {
+    if (!a.fft_only) {
+#pragma unroll
+      for (int k = 0; k < E; ++k) {
+        const int q = threadIdx.x + k * THREADS;
+        const int row = q / W, c = q % W;
+        if (col0 + c < a.ncols) cp_async8(hs + c * HLS + row, Hg + (long long)row * a.ncols + c);
+      }
+    }
+  }
+  if (f0 < f1) prefetch(f0, st0);
+  cp_async_commit();
+
+  for (int f = f0; f < f1; ++f) {
+    float2* cur = ((f - f0) & 1) ? st1 : st0;
+    float2* nxt = ((f - f0) & 1) ? st0 : st1;
+    if (f + 1 < f1) prefetch(f + 1, nxt);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    float2* L = cur + lane * LS;
+    float2 v[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int p = t + i * T;
+      v[i] = (lane_ok && p < a.y_in) ? L[spad(p)] : make_float2(0.f, 0.f);
+    }
+    fft_forward<N, E, 1>(v, t, tw, L, lane + 1, T);
+    if (!a.fft_only) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        float2 hv;
+        if constexpr (HS)
+          hv = hs[lane * HLS + p];
+        else
+          hv = lane_ok ? Hg[(long long)p * a.ncols + lane] : make_float2(0.f, 0.f);
+        if (a.conj_h) hv = cconj(hv);
+        v[i] = cconj(cmul(v[i], hv));
+      }
+      fft_forward<N, E, 1>(v, t, tw, L, lane + 1, T);
+#pragma unroll
+      for (int i = 0; i < E; ++i) v[i] = cconj(v[i]);
+    }
+    fft_sync(lane + 1, T);  // the lane's last exchange reads are done
+#pragma unroll
+    for (int i = 0; i < E; ++i) L[spad(t + i * T)] = v[i];
+    __syncthreads();
+    float2* out = a.buf + (long long)field_of(f) * a.bstride + col0;
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int q = threadIdx.x + k * THREADS;
+      const int row = q / W, c = q % W;
+      if (row < a.y_out && col0 + c < a.ncols) out[(long long)row * a.ld + c] = cur[c * LS + spad(row)];
     }
     __syncthreads();  // `cur` is refilled by the prefetch of the next iteration
   }
@@ -362,19 +616,50 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
   return cudaGetLastError();
 }
 
-template <int N, int E, int W>
+// Column-pass shared memory: staging (1 or 2 padded tiles) plus, when it fits,
+// the transfer-function tile.
+template <int N, int W>
+constexpr size_t col_smem(bool pf, bool hs) {
+  return sizeof(float2) * ((size_t)(pf ? 2 : 1) * W * SmemSize<N>::value + (hs ? (size_t)N * W : 0));
+}
+constexpr size_t kMaxSmemPerCta = 227 * 1024;
+
+template <int N, int E, int W, int P>
 cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
-  constexpr int threads = W * (N / E);
-  const size_t smem = sizeof(float2) * (size_t)(pf ? 2 : 1) * W * SmemSize<N>::value;
+  constexpr int threads = (W / (P == 2 ? 2 : 1)) * (N / E);
   dim3 grid(a.n_items, (a.ncols + W - 1) / W);
   cudaError_t e;
-  if (pf) {
-    e = set_smem(col_pass_kernel<N, E, W, true>, smem);
-    if (e == cudaSuccess) col_pass_kernel<N, E, W, true><<<grid, threads, smem, s>>>(a, tw);
+#define FO_COL_GO(PFV, HSV)                                                                     \
+  do {                                                                                          \
+    constexpr size_t smem = col_smem<N, W>(PFV, HSV);                                           \
+    if constexpr (P == 2) {                                                                     \
+      e = set_smem(col_pass2_kernel<N, E, W, PFV, HSV>, smem);                                  \
+      if (e == cudaSuccess) col_pass2_kernel<N, E, W, PFV, HSV><<<grid, threads, smem, s>>>(a, tw); \
+    } else {                                                                                    \
+      e = set_smem(col_pass_kernel<N, E, W, PFV, HSV>, smem);                                   \
+      if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV><<<grid, threads, smem, s>>>(a, tw);  \
+    }                                                                                           \
+  } while (0)
+  if constexpr (P == 0) {
+    constexpr int LS = LaneStride<N>::value;
+    constexpr size_t smem_hs = sizeof(float2) * ((size_t)2 * W * LS + (size_t)W * (N + 4));
+    constexpr size_t smem_nohs = sizeof(float2) * ((size_t)2 * W * LS);
+    (void)pf;
+    if constexpr (smem_hs <= kMaxSmemPerCta) {
+      e = set_smem(col_lane_kernel<N, E, W, true>, smem_hs);
+      if (e == cudaSuccess) col_lane_kernel<N, E, W, true><<<grid, threads, smem_hs, s>>>(a, tw);
+    } else {
+      e = set_smem(col_lane_kernel<N, E, W, false>, smem_nohs);
+      if (e == cudaSuccess) col_lane_kernel<N, E, W, false><<<grid, threads, smem_nohs, s>>>(a, tw);
+    }
+  } else if (pf) {
+    if constexpr (col_smem<N, W>(true, true) <= kMaxSmemPerCta) FO_COL_GO(true, true);
+    else FO_COL_GO(true, false);
   } else {
-    e = set_smem(col_pass_kernel<N, E, W, false>, smem);
-    if (e == cudaSuccess) col_pass_kernel<N, E, W, false><<<grid, threads, smem, s>>>(a, tw);
+    if constexpr (col_smem<N, W>(false, true) <= kMaxSmemPerCta) FO_COL_GO(false, true);
+    else FO_COL_GO(false, false);
   }
+#undef FO_COL_GO
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

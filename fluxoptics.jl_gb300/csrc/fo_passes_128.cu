@@ -18,9 +18,9 @@ cudaError_t row_launch_128(int v, const RowPassArgs& a, const float2* tw, cudaSt
 
 cudaError_t col_launch_128(int v, const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
   switch (v) {
-#define X(I, E, W) \
-  case I:          \
-    return col_launch_shape<128, E, W>(a, tw, s, pf);
+#define X(I, E, W, P) \
+  case I:             \
+    return col_launch_shape<128, E, W, P>(a, tw, s, pf);
     FO_COL_VARIANTS_128(X)
 #undef X
     default:

@@ -32,11 +32,13 @@ Table col_table();
   template <>                                                     \
   Table col_table<NN>() {                                         \
     Table t;                                                      \
-    FO_COL_VARIANTS_##NN(FO_ADD) return t;                        \
+    FO_COL_VARIANTS_##NN(FO_ADDC) return t;                       \
   }
-#define FO_ADD(I, E, L) t.v[t.n++] = PassVariant{E, L};
+#define FO_ADD(I, E, L) t.v[t.n++] = PassVariant{E, L, 1};
+#define FO_ADDC(I, E, L, P) t.v[t.n++] = PassVariant{E, L, P};
 FO_FOR_EACH_N(FO_TABLES)
 #undef FO_ADD
+#undef FO_ADDC
 #undef FO_TABLES
 
 Table table_for(int N, bool row) {
@@ -68,7 +70,8 @@ size_t row_smem_bytes(int N, int v, bool pf) {
 }
 size_t col_smem_bytes(int N, int v, bool pf) {
   const PassVariant pv = col_variant(N, v);
-  return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);
+  if (pv.P == 0) return sizeof(float2) * 2 * pv.lanes * (size_t)(N + N / 16 + 4);  // always staged
+  return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);  // staging only
 }
 bool row_prefetch_fits(int N, int v) { return row_smem_bytes(N, v, true) <= kMaxSmem; }
 bool col_prefetch_fits(int N, int v) { return col_smem_bytes(N, v, true) <= kMaxSmem; }

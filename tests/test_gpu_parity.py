@@ -373,3 +373,33 @@ def test_graph_capture_replays_iteration(fo, orc):
     torch.cuda.synchronize()
     assert np.allclose(losses, losses_eager, rtol=1e-5)
     assert torch.allclose(ph.phi, phi_eager, rtol=1e-5, atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# Every launch-shape variant of the passes (forced through the environment)
+# ---------------------------------------------------------------------------
+
+_VARIANTS = {512: (3, 4), 1024: (4, 5), 2048: (4, 5), 4096: (2, 4)}
+
+
+@pytest.mark.parametrize("n", sorted(_VARIANTS))
+def test_every_pass_variant(fo, orc, n, monkeypatch):
+    rng = np.random.default_rng(n + 7)
+    lams = np.array([0.9, 0.7])
+    B = 4 if n <= 2048 else 2
+    u0 = rand_field(rng, (B // 2, 2, n, n))
+    phi = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    ref = orc.asprop(orc.phase_forward(u0.reshape(B, n, n), phi), 1.0, 1.0, np.tile(lams, B // 2), 400.0)
+    n_row, n_col = _VARIANTS[n]
+    combos = [(r, 0) for r in range(n_row)] + [(0, c) for c in range(1, n_col)]
+    for rv, cv in combos:
+        for pf in ("0", "1"):
+            monkeypatch.setenv("FO_ROW_VARIANT", str(rv))
+            monkeypatch.setenv("FO_COL_VARIANT", str(cv))
+            monkeypatch.setenv("FO_PREFETCH", pf)
+            monkeypatch.setenv("FO_AUTOTUNE", "0")
+            u = fo.ScalarField(u0, (1.0, 1.0), lams)
+            system = fo.ScalarSource(u) | fo.Phase(u, phi) | fo.ASProp(u, 400.0)
+            got = npy(system()["out"].electric).reshape(B, n, n)
+            err = orc.rel_l2(got, ref)
+            assert err < FIELD_TOL, (rv, cv, pf, err)
