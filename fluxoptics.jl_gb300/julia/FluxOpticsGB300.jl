@@ -1,0 +1,297 @@
+"""
+    FluxOpticsGB300
+
+Drop-in GB300 components for FluxOptics.jl: each type subtypes the reference's
+component hierarchy and implements its method set (propagate!, backpropagate!,
+propagate_and_save!, backpropagate_with_gradient!, trainable, ...) through
+`ccall` into libfluxoptics_gb300 (include/fluxoptics_gb300.h).  Fields must be
+`CuArray{ComplexF32}`; work is ordered on CUDA.jl's task-local stream.
+
+Replaces, for CuArray fields:
+- ASProp / RSProp  (src/optical_components/freespace_propagators/angular_spectrum.jl:193-234,
+                    rayleigh_sommerfeld.jl:128-169)
+- Phase / Mask     (src/optical_components/modulators/phasemask.jl:38-150, mask.jl:39-142)
+- AS_BPM           (src/optical_components/bulk_propagators/bpm.jl:130-142)
+- a fused run of the above (GB300Chain), the GPU counterpart of the merge rules
+  (src/optical_components/system/merge_rules.jl:45-52)
+"""
+module FluxOpticsGB300
+
+using CUDA
+using Functors
+using FluxOptics
+using FluxOptics.OpticalComponents: AbstractCustomComponent, Static, Trainable, Buffered, Unbuffered,
+                                    Direction, Forward, Backward
+import FluxOptics.OpticalComponents: propagate!, backpropagate!, propagate_and_save!,
+                                     backpropagate_with_gradient!, get_preallocated_gradient,
+                                     get_saved_buffer, alloc_saved_buffer, trainable, get_data
+
+const LIB = joinpath(@__DIR__, "..", "lib", "libfluxoptics_gb300.so")
+const FO_FLAG_AUTOTUNE = Cint(1)
+const FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN = Cint(0), Cint(1), Cint(2), Cint(3)
+
+struct FoMod            # mirrors `fo_mod`
+    kind::Cint
+    param::Ptr{Cvoid}
+    saved::Ptr{Cvoid}
+    grad::Ptr{Cvoid}
+    scale::Cdouble
+end
+
+function check(rc::Cint)
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:fo_last_error, LIB), Cstring, ()))
+    error("libfluxoptics_gb300 error $rc: $msg")
+end
+
+cstream() = CUDA.stream().handle
+dptr(x::CuArray) = reinterpret(Ptr{Cvoid}, pointer(x))
+dptr(::Nothing) = C_NULL
+dims_of(u::ScalarField) = (size(u.electric, 1), size(u.electric, 2), div(length(u.electric), size(u.electric, 1) * size(u.electric, 2)))
+dirsign(::Type{Forward}) = Cint(1)
+dirsign(::Type{Backward}) = Cint(-1)
+
+# one wavelength per field, in the column-major order of the trailing dims
+function lambdas_per_field(u::ScalarField)
+    lam = Array(FluxOptics.get_lambdas(u))
+    nx, ny, b = dims_of(u)
+    Float64.(vec(broadcast((l, _) -> l, lam, zeros(size(u.electric)[3:end]...))))
+end
+
+# ---------------------------------------------------------------------------
+# Propagators
+# ---------------------------------------------------------------------------
+mutable struct GB300Prop <: AbstractCustomComponent{Static}
+    plan::Ptr{Cvoid}
+    kind::Symbol
+    z::Float64
+end
+
+function _finalize(p::GB300Prop)
+    p.plan == C_NULL || ccall((:fo_prop_destroy, LIB), Cint, (Ptr{Cvoid},), p.plan)
+    p.plan = C_NULL
+end
+
+"""GB300ASProp(u, z; n0=1) -- angular-spectrum propagation on the GPU path."""
+function GB300ASProp(u::ScalarField, z::Real; n0::Real = 1)
+    nx, ny, b = dims_of(u)
+    lam = lambdas_per_field(u)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_asprop_create, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
+                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0, FO_FLAG_AUTOTUNE))
+    finalizer(_finalize, GB300Prop(h[], :AS, Float64(z)))
+end
+
+"""GB300RSProp(u, z) -- Rayleigh-Sommerfeld propagation on the GPU path."""
+function GB300RSProp(u::ScalarField, z::Real)
+    nx, ny, b = dims_of(u)
+    lam = lambdas_per_field(u)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_rsprop_create, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cint),
+                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, FO_FLAG_AUTOTUNE))
+    finalizer(_finalize, GB300Prop(h[], :RS, Float64(z)))
+end
+
+Functors.@functor GB300Prop ()
+get_data(p::GB300Prop) = ()
+
+function propagate!(u::ScalarField, p::GB300Prop, dir::Type{<:Direction})
+    check(ccall((:fo_propagate, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                p.plan, dptr(u.electric), dirsign(dir), cstream()))
+    u
+end
+
+backpropagate!(u::ScalarField, p::GB300Prop, dir::Type{<:Direction}) = propagate!(u, p, reverse(dir))
+
+# ---------------------------------------------------------------------------
+# Phase
+# ---------------------------------------------------------------------------
+struct GB300Phase{M, A, U} <: AbstractCustomComponent{M}
+    ϕ::A
+    ∂p::Union{Nothing, @NamedTuple{ϕ::A}}
+    u::Union{Nothing, U}
+end
+
+function GB300Phase(p::Phase)   # adopt a reference Phase (same arrays)
+    M = FluxOptics.OpticalComponents.get_trainability(p)
+    GB300Phase{M, typeof(p.ϕ), typeof(p.u)}(p.ϕ, p.∂p, p.u)
+end
+
+Functors.@functor GB300Phase (ϕ,)
+get_data(p::GB300Phase) = p.ϕ
+trainable(p::GB300Phase{<:Trainable}) = (; ϕ = p.ϕ)
+get_preallocated_gradient(p::GB300Phase{Trainable{Buffered}}) = p.∂p
+get_saved_buffer(p::GB300Phase{Trainable{Buffered}}) = p.u
+alloc_saved_buffer(u::ScalarField, p::GB300Phase{Trainable{Unbuffered}}) = similar(u.electric)
+
+function _phase_fwd!(u::ScalarField, p::GB300Phase, saved, dir)
+    nx, ny, b = dims_of(u)
+    check(ccall((:fo_phase_forward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(u.electric), dptr(p.ϕ), dptr(saved), nx, ny, b, dirsign(dir), cstream()))
+    u
+end
+
+propagate!(u::ScalarField, p::GB300Phase, dir::Type{<:Direction}) = _phase_fwd!(u, p, nothing, dir)
+propagate_and_save!(u::ScalarField, p::GB300Phase{Trainable{Buffered}}, dir::Type{<:Direction}) =
+    _phase_fwd!(u, p, p.u, dir)
+propagate_and_save!(u::ScalarField, u_saved::AbstractArray, p::GB300Phase{Trainable{Unbuffered}},
+                    dir::Type{<:Direction}) = _phase_fwd!(u, p, u_saved, dir)
+backpropagate!(u::ScalarField, p::GB300Phase, dir::Type{<:Direction}) = _phase_fwd!(u, p, nothing, reverse(dir))
+
+function backpropagate_with_gradient!(∂v::ScalarField, u_saved::AbstractArray, ∂p::NamedTuple,
+                                      p::GB300Phase{<:Trainable}, dir::Type{<:Direction})
+    nx, ny, b = dims_of(∂v)
+    check(ccall((:fo_phase_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(∂v.electric), dptr(p.ϕ), dptr(u_saved), dptr(∂p.ϕ), nx, ny, b, dirsign(dir), cstream()))
+    (∂v, ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# Mask
+# ---------------------------------------------------------------------------
+struct GB300Mask{M, A, U} <: AbstractCustomComponent{M}
+    m::A
+    ∂p::Union{Nothing, @NamedTuple{m::A}}
+    u::Union{Nothing, U}
+end
+
+function GB300Mask(p::Mask)
+    M = FluxOptics.OpticalComponents.get_trainability(p)
+    GB300Mask{M, typeof(p.m), typeof(p.u)}(p.m, p.∂p, p.u)
+end
+
+Functors.@functor GB300Mask (m,)
+get_data(p::GB300Mask) = p.m
+trainable(p::GB300Mask{<:Trainable}) = (; m = p.m)
+get_preallocated_gradient(p::GB300Mask{Trainable{Buffered}}) = p.∂p
+get_saved_buffer(p::GB300Mask{Trainable{Buffered}}) = p.u
+alloc_saved_buffer(u::ScalarField, p::GB300Mask{Trainable{Unbuffered}}) = similar(u.electric)
+
+function _mask_fwd!(u::ScalarField, p::GB300Mask, saved, dir)
+    nx, ny, b = dims_of(u)
+    check(ccall((:fo_mask_forward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(u.electric), dptr(p.m), dptr(saved), nx, ny, b, dirsign(dir), cstream()))
+    u
+end
+
+propagate!(u::ScalarField, p::GB300Mask, dir::Type{<:Direction}) = _mask_fwd!(u, p, nothing, dir)
+propagate_and_save!(u::ScalarField, p::GB300Mask{Trainable{Buffered}}, dir::Type{<:Direction}) =
+    _mask_fwd!(u, p, p.u, dir)
+propagate_and_save!(u::ScalarField, u_saved::AbstractArray, p::GB300Mask{Trainable{Unbuffered}},
+                    dir::Type{<:Direction}) = _mask_fwd!(u, p, u_saved, dir)
+
+function backpropagate_with_gradient!(∂v::ScalarField, u_saved::AbstractArray, ∂p::NamedTuple,
+                                      p::GB300Mask{<:Trainable}, dir::Type{<:Direction})
+    nx, ny, b = dims_of(∂v)
+    check(ccall((:fo_mask_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(∂v.electric), dptr(p.m), dptr(u_saved), dptr(∂p.m), nx, ny, b, dirsign(dir), cstream()))
+    (∂v, ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# Fused chain: [mod] prop [mod] prop ... [mod] on one grid
+# ---------------------------------------------------------------------------
+mutable struct GB300Chain{M, P, D} <: AbstractCustomComponent{M}
+    chain::Ptr{Cvoid}
+    props::P                 # GB300Prop, kept alive
+    mods::D                  # Tuple of Nothing / GB300Phase / GB300Mask, length(props)+1
+end
+
+function GB300Chain(props::Vector{GB300Prop}, mods::Vector)
+    @assert length(mods) == length(props) + 1
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    plans = [p.plan for p in props]
+    check(ccall((:fo_chain_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Cint, Ptr{Ptr{Cvoid}}), h, length(plans), plans))
+    M = any(m -> m !== nothing && FluxOptics.istrainable(m), mods) ? Trainable{Buffered} : Static
+    c = GB300Chain{M, typeof(Tuple(props)), typeof(Tuple(mods))}(h[], Tuple(props), Tuple(mods))
+    finalizer(x -> ccall((:fo_chain_destroy, LIB), Cint, (Ptr{Cvoid},), x.chain), c)
+end
+
+Functors.@functor GB300Chain (mods,)
+trainable(p::GB300Chain{<:Trainable}) = (; mods = p.mods)
+
+_fomod(::Nothing, saved, grad) = FoMod(FO_MOD_NONE, C_NULL, C_NULL, C_NULL, 0.0)
+_fomod(m::GB300Phase, saved, grad) = FoMod(FO_MOD_PHASE, dptr(m.ϕ), dptr(saved), dptr(grad), 1.0)
+_fomod(m::GB300Mask, saved, grad) = FoMod(FO_MOD_MASK, dptr(m.m), dptr(saved), dptr(grad), 1.0)
+_saved(m) = (m === nothing || !FluxOptics.istrainable(m)) ? nothing : m.u
+_grad(m::GB300Phase) = FluxOptics.istrainable(m) ? m.∂p.ϕ : nothing
+_grad(m::GB300Mask) = FluxOptics.istrainable(m) ? m.∂p.m : nothing
+_grad(::Nothing) = nothing
+
+function propagate!(u::ScalarField, p::GB300Chain, dir::Type{<:Direction})
+    mods = [_fomod(m, nothing, nothing) for m in p.mods]
+    check(ccall((:fo_chain_forward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Cint, Ptr{Cvoid}),
+                p.chain, dptr(u.electric), mods, dirsign(dir), cstream()))
+    u
+end
+
+function propagate_and_save!(u::ScalarField, p::GB300Chain{Trainable{Buffered}}, dir::Type{<:Direction})
+    mods = [_fomod(m, _saved(m), nothing) for m in p.mods]
+    check(ccall((:fo_chain_forward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Cint, Ptr{Cvoid}),
+                p.chain, dptr(u.electric), mods, dirsign(dir), cstream()))
+    u
+end
+
+get_preallocated_gradient(p::GB300Chain{Trainable{Buffered}}) = (; mods = map(m -> m === nothing ? nothing : m.∂p, p.mods))
+get_saved_buffer(p::GB300Chain{Trainable{Buffered}}) = map(_saved, p.mods)
+
+function backpropagate_with_gradient!(∂v::ScalarField, u_saved, ∂p::NamedTuple, p::GB300Chain{<:Trainable},
+                                      dir::Type{<:Direction})
+    mods = [_fomod(m, _saved(m), _grad(m)) for m in p.mods]
+    check(ccall((:fo_chain_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                p.chain, dptr(∂v.electric), mods, dirsign(dir), C_NULL, C_NULL, cstream()))
+    (∂v, ∂p)
+end
+
+backpropagate!(u::ScalarField, p::GB300Chain, dir::Type{<:Direction}) =
+    error("GB300Chain: use backpropagate_with_gradient! (the adjoint sweep needs the saved inputs)")
+
+"""
+    gb300(system::OpticalSystem) -> OpticalSystem
+
+Replace ASProp/RSProp/Phase/Mask components by their GB300 counterparts and fuse
+every maximal run [mod] prop [mod] prop ... [mod] into one GB300Chain.
+"""
+function gb300(system::OpticalSystem; template::ScalarField)
+    comps = FluxOptics.get_components(system)
+    out = Any[]
+    i = 1
+    while i <= length(comps)
+        c = comps[i]
+        if c isa ASProp || c isa RSProp || c isa Phase || c isa Mask
+            mods = Any[nothing]
+            props = GB300Prop[]
+            if c isa Phase || c isa Mask
+                mods[1] = c isa Phase ? GB300Phase(c) : GB300Mask(c)
+                i += 1
+            end
+            while i <= length(comps) && (comps[i] isa ASProp || comps[i] isa RSProp)
+                push!(props, _convert_prop(comps[i], template))
+                push!(mods, nothing)
+                i += 1
+                if i <= length(comps) && (comps[i] isa Phase || comps[i] isa Mask)
+                    mods[end] = comps[i] isa Phase ? GB300Phase(comps[i]) : GB300Mask(comps[i])
+                    i += 1
+                end
+            end
+            isempty(props) ? push!(out, mods[1]) : push!(out, GB300Chain(props, mods))
+        else
+            push!(out, c)
+            i += 1
+        end
+    end
+    OpticalSystem(FluxOptics.get_source(system), out...)
+end
+
+# the propagation distance is kept by the wrapped kernel component
+_convert_prop(c::ASProp, u) = GB300ASProp(u, c.optical_components[2].z; n0 = c.optical_components[2].n0)
+_convert_prop(c::RSProp, u) = GB300RSProp(u, c.optical_components[3].z)
+
+end # module
