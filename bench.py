@@ -192,6 +192,25 @@ def col_pass_bytes(n=N, batch=None):
     return batch * 16 * n * n + len(LAMBDAS) * 8 * n * n
 
 
+def max_over_ranks(ms, device="cuda"):
+    """The slowest rank's step time: every replica processed its own share, so the
+    job took as long as the slowest one (barrier on both sides)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def job_rate(props_per_rank_step, world, ms):
+    """Whole-job propagations/s of `world` replicas that each ran one step in ms."""
+    return props_per_rank_step * world / (ms * 1e-3)
+
+
 def run_gb300(args, rank, world):
     import torch
     from __graft_entry__ import build, load_package
@@ -233,13 +252,7 @@ def run_gb300(args, rank, world):
             e1.record(stream)
             stream.synchronize()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            dist.barrier()
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
         final_loss = float(loss_t.sum())
 
         # per-pass device times of the same iteration, eager, events around every pass
@@ -280,7 +293,7 @@ def run_gb300(args, rank, world):
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     achieved = col_pass_bytes() / (col_ms * 1e-3) / 1e9
     traffic = read_traffic()
-    value = props_per_step * world / (ms * 1e-3)
+    value = job_rate(props_per_step, world, ms)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
