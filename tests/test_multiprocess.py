@@ -32,7 +32,7 @@ def test_replica_timing_world2():
     pytest.importorskip("torch.distributed")
     world = 2
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
