@@ -430,6 +430,152 @@ def run_cpu_sample(budget_s=12.0, threads=None):
                       f"forward + adjoint, FP64 numpy/scipy.fft with {threads} workers, {el:.1f} s"}
 
 
+# ---------------------------------------------------------------------------
+# Other configurations (reported with --config 2 / 4 / 5)
+# ---------------------------------------------------------------------------
+def _graph_time(fo, lib, step_fn, steps, warmup):
+    """Capture step_fn once on a side stream, replay it; returns (ms/step, kernel nodes)."""
+    import torch
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        step_fn()
+        torch.cuda.synchronize()
+        sp = C.c_void_p(stream.cuda_stream)
+        g = C.c_void_p()
+        fo._capi.check(lib.fo_graph_begin(sp))
+        step_fn()
+        fo._capi.check(lib.fo_graph_end(sp, C.byref(g)))
+        nk = C.c_int()
+        fo._capi.check(lib.fo_graph_info(g, C.byref(nk)))
+        for _ in range(warmup):
+            fo._capi.check(lib.fo_graph_launch(g, sp))
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fo._capi.check(lib.fo_graph_launch(g, sp))
+        e1.record(stream)
+        stream.synchronize()
+        fo._capi.check(lib.fo_graph_destroy(g))
+    return e0.elapsed_time(e1) / steps, nk.value
+
+
+def run_config2(args):
+    """Two-DOE RSProp chain, 512^2 padded to 1024^2, forward + gradient + Fista."""
+    import torch
+    from __graft_entry__ import build, load_package
+    build()
+    fo = load_package()
+    lib = fo.load_library()
+    n, ds, lam = 512, (1.0, 1.0), 1.064
+    rng = np.random.default_rng(SEED + 2)
+    x, y = fo.spatial_vectors((n, n), ds)
+    u = fo.ScalarField(fo.gaussian(30.0, x, y).astype(np.complex64), ds, lam)
+    fo.normalize_power_(u)
+    t = fo.gaussian(30.0, x - 60.0, y) + fo.gaussian(30.0, x + 60.0, y)
+    t = np.abs(t) ** 2
+    t /= t.sum() * ds[0] * ds[1]
+    m1 = fo.Phase(u, rng.uniform(0, 2 * np.pi, (n, n)), trainable=True, buffered=True)
+    m2 = fo.Phase(u, rng.uniform(0, 2 * np.pi, (n, n)), trainable=True, buffered=True)
+    system = fo.ScalarSource(u) | fo.RSProp(u, 1500.0) | m1 | fo.RSProp(u, 2000.0) | m2 | fo.RSProp(u, 1500.0)
+    metric = fo.SquaredIntensityDifference((u, t))
+    opt = fo.setup(fo.Fista(1.0), system)
+    src = system.source.u0
+    x_, du = src.similar(), src.similar()
+    ms, nk = _graph_time(fo, lib, lambda: iteration(fo, system, metric, opt, x_, du, src), args.steps, args.warmup)
+    return {"config": "two-DOE RSProp chain 512^2 (pad 1024^2), fwd + adjoint + Fista, CUDA graph",
+            "props_per_step": 6, "ms_per_step": round(ms, 4), "value": round(6 / (ms * 1e-3), 1),
+            "unit": UNIT, "gpu_launches_per_step": nk}
+
+
+def run_config4(args):
+    """AS_BPM 1024^2 x 256 slices, gradient w.r.t. dn with sqrt(N) checkpoints."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+    from __graft_entry__ import build, load_package
+    build()
+    fo = load_package()
+    lib = fo.load_library()
+    n, ds, lam, n0, ns = 1024, (0.25, 0.25), 1.064, 1.45, 256
+    rng = np.random.default_rng(SEED + 4)
+    dn = gaussian_filter(rng.standard_normal((ns, n, n)).astype(np.float32), (8.0, 4.0, 4.0))
+    dn *= 5e-3 / np.max(np.abs(dn))
+    x, y = fo.spatial_vectors((n, n), ds)
+    th = np.deg2rad(rng.uniform(-2, 2))
+    env = np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 150.0 ** 2)
+    u0 = (env * np.exp(1j * 2 * np.pi * n0 / lam * np.sin(th) * x[None, :])).astype(np.complex64)
+    u = fo.ScalarField(u0, ds, lam)
+    fo.normalize_power_(u)
+    target = np.abs(gaussian_filter(rng.standard_normal((n, n)), 16.0)) ** 2
+    bpm = fo.AS_BPM(u, float(ns), n0, dn, trainable=True, buffered=True)
+    system = fo.ScalarSource(u) | bpm
+    metric = fo.SquaredIntensityDifference((u, target))
+    opt = fo.setup(fo.Fista(1e-3), system)
+    src = system.source.u0
+    x_, du = src.similar(), src.similar()
+    ms, nk = _graph_time(fo, lib, lambda: iteration(fo, system, metric, opt, x_, du, src), max(3, args.steps // 2),
+                         args.warmup)
+    props = 2 * (ns + 1)
+    return {"config": "AS_BPM 1024^2 x 256 slices (dz=1um, n0=1.45), d(dn) with sqrt(N)=16 checkpoints "
+                      "+ recompute, Fista on dn, CUDA graph",
+            "props_per_step": props, "recompute_props_per_step": ns - 16, "ms_per_step": round(ms, 3),
+            "value": round(props / (ms * 1e-3), 1), "unit": UNIT, "gpu_launches_per_step": nk}
+
+
+def ragged_problems(seed=SEED + 5, count=64, sizes=(256, 512, 1024, 2048, 4096)):
+    rng = np.random.default_rng(seed)
+    probs = []
+    for _ in range(count):
+        n = int(rng.choice(sizes))
+        probs.append({"n": n, "lam": float(rng.uniform(0.4, 1.6)), "z": float(np.exp(rng.uniform(np.log(100), np.log(2e4)))),
+                      "w0": float(rng.uniform(10, 200)), "off": tuple(rng.uniform(-0.1, 0.1, 2) * n),
+                      "seed": int(rng.integers(1 << 30))})
+    return probs
+
+
+def build_ragged(fo, probs):
+    systems = []
+    for pr in probs:
+        n = pr["n"]
+        rng = np.random.default_rng(pr["seed"])
+        x, y = fo.spatial_vectors((n, n), (1.0, 1.0))
+        u = fo.ScalarField(fo.gaussian(pr["w0"], x - pr["off"][0], y - pr["off"][1]).astype(np.complex64),
+                           (1.0, 1.0), pr["lam"])
+        fo.normalize_power_(u)
+        ph = fo.Phase(u, rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32), trainable=True, buffered=True)
+        system = fo.ScalarSource(u) | ph | fo.ASProp(u, pr["z"])
+        t = np.abs(fo.gaussian(pr["w0"], x, y)) ** 2
+        metric = fo.SquaredIntensityDifference((u, t))
+        src = system.source.u0
+        systems.append((system, metric, ph, src, src.similar(), src.similar()))
+    return systems
+
+
+def run_config5(args):
+    """Ragged batch of 64 ASProp forward + adjoint problems (256^2 .. 4096^2), one CUDA graph."""
+    from __graft_entry__ import build, load_package
+    build()
+    fo = load_package()
+    lib = fo.load_library()
+    probs = ragged_problems()
+    systems = build_ragged(fo, probs)
+
+    def step():
+        for system, metric, ph, src, x_, du in systems:
+            tape = []
+            system.forward(x_, tape, src=src)
+            metric(x_)
+            system.backward(du, tape, seed=(metric, x_))
+
+    ms, nk = _graph_time(fo, lib, step, max(3, args.steps // 2), args.warmup)
+    pix = sum(p["n"] ** 2 for p in probs)
+    return {"config": "ragged batch: 64 ASProp problems, N in {256..4096}^2 (seeded), random lambda/z/waist/"
+                      "offset/phase mask, intensity loss, fwd + adjoint, one CUDA graph of per-size launches",
+            "props_per_step": 2 * len(probs), "ms_per_step": round(ms, 3),
+            "value": round(2 * len(probs) / (ms * 1e-3), 1), "unit": UNIT, "gpu_launches_per_step": nk,
+            "pixels_per_step": pix, "algorithmic_gbs": round(2 * 16 * pix / (ms * 1e-3) / 1e9, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,6 +584,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain cuFFT comparison")
+    ap.add_argument("--config", type=int, default=3, choices=[2, 3, 4, 5],
+                    help="3: the 2048^2 x 48 headline (default); 2 / 4 / 5: the other configurations")
     ap.add_argument("--modes", type=int, default=16,
                     help="modes per wavelength (default 16; smaller values only for profiler captures)")
     args = ap.parse_args()
@@ -470,6 +618,11 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.config != 3:
+        if rank == 0:
+            fn = {2: run_config2, 4: run_config4, 5: run_config5}[args.config]
+            print(json.dumps(fn(args)))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")

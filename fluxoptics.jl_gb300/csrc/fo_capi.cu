@@ -507,6 +507,9 @@ void apply_overrides(fo_prop_plan p) {
   if (rv >= 0 && rv < row_variant_count(p->fx)) p->row_v = rv;
   if (cv >= 0 && cv < col_variant_count(p->fy)) p->col_v = cv;
   if (env_int("FO_PREFETCH", 1) == 0) p->row_pf = p->col_pf = false;
+  const int rpf = env_int("FO_ROW_PF", -1), cpf = env_int("FO_COL_PF", -1);
+  if (rpf >= 0) p->row_pf = rpf != 0;
+  if (cpf >= 0) p->col_pf = cpf != 0;
 }
 
 int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx, double dy,

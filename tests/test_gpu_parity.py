@@ -403,3 +403,23 @@ def test_every_pass_variant(fo, orc, n, monkeypatch):
             got = npy(system()["out"].electric).reshape(B, n, n)
             err = orc.rel_l2(got, ref)
             assert err < FIELD_TOL, (rv, cv, pf, err)
+
+
+def test_ragged_batch_per_problem(fo, orc):
+    """Ragged batch (sizes, wavelengths, distances, waists, offsets drawn per
+    problem, as in the benchmark's ragged configuration): every problem's loss and
+    mask gradient against the FP64 oracle."""
+    import bench
+    probs = bench.ragged_problems(seed=99, count=6, sizes=(64, 128, 256))
+    systems = bench.build_ragged(fo, probs)
+    for pr, (system, metric, ph, src, x_, du) in zip(probs, systems):
+        loss, grads = fo.withgradient(metric, system)
+        u0 = npy(src.electric)
+        phi = npy(ph.phi)
+        t = npy(metric.target)[0]
+        v = orc.asprop(orc.phase_forward(u0, phi), 1.0, 1.0, pr["lam"], pr["z"])
+        c, _ = orc.sid_value(v, t)
+        dv = orc.asprop(orc.sid_backward(v, t), 1.0, 1.0, pr["lam"], pr["z"], orc.BACKWARD)
+        _, g = orc.phase_backward(dv, phi, u0)
+        assert abs(float(loss) - c.sum()) / c.sum() < 1e-4
+        assert orc.rel_l2(npy(grads[ph]["phi"]), g) < GRAD_TOL
