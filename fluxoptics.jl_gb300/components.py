@@ -566,12 +566,20 @@ class OpticalSystem:
             u.electric.copy_(src.electric)
         return u
 
-    def backward(self, du: ScalarField, tape, seed=None):
-        """Adjoint sweep over a tape; returns {component: {name: grad}}."""
+    def backward(self, du: ScalarField, tape, seed=None, input_grad=None):
+        """Adjoint sweep over a tape; returns {component: {name: grad}}.
+
+        ``input_grad=False`` skips writing the gradient with respect to the system
+        input when a fused chain ends the sweep (default: only when the source is
+        not trainable)."""
         d = self.direction
+        if input_grad is None:
+            input_grad = self.source is None or getattr(self.source, "trainable", False)
         grads = {}
         first = True
-        for seg, saved in reversed(tape):
+        n_seg = len(tape)
+        for idx, (seg, saved) in enumerate(reversed(tape)):
+            last = idx == n_seg - 1
             if isinstance(seg, _Chain):
                 mods = (fo_mod * len(seg.mods))()
                 for k, m in enumerate(seg.mods):
@@ -582,15 +590,14 @@ class OpticalSystem:
                     mods[k] = m.fo_mod(saved=saved[k], grad=g)
                     if g is not None:
                         grads[m] = {m.pname: g}
+                flags = 0 if (input_grad or not last) else 1  # FO_BWD_DISCARD_INPUT_GRAD
                 if first and seed is not None:
                     sid, u_out = seed
-                    _capi.call("fo_chain_backward", self._chain_handle(seg, du), _ptr(du.electric), mods,
-                               int(d), sid.handle, _ptr(u_out.electric), _stream())
+                    _capi.call("fo_chain_backward_ex", self._chain_handle(seg, du), _ptr(du.electric), mods,
+                               int(d), sid.handle, _ptr(u_out.electric), flags, _stream())
                 else:
-                    if first and seed is not None:
-                        pass
-                    _capi.call("fo_chain_backward", self._chain_handle(seg, du), _ptr(du.electric), mods,
-                               int(d), None, None, _stream())
+                    _capi.call("fo_chain_backward_ex", self._chain_handle(seg, du), _ptr(du.electric), mods,
+                               int(d), None, None, flags, _stream())
             else:
                 if first and seed is not None:
                     sid, u_out = seed

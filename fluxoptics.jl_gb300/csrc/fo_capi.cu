@@ -344,7 +344,7 @@ int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, 
 // Adjoint sweep in reverse order, in place on du (src0 is du, or the forward
 // output when the sweep is seeded by the metric).
 int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du, const float2* src0,
-                 const Mod* mods, int s, const SeedArgs* seed, cudaStream_t st) {
+                 const Mod* mods, int s, const SeedArgs* seed, cudaStream_t st, bool discard_input_grad = false) {
   const int K = (int)props.size();
   const Layout L = layout_of(props[0]);
   const float* il = props[0]->inv_lambda;
@@ -355,7 +355,8 @@ int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du
     if (k > 0)
       FO_TRY(row_pass(L, buf, buf, true, true, mods[k], true, sf, il, nullptr, props[0]->tw_x, st));
     else
-      FO_TRY(row_pass(L, buf, du, true, false, mods[0], true, sf, il, nullptr, props[0]->tw_x, st));
+      FO_TRY(row_pass(L, buf, discard_input_grad ? nullptr : du, true, false, mods[0], true, sf, il, nullptr,
+                      props[0]->tw_x, st));
   }
   return FO_OK;
 }
@@ -874,6 +875,11 @@ FO_API int fo_chain_forward_from(fo_chain chain, const void* u_in, void* u, cons
 
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,
                              const void* u_out, void* stream) {
+  return fo_chain_backward_ex(chain, du, mods, direction, sid, u_out, 0, stream);
+}
+
+FO_API int fo_chain_backward_ex(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,
+                                const void* u_out, int flags, void* stream) {
   if (!chain || !du || !mods) return fail(FO_ERR_ARG, "chain, du and mods must not be NULL");
   FO_TRY(check_dir(direction));
   const int K = (int)chain->props.size();
@@ -896,7 +902,8 @@ FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int d
     seed.dc = sid->ones;
     src0 = reinterpret_cast<const float2*>(u_out);
   }
-  return run_backward(chain->props, buf, d, src0, m.data(), direction, sid ? &seed : nullptr, S(stream));
+  return run_backward(chain->props, buf, d, src0, m.data(), direction, sid ? &seed : nullptr, S(stream),
+                      (flags & FO_BWD_DISCARD_INPUT_GRAD) != 0);
 }
 
 }  // extern "C"

@@ -50,7 +50,9 @@ __device__ __forceinline__ void cp_async_wait() {
 // PF: stage the next field's row through cp.async (needs load_n == N).
 // Shared memory: 2 * LANES * SLOTS float2 (PF) or LANES * SLOTS float2.
 // --------------------------------------------------------------------------
-template <int N, int E, int LANES, int GK, bool PF>
+// FULL: the row count is a multiple of LANES and n_valid == N, so no
+// per-element guards are needed.
+template <int N, int E, int LANES, int GK, bool PF, bool FULL>
 __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
     row_pass_kernel(const RowPassArgs a, const float2* __restrict__ tw) {
   constexpr int T = N / E;
@@ -60,12 +62,13 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
   const int t = threadIdx.x % T;
   const int lane = threadIdx.x / T;
   const int y = blockIdx.y * LANES + lane;
-  const bool row_ok = y < a.nrows;
+  const bool row_ok = FULL || y < a.nrows;
   float2* buf0 = dsm + lane * SLOTS;
   float2* buf1 = dsm + (LANES + lane) * SLOTS;
 
-  const int load_n = a.inv_first ? N : a.n_valid;
-  const int store_n = a.fwd_after ? N : a.n_valid;
+  const int n_valid = FULL ? N : a.n_valid;
+  const int load_n = a.inv_first ? N : n_valid;
+  const int store_n = a.fwd_after ? N : n_valid;
   constexpr int GR = (GK == 1) ? E : 1;
   constexpr int GC = (GK == 2) ? E : 1;
   float gacc[GR];
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        sv[i] = (row_ok && p < a.n_valid) ? svp[p] : make_float2(0.f, 0.f);
+        sv[i] = (row_ok && p < n_valid) ? svp[p] : make_float2(0.f, 0.f);
       }
     }
     const float fb = (a.mod_kind == MOD_DN) ? a.mod_scale * a.inv_lambda[b] : 1.f;
@@ -138,7 +141,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
         float2 w = make_float2(1.f, 0.f);
-        if (p < a.n_valid) {
+        if (p < n_valid) {
           const long long q = (long long)y * a.param_ld + p;
           if (a.mod_kind == MOD_MASK) {
             w = reinterpret_cast<const float2*>(a.mod_param)[q];
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        v[i] = (p < a.n_valid) ? cconj(v[i]) : make_float2(0.f, 0.f);  // crop / re-pad
+        v[i] = (p < n_valid) ? cconj(v[i]) : make_float2(0.f, 0.f);  // crop / re-pad
       }
     }
     // ---- real-space operations at positions p = t + i*T, p < n_valid ----
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        if (p < a.n_valid) v[i] = cscale(v[i], k4 * rr[p]);
+        if (p < n_valid) v[i] = cscale(v[i], k4 * rr[p]);
       }
     }
     if (a.mod_kind != MOD_NONE && row_ok) {
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 #pragma unroll
           for (int i = 0; i < E; ++i) {
             const int p = t + i * T;
-            if (p < a.n_valid) svw[p] = v[i];
+            if (p < n_valid) svw[p] = v[i];
           }
         }
 #pragma unroll
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
     if (a.fwd_after) {
       fft_forward<N, E, 1>(v, t, tw, PF ? cur : buf0);
     }
-    if (row_ok) {
+    if (row_ok && a.dst) {  // a null destination discards the pass output (gradients only)
       float2* dst = a.dst + (long long)b * a.dst_bstride + (long long)y * a.dst_ld;
 #pragma unroll
       for (int i = 0; i < E; ++i) {
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        if (p < a.n_valid) {
+        if (p < n_valid) {
           const long long q = (long long)y * a.param_ld + p;
           if constexpr (GK == 2)
             reinterpret_cast<float2*>(a.grad)[q] = gacc_c[i];
@@ -245,7 +248,9 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 
-template <int N, int E, int W, bool PF, bool HS>
+// FULL: every column of the tile exists and all N rows are read and written
+// (y_in == y_out == N), so no per-element guards are needed.
+template <int N, int E, int W, bool PF, bool HS, bool FULL>
 __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     col_pass_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
   static_assert(W % 2 == 0, "16-byte staging needs an even tile width");
@@ -263,7 +268,10 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
   const int t = threadIdx.x / W;
   const int col0 = blockIdx.y * W;
   const int col = col0 + c;
-  const bool col_ok = col < a.ncols;
+  const bool col_ok = FULL || col < a.ncols;
+  const int y_in = FULL ? N : a.y_in;
+  const int y_out = FULL ? N : a.y_out;
+  const int ld = a.ld;
   const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
   const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
   auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
@@ -276,8 +284,8 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     for (int k = 0; k < CHUNKS / THREADS; ++k) {
       const int q = threadIdx.x + k * THREADS;
       const int row = q / (W / 2), cp = q % (W / 2);
-      if (row < a.y_in && col0 + 2 * cp < a.ncols)
-        cp_async16(dst + spad(row) * W + 2 * cp, src + (long long)row * a.ld + 2 * cp);
+      if (FULL || (row < y_in && col0 + 2 * cp < a.ncols))
+        cp_async16(dst + spad(row) * W + 2 * cp, src + row * ld + 2 * cp);
     }
   };
   if constexpr (HS) {
@@ -286,7 +294,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       for (int k = 0; k < CHUNKS / THREADS; ++k) {
         const int q = threadIdx.x + k * THREADS;
         const int row = q / (W / 2), cp = q % (W / 2);
-        if (col0 + 2 * cp < a.ncols) cp_async16(hs + row * W + 2 * cp, Hg + (long long)row * a.ncols + 2 * cp);
+        if (FULL || col0 + 2 * cp < a.ncols) cp_async16(hs + row * W + 2 * cp, Hg + row * a.ncols + 2 * cp);
       }
     }
   }
@@ -298,6 +306,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     cp_async_wait<0>();
     __syncthreads();
   }
+  const float2 hconj = make_float2(1.f, a.conj_h ? -1.f : 1.f);
 
   for (int f = f0; f < f1; ++f) {
     float2* buf = a.buf + (long long)field_of(f) * a.bstride + col;
@@ -312,13 +321,13 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        v[i] = (col_ok && p < a.y_in) ? cur[spad(p) * W + c] : make_float2(0.f, 0.f);
+        v[i] = (FULL || (col_ok && p < y_in)) ? cur[spad(p) * W + c] : make_float2(0.f, 0.f);
       }
     } else {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
-        v[i] = (col_ok && p < a.y_in) ? buf[(long long)p * a.ld] : make_float2(0.f, 0.f);
+        v[i] = (FULL || (col_ok && p < y_in)) ? buf[p * ld] : make_float2(0.f, 0.f);
       }
     }
     float2* ex = (PF ? cur : st0) + c;
@@ -328,7 +337,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 #pragma unroll
         for (int i = 0; i < E; ++i) {
           const int p = t + i * T;
-          if (p < a.y_out) buf[(long long)p * a.ld] = v[i];
+          if (FULL || p < y_out) buf[p * ld] = v[i];
         }
       }
     } else {
@@ -340,16 +349,17 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
         if constexpr (HS)
           hv = hs[p * W + c];
         else
-          hv = col_ok ? Hg[(long long)p * a.ncols + c] : make_float2(0.f, 0.f);
-        if (a.conj_h) hv = cconj(hv);
-        v[i] = cconj(cmul(v[i], hv));
+          hv = col_ok ? Hg[p * a.ncols + c] : make_float2(0.f, 0.f);
+        hv.y *= hconj.y;  // conj(H) for the adjoint direction
+        // conj(X * H) = (xr hr - xi hi, -(xr hi + xi hr))
+        v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
       }
       fft_forward<N, E, W>(v, t, tw, ex);
       if (col_ok) {
 #pragma unroll
         for (int i = 0; i < E; ++i) {
           const int p = t + i * T;
-          if (p < a.y_out) buf[(long long)p * a.ld] = cconj(v[i]);
+          if (FULL || p < y_out) buf[p * ld] = cconj(v[i]);
         }
       }
     }
@@ -598,11 +608,17 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
   const size_t smem = SH::smem(pf);
   dim3 grid((a.batch + a.fields_per_cta - 1) / a.fields_per_cta, (a.nrows + LANES - 1) / LANES);
   const bool grad = a.mod_bwd && a.grad != nullptr && a.mod_kind != MOD_NONE;
+  const bool full = a.n_valid == N && a.nrows % LANES == 0;
   cudaError_t e = cudaSuccess;
-#define FO_ROW_GO(GK, PFV)                                                      \
-  do {                                                                          \
-    e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV>, smem);                  \
-    if (e == cudaSuccess) row_pass_kernel<N, E, LANES, GK, PFV><<<grid, SH::threads, smem, s>>>(a, tw); \
+#define FO_ROW_GO(GK, PFV)                                                                        \
+  do {                                                                                            \
+    if (full) {                                                                                   \
+      e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV, true>, smem);                            \
+      if (e == cudaSuccess) row_pass_kernel<N, E, LANES, GK, PFV, true><<<grid, SH::threads, smem, s>>>(a, tw); \
+    } else {                                                                                      \
+      e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV, false>, smem);                           \
+      if (e == cudaSuccess) row_pass_kernel<N, E, LANES, GK, PFV, false><<<grid, SH::threads, smem, s>>>(a, tw); \
+    }                                                                                             \
   } while (0)
   if (!grad) {
     if (pf) FO_ROW_GO(0, true); else FO_ROW_GO(0, false);
@@ -628,6 +644,7 @@ template <int N, int E, int W, int P>
 cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
   constexpr int threads = (W / (P == 2 ? 2 : 1)) * (N / E);
   dim3 grid(a.n_items, (a.ncols + W - 1) / W);
+  const bool full = a.y_in == N && a.y_out == N && a.ncols % W == 0;
   cudaError_t e;
 #define FO_COL_GO(PFV, HSV)                                                                     \
   do {                                                                                          \
@@ -635,9 +652,12 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     if constexpr (P == 2) {                                                                     \
       e = set_smem(col_pass2_kernel<N, E, W, PFV, HSV>, smem);                                  \
       if (e == cudaSuccess) col_pass2_kernel<N, E, W, PFV, HSV><<<grid, threads, smem, s>>>(a, tw); \
+    } else if (full) {                                                                          \
+      e = set_smem(col_pass_kernel<N, E, W, PFV, HSV, true>, smem);                             \
+      if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV, true><<<grid, threads, smem, s>>>(a, tw); \
     } else {                                                                                    \
-      e = set_smem(col_pass_kernel<N, E, W, PFV, HSV>, smem);                                   \
-      if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV><<<grid, threads, smem, s>>>(a, tw);  \
+      e = set_smem(col_pass_kernel<N, E, W, PFV, HSV, false>, smem);                            \
+      if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV, false><<<grid, threads, smem, s>>>(a, tw); \
     }                                                                                           \
   } while (0)
   if constexpr (P == 0) {

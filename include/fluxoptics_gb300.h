@@ -214,6 +214,13 @@ typedef struct fo_sid_s* fo_sid;
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction,
                              fo_sid sid, const void* u_out, void* stream);
 
+/* fo_chain_backward with flags.  FO_BWD_DISCARD_INPUT_GRAD: only the parameter
+ * gradients are wanted (the chain's input is not trainable); the final write of
+ * the input gradient is skipped and du is left holding scratch values. */
+#define FO_BWD_DISCARD_INPUT_GRAD 1
+FO_API int fo_chain_backward_ex(fo_chain chain, void* du, const fo_mod* mods, int direction,
+                                fo_sid sid, const void* u_out, int flags, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* AS_BPM                                                                  */
 /* ---------------------------------------------------------------------- */
