@@ -267,21 +267,46 @@ def run_gb300(args, rank, world):
                    "col": col_ms}
         pass_share = {k: arr_ms[i] / max(1e-9, sum(arr_ms)) for i, k in enumerate(pass_ms)}
 
-        # end to end through the public C ABI with host buffers: H2D of the 48 input
-        # fields from pinned memory, the captured iteration, D2H of the loss
+        # end to end through the public C ABI with host buffers: every step copies its
+        # 48 input fields host->device from pinned memory and reads the loss back.
+        # Two input buffers, each with its own captured iteration, let the copy of
+        # step k+1 (on a copy stream) overlap the compute of step k.
         host_in = torch.from_numpy(fields_np).pin_memory()
-        host_loss = torch.empty(len(LAMBDAS), dtype=torch.float32).pin_memory()
+        host_loss = torch.empty((max(1, min(args.steps, 5)), len(LAMBDAS)), dtype=torch.float32).pin_memory()
+        src_b = src.similar()
+        g_b = C.c_void_p()
+        fo._capi.check(lib.fo_graph_begin(sp))
+        iteration(fo, system, metric, opt, x, du, src_b)
+        fo._capi.check(lib.fo_graph_end(sp, C.byref(g_b)))
+        bufs, graphs = (src, src_b), (g, g_b)
+        copy_stream = torch.cuda.Stream()
+        ev_copied = [torch.cuda.Event(), torch.cuda.Event()]
+        ev_done = [torch.cuda.Event(), torch.cuda.Event()]
         torch.cuda.synchronize()
         e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e2_steps = max(1, min(args.steps, 5))
+        e2_steps = host_loss.shape[0]
         e2.record(stream)
-        for _ in range(e2_steps):
-            src.electric.copy_(host_in, non_blocking=True)
-            fo._capi.check(lib.fo_graph_launch(g, sp))
-            host_loss.copy_(metric.loss, non_blocking=True)
+        copy_stream.wait_event(e2)
+        with torch.cuda.stream(copy_stream):
+            bufs[0].electric.copy_(host_in, non_blocking=True)
+            ev_copied[0].record(copy_stream)
+        for k in range(e2_steps):
+            cur = k % 2
+            if k + 1 < e2_steps:
+                nxt = (k + 1) % 2
+                if k >= 1:
+                    copy_stream.wait_event(ev_done[nxt])
+                with torch.cuda.stream(copy_stream):
+                    bufs[nxt].electric.copy_(host_in, non_blocking=True)
+                    ev_copied[nxt].record(copy_stream)
+            stream.wait_event(ev_copied[cur])
+            fo._capi.check(lib.fo_graph_launch(graphs[cur], sp))
+            host_loss[k].copy_(metric.loss, non_blocking=True)
+            ev_done[cur].record(stream)
         e3.record(stream)
         stream.synchronize()
         e2e_ms = e2.elapsed_time(e3) / e2_steps
+        fo._capi.check(lib.fo_graph_destroy(g_b))
         fo._capi.check(lib.fo_graph_destroy(g))
 
     peaks = {}
@@ -313,7 +338,8 @@ def run_gb300(args, rank, world):
         "gpu_launches": int(nk.value) * args.steps,
         "gpu_launches_per_step": int(nk.value),
         "e2e": {"value": round(props_per_step / (e2e_ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
-                "h2d_bytes_per_step": int(fields_np.nbytes), "d2h_bytes_per_step": int(host_loss.numel() * 4)},
+                "h2d_bytes_per_step": int(fields_np.nbytes), "d2h_bytes_per_step": int(len(LAMBDAS) * 4),
+                "overlap": "input copy of step k+1 on a copy stream overlaps the compute of step k"},
         "clocks": clk.summary(),
         "final_loss": final_loss,
     }

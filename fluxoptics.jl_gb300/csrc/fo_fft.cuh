@@ -223,7 +223,13 @@ struct Dft<16> {
 };
 
 // Shared-memory slot of element `pos` (one pad slot per 16 elements).
-__device__ __forceinline__ int spad(int pos) { return pos + (pos >> 4); }
+__host__ __device__ __forceinline__ constexpr int spad(int pos) { return pos + (pos >> 4); }
+
+// For powers of two Ns, R and a Stockham destination d of span Ns (or a source
+// position j < M with M a power of two), the padded slot of d + r*Ns is
+// spad(d) + padoff(r*Ns): the low four bits of d never carry into the offset.
+// Addresses are then one padded base per butterfly plus compile-time offsets.
+__host__ __device__ constexpr int padoff(int k) { return k + k / 16; }
 
 template <int N>
 struct SmemSize {
@@ -247,8 +253,9 @@ __device__ __forceinline__ void stage_from_smem(V (&v)[E], int t, const float2* 
 #pragma unroll
   for (int m = 0; m < NB; ++m) {
     const int j = t + m * T;
+    const V* base = sm + spad(j) * PS;
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[m * R + r] = sm[spad(j + r * (N / R)) * PS];
+    for (int r = 0; r < R; ++r) v[m * R + r] = base[padoff(r * (N / R)) * PS];
     if constexpr (Ns > 1) {
       const int k = j & (Ns - 1);
 #pragma unroll
@@ -273,8 +280,9 @@ __device__ __forceinline__ void stage_to_smem(const V (&v)[E], int t, V* sm) {
   for (int m = 0; m < NB; ++m) {
     const int j = t + m * T;
     const int d = (j / Ns) * Ns * R + (j & (Ns - 1));
+    V* base = sm + spad(d) * PS;
 #pragma unroll
-    for (int r = 0; r < R; ++r) sm[spad(d + r * Ns) * PS] = v[m * R + Dft<R>::out(r)];
+    for (int r = 0; r < R; ++r) base[padoff(r * Ns) * PS] = v[m * R + Dft<R>::out(r)];
   }
 }
 
