@@ -916,8 +916,10 @@ struct fo_bpm_s {
   int nx = 0, ny = 0, batch = 0, n_slices = 0, every = 1, n_ckpt = 0;
   double kdz = 0;
   float2* ckpt = nullptr;  // n_ckpt x batch x ny x nx
-  float2* seg = nullptr;   // every x batch x ny x nx (slot 0 unused)
+  float2* seg = nullptr;   // 2 x every x batch x ny x nx (slot 0 of each half unused): segments alternate halves
   float2* rbuf = nullptr;  // recompute field
+  cudaStream_t aux = nullptr;  // recomputes the next segment while the adjoint sweeps the current one
+  cudaEvent_t ev_fork = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_use[2] = {nullptr, nullptr};
   size_t ws_bytes = 0;
 };
 
@@ -951,7 +953,7 @@ FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, doub
   b->kdz = 2.0 * M_PI * dz / cos_correction;
   const size_t field = (size_t)batch * ny * nx;
   if ((rc = dalloc(&b->ckpt, field * b->n_ckpt, "BPM checkpoints")) != FO_OK ||
-      (every > 1 && (rc = dalloc(&b->seg, field * every, "BPM segment")) != FO_OK) ||
+      (every > 1 && (rc = dalloc(&b->seg, 2 * field * every, "BPM segments")) != FO_OK) ||
       (every > 1 && (rc = dalloc(&b->rbuf, field, "BPM recompute field")) != FO_OK)) {
     cudaFree(b->ckpt);
     cudaFree(b->seg);
@@ -960,7 +962,19 @@ FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, doub
     delete b;
     return rc;
   }
-  b->ws_bytes = sizeof(float2) * field * (b->n_ckpt + (every > 1 ? every + 1 : 0)) + b->full->ws_bytes +
+  if (every > 1) {
+    cudaError_t e = cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+      e = cudaEventCreateWithFlags(&b->ev_rec[i], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_use[i], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+      fo_bpm_destroy(b);
+      return cuda_fail(e, "BPM helper stream");
+    }
+  }
+  b->ws_bytes = sizeof(float2) * field * (b->n_ckpt + (every > 1 ? 2 * every + 1 : 0)) + b->full->ws_bytes +
                 b->half->ws_bytes;
   *bpm = b;
   return FO_OK;
@@ -968,6 +982,12 @@ FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, doub
 
 FO_API int fo_bpm_destroy(fo_bpm b) {
   if (!b) return FO_OK;
+  if (b->aux) cudaStreamDestroy(b->aux);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  for (int i = 0; i < 2; ++i) {
+    if (b->ev_rec[i]) cudaEventDestroy(b->ev_rec[i]);
+    if (b->ev_use[i]) cudaEventDestroy(b->ev_use[i]);
+  }
   cudaFree(b->ckpt);
   cudaFree(b->seg);
   cudaFree(b->rbuf);
@@ -991,7 +1011,8 @@ namespace {
 float2* bpm_slot(fo_bpm b, int k) {
   const size_t field = (size_t)b->batch * b->ny * b->nx;
   if (k % b->every == 0) return b->ckpt + field * (k / b->every);
-  return b->seg + field * (k % b->every);
+  const int half = (k / b->every) & 1;  // consecutive segments use alternate halves
+  return b->seg + field * ((size_t)half * b->every + k % b->every);
 }
 
 Mod dn_mod(fo_bpm b, const float* dn, int k, void* saved, void* grad) {
@@ -1054,16 +1075,40 @@ FO_API int fo_bpm_backward(fo_bpm b, void* du, const float* dn, float* ddn, int 
   const Layout L = layout_of(b->full);
   const float* il = b->full->inv_lambda;
   const float2* tw = b->full->tw_x;
+  const int every = b->every;
+  const int top = (n - 1) / every;
+  bool use_recorded[2] = {false, false};
+  // Segment g is recomputed on the helper stream (into half g%2 of the segment
+  // buffer) while the adjoint sweeps segment g+1 on the caller's stream.
+  auto launch_recompute = [&](int g) -> int {
+    if (use_recorded[g & 1]) FO_LAUNCH(cudaStreamWaitEvent(b->aux, b->ev_use[g & 1], 0));
+    FO_TRY(bpm_recompute(b, dn, g, s, b->aux));
+    FO_LAUNCH(cudaEventRecord(b->ev_rec[g & 1], b->aux));
+    return FO_OK;
+  };
+  if (every > 1) {
+    FO_LAUNCH(cudaEventRecord(b->ev_fork, st));  // dn and the checkpoints are ready on st
+    FO_LAUNCH(cudaStreamWaitEvent(b->aux, b->ev_fork, 0));
+    FO_TRY(launch_recompute(top));
+  }
   Mod none;
   FO_TRY(row_pass(L, d, d, false, true, none, true, sf, il, nullptr, tw, st));
   FO_TRY(col_pass(b->half, d, s > 0, st));
-  for (int k = n - 1; k >= 0; --k) {
-    const int g = k / b->every;
-    const bool top = (k == n - 1) || ((k + 1) % b->every == 0);
-    if (top && b->every > 1) FO_TRY(bpm_recompute(b, dn, g, s, st));
-    Mod m = dn_mod(b, dn, k, bpm_slot(b, k), ddn ? (void*)(ddn + (size_t)k * b->ny * b->nx) : nullptr);
-    FO_TRY(row_pass(L, d, d, true, true, m, true, sf, il, nullptr, tw, st));
-    FO_TRY(col_pass(k > 0 ? b->full : b->half, d, s > 0, st));
+  for (int g = top; g >= 0; --g) {
+    if (every > 1) {
+      FO_LAUNCH(cudaStreamWaitEvent(st, b->ev_rec[g & 1], 0));
+      if (g > 0) FO_TRY(launch_recompute(g - 1));
+    }
+    const int k_hi = std::min(n - 1, (g + 1) * every - 1);
+    for (int k = k_hi; k >= g * every; --k) {
+      Mod m = dn_mod(b, dn, k, bpm_slot(b, k), ddn ? (void*)(ddn + (size_t)k * b->ny * b->nx) : nullptr);
+      FO_TRY(row_pass(L, d, d, true, true, m, true, sf, il, nullptr, tw, st));
+      FO_TRY(col_pass(k > 0 ? b->full : b->half, d, s > 0, st));
+    }
+    if (every > 1) {
+      FO_LAUNCH(cudaEventRecord(b->ev_use[g & 1], st));
+      use_recorded[g & 1] = true;
+    }
   }
   return row_pass(L, d, d, true, false, none, true, sf, il, nullptr, tw, st);
 }
