@@ -41,6 +41,7 @@ SIGNATURES = {
     "fo_version": (_i, []),
     "fo_last_error": (C.c_char_p, []),
     "fo_stream_synchronize": (_i, [_vp]),
+    "fo_device_status": (_i, [_vp]),
     "fo_profile_begin": (_i, []),
     "fo_profile_end": (_i, [_pd, _pi]),
     "fo_asprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i]),

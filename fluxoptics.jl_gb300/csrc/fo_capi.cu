@@ -16,6 +16,9 @@
 #include <vector>
 
 #include "../../include/fluxoptics_gb300.h"
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "fo_aux.h"
 #include "fo_fft.cuh"
 #include "fo_internal.h"
@@ -81,6 +84,67 @@ const float2* twiddles(int N, int E, int* err) {
   return d;
 }
 
+// ---------------------------------------------------------------------------
+// Device error word (one per device): kernels with bounded waits set bit 0 when
+// a wait gives up; fo_device_status reads and clears it.
+// ---------------------------------------------------------------------------
+static std::mutex g_err_mu;
+static std::map<int, unsigned int*> g_err_words;
+
+unsigned int* device_error_word(int* err) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    *err = cuda_fail(e, "cudaGetDevice");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  auto it = g_err_words.find(dev);
+  if (it != g_err_words.end()) return it->second;
+  unsigned int* w = nullptr;
+  e = cudaMalloc(&w, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(w, 0, sizeof(unsigned int));
+  if (e != cudaSuccess) {
+    *err = cuda_fail(e, "device error word");
+    return nullptr;
+  }
+  g_err_words[dev] = w;
+  return w;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on the driver library).
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder(int* err) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  if (!fn) *err = fail(FO_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  return fn;
+}
+
+int encode_tmap_2d(void* tmap, const void* base, long long rows, int cols, int ld, int box_cols, int box_rows) {
+  int err = FO_OK;
+  auto fn = tmap_encoder(&err);
+  if (!fn) return err;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(FO_ERR_ARG, "TMA base address not 16-byte aligned");
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float2)};
+  const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(reinterpret_cast<CUtensorMap*>(tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void*>(base),
+                  dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(FO_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return FO_OK;
+}
+
 }  // namespace fo
 
 using namespace fo;
@@ -97,6 +161,11 @@ int next_pow2(int n) {
 }
 
 cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  return (v && *v) ? atoi(v) : dflt;
+}
 
 int check_dir(int d) {
   if (d != FO_FORWARD && d != FO_BACKWARD) return fail(FO_ERR_ARG, "direction must be FO_FORWARD (1) or FO_BACKWARD (-1)");
@@ -147,6 +216,8 @@ struct fo_prop_plan_s {
   int n_items = 0;
   int row_v = 0, col_v = 0;     // launch-shape variants (autotuned or default)
   bool row_pf = true, col_pf = true;
+  unsigned int* err_word = nullptr;         // device error word (bounded waits)
+  unsigned long long wait_ns = 1000000000ull;  // limit of a bounded device wait
   float* inv_lambda = nullptr;  // device, per field
   const float2* tw_x = nullptr;
   const float2* tw_y = nullptr;
@@ -317,9 +388,30 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.field_list = p->sorted_fields;
   a.item_start = p->items;
   a.n_items = p->n_items;
-  const bool pf = p->col_pf && col_prefetch_fits(p->fy, p->col_v);
+  int v = p->col_v;
+  const float2* tw = p->tw_y;
+  alignas(64) CUtensorMap tm_buf, tm_h;
+  if (col_variant_uses_tma(p->fy, v)) {
+    const int W = col_variant(p->fy, v).lanes;
+    int rc = encode_tmap_2d(&tm_buf, buf, (long long)p->batch * p->ny, p->fx, p->fx, W, 256);
+    if (rc == FO_OK) rc = encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256);
+    if (rc != FO_OK) {  // e.g. an unaligned caller buffer: use the cp.async variant
+      v = 0;
+      int trc = FO_OK;
+      tw = twiddles(p->fy, col_variant(p->fy, 0).E, &trc);
+      if (!tw) return trc;
+    } else {
+      a.tmap_buf = &tm_buf;
+      a.tmap_h = &tm_h;
+      a.rows_per_field = p->ny;
+      a.err_word = p->err_word;
+      a.wait_ns = p->wait_ns;
+      a.test_skip_copy = env_int("FO_TEST_SKIP_COPY", 0);
+    }
+  }
+  const bool pf = p->col_pf && col_prefetch_fits(p->fy, v);
   ProfScope prof(2, st);
-  FO_LAUNCH(launch_col_pass(p->fy, p->col_v, pf, a, p->tw_y, st));
+  FO_LAUNCH(launch_col_pass(p->fy, v, pf, a, tw, st));
   return FO_OK;
 }
 
@@ -370,10 +462,6 @@ int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int, int>, std::tuple<int, bool, int, bool>> g_tune;
 
-int env_int(const char* name, int dflt) {
-  const char* v = getenv(name);
-  return (v && *v) ? atoi(v) : dflt;
-}
 
 float time_launches(const std::function<cudaError_t()>& fn, int reps) {
   cudaEvent_t a, b;
@@ -478,6 +566,19 @@ int autotune_plan(fo_prop_plan p) {
       a.field_list = idx;
       a.item_start = idx + nb;
       a.n_items = n_items;
+      alignas(64) CUtensorMap tm_buf, tm_h;
+      if (col_variant_uses_tma(p->fy, v)) {
+        if (pf) continue;  // staging is built in
+        const int W = col_variant(p->fy, v).lanes;
+        if (encode_tmap_2d(&tm_buf, tmp, (long long)nb * p->ny, p->fx, p->fx, W, 256) != FO_OK ||
+            encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256) != FO_OK)
+          continue;
+        a.tmap_buf = &tm_buf;
+        a.tmap_h = &tm_h;
+        a.rows_per_field = p->ny;
+        a.err_word = p->err_word;
+        a.wait_ns = p->wait_ns;
+      }
       int trc = FO_OK;
       const float2* tw = twiddles(p->fy, col_variant(p->fy, v).E, &trc);
       if (!tw) continue;
@@ -567,6 +668,15 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     return rc;
   }
   p->ws_bytes = sizeof(float2) * table * p->n_tables + (sizeof(int) + sizeof(float)) * batch;
+  p->err_word = device_error_word(&rc);
+  if (!p->err_word) {
+    plan_free(p);
+    return rc;
+  }
+  {
+    const char* w = getenv("FO_WAIT_NS");
+    if (w && *w) p->wait_ns = strtoull(w, nullptr, 10);
+  }
   if (kind == 1) {
     if ((rc = dalloc(&p->scratch, (size_t)batch * ny * fx, "padded scratch")) != FO_OK) {
       plan_free(p);
@@ -701,6 +811,20 @@ FO_API int fo_profile_end(double* ms, int* launches) {
     if (launches) launches[k] = cnt[k];
   }
   return rc;
+}
+
+FO_API int fo_device_status(void* stream) {
+  cudaError_t e = cudaStreamSynchronize(S(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  int rc = FO_OK;
+  unsigned int* w = device_error_word(&rc);
+  if (!w) return rc;
+  unsigned int h = 0;
+  e = cudaMemcpy(&h, w, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && h) e = cudaMemset(w, 0, sizeof(unsigned int));
+  if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
+  if (h & 1u) return fail(FO_ERR_TIMEOUT, "a bounded device wait gave up (TMA copy did not complete in time)");
+  return FO_OK;
 }
 
 FO_API int fo_stream_synchronize(void* stream) {

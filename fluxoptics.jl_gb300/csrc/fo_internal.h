@@ -80,7 +80,24 @@ struct ColPassArgs {
   const int* field_list;  // fields ordered so that each work item shares one table
   const int* item_start;  // n_items+1 offsets into field_list (null: one field per item)
   int n_items;
+  // TMA variants: host addresses of the tensor maps (CUtensorMap) of the buffer,
+  // viewed as rows_total x ncols, and of the transfer functions; the rows of one
+  // field in the buffer; the device error word and the wait limit.
+  const void* tmap_buf;
+  const void* tmap_h;
+  int rows_per_field;
+  unsigned int* err_word;
+  unsigned long long wait_ns;
+  int test_skip_copy;  // test knob: arm the barrier but issue no copy (the wait must time out)
 };
+
+// Device error word of the current device (allocated once, zero).  Bit 0: a bounded
+// wait in a kernel gave up.
+unsigned int* device_error_word(int* err);
+// Host helpers for the TMA variants: encode a 2-D tiled tensor map over a
+// float2 array of `rows` x `cols` (row stride `ld` elements) with boxes of
+// box_cols x box_rows.  Returns FO_OK or an FO_ERR_* code.
+int encode_tmap_2d(void* tmap, const void* base, long long rows, int cols, int ld, int box_cols, int box_rows);
 
 // Launch-shape variants (fo_variants.h): E elements per thread, `lanes` rows or
 // columns per CTA.  N is the FFT length along the transformed axis; supported:
@@ -99,6 +116,7 @@ size_t row_smem_bytes(int N, int v, bool pf);
 size_t col_smem_bytes(int N, int v, bool pf);
 bool row_prefetch_fits(int N, int v);
 bool col_prefetch_fits(int N, int v);
+bool col_variant_uses_tma(int N, int v);
 cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s);
 cudaError_t launch_col_pass(int N, int v, bool pf, const ColPassArgs& a, const float2* tw, cudaStream_t s);
 

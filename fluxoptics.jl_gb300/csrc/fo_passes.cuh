@@ -18,6 +18,8 @@
 // The staging buffer of the current field doubles as the FFT exchange buffer.
 #pragma once
 
+#include <cuda.h>
+
 #include "fo_fft.cuh"
 #include "fo_internal.h"
 
@@ -588,6 +590,163 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 }
 
 // --------------------------------------------------------------------------
+// TMA column pass: the tile of the next field is fetched by the tensor-memory
+// accelerator (cp.async.bulk.tensor, boxes of W columns x 256 rows, completion
+// on an mbarrier) into a dense staging buffer as soon as the current field's
+// registers are loaded; the H tile of the work item is fetched the same way.
+// FFT exchanges use a separate padded buffer.  Every mbarrier wait is bounded
+// by %globaltimer: on expiry the CTA sets bit 0 of the device error word and
+// returns (no copy is left in flight).
+// Shared memory: 128 (alignment) + 2 * N * W + W * SLOTS float2 + 16 bytes.
+// --------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait for phase `parity` of `bar`: false when `limit_ns` elapsed first.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, int y, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+template <int N, int E, int W>
+__global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
+    col_tma_kernel(const ColPassArgs a, const float2* __restrict__ tw, const __grid_constant__ CUtensorMap tm_buf,
+                   const __grid_constant__ CUtensorMap tm_h) {
+  constexpr int T = N / E;
+  constexpr int SLOTS = SmemSize<N>::value;
+  constexpr int BOX = 256;
+  extern __shared__ float4 dsm4[];
+  char* base = reinterpret_cast<char*>(((reinterpret_cast<unsigned long long>(dsm4) + 127) >> 7) << 7);
+  float2* stage = reinterpret_cast<float2*>(base);  // dense [N][W]
+  float2* hs = stage + N * W;                         // dense [N][W]
+  float2* ex = hs + N * W;                            // padded exchange [SLOTS][W]
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(ex + W * SLOTS);  // [0] tile, [1] H
+  __shared__ int s_abort;
+
+  const int c = threadIdx.x % W;
+  const int t = threadIdx.x / W;
+  const int col0 = blockIdx.y * W;
+  const int col = col0 + c;
+  const bool col_ok = col < a.ncols;
+  const int y_in = a.y_in, y_out = a.y_out, ld = a.ld;
+  const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
+  const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
+  auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
+  const int nbox = (y_in + BOX - 1) / BOX;
+  const unsigned tile_bytes = (unsigned)(nbox * BOX * W * sizeof(float2));
+
+  auto issue_tile = [&](int f) {  // one thread
+    mbar_expect_tx(&bar[0], tile_bytes);
+    if (a.test_skip_copy) return;
+    const int y0 = field_of(f) * a.rows_per_field;
+    for (int k = 0; k < nbox; ++k) tma_load_2d(stage + k * BOX * W, &tm_buf, col0, y0 + k * BOX, &bar[0]);
+  };
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_proxy_async();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!a.fft_only) {
+      mbar_expect_tx(&bar[1], (unsigned)(N * W * sizeof(float2)));
+      const int hy0 = a.h_index[field_of(f0)] * N;
+      for (int k = 0; k < N / BOX; ++k) tma_load_2d(hs + k * BOX * W, &tm_h, col0, hy0 + k * BOX, &bar[1]);
+    }
+    if (f0 < f1) issue_tile(f0);
+  }
+  bool ok = true;
+  if (!a.fft_only) ok = mbar_wait_bounded(&bar[1], 0, a.wait_ns);
+  unsigned phase = 0;
+  const float hsign = a.conj_h ? -1.f : 1.f;
+
+  for (int f = f0; f < f1; ++f) {
+    const unsigned wait_phase = phase;
+    if (ok) ok = mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
+    phase ^= 1u;
+    if (!ok) s_abort = 1;
+    float2 v[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+      const int p = t + i * T;
+      v[i] = (col_ok && p < y_in) ? stage[p * W + c] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();  // the staging buffer is free again; abort decision is uniform
+    if (s_abort) {
+      if (threadIdx.x == 0) {
+        atomicOr(a.err_word, 1u);
+        // let copies still in flight land (bounded) before the CTA's memory is released
+        if (!a.test_skip_copy) mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
+      }
+      return;
+    }
+    if (threadIdx.x == 0 && f + 1 < f1) {
+      fence_proxy_async();
+      issue_tile(f + 1);
+    }
+    fft_forward<N, E, W>(v, t, tw, ex + c);
+    float2* out = a.buf + (long long)field_of(f) * a.bstride + col;
+    if (a.fft_only) {
+      if (col_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          const int p = t + i * T;
+          if (p < y_out) out[p * ld] = v[i];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        float2 hv = hs[(t + i * T) * W + c];
+        hv.y *= hsign;
+        v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
+      }
+      fft_forward<N, E, W>(v, t, tw, ex + c);
+      if (col_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          const int p = t + i * T;
+          if (p < y_out) out[p * ld] = cconj(v[i]);
+        }
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
 // Launch helpers used by the per-size translation units.
 // --------------------------------------------------------------------------
 template <int N, int E, int LANES>
@@ -660,7 +819,16 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
       if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV, false><<<grid, threads, smem, s>>>(a, tw); \
     }                                                                                           \
   } while (0)
-  if constexpr (P == 0) {
+  if constexpr (P == 4) {
+    constexpr size_t smem_t = 128 + sizeof(float2) * ((size_t)2 * N * W + (size_t)W * SmemSize<N>::value) + 16;
+    static_assert(smem_t <= kMaxSmemPerCta, "TMA column variant does not fit");
+    (void)pf;
+    if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
+    e = set_smem(col_tma_kernel<N, E, W>, smem_t);
+    if (e == cudaSuccess)
+      col_tma_kernel<N, E, W><<<grid, threads, smem_t, s>>>(a, tw, *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
+                                                              *reinterpret_cast<const CUtensorMap*>(a.tmap_h));
+  } else if constexpr (P == 0) {
     constexpr int LS = LaneStride<N>::value;
     constexpr size_t smem_hs = sizeof(float2) * ((size_t)2 * W * LS + (size_t)W * (N + 4));
     constexpr size_t smem_nohs = sizeof(float2) * ((size_t)2 * W * LS);

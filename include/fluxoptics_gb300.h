@@ -70,6 +70,13 @@ FO_API const char* fo_last_error(void);
 /* Blocks until all work on `stream` is done; reports device-side errors. */
 FO_API int fo_stream_synchronize(void* stream);
 
+/* Synchronises `stream`, then reads and clears the device error word of the
+ * current device: FO_ERR_TIMEOUT when a kernel's bounded wait (an mbarrier wait
+ * on a TMA copy, limit FO_WAIT_NS nanoseconds, default 1 s) gave up since the
+ * last call.  Such a kernel returns without finishing its tile; the context stays
+ * usable.  No counterpart in the reference (it has no device-side waits). */
+FO_API int fo_device_status(void* stream);
+
 /* Per-pass timing of the calls made between begin and end (eager calls only,
  * not graph replays): CUDA events around every pass launch.  ms[3] / launches[3]
  * receive the summed device time and the launch count of the single row

@@ -379,7 +379,7 @@ def test_graph_capture_replays_iteration(fo, orc):
 # Every launch-shape variant of the passes (forced through the environment)
 # ---------------------------------------------------------------------------
 
-_VARIANTS = {512: (3, 4), 1024: (4, 5), 2048: (4, 5), 4096: (2, 4)}
+_VARIANTS = {512: (3, 6), 1024: (4, 6), 2048: (4, 7), 4096: (2, 5)}
 
 
 @pytest.mark.parametrize("n", sorted(_VARIANTS))
@@ -423,3 +423,32 @@ def test_ragged_batch_per_problem(fo, orc):
         _, g = orc.phase_backward(dv, phi, u0)
         assert abs(float(loss) - c.sum()) / c.sum() < 1e-4
         assert orc.rel_l2(npy(grads[ph]["phi"]), g) < GRAD_TOL
+
+
+def test_bounded_wait_reports_timeout(fo, orc, monkeypatch):
+    """Failure detection without a GPU fault: a TMA column pass whose barrier is
+    armed but whose copy is never issued must give up after its bounded wait (20 ms
+    here), report FO_ERR_TIMEOUT through fo_device_status, and leave the context
+    usable (the next, normal call is correct)."""
+    capi = fo._capi
+    lib = capi.load()
+    n = 512
+    rng = np.random.default_rng(77)
+    u0 = rand_field(rng, (n, n))
+    monkeypatch.setenv("FO_AUTOTUNE", "0")
+    monkeypatch.setenv("FO_COL_VARIANT", "4")  # a TMA variant for 512
+    monkeypatch.setenv("FO_WAIT_NS", "20000000")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.fo_device_status(stream) == 0
+    u = fo.ScalarField(u0, (1.0, 1.0), 1.064)
+    p = fo.ASProp(u, 300.0)
+    monkeypatch.setenv("FO_TEST_SKIP_COPY", "1")
+    v = u.copy()
+    p.propagate_(v)
+    rc = lib.fo_device_status(stream)
+    assert rc == 5, rc  # FO_ERR_TIMEOUT
+    assert "bounded device wait" in lib.fo_last_error().decode()
+    monkeypatch.setenv("FO_TEST_SKIP_COPY", "0")
+    v = p.propagate(u)
+    assert lib.fo_device_status(stream) == 0
+    assert orc.rel_l2(npy(v.electric), orc.asprop(u0, 1.0, 1.0, 1.064, 300.0)) < FIELD_TOL
