@@ -20,6 +20,8 @@
 
 #include <cuda.h>
 
+#include <utility>
+
 #include "fo_fft.cuh"
 #include "fo_internal.h"
 
@@ -29,6 +31,15 @@ namespace fo {
 // 96 per thread for E <= 8 and at 128 for E = 16.
 __host__ __device__ constexpr int min_blocks(int threads, int E) {
   return (65536 / (threads * (E <= 8 ? 96 : 128))) > 0 ? 65536 / (threads * (E <= 8 ? 96 : 128)) : 1;
+}
+
+// Programmatic dependent launch: let the next pass be launched while this one
+// drains, then wait until the previous pass has completed and flushed before
+// touching global memory.  Both are no-ops when the launch carries no
+// programmatic dependency.
+__device__ __forceinline__ void pdl_prologue() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
 }
 
 __device__ __forceinline__ float2 cis_f(float a) {
@@ -57,6 +68,7 @@ __device__ __forceinline__ void cp_async_wait() {
 template <int N, int E, int LANES, int GK, bool PF, bool FULL>
 __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
     row_pass_kernel(const RowPassArgs a, const float2* __restrict__ tw) {
+  pdl_prologue();
   constexpr int T = N / E;
   constexpr int SLOTS = SmemSize<N>::value;
   extern __shared__ float2 dsm[];
@@ -255,6 +267,7 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 template <int N, int E, int W, bool PF, bool HS, bool FULL>
 __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     col_pass_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
+  pdl_prologue();
   static_assert(W % 2 == 0, "16-byte staging needs an even tile width");
   constexpr int T = N / E;
   constexpr int SLOTS = SmemSize<N>::value;
@@ -377,6 +390,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 template <int N, int E, int W, bool PF, bool HS>
 __global__ void __launch_bounds__((W / 2) * (N / E), min_blocks((W / 2) * (N / E), 2 * E))
     col_pass2_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
+  pdl_prologue();
   static_assert(W % 2 == 0, "paired columns need an even tile width");
   constexpr int T = N / E;
   constexpr int SLOTS = SmemSize<N>::value;
@@ -502,6 +516,7 @@ struct LaneStride {
 template <int N, int E, int W, bool HS>
 __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     col_lane_kernel(const ColPassArgs a, const float2* __restrict__ tw) {
+  pdl_prologue();
   constexpr int T = N / E;
   static_assert(T % 32 == 0, "a lane must be whole warps");
   constexpr int LS = LaneStride<N>::value;
@@ -644,6 +659,7 @@ template <int N, int E, int W>
 __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     col_tma_kernel(const ColPassArgs a, const float2* __restrict__ tw, const __grid_constant__ CUtensorMap tm_buf,
                    const __grid_constant__ CUtensorMap tm_h) {
+  pdl_prologue();
   constexpr int T = N / E;
   constexpr int SLOTS = SmemSize<N>::value;
   constexpr int BOX = 256;
@@ -755,6 +771,25 @@ struct RowShape {
   static size_t smem(bool pf) { return sizeof(float2) * (size_t)(pf ? 2 : 1) * LANES * SmemSize<N>::value; }
 };
 
+// Whether pass launches carry the programmatic-dependent-launch attribute (FO_PDL=1 enables).
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pass(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                               Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <typename K>
 inline cudaError_t set_smem(K kernel, size_t bytes) {
   if (bytes <= 48 * 1024) return cudaSuccess;
@@ -773,10 +808,10 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
   do {                                                                                            \
     if (full) {                                                                                   \
       e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV, true>, smem);                            \
-      if (e == cudaSuccess) row_pass_kernel<N, E, LANES, GK, PFV, true><<<grid, SH::threads, smem, s>>>(a, tw); \
+      if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, true>, grid, dim3(SH::threads), smem, s, a, tw); \
     } else {                                                                                      \
       e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV, false>, smem);                           \
-      if (e == cudaSuccess) row_pass_kernel<N, E, LANES, GK, PFV, false><<<grid, SH::threads, smem, s>>>(a, tw); \
+      if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, false>, grid, dim3(SH::threads), smem, s, a, tw); \
     }                                                                                             \
   } while (0)
   if (!grad) {
@@ -810,13 +845,13 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     constexpr size_t smem = col_smem<N, W>(PFV, HSV);                                           \
     if constexpr (P == 2) {                                                                     \
       e = set_smem(col_pass2_kernel<N, E, W, PFV, HSV>, smem);                                  \
-      if (e == cudaSuccess) col_pass2_kernel<N, E, W, PFV, HSV><<<grid, threads, smem, s>>>(a, tw); \
+      if (e == cudaSuccess) e = launch_pass(col_pass2_kernel<N, E, W, PFV, HSV>, grid, dim3(threads), smem, s, a, tw); \
     } else if (full) {                                                                          \
       e = set_smem(col_pass_kernel<N, E, W, PFV, HSV, true>, smem);                             \
-      if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV, true><<<grid, threads, smem, s>>>(a, tw); \
+      if (e == cudaSuccess) e = launch_pass(col_pass_kernel<N, E, W, PFV, HSV, true>, grid, dim3(threads), smem, s, a, tw); \
     } else {                                                                                    \
       e = set_smem(col_pass_kernel<N, E, W, PFV, HSV, false>, smem);                            \
-      if (e == cudaSuccess) col_pass_kernel<N, E, W, PFV, HSV, false><<<grid, threads, smem, s>>>(a, tw); \
+      if (e == cudaSuccess) e = launch_pass(col_pass_kernel<N, E, W, PFV, HSV, false>, grid, dim3(threads), smem, s, a, tw); \
     }                                                                                           \
   } while (0)
   if constexpr (P == 4) {
@@ -826,8 +861,9 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
     e = set_smem(col_tma_kernel<N, E, W>, smem_t);
     if (e == cudaSuccess)
-      col_tma_kernel<N, E, W><<<grid, threads, smem_t, s>>>(a, tw, *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
-                                                              *reinterpret_cast<const CUtensorMap*>(a.tmap_h));
+      e = launch_pass(col_tma_kernel<N, E, W>, grid, dim3(threads), smem_t, s, a, tw,
+                      *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
+                      *reinterpret_cast<const CUtensorMap*>(a.tmap_h));
   } else if constexpr (P == 0) {
     constexpr int LS = LaneStride<N>::value;
     constexpr size_t smem_hs = sizeof(float2) * ((size_t)2 * W * LS + (size_t)W * (N + 4));
@@ -835,10 +871,10 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     (void)pf;
     if constexpr (smem_hs <= kMaxSmemPerCta) {
       e = set_smem(col_lane_kernel<N, E, W, true>, smem_hs);
-      if (e == cudaSuccess) col_lane_kernel<N, E, W, true><<<grid, threads, smem_hs, s>>>(a, tw);
+      if (e == cudaSuccess) e = launch_pass(col_lane_kernel<N, E, W, true>, grid, dim3(threads), smem_hs, s, a, tw);
     } else {
       e = set_smem(col_lane_kernel<N, E, W, false>, smem_nohs);
-      if (e == cudaSuccess) col_lane_kernel<N, E, W, false><<<grid, threads, smem_nohs, s>>>(a, tw);
+      if (e == cudaSuccess) e = launch_pass(col_lane_kernel<N, E, W, false>, grid, dim3(threads), smem_nohs, s, a, tw);
     }
   } else if (pf) {
     if constexpr (col_smem<N, W>(true, true) <= kMaxSmemPerCta) FO_COL_GO(true, true);

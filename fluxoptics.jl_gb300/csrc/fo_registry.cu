@@ -3,6 +3,8 @@
 #include "fo_internal.h"
 #include "fo_variants.h"
 
+#include <cstdlib>
+
 namespace fo {
 
 #define FO_DECL(NN)                                                                                  \
@@ -15,7 +17,7 @@ namespace {
 
 struct Table {
   int n = 0;
-  PassVariant v[8];
+  PassVariant v[12];
 };
 
 template <int N>
@@ -59,6 +61,18 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 bool fft_size_supported(int n) { return table_for(n, true).n > 0; }
 
+// Off by default: with the whole iteration captured as one graph, programmatic
+// edges between the passes measured slower (16.8 vs 15.4 ms for 2048^2 x 48 fields,
+// three propagations forward and back) and only the launch-bound BPM march
+// gained (about 2 %).  FO_PDL=1 turns it on.
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = getenv("FO_PDL");
+    return v && v[0] == '1';
+  }();
+  return on;
+}
+
 int row_variant_count(int N) { return table_for(N, true).n; }
 int col_variant_count(int N) { return table_for(N, false).n; }
 PassVariant row_variant(int N, int v) { return table_for(N, true).v[v]; }
@@ -71,7 +85,7 @@ size_t row_smem_bytes(int N, int v, bool pf) {
 size_t col_smem_bytes(int N, int v, bool pf) {
   const PassVariant pv = col_variant(N, v);
   if (pv.P == 0) return sizeof(float2) * 2 * pv.lanes * (size_t)(N + N / 16 + 4);  // always staged
-  if (pv.P == 4) return sizeof(float2) * pv.lanes * (size_t)(2 * N + N + N / 16);     // TMA staging
+  if (pv.P == 4) return sizeof(float2) * pv.lanes * (size_t)(2 * N + N + N / 16);  // TMA staging
   return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);  // staging only
 }
 bool row_prefetch_fits(int N, int v) { return row_smem_bytes(N, v, true) <= kMaxSmem; }
