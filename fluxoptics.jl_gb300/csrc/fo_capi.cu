@@ -145,6 +145,22 @@ int encode_tmap_2d(void* tmap, const void* base, long long rows, int cols, int l
   return FO_OK;
 }
 
+int encode_tmap_3d(void* tmap, const void* base, int fields, int rows, int cols, int ld, int box_cols, int box_rows) {
+  int err = FO_OK;
+  auto fn = tmap_encoder(&err);
+  if (!fn) return err;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(FO_ERR_ARG, "TMA base address not 16-byte aligned");
+  const cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)fields};
+  const cuuint64_t strides[2] = {(cuuint64_t)ld * sizeof(float2), (cuuint64_t)ld * rows * sizeof(float2)};
+  const cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(reinterpret_cast<CUtensorMap*>(tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void*>(base),
+                  dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(FO_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return FO_OK;
+}
+
 }  // namespace fo
 
 using namespace fo;
@@ -393,7 +409,7 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   alignas(64) CUtensorMap tm_buf, tm_h;
   if (col_variant_uses_tma(p->fy, v)) {
     const int W = col_variant(p->fy, v).lanes;
-    int rc = encode_tmap_2d(&tm_buf, buf, (long long)p->batch * p->ny, p->fx, p->fx, W, 256);
+    int rc = encode_tmap_3d(&tm_buf, buf, p->batch, p->ny, p->fx, p->fx, W, 256);
     if (rc == FO_OK) rc = encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256);
     if (rc != FO_OK) {  // e.g. an unaligned caller buffer: use the cp.async variant
       v = 0;
@@ -403,7 +419,6 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
     } else {
       a.tmap_buf = &tm_buf;
       a.tmap_h = &tm_h;
-      a.rows_per_field = p->ny;
       a.err_word = p->err_word;
       a.wait_ns = p->wait_ns;
       a.test_skip_copy = env_int("FO_TEST_SKIP_COPY", 0);
@@ -570,12 +585,11 @@ int autotune_plan(fo_prop_plan p) {
       if (col_variant_uses_tma(p->fy, v)) {
         if (pf) continue;  // staging is built in
         const int W = col_variant(p->fy, v).lanes;
-        if (encode_tmap_2d(&tm_buf, tmp, (long long)nb * p->ny, p->fx, p->fx, W, 256) != FO_OK ||
+        if (encode_tmap_3d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W, 256) != FO_OK ||
             encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256) != FO_OK)
           continue;
         a.tmap_buf = &tm_buf;
         a.tmap_h = &tm_h;
-        a.rows_per_field = p->ny;
         a.err_word = p->err_word;
         a.wait_ns = p->wait_ns;
       }

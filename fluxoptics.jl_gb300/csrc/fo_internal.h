@@ -81,11 +81,10 @@ struct ColPassArgs {
   const int* item_start;  // n_items+1 offsets into field_list (null: one field per item)
   int n_items;
   // TMA variants: host addresses of the tensor maps (CUtensorMap) of the buffer,
-  // viewed as rows_total x ncols, and of the transfer functions; the rows of one
-  // field in the buffer; the device error word and the wait limit.
+  // viewed as fields x rows x ncols, and of the transfer functions, viewed as
+  // (tables * N) x ncols; the device error word and the wait limit.
   const void* tmap_buf;
   const void* tmap_h;
-  int rows_per_field;
   unsigned int* err_word;
   unsigned long long wait_ns;
   int test_skip_copy;  // test knob: arm the barrier but issue no copy (the wait must time out)
@@ -98,6 +97,10 @@ unsigned int* device_error_word(int* err);
 // float2 array of `rows` x `cols` (row stride `ld` elements) with boxes of
 // box_cols x box_rows.  Returns FO_OK or an FO_ERR_* code.
 int encode_tmap_2d(void* tmap, const void* base, long long rows, int cols, int ld, int box_cols, int box_rows);
+// The same over `fields` consecutive rows x cols slabs (row stride ld, slab stride
+// rows * ld elements), boxes of box_cols x box_rows x 1: a box is clipped at the
+// last row of its slab.
+int encode_tmap_3d(void* tmap, const void* base, int fields, int rows, int cols, int ld, int box_cols, int box_rows);
 
 // Launch-shape variants (fo_variants.h): E elements per thread, `lanes` rows or
 // columns per CTA.  N is the FFT length along the transformed axis; supported:

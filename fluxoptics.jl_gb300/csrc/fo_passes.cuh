@@ -606,12 +606,16 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 
 // --------------------------------------------------------------------------
 // TMA column pass: the tile of the next field is fetched by the tensor-memory
-// accelerator (cp.async.bulk.tensor, boxes of W columns x 256 rows, completion
-// on an mbarrier) into a dense staging buffer as soon as the current field's
-// registers are loaded; the H tile of the work item is fetched the same way.
-// FFT exchanges use a separate padded buffer.  Every mbarrier wait is bounded
-// by %globaltimer: on expiry the CTA sets bit 0 of the device error word and
-// returns (no copy is left in flight).
+// accelerator (cp.async.bulk.tensor, boxes of W columns x 256 rows x 1 field,
+// completion on an mbarrier) into a dense staging buffer as soon as the current
+// field's registers are loaded; the H tile of the work item is fetched the same
+// way.  FFT exchanges use a separate padded buffer, which after the last stage
+// also holds the result tile [N][W] for a TMA tensor store: the field leaves as
+// whole boxes instead of W-column slivers of every row.  The field map is 3-D
+// (columns, rows of one field, fields), so boxes are clipped at the field's last
+// row: rows past it read as zeros and are never written.  Every mbarrier wait is
+// bounded by %globaltimer: on expiry the CTA sets bit 0 of the device error word
+// and returns (no copy is left in flight).
 // Shared memory: 128 (alignment) + 2 * N * W + W * SLOTS float2 + 16 bytes.
 // --------------------------------------------------------------------------
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -653,6 +657,24 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
       "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int x, int y, int z, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_3d(const void* tmap, int x, int y, int z, const void* src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];\n" ::"l"(
+                   reinterpret_cast<unsigned long long>(tmap)),
+               "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// The stores issued so far have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// The stores issued so far are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
 template <int N, int E, int W>
@@ -676,7 +698,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
   const int col0 = blockIdx.y * W;
   const int col = col0 + c;
   const bool col_ok = col < a.ncols;
-  const int y_in = a.y_in, y_out = a.y_out, ld = a.ld;
+  const int y_in = a.y_in, y_out = a.y_out;
   const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
   const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
   auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
@@ -686,9 +708,10 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
   auto issue_tile = [&](int f) {  // one thread
     mbar_expect_tx(&bar[0], tile_bytes);
     if (a.test_skip_copy) return;
-    const int y0 = field_of(f) * a.rows_per_field;
-    for (int k = 0; k < nbox; ++k) tma_load_2d(stage + k * BOX * W, &tm_buf, col0, y0 + k * BOX, &bar[0]);
+    const int fz = field_of(f);
+    for (int k = 0; k < nbox; ++k) tma_load_3d(stage + k * BOX * W, &tm_buf, col0, k * BOX, fz, &bar[0]);
   };
+  const int nbox_out = (y_out + BOX - 1) / BOX;
   if (threadIdx.x == 0) {
     s_abort = 0;
     mbar_init(&bar[0], 1);
@@ -720,12 +743,15 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       const int p = t + i * T;
       v[i] = (col_ok && p < y_in) ? stage[p * W + c] : make_float2(0.f, 0.f);
     }
+    // the previous field's result tile has been read out of `ex`
+    if (threadIdx.x == 0) bulk_wait_read_all();
     __syncthreads();  // the staging buffer is free again; abort decision is uniform
     if (s_abort) {
       if (threadIdx.x == 0) {
         atomicOr(a.err_word, 1u);
         // let copies still in flight land (bounded) before the CTA's memory is released
         if (!a.test_skip_copy) mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
+        bulk_wait_all();
       }
       return;
     }
@@ -734,32 +760,29 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       issue_tile(f + 1);
     }
     fft_forward<N, E, W>(v, t, tw, ex + c);
-    float2* out = a.buf + (long long)field_of(f) * a.bstride + col;
-    if (a.fft_only) {
-      if (col_ok) {
-#pragma unroll
-        for (int i = 0; i < E; ++i) {
-          const int p = t + i * T;
-          if (p < y_out) out[p * ld] = v[i];
-        }
-      }
-    } else {
+    if (!a.fft_only) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         float2 hv = hs[(t + i * T) * W + c];
         hv.y *= hsign;
+        // conj(X * H): the inverse transform runs as conj(FFT(conj(.)))
         v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
       }
       fft_forward<N, E, W>(v, t, tw, ex + c);
-      if (col_ok) {
+    }
+    const float osign = a.fft_only ? 1.f : -1.f;
+    __syncthreads();  // the last stage has read `ex`
 #pragma unroll
-        for (int i = 0; i < E; ++i) {
-          const int p = t + i * T;
-          if (p < y_out) out[p * ld] = cconj(v[i]);
-        }
-      }
+    for (int i = 0; i < E; ++i) ex[(t + i * T) * W + c] = make_float2(v[i].x, osign * v[i].y);
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0 && !a.test_skip_copy) {
+      const int fz = field_of(f);
+      for (int k = 0; k < nbox_out; ++k) tma_store_3d(&tm_buf, col0, k * BOX, fz, ex + k * BOX * W);
+      bulk_commit();
     }
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // --------------------------------------------------------------------------
