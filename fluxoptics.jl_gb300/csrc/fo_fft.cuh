@@ -328,4 +328,97 @@ __device__ __forceinline__ void fft_forward(V (&v)[E], int t, const float2* __re
   }
 }
 
+// Twiddles of one thread held in registers.  Stage s >= 1 needs w^{r k} for
+// r = 1..R-1 and k = j mod Ns of each of its E/R butterflies j = t + m*T; when T
+// is a multiple of Ns every butterfly has the same k and one set serves all.
+// The values do not depend on the data, so a kernel that transforms many
+// tiles loads them once.
+template <int N, int E>
+struct TwRegs {
+  using SC = Sched<N, E>;
+  __host__ __device__ static constexpr int radix(int s) { return 1 << SC::bits(s); }
+  __host__ __device__ static constexpr bool shared(int s) { return SC::T % SC::span(s) == 0; }
+  __host__ __device__ static constexpr int count(int s) {
+    return (s < 1 || s >= SC::S) ? 0 : (shared(s) ? radix(s) - 1 : (E / radix(s)) * (radix(s) - 1));
+  }
+  __host__ __device__ static constexpr int off(int s) { return s <= 1 ? 0 : off(s - 1) + count(s - 1); }
+  static constexpr int total = off(SC::S);
+  static constexpr int size = total > 0 ? total : 1;
+};
+
+template <int N, int E, int s>
+__device__ __forceinline__ void load_twiddles_from(float2 (&w)[TwRegs<N, E>::size], int t,
+                                                   const float2* __restrict__ tw) {
+  using SC = Sched<N, E>;
+  using TR = TwRegs<N, E>;
+  if constexpr (s < SC::S) {
+    constexpr int R = TR::radix(s);
+    constexpr int Ns = SC::span(s);
+    constexpr int NB = TR::shared(s) ? 1 : E / R;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+      const int k = (t + m * SC::T) & (Ns - 1);
+#pragma unroll
+      for (int r = 1; r < R; ++r) w[TR::off(s) + m * (R - 1) + r - 1] = tw[SC::twoff(s) + r * Ns + k];
+    }
+    load_twiddles_from<N, E, s + 1>(w, t, tw);
+  }
+}
+template <int N, int E>
+__device__ __forceinline__ void load_twiddles(float2 (&w)[TwRegs<N, E>::size], int t, const float2* __restrict__ tw) {
+  load_twiddles_from<N, E, 1>(w, t, tw);
+}
+
+// stage_from_smem with the twiddles taken from registers
+template <int N, int E, int s, int PS, typename V>
+__device__ __forceinline__ void stage_from_smem_r(V (&v)[E], int t, const float2 (&w)[TwRegs<N, E>::size],
+                                                  const V* sm) {
+  using SC = Sched<N, E>;
+  using TR = TwRegs<N, E>;
+  constexpr int R = TR::radix(s);
+  constexpr int T = SC::T;
+  constexpr int NB = E / R;
+#pragma unroll
+  for (int m = 0; m < NB; ++m) {
+    const int j = t + m * T;
+    const V* base = sm + spad(j) * PS;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[m * R + r] = base[padoff(r * (N / R)) * PS];
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+      const int wi = TR::off(s) + (TR::shared(s) ? 0 : m * (R - 1)) + r - 1;
+      v[m * R + r] = cmul(v[m * R + r], w[wi]);
+    }
+    Dft<R>::run(v, m * R);
+  }
+}
+
+template <int N, int E, int s, int PS, typename V>
+__device__ __forceinline__ void stages_from_r(V (&v)[E], int t, const float2 (&w)[TwRegs<N, E>::size], V* sm,
+                                              int bar_id, int bar_n) {
+  using SC = Sched<N, E>;
+  if constexpr (s < SC::S) {
+    fft_sync(bar_id, bar_n);
+    stage_to_smem<N, E, s - 1, PS>(v, t, sm);
+    fft_sync(bar_id, bar_n);
+    stage_from_smem_r<N, E, s, PS>(v, t, w, sm);
+    stages_from_r<N, E, s + 1, PS>(v, t, w, sm, bar_id, bar_n);
+  }
+}
+
+// fft_forward with register-resident twiddles (see TwRegs / load_twiddles).
+template <int N, int E, int PS, typename V>
+__device__ __forceinline__ void fft_forward_r(V (&v)[E], int t, const float2 (&w)[TwRegs<N, E>::size], V* sm,
+                                              int bar_id = 0, int bar_n = 0) {
+  Dft<E>::run(v, 0);
+  stages_from_r<N, E, 1, PS>(v, t, w, sm, bar_id, bar_n);
+  if constexpr (Dft<E>::out(1) != 1) {
+    V x[E];
+#pragma unroll
+    for (int r = 0; r < E; ++r) x[r] = v[Dft<E>::out(r)];
+#pragma unroll
+    for (int r = 0; r < E; ++r) v[r] = x[r];
+  }
+}
+
 }  // namespace fo

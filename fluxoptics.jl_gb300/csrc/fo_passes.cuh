@@ -677,7 +677,7 @@ __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bu
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
-template <int N, int E, int W>
+template <int N, int E, int W, bool TWR>
 __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     col_tma_kernel(const ColPassArgs a, const float2* __restrict__ tw, const __grid_constant__ CUtensorMap tm_buf,
                    const __grid_constant__ CUtensorMap tm_h) {
@@ -727,6 +727,14 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     }
     if (f0 < f1) issue_tile(f0);
   }
+  float2 wr[TwRegs<N, E>::size];
+  if constexpr (TWR) load_twiddles<N, E>(wr, t, tw);
+  auto fft = [&](float2(&x)[E]) {
+    if constexpr (TWR)
+      fft_forward_r<N, E, W>(x, t, wr, ex + c);
+    else
+      fft_forward<N, E, W>(x, t, tw, ex + c);
+  };
   bool ok = true;
   if (!a.fft_only) ok = mbar_wait_bounded(&bar[1], 0, a.wait_ns);
   unsigned phase = 0;
@@ -759,7 +767,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       fence_proxy_async();
       issue_tile(f + 1);
     }
-    fft_forward<N, E, W>(v, t, tw, ex + c);
+    fft(v);
     if (!a.fft_only) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
@@ -768,7 +776,7 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
         // conj(X * H): the inverse transform runs as conj(FFT(conj(.)))
         v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
       }
-      fft_forward<N, E, W>(v, t, tw, ex + c);
+      fft(v);
     }
     const float osign = a.fft_only ? 1.f : -1.f;
     __syncthreads();  // the last stage has read `ex`
@@ -877,14 +885,15 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
       if (e == cudaSuccess) e = launch_pass(col_pass_kernel<N, E, W, PFV, HSV, false>, grid, dim3(threads), smem, s, a, tw); \
     }                                                                                           \
   } while (0)
-  if constexpr (P == 4) {
+  if constexpr (P == 4 || P == 6) {
+    constexpr bool TWR = (P == 6);
     constexpr size_t smem_t = 128 + sizeof(float2) * ((size_t)2 * N * W + (size_t)W * SmemSize<N>::value) + 16;
     static_assert(smem_t <= kMaxSmemPerCta, "TMA column variant does not fit");
     (void)pf;
     if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
-    e = set_smem(col_tma_kernel<N, E, W>, smem_t);
+    e = set_smem(col_tma_kernel<N, E, W, TWR>, smem_t);
     if (e == cudaSuccess)
-      e = launch_pass(col_tma_kernel<N, E, W>, grid, dim3(threads), smem_t, s, a, tw,
+      e = launch_pass(col_tma_kernel<N, E, W, TWR>, grid, dim3(threads), smem_t, s, a, tw,
                       *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
                       *reinterpret_cast<const CUtensorMap*>(a.tmap_h));
   } else if constexpr (P == 0) {
