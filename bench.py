@@ -282,7 +282,16 @@ def run_gb300(args, rank, world):
         copy_stream = torch.cuda.Stream()
         ev_copied = [torch.cuda.Event(), torch.cuda.Event()]
         ev_done = [torch.cuda.Event(), torch.cuda.Event()]
+        # host->device bandwidth of this machine for the step's input, alone (the e2e
+        # rate is bounded by it when the copy takes longer than the compute)
         torch.cuda.synchronize()
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(copy_stream):
+            h0.record(copy_stream)
+            bufs[1].electric.copy_(host_in, non_blocking=True)
+            h1.record(copy_stream)
+        torch.cuda.synchronize()
+        h2d_gbs = host_in.numel() * host_in.element_size() / (h0.elapsed_time(h1) * 1e-3) / 1e9
         e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e2_steps = host_loss.shape[0]
         e2.record(stream)
@@ -339,7 +348,8 @@ def run_gb300(args, rank, world):
         "gpu_launches_per_step": int(nk.value),
         "e2e": {"value": round(props_per_step / (e2e_ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": int(fields_np.nbytes), "d2h_bytes_per_step": int(len(LAMBDAS) * 4),
-                "overlap": "input copy of step k+1 on a copy stream overlaps the compute of step k"},
+                "overlap": "input copy of step k+1 on a copy stream overlaps the compute of step k",
+                "h2d_gbs_measured": round(h2d_gbs, 1)},
         "clocks": clk.summary(),
         "final_loss": final_loss,
     }

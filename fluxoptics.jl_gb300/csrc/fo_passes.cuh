@@ -92,9 +92,37 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 #pragma unroll
   for (int i = 0; i < GC; ++i) gacc_c[i] = make_float2(0.f, 0.f);
 
-  // per-pixel modulation factor, cached across fields while the field factor is unchanged
-  float2 wm[E];
+  // per-pixel modulation factor, cached across fields while the field factor is
+  // unchanged: in registers, or for the gradient passes (which already hold the
+  // saved input and the accumulator) in this thread's own shared-memory slots
+  constexpr bool WMS = (GK != 0);
+  float2 wm[WMS ? 1 : E];
+  float2* wms = dsm + (PF ? 2 : 1) * LANES * SLOTS + lane * N;
+  auto wm_set = [&](int i, float2 w) {
+    if constexpr (WMS)
+      wms[t + i * T] = w;
+    else
+      wm[i] = w;
+  };
+  auto wm_get = [&](int i) -> float2 {
+    if constexpr (WMS)
+      return wms[t + i * T];
+    else
+      return wm[i];
+  };
   float wm_fb = -1.f;
+
+  // Passes without a gradient accumulator have the registers to keep this
+  // thread's twiddles for all the CTA's fields.
+  constexpr bool TWR = (GK == 0) && (E == 16) && FULL && TwRegs<N, E>::total <= 24;
+  float2 wr[TwRegs<N, E>::size];
+  if constexpr (TWR) load_twiddles<N, E>(wr, t, tw);
+  auto fft = [&](float2(&x)[E], float2* sm) {
+    if constexpr (TWR)
+      fft_forward_r<N, E, 1>(x, t, wr, sm);
+    else
+      fft_forward<N, E, 1>(x, t, tw, sm);
+  };
 
   const int f0 = blockIdx.x * a.fields_per_cta;
   const int f1 = min(a.batch, f0 + a.fields_per_cta);
@@ -166,13 +194,13 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
             w = cis_f((a.mod_bwd ? -s : s) * fb * ph);
           }
         }
-        wm[i] = w;
+        wm_set(i, w);
       }
       wm_fb = fb;
     }
 
     if (a.inv_first) {
-      fft_forward<N, E, 1>(v, t, tw, PF ? cur : buf0);
+      fft(v, PF ? cur : buf0);
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
@@ -201,7 +229,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
           }
         }
 #pragma unroll
-        for (int i = 0; i < E; ++i) v[i] = cmul(v[i], wm[i]);
+        for (int i = 0; i < E; ++i) v[i] = cmul(v[i], wm_get(i));
       } else {
         const float s = a.mod_sign;
 #pragma unroll
@@ -211,7 +239,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
             if (s < 0.f) g = cconj(g);
             gacc_c[i] = cadd(gacc_c[i], g);
           }
-          v[i] = cmul(v[i], wm[i]);
+          v[i] = cmul(v[i], wm_get(i));
           if constexpr (GK == 1) {
             // Im(du * conj(u_saved))
             const float im = v[i].y * sv[i].x - v[i].x * sv[i].y;
@@ -220,9 +248,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
         }
       }
     }
-    if (a.fwd_after) {
-      fft_forward<N, E, 1>(v, t, tw, PF ? cur : buf0);
-    }
+    if (a.fwd_after) fft(v, PF ? cur : buf0);
     if (row_ok && a.dst) {  // a null destination discards the pass output (gradients only)
       float2* dst = a.dst + (long long)b * a.dst_bstride + (long long)y * a.dst_ld;
 #pragma unroll
@@ -799,7 +825,10 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 template <int N, int E, int LANES>
 struct RowShape {
   static constexpr int threads = LANES * (N / E);
-  static size_t smem(bool pf) { return sizeof(float2) * (size_t)(pf ? 2 : 1) * LANES * SmemSize<N>::value; }
+  // staging / exchange tiles, plus the modulation cache of the gradient passes
+  static size_t smem(bool pf, bool grad) {
+    return sizeof(float2) * ((size_t)(pf ? 2 : 1) * LANES * SmemSize<N>::value + (grad ? (size_t)LANES * N : 0));
+  }
 };
 
 // Whether pass launches carry the programmatic-dependent-launch attribute (FO_PDL=1 enables).
@@ -830,9 +859,9 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
 template <int N, int E, int LANES>
 cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
   using SH = RowShape<N, E, LANES>;
-  const size_t smem = SH::smem(pf);
   dim3 grid((a.batch + a.fields_per_cta - 1) / a.fields_per_cta, (a.nrows + LANES - 1) / LANES);
   const bool grad = a.mod_bwd && a.grad != nullptr && a.mod_kind != MOD_NONE;
+  const size_t smem = SH::smem(pf && !(grad && a.mod_kind == MOD_MASK), grad);
   const bool full = a.n_valid == N && a.nrows % LANES == 0;
   cudaError_t e = cudaSuccess;
 #define FO_ROW_GO(GK, PFV)                                                                        \

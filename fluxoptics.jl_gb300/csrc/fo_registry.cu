@@ -80,7 +80,8 @@ PassVariant col_variant(int N, int v) { return table_for(N, false).v[v]; }
 
 size_t row_smem_bytes(int N, int v, bool pf) {
   const PassVariant pv = row_variant(N, v);
-  return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);
+  // the gradient passes add a modulation cache of N float2 per row
+  return sizeof(float2) * ((size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16) + (size_t)pv.lanes * N);
 }
 size_t col_smem_bytes(int N, int v, bool pf) {
   const PassVariant pv = col_variant(N, v);
