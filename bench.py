@@ -162,7 +162,7 @@ def build_system(fo, fields_np, masks_np, targets_np):
     metric = fo.SquaredIntensityDifference((u0, targets_np))
     rule = fo.ProxRule(fo.Fista(ETA), fo.ClampProx(-np.pi, np.pi))
     opt = fo.setup(rule, system)
-    return u0, system, metric, opt, phases
+    return u0, system, metric, opt, prop
 
 
 def iteration(fo, system, metric, opt, x, du, src):
@@ -220,7 +220,7 @@ def run_gb300(args, rank, world):
     fo = load_package()
     lib = fo.load_library()
     fields_np, masks_np, targets_np = make_inputs()
-    u0, system, metric, opt, phases = build_system(fo, fields_np, masks_np, targets_np)
+    u0, system, metric, opt, prop = build_system(fo, fields_np, masks_np, targets_np)
     batch = u0.batch
     props_per_step = 2 * N_MASKS * batch
     stream = torch.cuda.Stream()
@@ -325,8 +325,11 @@ def run_gb300(args, rank, world):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    achieved = col_pass_bytes() / (col_ms * 1e-3) / 1e9
-    traffic = read_traffic()
+    achieved = col_pass_bytes(batch=batch) / (col_ms * 1e-3) / 1e9
+    # the committed DRAM-traffic capture is of the 48-field launch
+    traffic = read_traffic() if batch == N_MODES * len(LAMBDAS) else None
+    row_name, col_name = C.create_string_buffer(160), C.create_string_buffer(160)
+    fo._capi.check(lib.fo_prop_variants(prop.plan_for(u0), None, None, row_name, col_name, 160))
     value = job_rate(props_per_step, world, ms)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -338,10 +341,12 @@ def run_gb300(args, rank, world):
                    "l2": "inputs larger than L2 (1.5 GiB field batch), no flush"},
         "algorithmic_gb_per_step": round(algorithmic_bytes_per_step() / 1e9, 3),
         "algorithmic_gbs": round(algorithmic_bytes_per_step() / (ms * 1e-3) / 1e9, 1),
-        "roofline": {"bound": "hbm", "kernel": "col_pass_kernel<2048> (FFT_y * H * IFFT_y over 48 fields)",
+        "roofline": {"bound": "hbm",
+                     "kernel": f"column pass {col_name.value.decode()} (FFT_y * H * IFFT_y over {batch} fields)",
                      "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                      "frac": round(achieved / hbm_peak, 4), "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": traffic, "algorithmic_bytes_per_launch": col_pass_bytes()},
+                     "traffic": traffic, "algorithmic_bytes_per_launch": col_pass_bytes(batch=batch)},
+        "row_kernel": row_name.value.decode(),
         "pass_ms": {k: round(v, 4) for k, v in pass_ms.items()},
         "pass_share": {k: round(v, 3) for k, v in pass_share.items()},
         "gpu_launches": int(nk.value) * args.steps,
@@ -358,7 +363,7 @@ def run_gb300(args, rank, world):
 
 def read_traffic():
     """DRAM bytes per column-pass launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "col_pass_2048x48_traffic.txt")
+    path = os.path.join(ROOT, "profiles", "col_tma_2048x48_traffic.txt")
     try:
         for ln in open(path):
             if ln.startswith("dram_bytes_per_launch"):

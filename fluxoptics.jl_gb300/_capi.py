@@ -48,6 +48,7 @@ SIGNATURES = {
     "fo_rsprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _i]),
     "fo_prop_destroy": (_i, [_vp]),
     "fo_prop_info": (_i, [_vp, _pi, _pi, C.POINTER(C.c_size_t)]),
+    "fo_prop_variants": (_i, [_vp, _pi, _pi, C.c_char_p, C.c_char_p, _i]),
     "fo_propagate": (_i, [_vp, _vp, _i, _vp]),
     "fo_phase_forward": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
     "fo_phase_backward": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),

@@ -145,6 +145,24 @@ int encode_tmap_2d(void* tmap, const void* base, long long rows, int cols, int l
   return FO_OK;
 }
 
+int encode_tmap_4d(void* tmap, const void* base, int fields, int rows, int cols, int ld, int box_cols) {
+  int err = FO_OK;
+  auto fn = tmap_encoder(&err);
+  if (!fn) return err;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0) return fail(FO_ERR_ARG, "TMA base address not 16-byte aligned");
+  if (rows % 256 != 0 || rows / 256 > 256) return fail(FO_ERR_ARG, "4-D tile view needs rows = 256 k, k <= 256");
+  const cuuint64_t dims[4] = {(cuuint64_t)cols, 256, (cuuint64_t)(rows / 256), (cuuint64_t)fields};
+  const cuuint64_t row = (cuuint64_t)ld * sizeof(float2);
+  const cuuint64_t strides[3] = {row, row * 256, row * rows};
+  const cuuint32_t box[4] = {(cuuint32_t)box_cols, 256, (cuuint32_t)(rows / 256), 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = fn(reinterpret_cast<CUtensorMap*>(tmap), CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<void*>(base),
+                  dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(FO_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return FO_OK;
+}
+
 int encode_tmap_3d(void* tmap, const void* base, int fields, int rows, int cols, int ld, int box_cols, int box_rows) {
   int err = FO_OK;
   auto fn = tmap_encoder(&err);
@@ -409,8 +427,14 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   alignas(64) CUtensorMap tm_buf, tm_h;
   if (col_variant_uses_tma(p->fy, v)) {
     const int W = col_variant(p->fy, v).lanes;
-    int rc = encode_tmap_3d(&tm_buf, buf, p->batch, p->ny, p->fx, p->fx, W, 256);
-    if (rc == FO_OK) rc = encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256);
+    // whole tiles in one TMA instruction when the field height is a multiple of 256
+    const bool t4 = p->ny % 256 == 0 && p->fy % 256 == 0 && env_int("FO_TILE4D", 1) != 0;
+    int rc = t4 ? encode_tmap_4d(&tm_buf, buf, p->batch, p->ny, p->fx, p->fx, W)
+                : encode_tmap_3d(&tm_buf, buf, p->batch, p->ny, p->fx, p->fx, W, 256);
+    if (rc == FO_OK)
+      rc = t4 ? encode_tmap_4d(&tm_h, p->H, p->n_tables, p->fy, p->fx, p->fx, W)
+              : encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256);
+    a.tile4d = t4 ? 1 : 0;
     if (rc != FO_OK) {  // e.g. an unaligned caller buffer: use the cp.async variant
       v = 0;
       int trc = FO_OK;
@@ -585,9 +609,13 @@ int autotune_plan(fo_prop_plan p) {
       if (col_variant_uses_tma(p->fy, v)) {
         if (pf) continue;  // staging is built in
         const int W = col_variant(p->fy, v).lanes;
-        if (encode_tmap_3d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W, 256) != FO_OK ||
-            encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256) != FO_OK)
+        const bool t4 = p->ny % 256 == 0 && p->fy % 256 == 0 && env_int("FO_TILE4D", 1) != 0;
+        if ((t4 ? encode_tmap_4d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W)
+                : encode_tmap_3d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W, 256)) != FO_OK ||
+            (t4 ? encode_tmap_4d(&tm_h, p->H, p->n_tables, p->fy, p->fx, p->fx, W)
+                : encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256)) != FO_OK)
           continue;
+        a.tile4d = t4 ? 1 : 0;
         a.tmap_buf = &tm_buf;
         a.tmap_h = &tm_h;
         a.err_word = p->err_word;
@@ -867,6 +895,31 @@ FO_API int fo_prop_info(fo_prop_plan plan, int* fft_nx, int* fft_ny, size_t* wor
   if (fft_nx) *fft_nx = plan->fx;
   if (fft_ny) *fft_ny = plan->fy;
   if (workspace_bytes) *workspace_bytes = plan->ws_bytes;
+  return FO_OK;
+}
+
+FO_API int fo_prop_variants(fo_prop_plan plan, int* row_v, int* col_v, char* row_kernel, char* col_kernel,
+                            int len) {
+  if (!plan) return fail(FO_ERR_ARG, "plan is NULL");
+  if (row_v) *row_v = plan->row_v;
+  if (col_v) *col_v = plan->col_v;
+  auto put = [len](char* dst, const std::string& s) {
+    if (!dst || len <= 0) return;
+    const size_t n = std::min((size_t)len - 1, s.size());
+    std::memcpy(dst, s.data(), n);
+    dst[n] = 0;
+  };
+  const PassVariant rv = row_variant(plan->fx, plan->row_v);
+  const PassVariant cv = col_variant(plan->fy, plan->col_v);
+  put(row_kernel, "row_pass_kernel<" + std::to_string(plan->fx) + ", E=" + std::to_string(rv.E) +
+                      ", rows/CTA=" + std::to_string(rv.lanes) + (plan->row_pf ? ", cp.async staging>" : ">"));
+  const char* form = cv.P == 6   ? "col_tma_kernel (TMA load/store, register twiddles)"
+                     : cv.P == 4 ? "col_tma_kernel (TMA load/store)"
+                     : cv.P == 2 ? "col_pass2_kernel (paired columns)"
+                     : cv.P == 0 ? "col_lane_kernel (lane-major)"
+                                 : (plan->col_pf ? "col_pass_kernel (cp.async staging)" : "col_pass_kernel");
+  put(col_kernel, std::string(form) + "<" + std::to_string(plan->fy) + ", E=" + std::to_string(cv.E) +
+                      ", columns/CTA=" + std::to_string(cv.lanes) + ">");
   return FO_OK;
 }
 

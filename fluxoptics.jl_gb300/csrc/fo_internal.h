@@ -88,6 +88,10 @@ struct ColPassArgs {
   unsigned int* err_word;
   unsigned long long wait_ns;
   int test_skip_copy;  // test knob: arm the barrier but issue no copy (the wait must time out)
+  // 1: tmap_buf is the 4-D view (columns, row within a 256-row block, row block,
+  // field) and tmap_h the 4-D view (columns, row within block, row block, table),
+  // so one TMA instruction moves a whole tile (rows a multiple of 256)
+  int tile4d;
 };
 
 // Device error word of the current device (allocated once, zero).  Bit 0: a bounded
@@ -101,6 +105,10 @@ int encode_tmap_2d(void* tmap, const void* base, long long rows, int cols, int l
 // rows * ld elements), boxes of box_cols x box_rows x 1: a box is clipped at the
 // last row of its slab.
 int encode_tmap_3d(void* tmap, const void* base, int fields, int rows, int cols, int ld, int box_cols, int box_rows);
+// 4-D view of `fields` slabs of rows x cols (rows a multiple of 256, at most
+// 65536): (column, row within a 256-row block, row block, slab), boxes of
+// box_cols x 256 x rows/256 x 1, i.e. a whole column strip of one slab.
+int encode_tmap_4d(void* tmap, const void* base, int fields, int rows, int cols, int ld, int box_cols);
 
 // Launch-shape variants (fo_variants.h): E elements per thread, `lanes` rows or
 // columns per CTA.  N is the FFT length along the transformed axis; supported:

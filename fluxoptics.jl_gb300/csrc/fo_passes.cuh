@@ -670,6 +670,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // Bounded wait for phase `parity` of `bar`: false when `limit_ns` elapsed first.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
                                                   unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;  // the common case reads no timer
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
     if (global_ns() - t0 > limit_ns) return false;
@@ -689,6 +690,20 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int x, 
           "r"(smem_u32(dst)),
       "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
+}
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, int x, int y, int z, int w,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::
+          "r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(tmap)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_4d(const void* tmap, int x, int y, int z, int w, const void* src) {
+  asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4, %5}], [%1];\n" ::"l"(
+                   reinterpret_cast<unsigned long long>(tmap)),
+               "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z), "r"(w)
+               : "memory");
 }
 __device__ __forceinline__ void tma_store_3d(const void* tmap, int x, int y, int z, const void* src) {
   asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];\n" ::"l"(
@@ -735,7 +750,10 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     mbar_expect_tx(&bar[0], tile_bytes);
     if (a.test_skip_copy) return;
     const int fz = field_of(f);
-    for (int k = 0; k < nbox; ++k) tma_load_3d(stage + k * BOX * W, &tm_buf, col0, k * BOX, fz, &bar[0]);
+    if (a.tile4d)
+      tma_load_4d(stage, &tm_buf, col0, 0, 0, fz, &bar[0]);
+    else
+      for (int k = 0; k < nbox; ++k) tma_load_3d(stage + k * BOX * W, &tm_buf, col0, k * BOX, fz, &bar[0]);
   };
   const int nbox_out = (y_out + BOX - 1) / BOX;
   if (threadIdx.x == 0) {
@@ -749,7 +767,10 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     if (!a.fft_only) {
       mbar_expect_tx(&bar[1], (unsigned)(N * W * sizeof(float2)));
       const int hy0 = a.h_index[field_of(f0)] * N;
-      for (int k = 0; k < N / BOX; ++k) tma_load_2d(hs + k * BOX * W, &tm_h, col0, hy0 + k * BOX, &bar[1]);
+      if (a.tile4d)
+        tma_load_4d(hs, &tm_h, col0, 0, 0, a.h_index[field_of(f0)], &bar[1]);
+      else
+        for (int k = 0; k < N / BOX; ++k) tma_load_2d(hs + k * BOX * W, &tm_h, col0, hy0 + k * BOX, &bar[1]);
     }
     if (f0 < f1) issue_tile(f0);
   }
@@ -812,7 +833,10 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
     __syncthreads();
     if (threadIdx.x == 0 && !a.test_skip_copy) {
       const int fz = field_of(f);
-      for (int k = 0; k < nbox_out; ++k) tma_store_3d(&tm_buf, col0, k * BOX, fz, ex + k * BOX * W);
+      if (a.tile4d)
+        tma_store_4d(&tm_buf, col0, 0, 0, fz, ex);
+      else
+        for (int k = 0; k < nbox_out; ++k) tma_store_3d(&tm_buf, col0, k * BOX, fz, ex + k * BOX * W);
       bulk_commit();
     }
   }

@@ -126,6 +126,15 @@ FO_API int fo_prop_destroy(fo_prop_plan plan);
 FO_API int fo_prop_info(fo_prop_plan plan, int* fft_nx, int* fft_ny, size_t* workspace_bytes);
 
 /*
+ * Launch shapes the plan runs (chosen by the autotuner or the defaults): the row
+ * and column pass variant indices and a readable name of each kernel, written
+ * NUL-terminated into row_kernel / col_kernel (up to len bytes each; either may
+ * be NULL).  No reference counterpart: FFT plans are opaque in FluxOptics.jl.
+ */
+FO_API int fo_prop_variants(fo_prop_plan plan, int* row_variant, int* col_variant, char* row_kernel,
+                            char* col_kernel, int len);
+
+/*
  * In-place propagation of u (batch x ny x nx complex float).  FO_BACKWARD applies
  * the exact adjoint (conj(H)).
  * Replaces: propagate!(u, p::ASProp|RSProp, dir) and backpropagate!
