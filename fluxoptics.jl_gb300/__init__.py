@@ -16,12 +16,13 @@ from .fields import ScalarField, coupling_efficiency, intensity, normalize_power
 from .metrics import SquaredIntensityDifference, withgradient
 from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
 from .optimisers import ClampProx, Fista, NoDescent, ProxRule, TVProx, make_rules, setup, update_
+from .ragged import RaggedBatch
 
 load_library = _capi.load
 
 __all__ = [
     "AS_BPM", "ASProp", "Backward", "ClampProx", "FieldProbe", "Fista", "FluxOpticsError", "Forward", "Mask",
-    "NoDescent", "OpticalSystem", "Phase", "ProxRule", "RSProp", "ScalarField", "ScalarSource",
+    "NoDescent", "OpticalSystem", "Phase", "ProxRule", "RSProp", "RaggedBatch", "ScalarField", "ScalarSource",
     "SquaredIntensityDifference", "TVProx", "backpropagate_", "build_library", "coupling_efficiency",
     "function_to_array", "gaussian", "hermite_gaussian", "hermite_gaussian_groups", "intensity",
     "load_library", "make_rules", "normalize_power_", "power", "propagate", "propagate_", "reverse",

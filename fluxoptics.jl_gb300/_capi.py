@@ -29,6 +29,12 @@ class fo_mod(C.Structure):
                 ("grad", C.c_void_p), ("scale", C.c_double)]
 
 
+class fo_ragged_problem(C.Structure):
+    _fields_ = [("n", C.c_int), ("dx", C.c_double), ("dy", C.c_double), ("lam", C.c_double), ("z", C.c_double),
+                ("n0", C.c_double), ("u_in", C.c_void_p), ("phase", C.c_void_p), ("target", C.c_void_p),
+                ("u_out", C.c_void_p), ("grad_phase", C.c_void_p), ("loss", C.c_void_p)]
+
+
 _vp = C.c_void_p
 _i = C.c_int
 _d = C.c_double
@@ -80,6 +86,11 @@ SIGNATURES = {
     "fo_graph_launch": (_i, [_vp, _vp]),
     "fo_graph_info": (_i, [_vp, _pi]),
     "fo_graph_destroy": (_i, [_vp]),
+    "fo_ragged_create": (_i, [C.POINTER(_vp), C.POINTER(fo_ragged_problem), _i, _i]),
+    "fo_ragged_batch": (_i, [_vp, _vp]),
+    "fo_ragged_info": (_i, [_vp, _pi, C.POINTER(C.c_size_t)]),
+    "fo_ragged_destroy": (_i, [_vp]),
+    "fo_ragged_pass_ms": (_i, [_vp, _pd]),
 }
 
 _LIB = None

@@ -866,6 +866,7 @@ FO_API int fo_device_status(void* stream) {
   if (e == cudaSuccess && h) e = cudaMemset(w, 0, sizeof(unsigned int));
   if (e != cudaSuccess) return cuda_fail(e, "reading the device error word");
   if (h & 1u) return fail(FO_ERR_TIMEOUT, "a bounded device wait gave up (TMA copy did not complete in time)");
+  if (h & 2u) return fail(FO_ERR_TIMEOUT, "a bounded device wait gave up (grid barrier of the ragged launch)");
   return FO_OK;
 }
 

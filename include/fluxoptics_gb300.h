@@ -72,8 +72,8 @@ FO_API int fo_stream_synchronize(void* stream);
 
 /* Synchronises `stream`, then reads and clears the device error word of the
  * current device: FO_ERR_TIMEOUT when a kernel's bounded wait (an mbarrier wait
- * on a TMA copy, limit FO_WAIT_NS nanoseconds, default 1 s) gave up since the
- * last call.  Such a kernel returns without finishing its tile; the context stays
+ * on a TMA copy or a grid barrier of the ragged launch, limit FO_WAIT_NS
+ * nanoseconds, default 1 s) gave up since the last call.  Such a kernel returns without finishing its tile; the context stays
  * usable.  No counterpart in the reference (it has no device-side waits). */
 FO_API int fo_device_status(void* stream);
 
@@ -353,6 +353,46 @@ FO_API int fo_graph_launch(fo_graph graph, void* stream);
 /* Number of kernel nodes in a captured graph. */
 FO_API int fo_graph_info(fo_graph graph, int* kernel_nodes);
 FO_API int fo_graph_destroy(fo_graph graph);
+
+/* ---------------------------------------------------------------------- */
+/* Ragged batch: many independent problems of different sizes, one launch  */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * One problem: Phase(phase) -> ASProp(z; n0) -> SquaredIntensityDifference(target)
+ * on an n x n grid (n a power of two from 256 to 4096), one field.  fo_ragged_batch
+ * computes, for every problem of the plan, the propagated field u_out, the loss
+ * sum((|u_out|^2 - target)^2) and its gradient with respect to the phase, i.e.
+ * forward + adjoint, in ONE persistent cooperative kernel launch (plus one
+ * memset of its counters).  All pointers are device pointers bound at creation;
+ * u_in is only read (it is the saved input of the phase) and must not alias u_out.
+ * Replaces, batched over independent problems, Zygote.withgradient of
+ * SquaredIntensityDifference over ScalarSource |> Phase |> ASProp
+ * (modulators/phasemask.jl:90-150, freespace_propagators/angular_spectrum.jl:193-234,
+ * metrics/squared_intensity_difference.jl:58-90, src/ChainRulesCoreExt.jl:21-111).
+ */
+typedef struct fo_ragged_s* fo_ragged_plan;
+typedef struct {
+  int n;
+  double dx, dy;
+  double lambda, z, n0; /* n0 <= 0 means 1 */
+  const void* u_in;     /* complex float[n][n] */
+  const float* phase;   /* float[n][n] */
+  const float* target;  /* float[n][n] intensity target */
+  void* u_out;          /* complex float[n][n] */
+  float* grad_phase;    /* float[n][n] */
+  float* loss;          /* float[1] */
+} fo_ragged_problem;
+
+FO_API int fo_ragged_create(fo_ragged_plan* plan, const fo_ragged_problem* problems, int count, int flags);
+FO_API int fo_ragged_batch(fo_ragged_plan plan, void* stream);
+/* CTAs of the persistent launch (one per SM) and the workspace the plan owns. */
+FO_API int fo_ragged_info(fo_ragged_plan plan, int* grid_ctas, size_t* workspace_bytes);
+/* Device time of the five passes of the last completed fo_ragged_batch (ms[5]: row,
+ * column, row, adjoint column, row + loss sums), from %globaltimer stamps taken by
+ * the first CTA after each grid barrier.  Synchronizes the device. */
+FO_API int fo_ragged_pass_ms(fo_ragged_plan plan, double* ms);
+FO_API int fo_ragged_destroy(fo_ragged_plan plan);
 
 #ifdef __cplusplus
 }

@@ -78,4 +78,18 @@ def test_bad_arguments_are_rejected(capi):
     assert lib.fo_chain_create(C.byref(C.c_void_p()), 0, None) == 1
     assert lib.fo_sid_create(C.byref(C.c_void_p()), 8, 8, 2, 2, capi.ivec([0, 5])) == 1
     assert lib.fo_tv_create(C.byref(C.c_void_p()), 1, 8, 0.1, 10, 1, 0.25) == 2
+    # ragged batch: sizes and aliasing are checked before anything touches the GPU
+    probs = (capi.fo_ragged_problem * 2)()
+    for i, q in enumerate(probs):
+        q.n, q.dx, q.dy, q.lam, q.z, q.n0 = 256, 1.0, 1.0, 1.064, 100.0, 1.0
+        q.u_in, q.phase, q.target, q.u_out, q.grad_phase, q.loss = 16, 32, 48, 64 + 16 * i, 96, 112
+    probs[1].n = 300
+    h = C.c_void_p()
+    assert lib.fo_ragged_create(C.byref(h), probs, 2, 0) == 2
+    assert "power of two" in lib.fo_last_error().decode()
+    probs[1].n = 256
+    probs[1].u_out = probs[1].u_in
+    assert lib.fo_ragged_create(C.byref(h), probs, 2, 0) == 1
+    assert "alias" in lib.fo_last_error().decode()
+    assert lib.fo_ragged_create(C.byref(h), probs, 0, 0) == 1
     assert lib.fo_fista_step(None, None, None, None, 10, 0.1, None, None) == 1

@@ -425,6 +425,44 @@ def test_ragged_batch_per_problem(fo, orc):
         assert orc.rel_l2(npy(grads[ph]["phi"]), g) < GRAD_TOL
 
 
+def test_ragged_persistent_launch(fo, orc):
+    """fo_ragged_batch: problems of different sizes (256..1024, with sizes,
+    wavelengths, distances, waists, offsets and masks drawn per problem) run forward
+    + adjoint in one persistent cooperative launch; every problem's propagated field,
+    loss and mask gradient against the FP64 oracle, on two consecutive runs (the
+    launch resets its own counters)."""
+    import bench
+    probs = bench.ragged_problems(seed=123, count=7, sizes=(256, 512, 1024))
+    specs, refs = [], []
+    for pr in probs:
+        n = pr["n"]
+        rng = np.random.default_rng(pr["seed"])
+        x, y = fo.spatial_vectors((n, n), (1.0, 1.0))
+        u0 = fo.gaussian(pr["w0"], x - pr["off"][0], y - pr["off"][1]).astype(np.complex64)
+        u0 = (u0 / np.sqrt(np.sum(np.abs(u0) ** 2))).astype(np.complex64)
+        phi = rng.uniform(0, 2 * np.pi, (n, n)).astype(np.float32)
+        t = (np.abs(fo.gaussian(pr["w0"], x, y)) ** 2).astype(np.float32)
+        t = (t / t.sum()).astype(np.float32)
+        u = fo.ScalarField(u0, (1.0, 1.0), pr["lam"])
+        specs.append({"u": u, "phase": phi, "target": t, "z": pr["z"]})
+        v = orc.asprop(orc.phase_forward(u0, phi), 1.0, 1.0, pr["lam"], pr["z"])
+        c, _ = orc.sid_value(v, t)
+        dv = orc.asprop(orc.sid_backward(v, t), 1.0, 1.0, pr["lam"], pr["z"], orc.BACKWARD)
+        _, g = orc.phase_backward(dv, phi, u0)
+        refs.append((v, float(c.sum()), g))
+    rb = fo.RaggedBatch(specs)
+    assert rb.info()["grid_ctas"] >= 1
+    for _ in range(2):
+        losses, outs, grads = rb.run()
+        torch.cuda.synchronize()
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        assert fo._capi.load().fo_device_status(stream) == 0
+        for k, (v, c, g) in enumerate(refs):
+            assert orc.rel_l2(npy(outs[k]), v) < FIELD_TOL, (k, probs[k]["n"])
+            assert abs(float(losses[k]) - c) / c < 1e-4, (k, float(losses[k]), c)
+            assert orc.rel_l2(npy(grads[k]), g) < GRAD_TOL, (k, probs[k]["n"])
+
+
 def test_bounded_wait_reports_timeout(fo, orc, monkeypatch):
     """Failure detection without a GPU fault: a TMA column pass whose barrier is
     armed but whose copy is never issued must give up after its bounded wait (20 ms
