@@ -50,7 +50,12 @@ constexpr int RG_HCHUNK = RG_HALF * RG_E;      // row chunk: 4096 elements
 constexpr int RG_HSLOTS = RG_HCHUNK + RG_HCHUNK / 16;  // padded exchange slots of one half
 constexpr int RG_XSLOTS = RG_CHUNK + RG_CHUNK / 16;    // padded exchange slots of a strip
 constexpr int RG_LG_MIN = 8, RG_LG_MAX = 12;           // n = 256 .. 4096
-constexpr size_t RG_SMEM = 128 + sizeof(float2) * ((size_t)2 * RG_CHUNK + RG_XSLOTS);
+// dynamic shared memory: the column layout (strip, H strip, padded exchange) or the
+// row layout (two padded exchange regions, then 4096 float2 + 4096 float of side
+// inputs per half), whichever is larger
+constexpr size_t RG_SMEM_COL = sizeof(float2) * ((size_t)2 * RG_CHUNK + RG_XSLOTS);
+constexpr size_t RG_SMEM_ROW = sizeof(float2) * ((size_t)2 * RG_HSLOTS + 2 * (RG_HCHUNK + RG_HCHUNK / 2));
+constexpr size_t RG_SMEM = 128 + (RG_SMEM_COL > RG_SMEM_ROW ? RG_SMEM_COL : RG_SMEM_ROW);
 
 enum RgRowKind { RG_ROW_FWD = 0, RG_ROW_MID = 1, RG_ROW_GRAD = 2 };
 
@@ -138,10 +143,21 @@ __device__ bool grid_sync(const RgArgs& a, int* s_flag) {
   return *s_flag != 0;
 }
 
+// 16-byte cp.async copies of `bytes` contiguous bytes (a multiple of 16) by the 256
+// threads of a half.
+__device__ __forceinline__ void half_copy16(void* dst, const void* src, int bytes, int ht) {
+  char* d = reinterpret_cast<char*>(dst);
+  const char* s = reinterpret_cast<const char*>(src);
+  for (int o = ht * 16; o < bytes; o += RG_HALF * 16) cp_async16(d + o, s + o);
+}
+
 // One row chunk of problem P: 4096/N rows, T = N/16 threads per row, 256 threads.
+// `side` (4096 float2 + 4096 float of this half) stages the inputs that are used
+// after the transform, copied while it runs.
 template <int N, int KIND>
 __device__ __forceinline__ void row_chunk(const RgProblem& P, int chunk, int ht, float2* sm, int bar_id,
-                                          const float2* __restrict__ tw, float* partials, float* red) {
+                                          const float2* __restrict__ tw, float* partials, float* red,
+                                          float2* side) {
   constexpr int T = N / RG_E;
   constexpr int LANES = RG_HCHUNK / N;
   constexpr int SLOTS = SmemSize<N>::value;
@@ -155,13 +171,21 @@ __device__ __forceinline__ void row_chunk(const RgProblem& P, int chunk, int ht,
   float2* __restrict__ u_out = P.u_out;
   float2* __restrict__ adj = P.adj;
   const float s = P.s;
+  const long long row0 = (long long)chunk * RG_HCHUNK;  // first element of the chunk
+  float2* side_c = side;                                  // complex side input, chunk order
+  float* side_r = reinterpret_cast<float*>(side + RG_HCHUNK);  // real side input
+  const int loc = lane * N;                               // this lane's row inside the chunk
   float2 v[RG_E];
   if constexpr (KIND == RG_ROW_FWD) {
+    float ph[RG_E];
 #pragma unroll
     for (int i = 0; i < RG_E; ++i) {
       const int p = t + i * T;
-      v[i] = cmul(u_in[row + p], cis_f(s * phase[row + p]));
+      v[i] = u_in[row + p];
+      ph[i] = phase[row + p];
     }
+#pragma unroll
+    for (int i = 0; i < RG_E; ++i) v[i] = cmul(v[i], cis_f(s * ph[i]));
     fft_forward<N, RG_E, 1>(v, t, tw, lsm, bar_id, RG_HALF);
 #pragma unroll
     for (int i = 0; i < RG_E; ++i) u_out[row + t + i * T] = v[i];
@@ -169,16 +193,25 @@ __device__ __forceinline__ void row_chunk(const RgProblem& P, int chunk, int ht,
     const float2* src = (KIND == RG_ROW_MID) ? u_out : adj;
 #pragma unroll
     for (int i = 0; i < RG_E; ++i) v[i] = cconj(src[row + t + i * T]);
-    fft_forward<N, RG_E, 1>(v, t, tw, lsm, bar_id, RG_HALF);
+    // side inputs of the chunk, copied while the inverse transform runs
     if constexpr (KIND == RG_ROW_MID) {
-      const float* __restrict__ target = P.target;
+      half_copy16(side_r, P.target + row0, RG_HCHUNK * 4, ht);
+    } else {
+      half_copy16(side_c, u_in + row0, RG_HCHUNK * 8, ht);
+      half_copy16(side_r, phase + row0, RG_HCHUNK * 4, ht);
+    }
+    cp_async_commit();
+    fft_forward<N, RG_E, 1>(v, t, tw, lsm, bar_id, RG_HALF);
+    cp_async_wait<0>();
+    named_sync(bar_id, RG_HALF);
+    if constexpr (KIND == RG_ROW_MID) {
       float part = 0.f;
 #pragma unroll
       for (int i = 0; i < RG_E; ++i) {
         const int p = t + i * T;
         const float2 u = cconj(v[i]);
         u_out[row + p] = u;
-        const float r = fmaf(u.x, u.x, u.y * u.y) - target[row + p];
+        const float r = fmaf(u.x, u.x, u.y * u.y) - side_r[loc + p];
         part = fmaf(r, r, part);
         v[i] = cscale(u, 4.f * r);  // seed of the adjoint: 4 (I - t) u
       }
@@ -201,8 +234,8 @@ __device__ __forceinline__ void row_chunk(const RgProblem& P, int chunk, int ht,
       for (int i = 0; i < RG_E; ++i) {
         const int p = t + i * T;
         const float2 dv = cconj(v[i]);
-        const float2 du = cmul(dv, cis_f(-s * phase[row + p]));
-        const float2 us = u_in[row + p];
+        const float2 du = cmul(dv, cis_f(-s * side_r[loc + p]));
+        const float2 us = side_c[loc + p];
         grad[row + p] = s * (du.y * us.x - du.x * us.y);  // s * Im(du * conj(u_in))
       }
     }
@@ -216,6 +249,8 @@ __device__ void row_pass(const RgArgs& a, float2* smem, unsigned* counter, int* 
   const int bar_id = 1 + half;
   float2* sm = smem + half * RG_HSLOTS;
   float* red = s_red + half * (RG_HALF / 32);
+  // side inputs: 4096 float2 + 4096 float per half, after both exchange regions
+  float2* side = smem + 2 * RG_HSLOTS + half * (RG_HCHUNK + RG_HCHUNK / 2);
   for (;;) {
     if (ht == 0) s_next[half] = (int)atomicAdd(counter, 1u);
     named_sync(bar_id, RG_HALF);
@@ -225,11 +260,11 @@ __device__ void row_pass(const RgArgs& a, float2* smem, unsigned* counter, int* 
     const int2 it = a.row_items[k];
     const RgProblem& P = a.probs[it.x];
     switch (P.lg) {
-      case 8: row_chunk<256, KIND>(P, it.y, ht, sm, bar_id, a.tw[0], a.partials, red); break;
-      case 9: row_chunk<512, KIND>(P, it.y, ht, sm, bar_id, a.tw[1], a.partials, red); break;
-      case 10: row_chunk<1024, KIND>(P, it.y, ht, sm, bar_id, a.tw[2], a.partials, red); break;
-      case 11: row_chunk<2048, KIND>(P, it.y, ht, sm, bar_id, a.tw[3], a.partials, red); break;
-      default: row_chunk<4096, KIND>(P, it.y, ht, sm, bar_id, a.tw[4], a.partials, red); break;
+      case 8: row_chunk<256, KIND>(P, it.y, ht, sm, bar_id, a.tw[0], a.partials, red, side); break;
+      case 9: row_chunk<512, KIND>(P, it.y, ht, sm, bar_id, a.tw[1], a.partials, red, side); break;
+      case 10: row_chunk<1024, KIND>(P, it.y, ht, sm, bar_id, a.tw[2], a.partials, red, side); break;
+      case 11: row_chunk<2048, KIND>(P, it.y, ht, sm, bar_id, a.tw[3], a.partials, red, side); break;
+      default: row_chunk<4096, KIND>(P, it.y, ht, sm, bar_id, a.tw[4], a.partials, red, side); break;
     }
   }
 }
