@@ -294,4 +294,65 @@ end
 _convert_prop(c::ASProp, u) = GB300ASProp(u, c.optical_components[2].z; n0 = c.optical_components[2].n0)
 _convert_prop(c::RSProp, u) = GB300RSProp(u, c.optical_components[3].z)
 
+# ---------------------------------------------------------------------------
+# Ragged batch: independent Phase |> ASProp |> SquaredIntensityDifference problems
+# of different sizes, forward + adjoint of all of them in one persistent launch.
+# ---------------------------------------------------------------------------
+struct FoRaggedProblem  # mirrors `fo_ragged_problem`
+    n::Cint
+    dx::Cdouble
+    dy::Cdouble
+    lambda::Cdouble
+    z::Cdouble
+    n0::Cdouble
+    u_in::Ptr{Cvoid}
+    phase::Ptr{Cvoid}
+    target::Ptr{Cvoid}
+    u_out::Ptr{Cvoid}
+    grad_phase::Ptr{Cvoid}
+    loss::Ptr{Cvoid}
+end
+
+mutable struct GB300Ragged
+    handle::Ptr{Cvoid}
+    outputs::Vector{CuArray{ComplexF32, 2}}
+    grads::Vector{CuArray{Float32, 2}}
+    losses::CuArray{Float32, 1}
+    keep::Vector{Any}          # the bound input arrays stay alive with the plan
+end
+
+# problems: tuples (u::ScalarField (one n x n field, n a power of two 256..4096),
+#                    ϕ::CuMatrix{Float32}, target::CuMatrix{Float32}, z; n0 = 1)
+function GB300Ragged(problems)
+    m = length(problems)
+    losses = CUDA.zeros(Float32, m)
+    outs = CuArray{ComplexF32, 2}[]
+    grads = CuArray{Float32, 2}[]
+    keep = Any[]
+    descs = FoRaggedProblem[]
+    for (k, (u, ϕ, t, z)) in enumerate(problems)
+        n = size(u.electric, 1)
+        uin = reshape(u.electric, n, n)
+        out = similar(uin)
+        g = similar(ϕ)
+        push!(outs, out); push!(grads, g); push!(keep, uin, ϕ, t)
+        ds = FluxOptics.get_ds(u)
+        push!(descs, FoRaggedProblem(n, ds[1], ds[2], lambdas_per_field(u)[1], z, 1.0,
+                                     dptr(uin), dptr(ϕ), dptr(t), dptr(out), dptr(g),
+                                     dptr(losses) + (k - 1) * sizeof(Float32)))
+    end
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_ragged_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Ptr{FoRaggedProblem}, Cint, Cint),
+                h, descs, m, 0))
+    r = GB300Ragged(h[], outs, grads, losses, keep)
+    finalizer(x -> ccall((:fo_ragged_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), r)
+    r
+end
+
+# withgradient of every problem at once: (losses, propagated fields, ∂ϕ)
+function run!(r::GB300Ragged)
+    check(ccall((:fo_ragged_batch, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), r.handle, cstream()))
+    (r.losses, r.outputs, r.grads)
+end
+
 end # module
