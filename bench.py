@@ -704,6 +704,9 @@ def main():
             line["speedup_vs_plain_cufft"] = round(line["value"] / line["plain_cufft"]["value"] / world, 2)
         if not args.no_cpu and world == 1:
             line["cpu_baseline"] = run_cpu_sample()
+            one = run_cpu_sample(budget_s=6.0, threads=1)
+            line["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": one["unit"], "cores": 1,
+                                                     "sample": one["sample"]}
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
