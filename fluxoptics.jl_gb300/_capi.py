@@ -10,7 +10,7 @@ from . import build as _build
 FO_OK = 0
 FO_FORWARD = 1
 FO_BACKWARD = -1
-FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN = 0, 1, 2, 3
+FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = 0, 1, 2, 3, 4
 
 ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
                5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
@@ -26,7 +26,7 @@ class FluxOpticsError(RuntimeError):
 
 class fo_mod(C.Structure):
     _fields_ = [("kind", C.c_int), ("param", C.c_void_p), ("saved", C.c_void_p),
-                ("grad", C.c_void_p), ("scale", C.c_double)]
+                ("grad", C.c_void_p), ("scale", C.c_double), ("field_coef", C.c_void_p)]
 
 
 class fo_ragged_problem(C.Structure):
@@ -87,6 +87,8 @@ SIGNATURES = {
     "fo_graph_info": (_i, [_vp, _pi]),
     "fo_graph_destroy": (_i, [_vp]),
     "fo_ragged_create": (_i, [C.POINTER(_vp), C.POINTER(fo_ragged_problem), _i, _i]),
+    "fo_tea_forward": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "fo_tea_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
     "fo_ragged_batch": (_i, [_vp, _vp]),
     "fo_ragged_info": (_i, [_vp, _pi, C.POINTER(C.c_size_t)]),
     "fo_ragged_destroy": (_i, [_vp]),

@@ -216,9 +216,9 @@ class _Modulator(Component):
     def get_data(self):
         return self.param
 
-    def fo_mod(self, saved=None, grad=None):
+    def fo_mod(self, saved=None, grad=None, u=None):
         return fo_mod(self.mod_kind, self.param.data_ptr(), saved.data_ptr() if saved is not None else None,
-                      grad.data_ptr() if grad is not None else None, 1.0)
+                      grad.data_ptr() if grad is not None else None, 1.0, None)
 
     def alloc_saved_buffer(self, u):
         return torch.empty_like(u.electric)
@@ -275,6 +275,77 @@ class Phase(_Modulator):
         _capi.call("fo_phase_backward", _ptr(dv.electric), _ptr(self.phi), _ptr(saved), _ptr(grad),
                    dv.nx, dv.ny, dv.batch, int(direction), _stream())
         return dv, {"phi": grad}
+
+
+class TeaDOE(_Modulator):
+    """Thin-element DOE: u -> r(λ) cis(2π dn(λ) h / λ) u, conj(r) and the opposite
+    phase backward (modulators/tea_doe.jl:38-215).  ``dn`` and ``r`` are numbers
+    or functions of the wavelength; the trainable parameter is the height ``h``."""
+
+    mod_kind = _capi.FO_MOD_TEA
+    pname = "h"
+
+    def __init__(self, u, dn, f=None, ds=None, r=1.0, trainable=False, buffered=False):
+        ds = tuple(ds) if ds is not None else u.ds
+        if f is None:
+            arr = np.zeros((u.ny, u.nx))
+        elif callable(f):
+            arr = np.real(function_to_array(f, (u.nx, u.ny), ds))
+        else:
+            arr = f.detach().cpu().numpy() if isinstance(f, torch.Tensor) else np.asarray(f)
+            if arr.shape != (u.ny, u.nx):
+                raise ValueError(f"height array must have shape (ny, nx) = {(u.ny, u.nx)}")
+        self.h = torch.as_tensor(np.asarray(arr, dtype=np.float32)).cuda().contiguous()
+        self.dn = dn if callable(dn) else (lambda lam, _v=float(dn): _v)
+        self.r = r if callable(r) else (lambda lam, _v=complex(r): _v)
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+        self._coefs = {}
+        self._alloc_buffers(u)
+
+    def field_coef(self, u: ScalarField):
+        """Device float[batch][4] = {2π dn(λ_b)/λ_b, Re r(λ_b), Im r(λ_b), 0}, per field."""
+        lams = tuple(float(v) for v in u.lambdas_per_field())
+        c = self._coefs.get(lams)
+        if c is None:
+            rows = []
+            for lam in lams:
+                rv = complex(self.r(lam))
+                rows.append([2.0 * math.pi * float(self.dn(lam)) / lam, rv.real, rv.imag, 0.0])
+            c = torch.tensor(np.asarray(rows, dtype=np.float32)).cuda().contiguous()
+            self._coefs[lams] = c
+        return c
+
+    def fo_mod(self, saved=None, grad=None, u=None):
+        if u is None:
+            raise ValueError("TeaDOE needs the field to build its per-wavelength coefficients")
+        return fo_mod(self.mod_kind, self.h.data_ptr(), saved.data_ptr() if saved is not None else None,
+                      grad.data_ptr() if grad is not None else None, 1.0, self.field_coef(u).data_ptr())
+
+    def propagate_(self, u, direction=Forward):
+        _capi.call("fo_tea_forward", _ptr(u.electric), _ptr(self.h), _ptr(self.field_coef(u)), None, u.nx,
+                   u.ny, u.batch, int(direction), _stream())
+        return u
+
+    def propagate_and_save_(self, u, saved, direction=Forward):
+        _capi.call("fo_tea_forward", _ptr(u.electric), _ptr(self.h), _ptr(self.field_coef(u)), _ptr(saved),
+                   u.nx, u.ny, u.batch, int(direction), _stream())
+        return u
+
+    def backpropagate_(self, dv, direction=Forward):
+        _capi.call("fo_tea_backward", _ptr(dv.electric), _ptr(self.h), _ptr(self.field_coef(dv)), None, None,
+                   dv.nx, dv.ny, dv.batch, int(direction), _stream())
+        return dv
+
+    def backpropagate_with_gradient_(self, dv, saved, grad, direction=Forward):
+        _capi.call("fo_tea_backward", _ptr(dv.electric), _ptr(self.h), _ptr(self.field_coef(dv)), _ptr(saved),
+                   _ptr(grad), dv.nx, dv.ny, dv.batch, int(direction), _stream())
+        return dv, {"h": grad}
+
+
+def TeaReflector(u, f=None, ds=None, r=1.0, trainable=False, buffered=False):
+    """Reflective thin element: TeaDOE with dn = 2 (phase 4π h / λ) (tea_doe.jl:84-127)."""
+    return TeaDOE(u, 2.0, f, ds=ds, r=r, trainable=trainable, buffered=buffered)
 
 
 class Mask(_Modulator):
@@ -428,7 +499,7 @@ class FieldProbe(Component):
 
 
 def _is_mod(c):
-    return isinstance(c, (Phase, Mask))
+    return isinstance(c, (Phase, Mask, TeaDOE))
 
 
 def _is_prop(c):
@@ -535,11 +606,11 @@ class OpticalSystem:
                 saved = []
                 for k, m in enumerate(seg.mods):
                     if m is None:
-                        mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0)
+                        mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0, None)
                         saved.append(None)
                         continue
                     sv = m.get_saved_buffer(u) if (tape is not None and m.trainable) else None
-                    mods[k] = m.fo_mod(saved=sv)
+                    mods[k] = m.fo_mod(saved=sv, u=u)
                     saved.append(sv)
                 if from_src:
                     _capi.call("fo_chain_forward_from", self._chain_handle(seg, u), _ptr(src.electric),
@@ -584,10 +655,10 @@ class OpticalSystem:
                 mods = (fo_mod * len(seg.mods))()
                 for k, m in enumerate(seg.mods):
                     if m is None:
-                        mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0)
+                        mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0, None)
                         continue
                     g = m.get_gradient_buffer() if m.trainable else None
-                    mods[k] = m.fo_mod(saved=saved[k], grad=g)
+                    mods[k] = m.fo_mod(saved=saved[k], grad=g, u=du)
                     if g is not None:
                         grads[m] = {m.pname: g}
                 flags = 0 if (input_grad or not last) else 1  # FO_BWD_DISCARD_INPUT_GRAD

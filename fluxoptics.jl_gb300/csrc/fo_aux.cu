@@ -121,6 +121,45 @@ __global__ void phase_bwd_kernel(float2* dv, const float* phi, const float2* sav
   }
 }
 
+// TeaDOE: field b is multiplied by r_b cis(s k_b h) (conj(r_b) for s < 0), with
+// coef[b] = {k_b, Re r_b, Im r_b, 0} (modulators/tea_doe.jl:150-156).
+__global__ void tea_fwd_kernel(float2* u, const float* h, const float4* coef, float2* saved, long long npix,
+                               int batch, float s) {
+  const long long n = npix * batch;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(q / npix);
+    const float4 c = coef[b];
+    const float2 r = make_float2(c.y, s < 0.f ? -c.z : c.z);
+    const float2 x = u[q];
+    if (saved) saved[q] = x;
+    u[q] = cmul(x, cmul(r, cis_f(s * c.x * h[q % npix])));
+  }
+}
+
+// Adjoint: du_b = conj(r_b cis(s k_b h)) dv_b; dh = sum_b s k_b Im(du_b conj(u_saved_b)),
+// one thread per pixel looping over the batch in order (tea_doe.jl:180-215).
+__global__ void tea_bwd_kernel(float2* dv, const float* h, const float4* coef, const float2* saved, float* dh,
+                               long long npix, int batch, float s) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    const float hp = h[p];
+    float acc = 0.f;
+    for (int b = 0; b < batch; ++b) {
+      const float4 c = coef[b];
+      const float2 r = make_float2(c.y, s < 0.f ? c.z : -c.z);  // conj of the forward amplitude
+      const long long q = (long long)b * npix + p;
+      const float2 du = cmul(dv[q], cmul(r, cis_f(-s * c.x * hp)));
+      dv[q] = du;
+      if (dh) {
+        const float2 u = saved[q];
+        acc = fmaf(s * c.x, du.y * u.x - du.x * u.y, acc);
+      }
+    }
+    if (dh) dh[p] = acc;
+  }
+}
+
 __global__ void mask_fwd_kernel(float2* u, const float2* m, float2* saved, long long npix, int batch,
                                 int conj_m) {
   const long long n = npix * batch;
@@ -410,6 +449,18 @@ cudaError_t launch_phase_fwd(float2* u, const float* phi, float2* saved, long lo
 cudaError_t launch_phase_bwd(float2* dv, const float* phi, const float2* saved, float* dphi,
                              long long npix, int batch, float s, cudaStream_t st) {
   phase_bwd_kernel<<<capped_grid(npix), kThreads, 0, st>>>(dv, phi, saved, dphi, npix, batch, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tea_fwd(float2* u, const float* h, const float4* coef, float2* saved, long long npix,
+                           int batch, float s, cudaStream_t st) {
+  tea_fwd_kernel<<<capped_grid(npix * batch), kThreads, 0, st>>>(u, h, coef, saved, npix, batch, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tea_bwd(float2* dv, const float* h, const float4* coef, const float2* saved, float* dh,
+                           long long npix, int batch, float s, cudaStream_t st) {
+  tea_bwd_kernel<<<capped_grid(npix), kThreads, 0, st>>>(dv, h, coef, saved, dh, npix, batch, s);
   return cudaGetLastError();
 }
 

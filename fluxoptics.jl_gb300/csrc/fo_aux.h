@@ -14,6 +14,10 @@ cudaError_t launch_phase_fwd(float2* u, const float* phi, float2* saved, long lo
                              float s, cudaStream_t st);
 cudaError_t launch_phase_bwd(float2* dv, const float* phi, const float2* saved, float* dphi,
                              long long npix, int batch, float s, cudaStream_t st);
+cudaError_t launch_tea_fwd(float2* u, const float* h, const float4* coef, float2* saved, long long npix,
+                           int batch, float s, cudaStream_t st);
+cudaError_t launch_tea_bwd(float2* dv, const float* h, const float4* coef, const float2* saved, float* dh,
+                           long long npix, int batch, float s, cudaStream_t st);
 cudaError_t launch_mask_fwd(float2* u, const float2* m, float2* saved, long long npix, int batch,
                             int conj_m, cudaStream_t st);
 cudaError_t launch_mask_bwd(float2* dv, const float2* m, const float2* saved, float2* dm,

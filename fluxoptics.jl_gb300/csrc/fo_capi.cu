@@ -322,6 +322,7 @@ struct Mod {
   void* saved = nullptr;
   void* grad = nullptr;
   float scale = 1.f;
+  const float4* field_coef = nullptr;
 };
 
 Mod mod_from(const fo_mod* m) {
@@ -332,6 +333,7 @@ Mod mod_from(const fo_mod* m) {
   r.saved = m->saved;
   r.grad = m->grad;
   r.scale = (float)m->scale;
+  r.field_coef = reinterpret_cast<const float4*>(m->field_coef);
   return r;
 }
 
@@ -342,8 +344,11 @@ struct SeedArgs {
 };
 
 int validate_mod(const Mod& m, bool backward) {
-  if (m.kind < MOD_NONE || m.kind > MOD_DN) return fail(FO_ERR_ARG, "unknown modulation kind");
+  if (m.kind < MOD_NONE || m.kind > MOD_TEA) return fail(FO_ERR_ARG, "unknown modulation kind");
   if (m.kind != MOD_NONE && !m.param) return fail(FO_ERR_ARG, "modulation parameter pointer is NULL");
+  if (m.kind == MOD_TEA && !m.field_coef) return fail(FO_ERR_ARG, "FO_MOD_TEA needs field_coef");
+  if (m.kind == MOD_TEA && (reinterpret_cast<uintptr_t>(m.field_coef) & 15) != 0)
+    return fail(FO_ERR_ARG, "field_coef must be 16-byte aligned");
   if (backward && m.kind != MOD_NONE && m.grad && !m.saved)
     return fail(FO_ERR_ARG, "a gradient needs the saved forward input");
   return FO_OK;
@@ -378,6 +383,7 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
   a.param_ld = L.nx;
   a.mod_scale = mod.scale;
   a.inv_lambda = inv_lambda;
+  a.field_coef = mod.field_coef;
   if (!bwd) {
     a.save = reinterpret_cast<float2*>(mod.saved);
     a.save_bstride = real_bs;
@@ -956,6 +962,29 @@ FO_API int fo_phase_backward(void* dv, const float* phi, const void* u_saved, fl
   FO_TRY(check_dir(direction));
   FO_LAUNCH(launch_phase_bwd(reinterpret_cast<float2*>(dv), phi, reinterpret_cast<const float2*>(u_saved),
                              dphi, (long long)nx * ny, batch, (float)direction, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_tea_forward(void* u, const float* h, const void* field_coef, void* u_saved, int nx, int ny,
+                          int batch, int direction, void* stream) {
+  if (!u || !h || !field_coef) return fail(FO_ERR_ARG, "u, h and field_coef must not be NULL");
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  FO_TRY(check_dir(direction));
+  FO_LAUNCH(launch_tea_fwd(reinterpret_cast<float2*>(u), h, reinterpret_cast<const float4*>(field_coef),
+                           reinterpret_cast<float2*>(u_saved), (long long)nx * ny, batch, (float)direction,
+                           S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_tea_backward(void* dv, const float* h, const void* field_coef, const void* u_saved, float* dh,
+                           int nx, int ny, int batch, int direction, void* stream) {
+  if (!dv || !h || !field_coef) return fail(FO_ERR_ARG, "dv, h and field_coef must not be NULL");
+  if (dh && !u_saved) return fail(FO_ERR_ARG, "dh needs u_saved");
+  if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
+  FO_TRY(check_dir(direction));
+  FO_LAUNCH(launch_tea_bwd(reinterpret_cast<float2*>(dv), h, reinterpret_cast<const float4*>(field_coef),
+                           reinterpret_cast<const float2*>(u_saved), dh, (long long)nx * ny, batch,
+                           (float)direction, S(stream)));
   return FO_OK;
 }
 

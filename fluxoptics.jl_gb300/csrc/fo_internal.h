@@ -23,7 +23,7 @@ int cuda_fail(cudaError_t e, const char* what);
   } while (0)
 
 // Modulation kinds applied in real space inside the row passes.
-enum ModKind : int { MOD_NONE = 0, MOD_PHASE = 1, MOD_MASK = 2, MOD_DN = 3 };
+enum ModKind : int { MOD_NONE = 0, MOD_PHASE = 1, MOD_MASK = 2, MOD_DN = 3, MOD_TEA = 4 };
 
 // One row pass over `batch` fields: for every row y < nrows of every field,
 // load -> [inverse FFT along x] -> [seed] -> [modulation] -> [forward FFT along x] -> store.
@@ -47,6 +47,7 @@ struct RowPassArgs {
   int param_ld;
   float mod_scale;            // MOD_DN: kdz; the phase factor of field b is mod_scale * inv_lambda[b]
   const float* inv_lambda;    // MOD_DN: per field id, 1 / lambda
+  const float4* field_coef;   // MOD_TEA: per field id {2 pi dn(lambda) / lambda, Re r, Im r, 0}
   float2* save;               // forward: modulation input written here (nullable)
   long long save_bstride;
   int save_ld;

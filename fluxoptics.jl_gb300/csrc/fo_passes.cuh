@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
       return wm[i];
   };
   float wm_fb = -1.f;
+  float2 wm_amp = make_float2(1.f, 0.f);
 
   // Passes without a gradient accumulator have the registers to keep this
   // thread's twiddles for all the CTA's fields.
@@ -176,9 +177,21 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
         sv[i] = (row_ok && p < n_valid) ? svp[p] : make_float2(0.f, 0.f);
       }
     }
-    const float fb = (a.mod_kind == MOD_DN) ? a.mod_scale * a.inv_lambda[b] : 1.f;
-    if (a.mod_kind != MOD_NONE && row_ok && fb != wm_fb) {
+    // per-field factor of the phase-like kinds (dn: kdz / lambda; TeaDOE: 2 pi dn(lambda) /
+    // lambda) and TeaDOE's per-field amplitude r(lambda)
+    float fb = 1.f;
+    float2 famp = make_float2(1.f, 0.f);
+    if (a.mod_kind == MOD_DN) {
+      fb = a.mod_scale * a.inv_lambda[b];
+    } else if (a.mod_kind == MOD_TEA) {
+      const float4 fc = a.field_coef[b];
+      fb = fc.x;
+      famp = make_float2(fc.y, fc.z);
+    }
+    if (a.mod_kind != MOD_NONE && row_ok && (fb != wm_fb || famp.x != wm_amp.x || famp.y != wm_amp.y)) {
       const float s = a.mod_sign;
+      // forward: r (conj for s < 0); adjoint: conj(r) (r for s < 0)
+      const float2 amp = ((s < 0.f) != (a.mod_bwd != 0)) ? cconj(famp) : famp;
 #pragma unroll
       for (int i = 0; i < E; ++i) {
         const int p = t + i * T;
@@ -192,11 +205,13 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
           } else {
             const float ph = reinterpret_cast<const float*>(a.mod_param)[q];
             w = cis_f((a.mod_bwd ? -s : s) * fb * ph);
+            if (a.mod_kind == MOD_TEA) w = cmul(w, amp);
           }
         }
         wm_set(i, w);
       }
       wm_fb = fb;
+      wm_amp = famp;
     }
 
     if (a.inv_first) {

@@ -28,7 +28,7 @@ import FluxOptics.OpticalComponents: propagate!, backpropagate!, propagate_and_s
 
 const LIB = joinpath(@__DIR__, "..", "lib", "libfluxoptics_gb300.so")
 const FO_FLAG_AUTOTUNE = Cint(1)
-const FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN = Cint(0), Cint(1), Cint(2), Cint(3)
+const FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = Cint(0), Cint(1), Cint(2), Cint(3), Cint(4)
 
 struct FoMod            # mirrors `fo_mod`
     kind::Cint
@@ -36,7 +36,9 @@ struct FoMod            # mirrors `fo_mod`
     saved::Ptr{Cvoid}
     grad::Ptr{Cvoid}
     scale::Cdouble
+    field_coef::Ptr{Cvoid}  # FO_MOD_TEA only
 end
+FoMod(kind, param, saved, grad, scale) = FoMod(kind, param, saved, grad, scale, C_NULL)
 
 function check(rc::Cint)
     rc == 0 && return nothing

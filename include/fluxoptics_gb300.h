@@ -56,6 +56,8 @@ extern "C" {
 #define FO_MOD_PHASE 1 /* u *= cis(s*phi)        param: float[ny*nx]        */
 #define FO_MOD_MASK 2  /* u *= m (conj(m) if s<0) param: complex float[ny*nx] */
 #define FO_MOD_DN 3    /* u *= cis(s*scale/lambda_b*dn)  param: float[ny*nx]   */
+#define FO_MOD_TEA 4   /* u *= r_b*cis(s*k_b*h) (conj(r_b) if s<0)  param: float[ny*nx] height,
+                          field_coef: float[batch][4] = {k_b = 2 pi dn(lambda_b)/lambda_b, Re r_b, Im r_b, 0} */
 
 /* ---------------------------------------------------------------------- */
 /* Library                                                                 */
@@ -177,6 +179,20 @@ FO_API int fo_mask_forward(void* u, const void* m, void* u_saved, int nx, int ny
 FO_API int fo_mask_backward(void* dv, const void* m, const void* u_saved, void* dm, int nx, int ny,
                             int batch, int direction, void* stream);
 
+/*
+ * TeaDOE (thin-element DOE, also TeaReflector with dn = 2): u *= r_b cis(s k_b h) on
+ * every field b, with k_b = 2 pi dn(lambda_b) / lambda_b and r_b = r(lambda_b) given
+ * per field in `field_coef` (device float[batch][4] = {k_b, Re r_b, Im r_b, 0});
+ * the conjugate amplitude for s < 0.  The backward call applies the adjoint and,
+ * when dh is not NULL, writes dh = sum_b s k_b Im(du_b conj(u_saved_b)).
+ * Replaces: propagate!/propagate_and_save!/backpropagate_with_gradient! of TeaDOE
+ * (modulators/tea_doe.jl:150-215).
+ */
+FO_API int fo_tea_forward(void* u, const float* h, const void* field_coef, void* u_saved, int nx, int ny,
+                          int batch, int direction, void* stream);
+FO_API int fo_tea_backward(void* dv, const float* h, const void* field_coef, const void* u_saved, float* dh,
+                           int nx, int ny, int batch, int direction, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* Fused chains: mod_0 -> prop_0 -> mod_1 -> ... -> prop_{K-1} -> mod_K     */
 /* ---------------------------------------------------------------------- */
@@ -189,6 +205,7 @@ typedef struct {
   void* grad;        /* backward: gradient written here when not NULL
                         (phase / dn: float[ny*nx]; mask: complex float[ny*nx]) */
   double scale;      /* FO_MOD_DN: kdz = 2 pi dz / cos(theta); unused otherwise */
+  const void* field_coef; /* FO_MOD_TEA: device float[batch][4] per-field coefficients; else unused */
 } fo_mod;
 
 typedef struct fo_chain_s* fo_chain;

@@ -279,6 +279,36 @@ def phase_backward(dv, phi, u_saved, direction=FORWARD):
     return du, dphi
 
 
+def tea_coefs(lambdas, dn, r=1.0):
+    """Per-field (k_b, r_b) of TeaDOE: k = 2π dn(λ)/λ and r(λ) (tea_doe.jl:54-76);
+    dn and r are numbers or functions of λ."""
+    lams = np.atleast_1d(np.asarray(lambdas, dtype=np.float64))
+    dnf = dn if callable(dn) else (lambda lam: dn)
+    rf = r if callable(r) else (lambda lam: r)
+    k = np.array([2 * np.pi * dnf(l) / l for l in lams])
+    rv = np.array([complex(rf(l)) for l in lams])
+    return k, rv
+
+
+def tea_forward(u, h, k, r, direction=FORWARD):
+    """u_b * r_b cis(s k_b h), conj(r_b) for s < 0 (tea_doe.jl:150-156); u is
+    (batch, ny, nx), k and r hold one value per field."""
+    u = np.asarray(u)
+    rr = r if direction > 0 else np.conj(r)
+    t = rr[:, None, None] * np.exp(1j * direction * k[:, None, None] * np.asarray(h, dtype=np.float64))
+    return u * t
+
+
+def tea_backward(dv, h, k, r, u_saved, direction=FORWARD):
+    """Adjoint of TeaDOE and the height gradient (tea_doe.jl:180-215):
+    du_b = conj(r_b cis(s k_b h)) dv_b;  dh = sum_b s k_b Im(du_b conj(u_saved_b))."""
+    dv = np.asarray(dv)
+    rr = np.conj(r) if direction > 0 else r
+    du = dv * rr[:, None, None] * np.exp(-1j * direction * k[:, None, None] * np.asarray(h, dtype=np.float64))
+    g = direction * k[:, None, None] * np.imag(du * np.conj(u_saved))
+    return du, g.sum(axis=0)
+
+
 def mask_forward(u, m, direction=FORWARD):
     """u * conj_direction(m) (mask.jl:241-248)."""
     m = np.asarray(m, dtype=np.complex128)

@@ -211,6 +211,60 @@ def test_chain_gradients(fo, orc, kind, d):
     assert orc.rel_l2(npy(grads[c0]["phi"]), g0) < GRAD_TOL
 
 
+@pytest.mark.parametrize("d", [1, -1])
+def test_tea_doe_standalone_and_fused(fo, orc, d):
+    """TeaDOE with a dispersive dn(λ) and a complex r(λ) on a two-wavelength batch:
+    the standalone kernels (forward, adjoint, height gradient) and the same element
+    fused into a chain (Tea -> AS -> Mask -> AS -> SID) with its gradient."""
+    rng = np.random.default_rng(31)
+    n, B = 128, 4
+    ds, lams = (1.0, 1.0), np.array([0.64, 0.455, 0.64, 0.455])
+    dn = lambda lam: 0.45 + 0.01 / lam ** 2
+    r = lambda lam: 0.95 * np.exp(0.2j * lam)
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(14.0, x, y)] * B) * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    h = f32(rng.uniform(0, 1.2, (n, n)))
+    k, rv = orc.tea_coefs(lams, dn, r)
+
+    u = fo.ScalarField(u0, ds, lams)
+    tea = fo.TeaDOE(u, dn, h, r=r, trainable=True)
+    v = u.copy()
+    saved = torch.empty_like(v.electric)
+    tea.propagate_and_save_(v, saved, d)
+    ref = orc.tea_forward(u0, h, k, rv, d)
+    assert orc.rel_l2(npy(v.electric).reshape(B, n, n), ref) < FIELD_TOL
+    w0 = c64(rng.standard_normal((B, n, n)) + 1j * rng.standard_normal((B, n, n)))
+    dvf = fo.ScalarField(w0, ds, lams)
+    g = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    tea.backpropagate_with_gradient_(dvf, saved, g, d)
+    du_ref, g_ref = orc.tea_backward(w0, h, k, rv, u0, d)
+    assert orc.rel_l2(npy(dvf.electric).reshape(B, n, n), du_ref) < FIELD_TOL
+    assert orc.rel_l2(npy(g), g_ref) < GRAD_TOL
+
+    m1 = c64(0.5 + rng.uniform(0, 1, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+    target = f32(np.abs(orc.gaussian(10.0, x - 4, y)) ** 2)
+    c1 = fo.Mask(u, m1, trainable=True)
+    zs = [350.0, 250.0]
+    system = fo.OpticalSystem(fo.ScalarSource(u), [tea, fo.ASProp(u, zs[0]), c1, fo.ASProp(u, zs[1])],
+                              direction=d)
+    assert len(system.segments(u)) == 1  # fused: Tea -> AS -> Mask -> AS
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    a0 = orc.tea_forward(u0, h, k, rv, d)
+    a1 = orc.asprop(a0, 1.0, 1.0, lams, zs[0], d)
+    a2 = orc.mask_forward(a1, m1, d)
+    out = orc.asprop(a2, 1.0, 1.0, lams, zs[1], d)
+    assert orc.rel_l2(npy(system()["out"].electric).reshape(B, n, n), out) < FIELD_TOL
+    c_ref, _ = orc.sid_value(out, target)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    dv = orc.asprop(orc.sid_backward(out, target), 1.0, 1.0, lams, zs[1], -d)
+    dv, gm = orc.mask_backward(dv, m1, a1, d)
+    dv = orc.asprop(dv, 1.0, 1.0, lams, zs[0], -d)
+    _, gh = orc.tea_backward(dv, h, k, rv, u0, d)
+    assert orc.rel_l2(npy(grads[c1]["m"]), gm) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[tea]["h"]), gh) < GRAD_TOL
+
+
 # ---------------------------------------------------------------------------
 # AS_BPM
 # ---------------------------------------------------------------------------

@@ -288,3 +288,30 @@ def test_tv_prox_smooths():
     v0 = np.var(x)
     orc.tv_prox(x, 0.1, 100)
     assert np.var(x) < v0
+
+
+def test_tea_doe_reduces_to_phase_and_matches_finite_differences(orc):
+    """TeaDOE with r = 1 and constant dn is Phase(2π dn h / λ) field by field, and
+    its height gradient matches central finite differences of a real loss."""
+    rng = np.random.default_rng(8)
+    lams = np.array([0.5, 0.8, 1.1])
+    u = rng.standard_normal((3, 12, 10)) + 1j * rng.standard_normal((3, 12, 10))
+    h = rng.uniform(0, 0.5, (12, 10))
+    k, r = orc.tea_coefs(lams, 0.45)
+    v = orc.tea_forward(u, h, k, r)
+    for b in range(3):
+        assert np.allclose(v[b], orc.phase_forward(u[b], 2 * np.pi * 0.45 * h / lams[b]))
+    k, r = orc.tea_coefs(lams, lambda l: 0.4 + 0.02 / l, r=lambda l: 0.9 * np.exp(0.3j * l))
+    w = rng.standard_normal((3, 12, 10)) + 1j * rng.standard_normal((3, 12, 10))
+
+    def loss(hh):
+        return float(np.real(np.vdot(w, orc.tea_forward(u, hh, k, r))))
+
+    _, g = orc.tea_backward(w, h, k, r, u)
+    eps = 1e-6
+    for (i, j) in [(0, 0), (5, 7), (11, 9)]:
+        hp, hm = h.copy(), h.copy()
+        hp[i, j] += eps
+        hm[i, j] -= eps
+        fd = (loss(hp) - loss(hm)) / (2 * eps)
+        assert abs(fd - g[i, j]) < 1e-6 * max(1.0, abs(fd))
