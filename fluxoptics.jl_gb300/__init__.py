@@ -9,7 +9,8 @@ fails loudly when the library cannot be loaded.
 from . import _capi
 from ._capi import FluxOpticsError
 from .build import build as build_library
-from .components import (AS_BPM, ASProp, Backward, FieldProbe, Forward, Mask, OpticalSystem, Phase, RSProp,
+from .components import (AS_BPM, ASProp, Backward, FieldProbe, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
+                         RSProp,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate_, function_to_array, propagate, propagate_,
                          reverse, spatial_vectors)
 from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
@@ -22,7 +23,7 @@ load_library = _capi.load
 
 __all__ = [
     "AS_BPM", "ASProp", "Backward", "ClampProx", "FieldProbe", "Fista", "FluxOpticsError", "Forward", "Mask",
-    "NoDescent", "OpticalSystem", "Phase", "ProxRule", "RSProp", "RaggedBatch", "ScalarField", "ScalarSource",
+    "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "ProxRule", "RSProp", "RaggedBatch", "ScalarField", "ScalarSource",
     "SquaredIntensityDifference", "TVProx", "TeaDOE", "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency",
     "function_to_array", "gaussian", "hermite_gaussian", "hermite_gaussian_groups", "intensity",
     "load_library", "make_rules", "normalize_power_", "power", "propagate", "propagate_", "reverse",

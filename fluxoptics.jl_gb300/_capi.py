@@ -29,6 +29,15 @@ class fo_mod(C.Structure):
                 ("grad", C.c_void_p), ("scale", C.c_double), ("field_coef", C.c_void_p)]
 
 
+fo_filter_fn = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong,
+                           C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
+
+
+class fo_as_options(C.Structure):
+    _fields_ = [("paraxial", C.c_int), ("track_tilts", C.c_int), ("tilts", C.POINTER(C.c_double)),
+                ("n_tilts", C.c_int), ("filter", fo_filter_fn), ("filter_ctx", C.c_void_p)]
+
+
 class fo_ragged_problem(C.Structure):
     _fields_ = [("n", C.c_int), ("dx", C.c_double), ("dy", C.c_double), ("lam", C.c_double), ("z", C.c_double),
                 ("n0", C.c_double), ("u_in", C.c_void_p), ("phase", C.c_void_p), ("target", C.c_void_p),
@@ -54,6 +63,8 @@ SIGNATURES = {
     "fo_rsprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _i]),
     "fo_prop_destroy": (_i, [_vp]),
     "fo_prop_info": (_i, [_vp, _pi, _pi, C.POINTER(C.c_size_t)]),
+    "fo_asprop_create_ex": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d,
+                                 C.POINTER(fo_as_options), _i]),
     "fo_prop_variants": (_i, [_vp, _pi, _pi, C.c_char_p, C.c_char_p, _i]),
     "fo_propagate": (_i, [_vp, _vp, _i, _vp]),
     "fo_phase_forward": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),

@@ -110,7 +110,7 @@ class _Propagator(Component):
 
     def plan_for(self, u: ScalarField):
         lam = tuple(float(v) for v in u.lambdas_per_field())
-        key = (u.nx, u.ny, u.batch, lam)
+        key = (u.nx, u.ny, u.batch, lam, tuple(map(float, u.tilts_per_field().ravel())))
         p = self._plans.get(key)
         if p is None:
             p = self._create(u, lam)
@@ -146,16 +146,47 @@ class ASProp(_Propagator):
 
     def __init__(self, u, z, ds=None, n0=1.0, use_cache=True, double_precision_kernel=True,
                  filter=None, paraxial=False, track_tilts=False):
-        if filter is not None or paraxial or track_tilts:
-            raise NotImplementedError("filtered / paraxial / tilt-tracking ASProp is not in the GB300 path")
         self.n0 = float(n0)
+        self.filter = filter              # (fx, fy) -> transmission, numpy-vectorised
+        self.paraxial = bool(paraxial)
+        self.track_tilts = bool(track_tilts)
         super().__init__(u, z, ds)
 
     def _create(self, u, lam):
         h = C.c_void_p()
-        _capi.call("fo_asprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
-                   _capi.dvec(lam), len(lam), self.z, self.n0, int(self.autotune))
+        tilts = u.tilts_per_field()
+        if not (self.paraxial or self.track_tilts or self.filter is not None or np.any(tilts != 0.0)):
+            _capi.call("fo_asprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                       _capi.dvec(lam), len(lam), self.z, self.n0, int(self.autotune))
+            return h
+        opt = _capi.fo_as_options()
+        opt.paraxial = int(self.paraxial)
+        opt.track_tilts = int(self.track_tilts)
+        tv = _capi.dvec(tilts.ravel())
+        opt.tilts = C.cast(tv, C.POINTER(C.c_double))
+        opt.n_tilts = len(tilts)
+        cb = None
+        if self.filter is not None:
+            flt = self.filter
+
+            def _eval(fx, fy, n, re, im, _ctx):
+                fxv = np.ctypeslib.as_array(fx, shape=(n,))
+                fyv = np.ctypeslib.as_array(fy, shape=(n,))
+                val = np.broadcast_to(np.asarray(flt(fxv, fyv), dtype=np.complex128), (n,))
+                np.ctypeslib.as_array(re, shape=(n,))[:] = val.real
+                np.ctypeslib.as_array(im, shape=(n,))[:] = val.imag
+
+            cb = _capi.fo_filter_fn(_eval)
+            opt.filter = cb
+        _capi.call("fo_asprop_create_ex", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                   _capi.dvec(lam), len(lam), self.z, self.n0, C.byref(opt), int(self.autotune))
         return h
+
+
+def ParaxialProp(u, z, ds=None, n0=1.0, filter=None, track_tilts=False, **kw):
+    """Fresnel (paraxial) angular-spectrum propagation: ASProp(paraxial=true)
+    (angular_spectrum.jl:27-44)."""
+    return ASProp(u, z, ds=ds, n0=n0, filter=filter, paraxial=True, track_tilts=track_tilts)
 
 
 def rs_valid_distance(nx, ny, dx, dy, lam):
@@ -174,8 +205,8 @@ class RSProp(_Propagator):
     kind = "RS"
 
     def __init__(self, u, z, ds=None, use_cache=True, double_precision_kernel=True, track_tilts=False):
-        if track_tilts:
-            raise NotImplementedError("tilt tracking is not in the GB300 path")
+        if track_tilts or not u.is_on_axis():
+            raise NotImplementedError("tilted fields in RSProp are not in the GB300 path")
         dsv = tuple(ds) if ds is not None else u.ds
         zc = rs_valid_distance(u.nx, u.ny, dsv[0], dsv[1], float(np.min(u.lambdas_per_field())))
         if abs(z) < zc:

@@ -55,6 +55,51 @@ __global__ void as_h_kernel(float2* H, int fx_n, int fy_n, double dx, double dy,
   }
 }
 
+// General angular-spectrum transfer function (angular_spectrum.jl:1-76), FP64:
+//   mode 0 on axis : cis(2 pi z sqrt(1/lm^2 - fx^2 - fy^2))
+//   mode 1 tilted  : cis(2 pi z (sqrt(1/lm^2 - (fx+f0x)^2 - (fy+f0y)^2) + off)), off = track ? (f0x fx + f0y fy) lm : 0
+//   mode 2 paraxial: cis(-pi lm z ((fx+f0x)^2 + (fy+f0y)^2) - off + 2 pi z / lm), off = track ? 2 (f0x fx + f0y fy) : 0
+// with lm = lambda / n0 and f0 = sin(theta) / lm; complex square root (evanescent
+// components decay); modes 0 and 1 take conj(H(-z)) for z < 0.  Multiplied by the
+// optional filter values (same layout) and by `scale`.
+__global__ void as_h_general_kernel(float2* H, int fx_n, int fy_n, double dx, double dy, double lm, double z,
+                                    double scale, int mode, double f0x, double f0y, int track,
+                                    const double2* filter) {
+  const long long n = (long long)fx_n * fy_n;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(q % fx_n), ky = (int)(q / fx_n);
+    const double fx = fftfreq_d(kx, fx_n, dx), fy = fftfreq_d(ky, fy_n, dy);
+    double re, im;
+    if (mode == 2) {
+      const double gx = fx + f0x, gy = fy + f0y;
+      const double off = track ? 2.0 * (f0x * fx + f0y * fy) : 0.0;
+      const double ph = -M_PI * lm * z * (gx * gx + gy * gy) - off + 2.0 * M_PI * z / lm;
+      sincos(ph, &im, &re);
+    } else {
+      const double gx = mode == 1 ? fx + f0x : fx, gy = mode == 1 ? fy + f0y : fy;
+      const double off = (mode == 1 && track) ? (f0x * fx + f0y * fy) * lm : 0.0;
+      const double arg = 1.0 / (lm * lm) - gx * gx - gy * gy;
+      const double za = fabs(z);
+      // cis(2 pi za (sqrt(arg) + off)); sqrt(arg) = i sqrt(-arg) when arg < 0
+      const double amp = arg >= 0.0 ? 1.0 : exp(-2.0 * M_PI * za * sqrt(-arg));
+      const double ph = 2.0 * M_PI * za * ((arg >= 0.0 ? sqrt(arg) : 0.0) + off);
+      double s, c;
+      sincos(ph, &s, &c);
+      re = amp * c;
+      im = amp * s;
+      if (z < 0.0) im = -im;
+    }
+    if (filter) {
+      const double2 f = filter[q];
+      const double r2 = re * f.x - im * f.y;
+      im = re * f.y + im * f.x;
+      re = r2;
+    }
+    H[q] = make_float2((float)(re * scale), (float)(im * scale));
+  }
+}
+
 // Rayleigh-Sommerfeld impulse response on the circular (py x px) offset grid:
 // offsets 0..n-1 at the start and -(n-1)..-1 at the end of each axis, zero between.
 __global__ void rs_h_spatial_kernel(float2* h, int nx, int ny, int px, int py, double dx, double dy,
@@ -430,6 +475,15 @@ cudaError_t launch_as_h(float2* H, int fx_n, int fy_n, double dx, double dy, dou
   const double lm = lambda / n0;
   as_h_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(H, fx_n, fy_n, dx, dy,
                                                                        1.0 / (lm * lm), z, scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_as_h_general(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
+                                double z, double scale, int mode, double theta_x, double theta_y, int track,
+                                const double2* filter, cudaStream_t s) {
+  const double lm = lambda / n0;
+  as_h_general_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(
+      H, fx_n, fy_n, dx, dy, lm, z, scale, mode, sin(theta_x) / lm, sin(theta_y) / lm, track, filter);
   return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 #include <cmath>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -663,7 +664,8 @@ void apply_overrides(fo_prop_plan p) {
 }
 
 int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx, double dy,
-              const double* lambdas, int n_lambdas, double z, double n0, int flags) {
+              const double* lambdas, int n_lambdas, double z, double n0, int flags,
+              const fo_as_options* opt = nullptr) {
   if (!out) return fail(FO_ERR_ARG, "plan output pointer is NULL");
   *out = nullptr;
   if (nx <= 0 || ny <= 0 || batch <= 0) return fail(FO_ERR_SHAPE, "nx, ny and batch must be positive");
@@ -674,6 +676,11 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     if (!(lambdas[i] > 0)) return fail(FO_ERR_ARG, "wavelengths must be positive");
   if (!std::isfinite(z)) return fail(FO_ERR_ARG, "z must be finite");
   if (kind == 0 && !(n0 > 0)) return fail(FO_ERR_ARG, "n0 must be positive");
+  if (opt && opt->tilts && opt->n_tilts != 1 && opt->n_tilts != batch)
+    return fail(FO_ERR_ARG, "tilts must hold 1 or batch (theta_x, theta_y) pairs");
+  if (opt && opt->tilts)
+    for (int i = 0; i < 2 * opt->n_tilts; ++i)
+      if (!std::isfinite(opt->tilts[i])) return fail(FO_ERR_ARG, "tilt angles must be finite");
   const int fx = kind == 0 ? nx : next_pow2(2 * nx - 1);
   const int fy = kind == 0 ? ny : next_pow2(2 * ny - 1);
   if (!fft_size_supported(fx) || !fft_size_supported(fy))
@@ -692,14 +699,26 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   p->n0 = n0;
   p->lambdas.resize(batch);
   for (int b = 0; b < batch; ++b) p->lambdas[b] = lambdas[n_lambdas == 1 ? 0 : b];
-  // distinct wavelengths -> one transfer function each
-  std::vector<double> uniq;
+  // transfer-function kind: on axis, tilted (any field with a non-zero tilt) or paraxial
+  const bool paraxial = opt && opt->paraxial;
+  std::vector<std::array<double, 2>> tilt(batch, {0.0, 0.0});
+  bool tilted = false;
+  if (opt && opt->tilts)
+    for (int b = 0; b < batch; ++b) {
+      const int t = opt->n_tilts == 1 ? 0 : b;
+      tilt[b] = {opt->tilts[2 * t], opt->tilts[2 * t + 1]};
+      tilted = tilted || tilt[b][0] != 0.0 || tilt[b][1] != 0.0;
+    }
+  const int h_mode = paraxial ? 2 : (tilted ? 1 : 0);
+  // distinct (wavelength, tilts) -> one transfer function each
+  std::vector<std::array<double, 3>> uniq;
   std::vector<int> hidx(batch);
   for (int b = 0; b < batch; ++b) {
-    auto it = std::find(uniq.begin(), uniq.end(), p->lambdas[b]);
+    const std::array<double, 3> key{p->lambdas[b], h_mode ? tilt[b][0] : 0.0, h_mode ? tilt[b][1] : 0.0};
+    auto it = std::find(uniq.begin(), uniq.end(), key);
     if (it == uniq.end()) {
       hidx[b] = (int)uniq.size();
-      uniq.push_back(p->lambdas[b]);
+      uniq.push_back(key);
     } else {
       hidx[b] = (int)(it - uniq.begin());
     }
@@ -765,12 +784,48 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     return cuda_fail(e, "cudaMemcpy plan tables");
   }
   const double scale = 1.0 / ((double)fx * (double)fy);
+  double2* d_filter = nullptr;
+  if (kind == 0 && opt && opt->filter) {
+    if ((rc = dalloc(&d_filter, table, "filter values")) != FO_OK) {
+      plan_free(p);
+      return rc;
+    }
+  }
+  std::vector<double> ffx, ffy, fre, fim;
+  std::vector<double2> fval;
   for (int i = 0; i < p->n_tables && e == cudaSuccess; ++i) {
     float2* Hi = p->H + table * i;
     if (kind == 0) {
-      e = launch_as_h(Hi, fx, fy, dx, dy, uniq[i], n0, z, scale, 0);
+      const double lam = uniq[i][0];
+      if (d_filter) {
+        // the reference evaluates the filter at the (tilt-shifted for the tilted
+        // kernel) frequencies: filter(fx + f0x, fy + f0y), f0 = sin(theta) n0 / lambda
+        const double lm = lam / n0;
+        const double f0x = h_mode == 1 ? sin(uniq[i][1]) / lm : 0.0, f0y = h_mode == 1 ? sin(uniq[i][2]) / lm : 0.0;
+        ffx.resize(table);
+        ffy.resize(table);
+        fre.assign(table, 1.0);
+        fim.assign(table, 0.0);
+        for (int ky = 0; ky < fy; ++ky)
+          for (int kx = 0; kx < fx; ++kx) {
+            const size_t q = (size_t)ky * fx + kx;
+            ffx[q] = (kx < (fx + 1) / 2 ? kx : kx - fx) / (fx * dx) + f0x;
+            ffy[q] = (ky < (fy + 1) / 2 ? ky : ky - fy) / (fy * dy) + f0y;
+          }
+        opt->filter(ffx.data(), ffy.data(), (long long)table, fre.data(), fim.data(), opt->filter_ctx);
+        fval.resize(table);
+        for (size_t q = 0; q < table; ++q) fval[q] = make_double2(fre[q], fim[q]);
+        e = cudaMemcpy(d_filter, fval.data(), sizeof(double2) * table, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) break;
+      }
+      if (h_mode == 0 && !d_filter)
+        e = launch_as_h(Hi, fx, fy, dx, dy, lam, n0, z, scale, 0);
+      else
+        e = launch_as_h_general(Hi, fx, fy, dx, dy, lam, n0, z, scale, h_mode, uniq[i][1], uniq[i][2],
+                                opt && opt->track_tilts ? 1 : 0, d_filter, 0);
+      if (d_filter && e == cudaSuccess) e = cudaDeviceSynchronize();  // d_filter is refilled next
     } else {
-      e = launch_rs_h_spatial(Hi, nx, ny, fx, fy, dx, dy, uniq[i], z, scale, 0);
+      e = launch_rs_h_spatial(Hi, nx, ny, fx, fy, dx, dy, uniq[i][0], z, scale, 0);
       if (e == cudaSuccess) {
         // H_RS = FFT2(h): row transforms of all fy rows, then column transforms
         Layout L{fx, fy, 1, fx, fy, false, 0, false};
@@ -796,6 +851,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     }
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (d_filter) cudaFree(d_filter);
   if (e != cudaSuccess) {
     plan_free(p);
     return cuda_fail(e, "building transfer functions");
@@ -885,6 +941,12 @@ FO_API int fo_stream_synchronize(void* stream) {
 FO_API int fo_asprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
                             const double* lambdas, int n_lambdas, double z, double n0, int flags) {
   return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0, flags);
+}
+
+FO_API int fo_asprop_create_ex(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
+                               const double* lambdas, int n_lambdas, double z, double n0,
+                               const fo_as_options* options, int flags) {
+  return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0, flags, options);
 }
 
 FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,

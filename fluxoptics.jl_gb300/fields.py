@@ -49,7 +49,8 @@ class ScalarField:
 
     ``data``: complex tensor/array of shape ``(..., ny, nx)``; ``ds = (dx, dy)``;
     ``lambdas``: a wavelength or an array broadcast over the trailing dims
-    (Julia order); ``tilts``: must be zero (tilted kernels are not in this path)."""
+    (Julia order); ``tilts = (theta_x, theta_y)`` in radians, each a number or an
+    array broadcast the same way (src/Fields.jl:34-38, :130-141)."""
 
     def __init__(self, data, ds, lambdas, tilts=None):
         self.electric = _as_device_field(data)
@@ -57,9 +58,7 @@ class ScalarField:
             raise ValueError("a field needs two spatial dims")
         self.ds = (float(ds[0]), float(ds[1]))
         self.lambdas = lambdas
-        if tilts is not None and np.any(np.asarray(tilts, dtype=float) != 0):
-            raise NotImplementedError("tilted fields are not supported by the GB300 path")
-        self.tilts = (0.0, 0.0)
+        self.tilts = (0.0, 0.0) if tilts is None else (tilts[0], tilts[1])
 
     # -- shape -------------------------------------------------------------
     @property
@@ -85,19 +84,25 @@ class ScalarField:
     def lambdas_per_field(self):
         return per_field(self.lambdas, self.julia_batch_shape)
 
+    def tilts_per_field(self):
+        """(batch, 2) array of (theta_x, theta_y) per field."""
+        tx = per_field(self.tilts[0], self.julia_batch_shape)
+        ty = per_field(self.tilts[1], self.julia_batch_shape)
+        return np.stack([np.broadcast_to(tx, (self.batch,)), np.broadcast_to(ty, (self.batch,))], axis=1)
+
     # -- helpers of the reference API -------------------------------------------
     def copy(self):
-        return ScalarField(self.electric.clone(), self.ds, self.lambdas)
+        return ScalarField(self.electric.clone(), self.ds, self.lambdas, self.tilts)
 
     def similar(self):
-        return ScalarField(torch.empty_like(self.electric), self.ds, self.lambdas)
+        return ScalarField(torch.empty_like(self.electric), self.ds, self.lambdas, self.tilts)
 
     def set_field_data(self, data):
-        """New field sharing grid and wavelengths (src/Fields.jl:213-215)."""
-        return ScalarField(data, self.ds, self.lambdas)
+        """New field sharing grid, wavelengths and tilts (src/Fields.jl:213-215)."""
+        return ScalarField(data, self.ds, self.lambdas, self.tilts)
 
     def is_on_axis(self):
-        return True
+        return not bool(np.any(self.tilts_per_field() != 0.0))
 
 
 def power(u: ScalarField):

@@ -109,6 +109,39 @@ FO_API int fo_asprop_create(fo_prop_plan* plan, int nx, int ny, int batch, doubl
                             const double* lambdas, int n_lambdas, double z, double n0, int flags);
 
 /*
+ * Options of fo_asprop_create_ex; a zeroed struct gives fo_asprop_create.
+ *   paraxial    : Fresnel transfer function
+ *                 cis(-pi lm z ((fx+f0x)^2 + (fy+f0y)^2) - off + 2 pi z / lm),
+ *                 off = track_tilts ? 2 (f0x fx + f0y fy) : 0, lm = lambda / n0
+ *   tilts       : (theta_x, theta_y) in radians, one pair shared or one per field; any
+ *                 non-zero tilt selects the tilted kernel
+ *                 cis(2 pi z (sqrt(1/lm^2 - (fx+f0x)^2 - (fy+f0y)^2) + off)),
+ *                 off = track_tilts ? (f0x fx + f0y fy) lm : 0, f0 = sin(theta) / lm
+ *                 (conj(H(-z)) for z < 0)
+ *   filter      : optional host callback filling re/im with the filter's value at n
+ *                 frequencies (fx, fy) -- shifted by f0 for the tilted kernel, as the
+ *                 reference evaluates filter(fx + f0x, fy + f0y) -- called once per
+ *                 table at plan creation.
+ * One transfer function is built per distinct (wavelength, tilts).
+ * Replaces: as_paraxial_kernel / tilted_as_kernel / the filter argument of
+ * ASKernelProp (angular_spectrum.jl:27-76, :78-146) and ParaxialProp.
+ */
+typedef void (*fo_filter_fn)(const double* fx, const double* fy, long long n, double* re, double* im,
+                             void* ctx);
+typedef struct {
+  int paraxial;
+  int track_tilts;
+  const double* tilts; /* NULL or 2 * n_tilts angles */
+  int n_tilts;         /* 1 or batch */
+  fo_filter_fn filter; /* NULL: no filter */
+  void* filter_ctx;
+} fo_as_options;
+
+FO_API int fo_asprop_create_ex(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
+                               const double* lambdas, int n_lambdas, double z, double n0,
+                               const fo_as_options* options, int flags);
+
+/*
  * RSProp: zero-pad to (px, py) = the smallest powers of two >= (2nx-1, 2ny-1),
  * FFT, multiply by H_RS = FFT of the Rayleigh-Sommerfeld impulse response
  * h = dx dy/(2 pi) cis(k r)/r (z/r)(1/r - i k) sampled on the circular offset

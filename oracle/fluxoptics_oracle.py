@@ -159,6 +159,39 @@ def as_kernel(nx, ny, dx, dy, lam, z, n0=1.0):
     return h if z >= 0 else np.conj(h)
 
 
+def as_kernel_general(nx, ny, dx, dy, lam, z, n0=1.0, paraxial=False, theta=(0.0, 0.0), track_tilts=False,
+                      filt=None):
+    """Paraxial and tilted angular-spectrum transfer functions, shape (ny, nx)
+    (angular_spectrum.jl:27-76); lm = lam / n0, f0 = sin(theta) / lm.
+
+    paraxial: cis(-pi lm z ((fx+f0x)^2 + (fy+f0y)^2) - off + 2 pi z / lm),
+              off = track_tilts ? 2 (f0x fx + f0y fy) : 0, filter(fx, fy);
+    tilted  : cis(2 pi z (sqrt(1/lm^2 - (fx+f0x)^2 - (fy+f0y)^2) + off)),
+              off = track_tilts ? (f0x fx + f0y fy) lm : 0, filter(fx+f0x, fy+f0y),
+              conj(H(-z)) for z < 0;
+    neither : the on-axis kernel times filter(fx, fy)."""
+    fx, fy = fftfreqs(nx, ny, dx, dy)
+    FX, FY = fx[None, :] + 0 * fy[:, None], fy[:, None] + 0 * fx[None, :]
+    lm = lam / n0
+    f0x, f0y = np.sin(theta[0]) / lm, np.sin(theta[1]) / lm
+    if paraxial:
+        off = 2 * (f0x * FX + f0y * FY) if track_tilts else 0.0
+        h = np.exp(1j * (-np.pi * lm * z * ((FX + f0x) ** 2 + (FY + f0y) ** 2) - off + 2 * np.pi * z / lm))
+        if filt is not None:
+            h = h * filt(FX, FY)
+        return h
+    tilted = theta[0] != 0.0 or theta[1] != 0.0
+    gx, gy = (FX + f0x, FY + f0y) if tilted else (FX, FY)
+    off = (f0x * FX + f0y * FY) * lm if (tilted and track_tilts) else 0.0
+    za = abs(z)
+    h = np.exp(1j * 2 * np.pi * za * (np.sqrt((1 / lm ** 2 - gx ** 2 - gy ** 2).astype(np.complex128)) + off))
+    if z < 0:
+        h = np.conj(h)
+    if filt is not None:
+        h = h * filt(gx, gy)
+    return h
+
+
 def rs_kernel_spatial(n_x, n_y, dx, dy, lam, z, m_x=None, m_y=None):
     """Rayleigh-Sommerfeld impulse response sampled on offsets in FFT order.
 
@@ -214,23 +247,34 @@ def _lams(lambdas, nb):
 # Free-space propagators
 # ---------------------------------------------------------------------------
 
-def asprop(u, dx, dy, lambdas, z, direction=FORWARD, n0=1.0):
+def asprop(u, dx, dy, lambdas, z, direction=FORWARD, n0=1.0, paraxial=False, tilts=None, track_tilts=False,
+           filt=None):
     """ASProp: u <- IFFT2(conj_direction(H) * FFT2(u)) per field.
 
     Sequence (ft, ASKernelProp, ift) of angular_spectrum.jl:193-234; Backward
     applies conj(H) (abstract_kernel.jl:36,45 with OpticalComponents.jl:919-925).
-    ``u`` has shape (..., ny, nx); ``lambdas`` is a scalar or one value per field."""
+    ``u`` has shape (..., ny, nx); ``lambdas`` is a scalar or one value per field;
+    ``tilts`` is None or one (theta_x, theta_y) pair (shared) or one per field;
+    ``paraxial``, ``track_tilts`` and ``filt`` (a function of (fx, fy)) select
+    as_kernel_general."""
     u = np.asarray(u, dtype=np.complex128)
     shp = u.shape
     ny, nx = shp[-2:]
     v = u.reshape(-1, ny, nx)
     lam = _lams(lambdas, v.shape[0])
+    th = np.zeros((v.shape[0], 2))
+    if tilts is not None:
+        th[:] = np.asarray(tilts, dtype=np.float64).reshape(-1, 2)
+    general = paraxial or filt is not None or bool(np.any(th != 0.0))
     out = np.empty_like(v)
     cache = {}
     for b in range(v.shape[0]):
-        key = float(lam[b])
+        key = (float(lam[b]), float(th[b, 0]), float(th[b, 1]))
         if key not in cache:
-            cache[key] = as_kernel(nx, ny, dx, dy, key, z, n0)
+            if general:
+                cache[key] = as_kernel_general(nx, ny, dx, dy, key[0], z, n0, paraxial, key[1:], track_tilts, filt)
+            else:
+                cache[key] = as_kernel(nx, ny, dx, dy, key[0], z, n0)
         h = cache[key] if direction == FORWARD else np.conj(cache[key])
         out[b] = ifft2(fft2(v[b]) * h)
     return out.reshape(shp)

@@ -315,3 +315,25 @@ def test_tea_doe_reduces_to_phase_and_matches_finite_differences(orc):
         hm[i, j] -= eps
         fd = (loss(hp) - loss(hm)) / (2 * eps)
         assert abs(fd - g[i, j]) < 1e-6 * max(1.0, abs(fd))
+
+
+def test_tilted_and_paraxial_kernels(orc):
+    """Tilted kernel with zero tilts is the on-axis kernel; a tilted kernel without
+    carrier tracking propagates a tilted plane wave as a plane wave (intensity
+    unchanged); the paraxial kernel approaches the exact one for small angles."""
+    n, d, lam, z = 64, 1.0, 1.0, 200.0
+    h0 = orc.as_kernel(n, n, d, d, lam, z)
+    assert np.allclose(orc.as_kernel_general(n, n, d, d, lam, z, theta=(0.0, 0.0)), h0)
+    hz = orc.as_kernel_general(n, n, d, d, lam, -z, theta=(0.05, -0.02), track_tilts=True)
+    assert np.allclose(hz, np.conj(orc.as_kernel_general(n, n, d, d, lam, z, theta=(0.05, -0.02),
+                                                         track_tilts=True)))
+    x, y = orc.spatial_vectors((n, n), (d, d))
+    u = orc.gaussian(12.0, x, y)
+    exact = orc.asprop(u, d, d, lam, 50.0)
+    parax = orc.asprop(u, d, d, lam, 50.0, paraxial=True)
+    # same up to the global phase convention of the Fresnel kernel's carrier term
+    c = np.vdot(exact, parax)
+    assert orc.rel_l2(parax * np.conj(c) / abs(c), exact) < 2e-3
+    filt = lambda fx, fy: (np.hypot(fx, fy) < 0.2).astype(np.float64)
+    hf = orc.as_kernel_general(n, n, d, d, lam, z, filt=filt)
+    assert np.allclose(hf, h0 * filt(*np.meshgrid(np.fft.fftfreq(n, d), np.fft.fftfreq(n, d))))
