@@ -14,7 +14,7 @@ from .components import (AS_BPM, ASProp, Backward, FieldProbe, Forward, Mask, Op
                          ScalarSource, TeaDOE, TeaReflector, backpropagate_, function_to_array, propagate, propagate_,
                          reverse, spatial_vectors)
 from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
-from .metrics import SquaredIntensityDifference, withgradient
+from .metrics import DotProduct, PowerCoupling, SquaredIntensityDifference, withgradient
 from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
 from .optimisers import ClampProx, Fista, NoDescent, ProxRule, TVProx, make_rules, setup, update_
 from .ragged import RaggedBatch
@@ -22,10 +22,11 @@ from .ragged import RaggedBatch
 load_library = _capi.load
 
 __all__ = [
-    "AS_BPM", "ASProp", "Backward", "ClampProx", "FieldProbe", "Fista", "FluxOpticsError", "Forward", "Mask",
-    "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "ProxRule", "RSProp", "RaggedBatch", "ScalarField", "ScalarSource",
-    "SquaredIntensityDifference", "TVProx", "TeaDOE", "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency",
-    "function_to_array", "gaussian", "hermite_gaussian", "hermite_gaussian_groups", "intensity",
-    "load_library", "make_rules", "normalize_power_", "power", "propagate", "propagate_", "reverse",
-    "setup", "spatial_vectors", "update_", "withgradient",
+    "ASProp", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError",
+    "Forward", "Mask", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PowerCoupling", "ProxRule",
+    "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredIntensityDifference", "TVProx", "TeaDOE",
+    "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
+    "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
+    "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "update_",
+    "withgradient",
 ]

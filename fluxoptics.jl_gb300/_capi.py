@@ -99,6 +99,10 @@ SIGNATURES = {
     "fo_graph_destroy": (_i, [_vp]),
     "fo_ragged_create": (_i, [C.POINTER(_vp), C.POINTER(fo_ragged_problem), _i, _i]),
     "fo_tea_forward": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "fo_overlap_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _vp, _i, _i]),
+    "fo_overlap_forward": (_i, [_vp, _vp, _vp, _vp]),
+    "fo_overlap_backward": (_i, [_vp, _vp, _vp, _vp]),
+    "fo_overlap_destroy": (_i, [_vp]),
     "fo_tea_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp]),
     "fo_ragged_batch": (_i, [_vp, _vp]),
     "fo_ragged_info": (_i, [_vp, _pi, C.POINTER(C.c_size_t)]),

@@ -1,4 +1,6 @@
-"""SquaredIntensityDifference on the GPU (metrics/squared_intensity_difference.jl:58-90)."""
+"""Metrics on the GPU: SquaredIntensityDifference
+(metrics/squared_intensity_difference.jl:58-90), DotProduct (metrics/dot_product.jl:47-100)
+and PowerCoupling (metrics/power_coupling.jl:48-66)."""
 
 from __future__ import annotations
 
@@ -55,15 +57,73 @@ class SquaredIntensityDifference:
             lib.fo_sid_destroy(self.handle)
 
 
-def withgradient(metric: SquaredIntensityDifference, system: OpticalSystem, x=None):
-    """Loss sum_t c_t and the gradients of every trainable component, through
-    the hand-written adjoint (the GPU counterpart of Zygote.withgradient over
-    the reference's rrules, src/ChainRulesCoreExt.jl:21-111)."""
+class _Overlap:
+    """Common part of DotProduct and PowerCoupling: fields v of the same grid and
+    batch as the fields the metric is applied to (one reference field per field)."""
+
+    power = 0
+
+    def __init__(self, v: ScalarField, mode_selective=True):
+        self.v = v
+        self.mode_selective = bool(mode_selective)
+        self.nx, self.ny, self.batch = v.nx, v.ny, v.batch
+        self.handle = C.c_void_p()
+        _capi.call("fo_overlap_create", C.byref(self.handle), v.nx, v.ny, v.batch, v.ds[0], v.ds[1],
+                   _ptr(v.electric), int(self.mode_selective), self.power)
+        shape = (self.batch,) if self.mode_selective else (self.batch, self.batch)
+        self.out = torch.zeros(shape, dtype=torch.float32 if self.power else torch.complex64, device="cuda")
+
+    def __call__(self, u: ScalarField):
+        """Per-field values (mode selective) or the batch x batch matrix; for the
+        matrix, out[j, i] is the reference's c[i, j] (column-major storage)."""
+        _capi.call("fo_overlap_forward", self.handle, _ptr(u.electric), _ptr(self.out), _stream())
+        return self.out
+
+    def backpropagate_into(self, u: ScalarField, du: ScalarField, dc=None):
+        if dc is None:
+            dc = torch.ones_like(self.out)
+        dc = dc.to(self.out.dtype).contiguous()
+        _capi.call("fo_overlap_backward", self.handle, _ptr(dc), _ptr(du.electric), _stream())
+        return du
+
+    def backpropagate(self, u: ScalarField, dc=None):
+        du = u.similar()
+        return self.backpropagate_into(u, du, dc)
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is not None and getattr(self, "handle", None):
+            lib.fo_overlap_destroy(self.handle)
+
+
+class DotProduct(_Overlap):
+    """c_b = dx dy sum u_b conj(v_b) (or the matrix v' u with mode_selective=False)."""
+
+    power = 0
+
+
+class PowerCoupling(_Overlap):
+    """|DotProduct(u, v_hat)|^2 against unit-power copies v_hat of v."""
+
+    power = 1
+
+
+def withgradient(metric, system: OpticalSystem, x=None, dc=None):
+    """Loss sum(dc * c) (dc = 1 by default) and the gradients of every trainable
+    component, through the hand-written adjoint (the GPU counterpart of
+    Zygote.withgradient over the reference's rrules, src/ChainRulesCoreExt.jl:21-111).
+    SquaredIntensityDifference seeds the adjoint inside the first fused pass; the
+    overlap metrics write their pull-back first."""
     src = system.source.u0 if x is None else x
     u = src.similar()
     tape = []
     system.forward(u, tape, src=src)
-    loss = metric(u)
+    c = metric(u)
     du = u.similar()
-    grads = system.backward(du, tape, seed=(metric, u))
-    return loss.sum(), grads
+    if isinstance(metric, SquaredIntensityDifference) and dc is None:
+        grads = system.backward(du, tape, seed=(metric, u))
+        return c.sum(), grads
+    metric.backpropagate_into(u, du, dc)
+    grads = system.backward(du, tape)
+    w = torch.ones_like(c) if dc is None else dc.to(c.dtype)
+    return (w * c).sum().real if c.is_complex() else (w * c).sum(), grads

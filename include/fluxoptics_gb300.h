@@ -405,6 +405,30 @@ FO_API int fo_graph_info(fo_graph graph, int* kernel_nodes);
 FO_API int fo_graph_destroy(fo_graph graph);
 
 /* ---------------------------------------------------------------------- */
+/* Overlap metrics: DotProduct and PowerCoupling                            */
+/* ---------------------------------------------------------------------- */
+
+/*
+ * Against reference fields v (batch x ny x nx complex float, borrowed for DotProduct;
+ * PowerCoupling keeps unit-power copies made at creation):
+ *   mode_selective = 1: c[b] = dx dy sum_p u_b[p] conj(v_b[p])                 (batch values)
+ *   mode_selective = 0: c[i + j batch] = dx dy sum_p conj(v_i[p]) u_j[p]       (batch^2 values,
+ *                       the column-major v' u of the reference; batch <= 64)
+ * DotProduct (power = 0) writes complex float c; PowerCoupling (power = 1) writes
+ * float |c|^2.  fo_overlap_backward writes du = v g (du_j = sum_i v_i G[i + j batch] for
+ * the matrix form) with g = dc (complex) or 2 dc c (dc real, c of the last forward).
+ * Reductions run in a fixed order (deterministic).
+ * Replaces: compute_metric / backpropagate_metric of DotProduct (metrics/dot_product.jl:47-100)
+ * and PowerCoupling (metrics/power_coupling.jl:48-66).
+ */
+typedef struct fo_overlap_s* fo_overlap;
+FO_API int fo_overlap_create(fo_overlap* ov, int nx, int ny, int batch, double dx, double dy, const void* v,
+                             int mode_selective, int power);
+FO_API int fo_overlap_forward(fo_overlap ov, const void* u, void* c, void* stream);
+FO_API int fo_overlap_backward(fo_overlap ov, const void* dc, void* du, void* stream);
+FO_API int fo_overlap_destroy(fo_overlap ov);
+
+/* ---------------------------------------------------------------------- */
 /* Ragged batch: many independent problems of different sizes, one launch  */
 /* ---------------------------------------------------------------------- */
 

@@ -486,6 +486,44 @@ class FistaState:
         self.newdx = np.zeros_like(self.xk)
 
 
+def dot_product(u, v, ds, mode_selective=True):
+    """DotProduct metric (metrics/dot_product.jl:70-87): per field
+    c_b = sum u_b conj(v_b) dx dy, or with mode_selective=False the matrix
+    c[i, j] = sum conj(v_i) u_j dx dy (v' u of the (npix, n) views).  u, v: (batch, ny, nx)."""
+    u = np.asarray(u, dtype=np.complex128).reshape(-1, *np.shape(u)[-2:])
+    v = np.asarray(v, dtype=np.complex128).reshape(-1, *np.shape(v)[-2:])
+    a = ds[0] * ds[1]
+    if mode_selective:
+        return (u * np.conj(v)).reshape(len(u), -1).sum(axis=1) * a
+    U = u.reshape(len(u), -1).T
+    V = v.reshape(len(v), -1).T
+    return (V.conj().T @ U) * a
+
+
+def dot_product_backward(v, dc, mode_selective=True):
+    """Pull-back of DotProduct (dot_product.jl:89-100): du_b = v_b dc_b, or
+    du = V dc for the matrix form (columns of V are the fields)."""
+    v = np.asarray(v, dtype=np.complex128).reshape(-1, *np.shape(v)[-2:])
+    if mode_selective:
+        return v * np.asarray(dc)[:, None, None]
+    V = v.reshape(len(v), -1).T
+    return (V @ np.asarray(dc)).T.reshape(v.shape)
+
+
+def power_coupling(u, v, ds, mode_selective=True):
+    """PowerCoupling (metrics/power_coupling.jl:48-66): |DotProduct(u, v_hat)|^2 with
+    v_hat the unit-power copies of v.  Returns (values, dot products, v_hat)."""
+    v = np.asarray(v, dtype=np.complex128).reshape(-1, *np.shape(v)[-2:])
+    vh = np.stack([normalize_power(x, ds) for x in v])
+    c = dot_product(u, vh, ds, mode_selective)
+    return np.abs(c) ** 2, c, vh
+
+
+def power_coupling_backward(vh, c_dot, dc, mode_selective=True):
+    """Pull-back of PowerCoupling: DotProduct's with dc' = 2 dc c_dot (power_coupling.jl:63-66)."""
+    return dot_product_backward(vh, 2 * np.asarray(dc) * c_dot, mode_selective)
+
+
 def fista_apply(eta, state, x, dx):
     """One Fista step, in place on x; the rule stores eta^2 (OptimisersExt.jl:33-54).
 

@@ -242,6 +242,52 @@ def test_asprop_paraxial_tilted_filtered(fo, orc, mode, d):
     assert orc.rel_l2(npy(v.electric).reshape(B, n, n), ref) < FIELD_TOL
 
 
+@pytest.mark.parametrize("selective", [True, False])
+def test_dot_product_power_coupling(fo, orc, selective):
+    """DotProduct and PowerCoupling (values and pull-backs) against the oracle, and
+    the gradient of a phase mask through Phase -> ASProp -> PowerCoupling."""
+    rng = np.random.default_rng(17)
+    n, B = 256, 5
+    ds, lams = (0.8, 0.8), np.array([0.64, 0.538, 0.455, 0.64, 0.538])
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.hermite_gaussian(20.0, b % 3, b // 3, x, y) for b in range(B)])
+             * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    v0 = c64(np.stack([orc.hermite_gaussian(18.0, (b + 1) % 3, b // 2, x - 2, y + 1) for b in range(B)]))
+    u = fo.ScalarField(u0, ds, lams)
+    v = fo.ScalarField(v0, ds, lams)
+    dp = fo.DotProduct(v, mode_selective=selective)
+    c = dp(u).cpu().numpy()
+    c_ref = orc.dot_product(u0, v0, ds, selective)
+    got = c if selective else c.T  # out[j, i] = c[i, j]
+    assert orc.rel_l2(got, c_ref) < 1e-5
+    w = c64(rng.standard_normal(c.shape) + 1j * rng.standard_normal(c.shape))
+    du = dp.backpropagate(u, torch.tensor(w, device="cuda"))
+    du_ref = orc.dot_product_backward(v0, w if selective else w.T, selective)
+    assert orc.rel_l2(npy(du.electric).reshape(B, n, n), du_ref) < FIELD_TOL
+
+    pc = fo.PowerCoupling(v, mode_selective=selective)
+    p = pc(u).cpu().numpy()
+    p_ref, cd, vh = orc.power_coupling(u0, v0, ds, selective)
+    assert orc.rel_l2(p if selective else p.T, p_ref) < 1e-5
+    wr = f32(rng.standard_normal(p.shape))
+    du = pc.backpropagate(u, torch.tensor(wr, device="cuda"))
+    du_ref = orc.power_coupling_backward(vh, cd, wr if selective else wr.T, selective)
+    assert orc.rel_l2(npy(du.electric).reshape(B, n, n), du_ref) < GRAD_TOL
+
+    if selective:
+        phi = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+        ph = fo.Phase(u, phi, trainable=True)
+        system = fo.ScalarSource(u) | ph | fo.ASProp(u, 300.0)
+        loss, grads = fo.withgradient(pc, system)
+        a = orc.asprop(orc.phase_forward(u0, phi), ds[0], ds[1], lams, 300.0)
+        pr, cdr, vh = orc.power_coupling(a, v0, ds, True)
+        assert abs(float(loss) - pr.sum()) / pr.sum() < 1e-4
+        g = orc.power_coupling_backward(vh, cdr, np.ones(B), True)
+        g = orc.asprop(g, ds[0], ds[1], lams, 300.0, orc.BACKWARD)
+        _, gphi = orc.phase_backward(g, phi, u0)
+        assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+
 @pytest.mark.parametrize("d", [1, -1])
 def test_tea_doe_standalone_and_fused(fo, orc, d):
     """TeaDOE with a dispersive dn(λ) and a complex r(λ) on a two-wavelength batch:

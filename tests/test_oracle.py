@@ -337,3 +337,48 @@ def test_tilted_and_paraxial_kernels(orc):
     filt = lambda fx, fy: (np.hypot(fx, fy) < 0.2).astype(np.float64)
     hf = orc.as_kernel_general(n, n, d, d, lam, z, filt=filt)
     assert np.allclose(hf, h0 * filt(*np.meshgrid(np.fft.fftfreq(n, d), np.fft.fftfreq(n, d))))
+
+
+def _kat_field():
+    # the docstring example of dot_product.jl / power_coupling.jl: ones(4, 4, 2) with
+    # data[3:end, :, 2] = -1 (Julia x-fastest), power-normalised field by field
+    d = np.ones((2, 4, 4), dtype=np.complex128)
+    d[1, :, 2:] = -1
+    return np.stack([f for f in d])
+
+
+def test_dot_product_and_power_coupling_known_answers(orc):
+    """Known answers printed in the reference's docstrings (dot_product.jl:29-41,
+    power_coupling.jl:28-40): selective [1, 1]; non-selective identity 2x2."""
+    u = np.stack([orc.normalize_power(f, (1.0, 1.0)) for f in _kat_field()])
+    assert np.allclose(orc.dot_product(u, u, (1.0, 1.0)), [1.0, 1.0])
+    assert np.allclose(orc.dot_product(u, u, (1.0, 1.0), mode_selective=False), np.eye(2))
+    p, _, _ = orc.power_coupling(u, u, (1.0, 1.0))
+    assert np.allclose(p, [1.0, 1.0])
+    p, _, _ = orc.power_coupling(u, u, (1.0, 1.0), mode_selective=False)
+    assert np.allclose(p, np.eye(2))
+
+
+def test_overlap_pullbacks_match_finite_differences(orc):
+    """Real losses Re(w . c) of the DotProduct and PowerCoupling outputs: the
+    pull-backs give the gradient (dL/dRe u + i dL/dIm u) up to the reference's
+    convention, checked by central differences on a few pixels."""
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((3, 6, 5)) + 1j * rng.standard_normal((3, 6, 5))
+    v = rng.standard_normal((3, 6, 5)) + 1j * rng.standard_normal((3, 6, 5))
+    ds = (0.5, 0.7)
+    for sel in (True, False):
+        w = rng.standard_normal((3,) if sel else (3, 3))
+        p, c, vh = orc.power_coupling(u, v, ds, sel)
+        loss = lambda uu: float(np.sum(w * orc.power_coupling(uu, v, ds, sel)[0]))
+        g = orc.power_coupling_backward(vh, c, w, sel)
+        eps = 1e-6
+        for (b, i, j) in [(0, 0, 0), (2, 3, 4), (1, 5, 2)]:
+            for part, unit in (("re", 1.0), ("im", 1j)):
+                up, um = u.copy(), u.copy()
+                up[b, i, j] += eps * unit
+                um[b, i, j] -= eps * unit
+                fd = (loss(up) - loss(um)) / (2 * eps)
+                # the reference's pull-back is the conjugate Wirtinger form times dx dy
+                ref = (g[b, i, j].real if part == "re" else g[b, i, j].imag) * ds[0] * ds[1]
+                assert abs(fd - ref) < 1e-5 * max(1.0, abs(fd)), (sel, part, fd, ref)
