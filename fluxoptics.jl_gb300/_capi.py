@@ -11,6 +11,7 @@ FO_OK = 0
 FO_FORWARD = 1
 FO_BACKWARD = -1
 FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = 0, 1, 2, 3, 4
+FO_FOURIER_TRAINABLE = 2
 
 ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
                5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
@@ -63,6 +64,9 @@ SIGNATURES = {
     "fo_rsprop_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _i]),
     "fo_prop_destroy": (_i, [_vp]),
     "fo_prop_info": (_i, [_vp, _pi, _pi, C.POINTER(C.c_size_t)]),
+    "fo_fourier_create": (_i, [C.POINTER(_vp), _i, _i, _i, _i]),
+    "fo_fourier_set": (_i, [_vp, _i, _vp, _vp]),
+    "fo_fourier_gradient": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i, _vp]),
     "fo_asprop_create_ex": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d,
                                  C.POINTER(fo_as_options), _i]),
     "fo_prop_variants": (_i, [_vp, _pi, _pi, C.c_char_p, C.c_char_p, _i]),

@@ -51,10 +51,13 @@ def spatial_vectors(ns, ds, offset=None):
     return tuple((np.arange(n) - (n - 1) / 2.0) * d - c for n, d, c in zip(ns, ds, offset))
 
 
-def function_to_array(f, ns, ds):
-    """Evaluate f(x, y) on the spatial grid; returns an (ny, nx) array
-    (OpticalComponents.jl:927-935)."""
-    x, y = spatial_vectors(ns, ds)
+def function_to_array(f, ns, ds, isfourier=False):
+    """Evaluate f(x, y) on the spatial grid, or on the FFT-ordered frequency grid
+    (fftfreq) when ``isfourier``; returns an (ny, nx) array (OpticalComponents.jl:927-935)."""
+    if isfourier:
+        x, y = np.fft.fftfreq(ns[0], ds[0]), np.fft.fftfreq(ns[1], ds[1])
+    else:
+        x, y = spatial_vectors(ns, ds)
     xv = x[None, :]
     yv = y[:, None]
     out = np.vectorize(f, otypes=[np.complex128])(np.broadcast_to(xv, (len(y), len(x))),
@@ -379,6 +382,104 @@ def TeaReflector(u, f=None, ds=None, r=1.0, trainable=False, buffered=False):
     return TeaDOE(u, 2.0, f, ds=ds, r=r, trainable=trainable, buffered=buffered)
 
 
+class _FourierModulator(_Modulator):
+    """u -> IFFT2(w FFT2(u)), w = cis(phi) or m on the FFT-ordered frequency grid
+    (FourierWrapper(ft, Phase|Mask, ift), fourier/fourier_wrapper.jl:1-5).  A static
+    one is a propagator of the fused chains (the multiplier rides in the column pass);
+    a trainable one runs on its own and gets its gradient from fo_fourier_gradient."""
+
+    kind = "AS"  # unpadded pass layout: chains with ASProps
+
+    def _init_param(self, u, arr, dtype, trainable, buffered):
+        setattr(self, self.pname, torch.as_tensor(np.asarray(arr, dtype=dtype)).cuda().contiguous())
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+        self._plans = {}
+        self._alloc_buffers(u)
+        self.plan_for(u)
+
+    def plan_for(self, u: ScalarField):
+        key = (u.nx, u.ny, u.batch)
+        p = self._plans.get(key)
+        if p is None:
+            p = C.c_void_p()
+            flags = 1 | (_capi.FO_FOURIER_TRAINABLE if self.trainable else 0)
+            _capi.call("fo_fourier_create", C.byref(p), u.nx, u.ny, u.batch, flags)
+            self._plans[key] = p
+        return p
+
+    def layout(self, u: ScalarField):
+        h = self.plan_for(u)
+        fx, fy = C.c_int(), C.c_int()
+        _capi.call("fo_prop_info", h, C.byref(fx), C.byref(fy), None)
+        return (self.kind, u.nx, u.ny, u.batch, fx.value, fy.value)
+
+    def refresh(self, u: ScalarField):
+        """Rebuild the multiplier from the current parameter (stream-ordered)."""
+        _capi.call("fo_fourier_set", self.plan_for(u), self.mod_kind, _ptr(self.param), _stream())
+
+    def propagate_(self, u, direction=Forward):
+        self.refresh(u)
+        _capi.call("fo_propagate", self.plan_for(u), _ptr(u.electric), int(direction), _stream())
+        return u
+
+    def propagate_and_save_(self, u, saved, direction=Forward):
+        saved.copy_(u.electric)
+        return self.propagate_(u, direction)
+
+    def backpropagate_(self, dv, direction=Forward):
+        _capi.call("fo_propagate", self.plan_for(dv), _ptr(dv.electric), int(reverse(direction)), _stream())
+        return dv
+
+    def backpropagate_with_gradient_(self, dv, saved, grad, direction=Forward):
+        _capi.call("fo_fourier_gradient", self.plan_for(dv), self.mod_kind, _ptr(self.param), _ptr(saved),
+                   _ptr(dv.electric), _ptr(grad), int(direction), _stream())
+        self.backpropagate_(dv, direction)
+        return dv, {self.pname: grad}
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is None:
+            return
+        for h in getattr(self, "_plans", {}).values():
+            lib.fo_prop_destroy(h)
+
+
+class FourierPhase(_FourierModulator):
+    """Phase mask applied in the Fourier domain (fourier/fourier_phase.jl:29-65); ``f``
+    is a function of (fx, fy) or an (ny, nx) array on the FFT-ordered frequency grid."""
+
+    mod_kind = _capi.FO_MOD_PHASE
+    pname = "phi"
+
+    def __init__(self, u, f=None, ds=None, trainable=False, buffered=False):
+        ds = tuple(ds) if ds is not None else u.ds
+        if f is None:
+            arr = np.zeros((u.ny, u.nx))
+        elif callable(f):
+            arr = np.real(function_to_array(f, (u.nx, u.ny), ds, isfourier=True))
+        else:
+            arr = f.detach().cpu().numpy() if isinstance(f, torch.Tensor) else np.asarray(f)
+        self._init_param(u, arr, np.float32, trainable, buffered)
+
+
+class FourierMask(_FourierModulator):
+    """Complex mask applied in the Fourier domain (fourier/fourier_mask.jl)."""
+
+    mod_kind = _capi.FO_MOD_MASK
+    pname = "m"
+
+    def __init__(self, u, f=None, ds=None, trainable=False, buffered=False):
+        ds = tuple(ds) if ds is not None else u.ds
+        if f is None:
+            arr = np.ones((u.ny, u.nx), dtype=np.complex128)
+        elif callable(f):
+            arr = function_to_array(f, (u.nx, u.ny), ds, isfourier=True)
+        else:
+            arr = f.detach().cpu().numpy() if isinstance(f, torch.Tensor) else np.asarray(f)
+        self._init_param(u, arr, np.complex64, trainable, buffered)
+
+
 class Mask(_Modulator):
     """u -> u * m (conj(m) backward) (modulators/mask.jl:39-142)."""
 
@@ -534,7 +635,7 @@ def _is_mod(c):
 
 
 def _is_prop(c):
-    return isinstance(c, _Propagator)
+    return isinstance(c, _Propagator) or (isinstance(c, _FourierModulator) and not c.trainable)
 
 
 class _Chain:
@@ -633,6 +734,9 @@ class OpticalSystem:
                 u.electric.copy_(src.electric)
                 from_src = False
             if isinstance(seg, _Chain):
+                for p in seg.props:
+                    if isinstance(p, _FourierModulator):
+                        p.refresh(u)
                 mods = (fo_mod * len(seg.mods))()
                 saved = []
                 for k, m in enumerate(seg.mods):

@@ -100,6 +100,55 @@ __global__ void as_h_general_kernel(float2* H, int fx_n, int fy_n, double dx, do
   }
 }
 
+// Fourier-domain modulator multiplier: H = cis(phi) / N (phase) or m / N (mask);
+// the Backward direction applies conj(H) in the column pass.
+__global__ void fourier_h_kernel(float2* H, int kind, const void* param, long long n, float scale) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    float2 w;
+    if (kind == 1) {
+      float s, c;
+      sincosf(reinterpret_cast<const float*>(param)[q], &s, &c);
+      w = make_float2(c, s);
+    } else {
+      w = reinterpret_cast<const float2*>(param)[q];
+    }
+    H[q] = make_float2(w.x * scale, w.y * scale);
+  }
+}
+
+// Gradient of a Fourier-domain modulator from the spectra U = FFT2(input) and
+// A = FFT2(adjoint at the output), per frequency pixel over the batch in order:
+// phase: s sum_b Im(cis(-s phi) A_b conj(U_b)); mask: sum_b conj_s(A_b conj(U_b))
+// (the Phase and Mask gradients of phasemask.jl:115-150 and mask.jl:263-291 applied
+// to the spectra, as FourierWrapper runs them, fourier/fourier_wrapper.jl:1-5).
+__global__ void fourier_grad_kernel(int kind, const void* param, const float2* U, const float2* A, void* grad,
+                                    long long npix, int batch, float s) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (kind == 1) {
+      const float2 w = cis_f(-s * reinterpret_cast<const float*>(param)[p]);
+      float acc = 0.f;
+      for (int b = 0; b < batch; ++b) {
+        const long long q = (long long)b * npix + p;
+        const float2 du = cmul(A[q], w);
+        const float2 u = U[q];
+        acc += du.y * u.x - du.x * u.y;
+      }
+      reinterpret_cast<float*>(grad)[p] = s * acc;
+    } else {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int b = 0; b < batch; ++b) {
+        const long long q = (long long)b * npix + p;
+        float2 g = cmul(A[q], cconj(U[q]));
+        if (s < 0.f) g = cconj(g);
+        acc = cadd(acc, g);
+      }
+      reinterpret_cast<float2*>(grad)[p] = acc;
+    }
+  }
+}
+
 // Rayleigh-Sommerfeld impulse response on the circular (py x px) offset grid:
 // offsets 0..n-1 at the start and -(n-1)..-1 at the end of each axis, zero between.
 __global__ void rs_h_spatial_kernel(float2* h, int nx, int ny, int px, int py, double dx, double dy,
@@ -484,6 +533,17 @@ cudaError_t launch_as_h_general(float2* H, int fx_n, int fy_n, double dx, double
   const double lm = lambda / n0;
   as_h_general_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(
       H, fx_n, fy_n, dx, dy, lm, z, scale, mode, sin(theta_x) / lm, sin(theta_y) / lm, track, filter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fourier_h(float2* H, int kind, const void* param, long long n, double scale, cudaStream_t s) {
+  fourier_h_kernel<<<capped_grid(n), kThreads, 0, s>>>(H, kind, param, n, (float)scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fourier_grad(int kind, const void* param, const float2* U, const float2* A, void* grad,
+                                long long npix, int batch, float s, cudaStream_t st) {
+  fourier_grad_kernel<<<capped_grid(npix), kThreads, 0, st>>>(kind, param, U, A, grad, npix, batch, s);
   return cudaGetLastError();
 }
 

@@ -10,6 +10,9 @@ cudaError_t launch_as_h(float2* H, int fx_n, int fy_n, double dx, double dy, dou
 cudaError_t launch_as_h_general(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
                                 double z, double scale, int mode, double theta_x, double theta_y, int track,
                                 const double2* filter, cudaStream_t s);
+cudaError_t launch_fourier_h(float2* H, int kind, const void* param, long long n, double scale, cudaStream_t s);
+cudaError_t launch_fourier_grad(int kind, const void* param, const float2* U, const float2* A, void* grad,
+                                long long npix, int batch, float s, cudaStream_t st);
 cudaError_t launch_rs_h_spatial(float2* h, int nx, int ny, int px, int py, double dx, double dy,
                                 double lambda, double z, double scale, cudaStream_t s);
 

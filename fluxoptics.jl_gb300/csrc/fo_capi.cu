@@ -243,6 +243,8 @@ struct fo_prop_plan_s {
   int fx = 0, fy = 0;  // transform sizes
   double dx = 0, dy = 0, z = 0, n0 = 1;
   std::vector<double> lambdas;  // per field
+  float2* spec_a = nullptr;      // Fourier modulators: spectra of the gradient call
+  float2* spec_b = nullptr;
   int n_tables = 0;
   float2* H = nullptr;          // n_tables x fy x fx, scaled by 1/(fx*fy)
   int* h_index = nullptr;       // device, per field
@@ -270,6 +272,8 @@ void plan_free(fo_prop_plan p) {
   cudaFree(p->items);
   cudaFree(p->inv_lambda);
   cudaFree(p->scratch);
+  cudaFree(p->spec_a);
+  cudaFree(p->spec_b);
   delete p;
 }
 
@@ -681,8 +685,9 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   if (opt && opt->tilts)
     for (int i = 0; i < 2 * opt->n_tilts; ++i)
       if (!std::isfinite(opt->tilts[i])) return fail(FO_ERR_ARG, "tilt angles must be finite");
-  const int fx = kind == 0 ? nx : next_pow2(2 * nx - 1);
-  const int fy = kind == 0 ? ny : next_pow2(2 * ny - 1);
+  // kind 0 ASProp, 1 RSProp (padded), 2 Fourier-domain modulator (multiplier set later)
+  const int fx = kind == 1 ? next_pow2(2 * nx - 1) : nx;
+  const int fy = kind == 1 ? next_pow2(2 * ny - 1) : ny;
   if (!fft_size_supported(fx) || !fft_size_supported(fy))
     return fail(FO_ERR_SHAPE, "transform size " + std::to_string(fx) + " x " + std::to_string(fy) +
                                   " is not supported (powers of two from 16 to 4096)");
@@ -793,7 +798,8 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   }
   std::vector<double> ffx, ffy, fre, fim;
   std::vector<double2> fval;
-  for (int i = 0; i < p->n_tables && e == cudaSuccess; ++i) {
+  if (kind == 2) e = cudaMemset(p->H, 0, sizeof(float2) * table * p->n_tables);
+  for (int i = 0; i < p->n_tables && e == cudaSuccess && kind != 2; ++i) {
     float2* Hi = p->H + table * i;
     if (kind == 0) {
       const double lam = uniq[i][0];
@@ -947,6 +953,70 @@ FO_API int fo_asprop_create_ex(fo_prop_plan* plan, int nx, int ny, int batch, do
                                const double* lambdas, int n_lambdas, double z, double n0,
                                const fo_as_options* options, int flags) {
   return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0, flags, options);
+}
+
+FO_API int fo_fourier_create(fo_prop_plan* plan, int nx, int ny, int batch, int flags) {
+  const double one = 1.0;
+  int rc = make_plan(plan, 2, nx, ny, batch, 1.0, 1.0, &one, 1, 0.0, 1.0, flags & FO_FLAG_AUTOTUNE);
+  if (rc != FO_OK) return rc;
+  fo_prop_plan p = *plan;
+  if (flags & FO_FOURIER_TRAINABLE) {
+    const size_t n = (size_t)batch * nx * ny;
+    if ((rc = dalloc(&p->spec_a, n, "Fourier gradient spectra")) != FO_OK ||
+        (rc = dalloc(&p->spec_b, n, "Fourier gradient spectra")) != FO_OK) {
+      plan_free(p);
+      *plan = nullptr;
+      return rc;
+    }
+    p->ws_bytes += 2 * sizeof(float2) * n;
+  }
+  return FO_OK;
+}
+
+FO_API int fo_fourier_set(fo_prop_plan plan, int kind, const void* param, void* stream) {
+  if (!plan || !param) return fail(FO_ERR_ARG, "plan and param must not be NULL");
+  if (plan->kind != 2) return fail(FO_ERR_ARG, "not a Fourier-modulator plan");
+  if (kind != MOD_PHASE && kind != MOD_MASK) return fail(FO_ERR_ARG, "kind must be FO_MOD_PHASE or FO_MOD_MASK");
+  FO_LAUNCH(launch_fourier_h(plan->H, kind, param, (long long)plan->fx * plan->fy,
+                             1.0 / ((double)plan->fx * (double)plan->fy), S(stream)));
+  return FO_OK;
+}
+
+// Unnormalised 2-D FFT of every field of `src` into `dst` (row transforms, then
+// column transforms with the plain cp.async column kernel).
+static int fft2_into(const fo_prop_plan_s* p, const float2* src, float2* dst, cudaStream_t st) {
+  Mod none;
+  FO_TRY(row_pass(layout_of(p), src, dst, false, true, none, false, 1.f, p->inv_lambda, nullptr, p->tw_x, st));
+  ColPassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.buf = dst;
+  a.bstride = (long long)p->fx * p->ny;
+  a.ld = p->fx;
+  a.ncols = p->fx;
+  a.y_in = a.y_out = p->ny;
+  a.fft_only = 1;
+  a.batch = p->batch;
+  a.n_items = p->batch;
+  int trc = FO_OK;
+  const float2* tw = twiddles(p->fy, col_variant(p->fy, 0).E, &trc);
+  if (!tw) return trc;
+  FO_LAUNCH(launch_col_pass(p->fy, 0, false, a, tw, st));
+  return FO_OK;
+}
+
+FO_API int fo_fourier_gradient(fo_prop_plan plan, int kind, const void* param, const void* u_saved, const void* dv,
+                               void* grad, int direction, void* stream) {
+  if (!plan || !param || !u_saved || !dv || !grad)
+    return fail(FO_ERR_ARG, "plan, param, u_saved, dv and grad must not be NULL");
+  if (plan->kind != 2 || !plan->spec_a) return fail(FO_ERR_ARG, "needs a Fourier plan created with FO_FOURIER_TRAINABLE");
+  if (kind != MOD_PHASE && kind != MOD_MASK) return fail(FO_ERR_ARG, "kind must be FO_MOD_PHASE or FO_MOD_MASK");
+  FO_TRY(check_dir(direction));
+  cudaStream_t st = S(stream);
+  FO_TRY(fft2_into(plan, reinterpret_cast<const float2*>(u_saved), plan->spec_a, st));
+  FO_TRY(fft2_into(plan, reinterpret_cast<const float2*>(dv), plan->spec_b, st));
+  FO_LAUNCH(launch_fourier_grad(kind, param, plan->spec_a, plan->spec_b, grad, (long long)plan->fx * plan->fy,
+                                plan->batch, (float)direction, st));
+  return FO_OK;
 }
 
 FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,

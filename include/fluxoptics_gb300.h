@@ -50,6 +50,7 @@ extern "C" {
 
 /* Plan flags */
 #define FO_FLAG_AUTOTUNE 1 /* time every launch shape of the passes and keep the fastest */
+#define FO_FOURIER_TRAINABLE 2 /* fo_fourier_create: allocate the spectra of fo_fourier_gradient */
 
 /* Modulation kinds (fo_mod.kind) */
 #define FO_MOD_NONE 0
@@ -154,6 +155,27 @@ FO_API int fo_asprop_create_ex(fo_prop_plan* plan, int nx, int ny, int batch, do
  */
 FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, double dx, double dy,
                             const double* lambdas, int n_lambdas, double z, int flags);
+
+/*
+ * Fourier-domain modulators (FourierPhase / FourierMask): u <- IFFT2(w . FFT2(u)) with
+ * w = cis(phi) (kind FO_MOD_PHASE) or m (FO_MOD_MASK), the parameter given on the
+ * FFT-ordered frequency grid (fftfreq, function_to_array(f, ns, ds, true)); conj(w)
+ * for the Backward direction.  The plan is a propagator: fo_propagate and chains run
+ * it through the fused passes, so a Fourier filter between propagators costs no extra
+ * pass.  fo_fourier_set rebuilds w from the parameter on the stream (call it after the
+ * parameter changes; graph-capturable).  fo_fourier_gradient (plans created with
+ * FO_FOURIER_TRAINABLE) computes the parameter gradient from the modulator's input
+ * u_saved and the adjoint dv at its output, both in real space:
+ *   phase: dphi = s sum_b Im(cis(-s phi) A_b conj(U_b)),  mask: dm = sum_b conj_s(A_b conj(U_b)),
+ * U = FFT2(u_saved), A = FFT2(dv) (unnormalised), s = direction.
+ * Replaces: FourierPhase / FourierMask = FourierWrapper(ft, Phase|Mask, ift)
+ * (fourier/fourier_phase.jl:29-65, fourier/fourier_mask.jl, fourier/fourier_wrapper.jl:1-5,
+ * fourier/fourier_operator.jl:37-83).
+ */
+FO_API int fo_fourier_create(fo_prop_plan* plan, int nx, int ny, int batch, int flags);
+FO_API int fo_fourier_set(fo_prop_plan plan, int kind, const void* param, void* stream);
+FO_API int fo_fourier_gradient(fo_prop_plan plan, int kind, const void* param, const void* u_saved,
+                               const void* dv, void* grad, int direction, void* stream);
 
 FO_API int fo_prop_destroy(fo_prop_plan plan);
 

@@ -353,6 +353,42 @@ def tea_backward(dv, h, k, r, u_saved, direction=FORWARD):
     return du, g.sum(axis=0)
 
 
+def fourier_forward(u, w, direction=FORWARD):
+    """FourierPhase / FourierMask forward: IFFT2(w FFT2(u)), conj(w) for Backward
+    (fourier/fourier_wrapper.jl:1-5 with fourier_operator.jl:37-83); w = cis(phi) or m
+    on the FFT-ordered frequency grid."""
+    u = np.asarray(u, dtype=np.complex128)
+    ww = w if direction > 0 else np.conj(w)
+    return ifft2(fft2(u) * ww)
+
+
+def fourier_phase_backward(dv, phi, u_saved, direction=FORWARD):
+    """Adjoint of FourierPhase and its gradient: the Backward sequence is FFT (the
+    ift operator reversed), Phase's backpropagate_with_gradient! on the spectra, IFFT
+    (the ft operator reversed):  dU = cis(-s phi) FFT2(dv),
+    dphi = s sum_b Im(dU_b conj(FFT2(u_saved)_b)),  du = IFFT2(dU)."""
+    s = direction
+    dU = fft2(np.asarray(dv, dtype=np.complex128)) * np.exp(-1j * s * np.asarray(phi, dtype=np.float64))
+    U = fft2(np.asarray(u_saved, dtype=np.complex128))
+    g = s * np.imag(dU * np.conj(U))
+    return ifft2(dU), g.reshape(-1, *g.shape[-2:]).sum(axis=0)
+
+
+def fourier_mask_backward(dv, m, u_saved, direction=FORWARD):
+    """Adjoint of FourierMask and its gradient (Mask's rules, mask.jl:263-291, on the
+    spectra): A = FFT2(dv), dm = sum_b conj_s(A_b conj(FFT2(u_saved)_b)),
+    du = IFFT2(conj_s(m)... ) with the adjoint multiplier conj(m) (m for s < 0)."""
+    s = direction
+    A = fft2(np.asarray(dv, dtype=np.complex128))
+    U = fft2(np.asarray(u_saved, dtype=np.complex128))
+    g = A * np.conj(U)
+    if s < 0:
+        g = np.conj(g)
+    m = np.asarray(m, dtype=np.complex128)
+    madj = np.conj(m) if s > 0 else m
+    return ifft2(A * madj), g.reshape(-1, *g.shape[-2:]).sum(axis=0)
+
+
 def mask_forward(u, m, direction=FORWARD):
     """u * conj_direction(m) (mask.jl:241-248)."""
     m = np.asarray(m, dtype=np.complex128)

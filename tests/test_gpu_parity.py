@@ -289,6 +289,56 @@ def test_dot_product_power_coupling(fo, orc, selective):
 
 
 @pytest.mark.parametrize("d", [1, -1])
+def test_fourier_phase_and_mask(fo, orc, d):
+    """FourierPhase / FourierMask: a static Fourier filter fused into a chain as a
+    propagator (AS -> FourierPhase -> Mask -> AS, one fused segment), and trainable
+    FourierPhase / FourierMask with their spectral-domain gradients, against the
+    oracle (the reference's conventions, unnormalised spectra included)."""
+    rng = np.random.default_rng(23)
+    n, B = 128, 3
+    ds, lams = (1.0, 1.0), np.array([0.64, 0.8, 0.455])
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(11.0, x + 2 * b, y) for b in range(B)]) * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    fphi = lambda fx, fy: 40.0 * (fx ** 2 + fy ** 2) + 3.0 * fx
+    FX, FY = np.meshgrid(np.fft.fftfreq(n, ds[0]), np.fft.fftfreq(n, ds[1]))
+    phiF = fphi(FX, FY)
+    m1 = c64(0.5 + rng.uniform(0, 1, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+    target = f32(np.abs(orc.gaussian(9.0, x - 3, y)) ** 2)
+    u = fo.ScalarField(u0, ds, lams)
+
+    fp = fo.FourierPhase(u, fphi)
+    c1 = fo.Mask(u, m1, trainable=True)
+    system = fo.OpticalSystem(fo.ScalarSource(u), [fo.ASProp(u, 200.0), fp, c1, fo.ASProp(u, 150.0)], direction=d)
+    assert len(system.segments(u)) == 1  # the Fourier phase rides in a column pass
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    a1 = orc.asprop(u0, 1.0, 1.0, lams, 200.0, d)
+    a2 = orc.fourier_forward(a1, np.exp(1j * phiF), d)
+    a3 = orc.mask_forward(a2, m1, d)
+    out = orc.asprop(a3, 1.0, 1.0, lams, 150.0, d)
+    assert orc.rel_l2(npy(system()["out"].electric).reshape(B, n, n), out) < FIELD_TOL
+    dv = orc.asprop(orc.sid_backward(out, target), 1.0, 1.0, lams, 150.0, -d)
+    _, gm = orc.mask_backward(dv, m1, a2, d)
+    assert orc.rel_l2(npy(grads[c1]["m"]), gm) < GRAD_TOL
+
+    for cls, param in ((fo.FourierPhase, f32(phiF)), (fo.FourierMask, m1)):
+        comp = cls(u, param, trainable=True)
+        system = fo.OpticalSystem(fo.ScalarSource(u), [fo.ASProp(u, 200.0), comp, fo.ASProp(u, 150.0)], direction=d)
+        loss, grads = fo.withgradient(metric, system)
+        w = np.exp(1j * np.asarray(param, dtype=np.float64)) if cls is fo.FourierPhase else param
+        a2 = orc.fourier_forward(a1, w, d)
+        out = orc.asprop(a2, 1.0, 1.0, lams, 150.0, d)
+        c_ref, _ = orc.sid_value(out, target)
+        assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+        dv = orc.asprop(orc.sid_backward(out, target), 1.0, 1.0, lams, 150.0, -d)
+        if cls is fo.FourierPhase:
+            _, g = orc.fourier_phase_backward(dv, param, a1, d)
+        else:
+            _, g = orc.fourier_mask_backward(dv, param, a1, d)
+        assert orc.rel_l2(npy(grads[comp][comp.pname]), g) < GRAD_TOL
+
+
+@pytest.mark.parametrize("d", [1, -1])
 def test_tea_doe_standalone_and_fused(fo, orc, d):
     """TeaDOE with a dispersive dn(λ) and a complex r(λ) on a two-wavelength batch:
     the standalone kernels (forward, adjoint, height gradient) and the same element

@@ -382,3 +382,25 @@ def test_overlap_pullbacks_match_finite_differences(orc):
                 # the reference's pull-back is the conjugate Wirtinger form times dx dy
                 ref = (g[b, i, j].real if part == "re" else g[b, i, j].imag) * ds[0] * ds[1]
                 assert abs(fd - ref) < 1e-5 * max(1.0, abs(fd)), (sel, part, fd, ref)
+
+
+def test_fourier_phase_gradient_matches_finite_differences(orc):
+    """FourierPhase: the spectral-domain phase gradient of a real loss Re<w, out>
+    matches central differences; FourierMask with m = cis(phi) gives the same field."""
+    rng = np.random.default_rng(6)
+    u = rng.standard_normal((2, 8, 8)) + 1j * rng.standard_normal((2, 8, 8))
+    w = rng.standard_normal((2, 8, 8)) + 1j * rng.standard_normal((2, 8, 8))
+    phi = rng.uniform(0, 2 * np.pi, (8, 8))
+    out = orc.fourier_forward(u, np.exp(1j * phi))
+    assert np.allclose(out, orc.fourier_forward(u, np.exp(1j * phi), 1))
+    loss = lambda p: float(np.real(np.vdot(w, orc.fourier_forward(u, np.exp(1j * p)))))
+    _, g = orc.fourier_phase_backward(w, phi, u)
+    eps = 1e-6
+    for (i, j) in [(0, 0), (3, 5), (7, 2)]:
+        pp, pm = phi.copy(), phi.copy()
+        pp[i, j] += eps
+        pm[i, j] -= eps
+        fd = (loss(pp) - loss(pm)) / (2 * eps)
+        # the reference's spectra are unnormalised: its gradient is N times the
+        # derivative of the normalised-IFFT loss
+        assert abs(fd * u.shape[-1] * u.shape[-2] - g[i, j]) < 1e-6 * max(1.0, abs(g[i, j]))
