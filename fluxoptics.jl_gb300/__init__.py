@@ -9,7 +9,7 @@ fails loudly when the library cannot be loaded.
 from . import _capi
 from ._capi import FluxOpticsError
 from .build import build as build_library
-from .components import (AS_BPM, ASProp, Backward, FieldProbe, FourierMask, FourierPhase, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
+from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierPhase, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
                          RSProp,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate_, function_to_array, propagate, propagate_,
                          reverse, spatial_vectors)
@@ -22,7 +22,7 @@ from .ragged import RaggedBatch
 load_library = _capi.load
 
 __all__ = [
-    "ASProp", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierPhase",
+    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierPhase",
     "Forward", "Mask", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",

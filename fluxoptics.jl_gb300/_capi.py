@@ -12,6 +12,7 @@ FO_FORWARD = 1
 FO_BACKWARD = -1
 FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = 0, 1, 2, 3, 4
 FO_FOURIER_TRAINABLE = 2
+FO_FLAG_GRAD_SPECTRA = 2
 
 ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
                5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
@@ -65,6 +66,8 @@ SIGNATURES = {
     "fo_prop_destroy": (_i, [_vp]),
     "fo_prop_info": (_i, [_vp, _pi, _pi, C.POINTER(C.c_size_t)]),
     "fo_fourier_create": (_i, [C.POINTER(_vp), _i, _i, _i, _i]),
+    "fo_prop_set_z": (_i, [_vp, _vp, _vp]),
+    "fo_prop_z_gradient": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "fo_fourier_set": (_i, [_vp, _i, _vp, _vp]),
     "fo_fourier_gradient": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i, _vp]),
     "fo_asprop_create_ex": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d,

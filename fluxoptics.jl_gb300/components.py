@@ -382,6 +382,68 @@ def TeaReflector(u, f=None, ds=None, r=1.0, trainable=False, buffered=False):
     return TeaDOE(u, 2.0, f, ds=ds, r=r, trainable=trainable, buffered=buffered)
 
 
+class ASPropZ(_Modulator):
+    """Angular-spectrum propagation with a trainable distance z
+    (angular_spectrum.jl:236-344).  z lives in device memory; every forward rebuilds
+    the transfer functions from it in FP64, and the adjoint sweep gets dL/dz from
+    fo_prop_z_gradient.  On-axis, non-paraxial, unfiltered fields only."""
+
+    pname = "z"
+
+    def __init__(self, u, z, ds=None, n0=1.0, trainable=False, track_tilts=False, paraxial=False,
+                 filter=None, double_precision_kernel=False):
+        if paraxial or track_tilts or filter is not None or not u.is_on_axis():
+            raise NotImplementedError("ASPropZ on the GB300 path is on-axis, non-paraxial and unfiltered")
+        self.ds = tuple(float(d) for d in (ds if ds is not None else u.ds))
+        self.n0 = float(n0)
+        self.z = torch.tensor([float(z)], dtype=torch.float32, device="cuda")
+        self.trainable = bool(trainable)
+        self.buffered = False
+        self.grad_buffer = None
+        self.saved_buffer = None
+        self._plans = {}
+        self.plan_for(u)
+
+    def plan_for(self, u: ScalarField):
+        lam = tuple(float(v) for v in u.lambdas_per_field())
+        key = (u.nx, u.ny, u.batch, lam)
+        p = self._plans.get(key)
+        if p is None:
+            p = C.c_void_p()
+            flags = 1 | (_capi.FO_FLAG_GRAD_SPECTRA if self.trainable else 0)
+            _capi.call("fo_asprop_create", C.byref(p), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                       _capi.dvec(lam), len(lam), float(self.z.item()), self.n0, flags)
+            self._plans[key] = p
+        return p
+
+    def propagate_(self, u, direction=Forward):
+        h = self.plan_for(u)
+        _capi.call("fo_prop_set_z", h, _ptr(self.z), _stream())
+        _capi.call("fo_propagate", h, _ptr(u.electric), int(direction), _stream())
+        return u
+
+    def propagate_and_save_(self, u, saved, direction=Forward):
+        saved.copy_(u.electric)
+        return self.propagate_(u, direction)
+
+    def backpropagate_(self, dv, direction=Forward):
+        _capi.call("fo_propagate", self.plan_for(dv), _ptr(dv.electric), int(reverse(direction)), _stream())
+        return dv
+
+    def backpropagate_with_gradient_(self, dv, saved, grad, direction=Forward):
+        _capi.call("fo_prop_z_gradient", self.plan_for(dv), _ptr(self.z), _ptr(saved), _ptr(dv.electric),
+                   int(direction), _ptr(grad), _stream())
+        self.backpropagate_(dv, direction)
+        return dv, {"z": grad}
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is None:
+            return
+        for h in getattr(self, "_plans", {}).values():
+            lib.fo_prop_destroy(h)
+
+
 class _FourierModulator(_Modulator):
     """u -> IFFT2(w FFT2(u)), w = cis(phi) or m on the FFT-ordered frequency grid
     (FourierWrapper(ft, Phase|Mask, ift), fourier/fourier_wrapper.jl:1-5).  A static
@@ -813,7 +875,7 @@ class OpticalSystem:
                     g = c.get_gradient_buffer()
                     _, gd = c.backpropagate_with_gradient_(du, saved, g, d)
                     grads[c] = gd
-                elif _is_prop(c) or _is_mod(c):
+                elif _is_prop(c) or _is_mod(c) or isinstance(c, (ASPropZ, _FourierModulator)):
                     c.backpropagate_(du, d)
                 elif isinstance(c, AS_BPM):
                     c.backpropagate_with_gradient_(du, None, None, d)

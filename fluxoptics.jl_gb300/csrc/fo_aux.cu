@@ -100,6 +100,80 @@ __global__ void as_h_general_kernel(float2* H, int fx_n, int fy_n, double dx, do
   }
 }
 
+// On-axis transfer function with the distance read from device memory (ASPropZ,
+// trainable z): as as_h_kernel, in FP64 from the float z.
+__global__ void as_h_z_kernel(float2* H, int fx_n, int fy_n, double dx, double dy, double f2, const float* zp,
+                              double scale) {
+  const double z = (double)*zp;
+  const long long n = (long long)fx_n * fy_n;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(q % fx_n), ky = (int)(q / fx_n);
+    const double fx = fftfreq_d(kx, fx_n, dx), fy = fftfreq_d(ky, fy_n, dy);
+    const double arg = f2 - fx * fx - fy * fy;
+    const double za = fabs(z);
+    double re, im;
+    if (arg >= 0.0) {
+      sincos(2.0 * M_PI * za * sqrt(arg), &im, &re);
+    } else {
+      re = exp(-2.0 * M_PI * za * sqrt(-arg));
+      im = 0.0;
+    }
+    if (z < 0.0) im = -im;
+    H[q] = make_float2((float)(re * scale), (float)(im * scale));
+  }
+}
+
+// d loss / d z of ASPropZ: per block, sum over its frequency pixels k and the fields
+// b of Re(U_b[k] conj(G_b[k]) dH_b[k]) with dH = 2 pi i kz H (z > 0) or 2 pi i conj(kz) H
+// (z < 0), conjugated for the Backward direction; U = FFT2(input), G = FFT2(adjoint
+// at the output), H the stored table (which carries the 1/N of the inverse transform).
+__global__ void as_z_grad_partial_kernel(const float2* U, const float2* G, const float2* H, const int* h_index,
+                                         const float* lam_eff, int fx_n, int fy_n, double dx, double dy,
+                                         const float* zp, int batch, int backward, double* partials) {
+  __shared__ double red[kThreads / 32];
+  const long long npix = (long long)fx_n * fy_n;
+  const bool zneg = *zp < 0.f;
+  double acc = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < npix;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(q % fx_n), ky = (int)(q / fx_n);
+    const float fx = (float)fftfreq_d(kx, fx_n, dx), fy = (float)fftfreq_d(ky, fy_n, dy);
+    float t = 0.f;
+    for (int b = 0; b < batch; ++b) {
+      const float li = lam_eff[b];  // n0 / lambda
+      const float arg = li * li - fx * fx - fy * fy;
+      // kz = sqrt(complex(arg)); conj(kz) for z < 0
+      float2 kz = arg >= 0.f ? make_float2(sqrtf(arg), 0.f) : make_float2(0.f, sqrtf(-arg));
+      if (zneg) kz.y = -kz.y;
+      float2 h = H[(long long)h_index[b] * npix + q];
+      // dH = 2 pi i kz H
+      float2 dh = cmul(make_float2(-6.283185307179586f * kz.y, 6.283185307179586f * kz.x), h);
+      if (backward) dh = cconj(dh);
+      const long long o = (long long)b * npix + q;
+      const float2 ug = cmul(U[o], cconj(G[o]));
+      t += ug.x * dh.x - ug.y * dh.y;  // Re(U conj(G) dH)
+    }
+    acc += (double)t;
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) s += red[w];
+    partials[blockIdx.x] = s;
+  }
+}
+
+__global__ void as_z_grad_final_kernel(const double* partials, int nblk, float* dz) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += partials[b];
+    *dz = (float)s;
+  }
+}
+
 // Fourier-domain modulator multiplier: H = cis(phi) / N (phase) or m / N (mask);
 // the Backward direction applies conj(H) in the column pass.
 __global__ void fourier_h_kernel(float2* H, int kind, const void* param, long long n, float scale) {
@@ -533,6 +607,27 @@ cudaError_t launch_as_h_general(float2* H, int fx_n, int fy_n, double dx, double
   const double lm = lambda / n0;
   as_h_general_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(
       H, fx_n, fy_n, dx, dy, lm, z, scale, mode, sin(theta_x) / lm, sin(theta_y) / lm, track, filter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_as_h_z(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
+                          const float* z, double scale, cudaStream_t s) {
+  const double lm = lambda / n0;
+  as_h_z_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(H, fx_n, fy_n, dx, dy, 1.0 / (lm * lm), z,
+                                                                        scale);
+  return cudaGetLastError();
+}
+
+int as_z_grad_blocks() { return 304; }
+
+cudaError_t launch_as_z_grad(const float2* U, const float2* G, const float2* H, const int* h_index,
+                             const float* lam_eff, int fx_n, int fy_n, double dx, double dy, const float* z, int batch,
+                             int backward, double* partials, float* dz, cudaStream_t st) {
+  as_z_grad_partial_kernel<<<as_z_grad_blocks(), kThreads, 0, st>>>(U, G, H, h_index, lam_eff, fx_n, fy_n, dx, dy, z,
+                                                                   batch, backward, partials);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  as_z_grad_final_kernel<<<1, 32, 0, st>>>(partials, as_z_grad_blocks(), dz);
   return cudaGetLastError();
 }
 

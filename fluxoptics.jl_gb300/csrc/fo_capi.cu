@@ -243,8 +243,12 @@ struct fo_prop_plan_s {
   int fx = 0, fy = 0;  // transform sizes
   double dx = 0, dy = 0, z = 0, n0 = 1;
   std::vector<double> lambdas;  // per field
-  float2* spec_a = nullptr;      // Fourier modulators: spectra of the gradient call
+  float2* spec_a = nullptr;      // gradient calls (Fourier modulators, ASPropZ): spectra
   float2* spec_b = nullptr;
+  int h_mode = 0;                   // 0 on axis, 1 tilted, 2 paraxial
+  std::vector<double> table_lambda; // wavelength of each transfer-function table
+  double* zgrad_partials = nullptr; // ASPropZ gradient: block partial sums
+  float* lam_eff = nullptr;         // ASPropZ gradient: n0 / lambda per field
   int n_tables = 0;
   float2* H = nullptr;          // n_tables x fy x fx, scaled by 1/(fx*fy)
   int* h_index = nullptr;       // device, per field
@@ -274,6 +278,8 @@ void plan_free(fo_prop_plan p) {
   cudaFree(p->scratch);
   cudaFree(p->spec_a);
   cudaFree(p->spec_b);
+  cudaFree(p->zgrad_partials);
+  cudaFree(p->lam_eff);
   delete p;
 }
 
@@ -729,6 +735,8 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     }
   }
   p->n_tables = (int)uniq.size();
+  p->h_mode = h_mode;
+  for (const auto& k : uniq) p->table_lambda.push_back(k[0]);
   int rc = FO_OK;
   const size_t table = (size_t)fx * fy;
   if ((rc = dalloc(&p->H, table * p->n_tables, "transfer functions")) != FO_OK ||
@@ -856,6 +864,21 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
       }
     }
   }
+  if (e == cudaSuccess && kind == 0 && (flags & FO_FLAG_GRAD_SPECTRA)) {
+    const size_t nf = (size_t)batch * fx * fy;
+    if ((rc = dalloc(&p->spec_a, nf, "gradient spectra")) != FO_OK ||
+        (rc = dalloc(&p->spec_b, nf, "gradient spectra")) != FO_OK ||
+        (rc = dalloc(&p->zgrad_partials, (size_t)as_z_grad_blocks(), "z-gradient partials")) != FO_OK ||
+        (rc = dalloc(&p->lam_eff, batch, "n0 / lambda")) != FO_OK) {
+      if (d_filter) cudaFree(d_filter);
+      plan_free(p);
+      return rc;
+    }
+    p->ws_bytes += 2 * sizeof(float2) * nf;
+    std::vector<float> le(batch);
+    for (int b = 0; b < batch; ++b) le[b] = (float)(n0 / p->lambdas[b]);
+    e = cudaMemcpy(p->lam_eff, le.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (d_filter) cudaFree(d_filter);
   if (e != cudaSuccess) {
@@ -955,6 +978,53 @@ FO_API int fo_asprop_create_ex(fo_prop_plan* plan, int nx, int ny, int batch, do
   return make_plan(plan, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, z, n0, flags, options);
 }
 
+// Unnormalised 2-D FFT of every field of `src` into `dst` (row transforms, then
+// column transforms with the plain cp.async column kernel).
+static int fft2_into(const fo_prop_plan_s* p, const float2* src, float2* dst, cudaStream_t st) {
+  Mod none;
+  FO_TRY(row_pass(layout_of(p), src, dst, false, true, none, false, 1.f, p->inv_lambda, nullptr, p->tw_x, st));
+  ColPassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.buf = dst;
+  a.bstride = (long long)p->fx * p->ny;
+  a.ld = p->fx;
+  a.ncols = p->fx;
+  a.y_in = a.y_out = p->ny;
+  a.fft_only = 1;
+  a.batch = p->batch;
+  a.n_items = p->batch;
+  int trc = FO_OK;
+  const float2* tw = twiddles(p->fy, col_variant(p->fy, 0).E, &trc);
+  if (!tw) return trc;
+  FO_LAUNCH(launch_col_pass(p->fy, 0, false, a, tw, st));
+  return FO_OK;
+}
+
+FO_API int fo_prop_set_z(fo_prop_plan plan, const float* z, void* stream) {
+  if (!plan || !z) return fail(FO_ERR_ARG, "plan and z must not be NULL");
+  if (plan->kind != 0 || plan->h_mode != 0) return fail(FO_ERR_ARG, "fo_prop_set_z needs an on-axis ASProp plan");
+  const double scale = 1.0 / ((double)plan->fx * (double)plan->fy);
+  const size_t table = (size_t)plan->fx * plan->fy;
+  for (int i = 0; i < plan->n_tables; ++i)
+    FO_LAUNCH(launch_as_h_z(plan->H + table * i, plan->fx, plan->fy, plan->dx, plan->dy, plan->table_lambda[i],
+                            plan->n0, z, scale, S(stream)));
+  return FO_OK;
+}
+
+FO_API int fo_prop_z_gradient(fo_prop_plan plan, const float* z, const void* u_saved, const void* du, int direction,
+                              float* dz, void* stream) {
+  if (!plan || !z || !u_saved || !du || !dz) return fail(FO_ERR_ARG, "plan, z, u_saved, du and dz must not be NULL");
+  if (plan->kind != 0 || plan->h_mode != 0 || !plan->spec_a)
+    return fail(FO_ERR_ARG, "needs an on-axis ASProp plan created with FO_FLAG_GRAD_SPECTRA");
+  FO_TRY(check_dir(direction));
+  cudaStream_t st = S(stream);
+  FO_TRY(fft2_into(plan, reinterpret_cast<const float2*>(u_saved), plan->spec_a, st));
+  FO_TRY(fft2_into(plan, reinterpret_cast<const float2*>(du), plan->spec_b, st));
+  FO_LAUNCH(launch_as_z_grad(plan->spec_a, plan->spec_b, plan->H, plan->h_index, plan->lam_eff, plan->fx, plan->fy,
+                             plan->dx, plan->dy, z, plan->batch, direction < 0, plan->zgrad_partials, dz, st));
+  return FO_OK;
+}
+
 FO_API int fo_fourier_create(fo_prop_plan* plan, int nx, int ny, int batch, int flags) {
   const double one = 1.0;
   int rc = make_plan(plan, 2, nx, ny, batch, 1.0, 1.0, &one, 1, 0.0, 1.0, flags & FO_FLAG_AUTOTUNE);
@@ -979,28 +1049,6 @@ FO_API int fo_fourier_set(fo_prop_plan plan, int kind, const void* param, void* 
   if (kind != MOD_PHASE && kind != MOD_MASK) return fail(FO_ERR_ARG, "kind must be FO_MOD_PHASE or FO_MOD_MASK");
   FO_LAUNCH(launch_fourier_h(plan->H, kind, param, (long long)plan->fx * plan->fy,
                              1.0 / ((double)plan->fx * (double)plan->fy), S(stream)));
-  return FO_OK;
-}
-
-// Unnormalised 2-D FFT of every field of `src` into `dst` (row transforms, then
-// column transforms with the plain cp.async column kernel).
-static int fft2_into(const fo_prop_plan_s* p, const float2* src, float2* dst, cudaStream_t st) {
-  Mod none;
-  FO_TRY(row_pass(layout_of(p), src, dst, false, true, none, false, 1.f, p->inv_lambda, nullptr, p->tw_x, st));
-  ColPassArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.buf = dst;
-  a.bstride = (long long)p->fx * p->ny;
-  a.ld = p->fx;
-  a.ncols = p->fx;
-  a.y_in = a.y_out = p->ny;
-  a.fft_only = 1;
-  a.batch = p->batch;
-  a.n_items = p->batch;
-  int trc = FO_OK;
-  const float2* tw = twiddles(p->fy, col_variant(p->fy, 0).E, &trc);
-  if (!tw) return trc;
-  FO_LAUNCH(launch_col_pass(p->fy, 0, false, a, tw, st));
   return FO_OK;
 }
 

@@ -51,6 +51,7 @@ extern "C" {
 /* Plan flags */
 #define FO_FLAG_AUTOTUNE 1 /* time every launch shape of the passes and keep the fastest */
 #define FO_FOURIER_TRAINABLE 2 /* fo_fourier_create: allocate the spectra of fo_fourier_gradient */
+#define FO_FLAG_GRAD_SPECTRA 2 /* fo_asprop_create(_ex): allocate the spectra of fo_prop_z_gradient */
 
 /* Modulation kinds (fo_mod.kind) */
 #define FO_MOD_NONE 0
@@ -172,6 +173,21 @@ FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, doubl
  * (fourier/fourier_phase.jl:29-65, fourier/fourier_mask.jl, fourier/fourier_wrapper.jl:1-5,
  * fourier/fourier_operator.jl:37-83).
  */
+/*
+ * ASPropZ (trainable distance) on an on-axis ASProp plan: fo_prop_set_z rebuilds the
+ * transfer functions in FP64 from the distance held in device memory (float z, read
+ * on the stream, so an iteration that updates z can be captured as one graph).
+ * fo_prop_z_gradient (plan created with FO_FLAG_GRAD_SPECTRA) writes to *dz the
+ * derivative of the loss with respect to z, from the propagator's input u_saved and
+ * the adjoint du at its output: Re sum_b sum_k U conj(G) dH/dz / N with U = FFT2(u_saved),
+ * G = FFT2(du), dH/dz = 2 pi i kz H (kz = sqrt(complex(n0^2/lambda^2 - f^2)); conj(kz) for
+ * z < 0), conjugated for the Backward direction -- what Zygote computes through the
+ * reference's propagate(u, ::ASPropZ) (angular_spectrum.jl:274-344).
+ */
+FO_API int fo_prop_set_z(fo_prop_plan plan, const float* z, void* stream);
+FO_API int fo_prop_z_gradient(fo_prop_plan plan, const float* z, const void* u_saved, const void* du,
+                              int direction, float* dz, void* stream);
+
 FO_API int fo_fourier_create(fo_prop_plan* plan, int nx, int ny, int batch, int flags);
 FO_API int fo_fourier_set(fo_prop_plan plan, int kind, const void* param, void* stream);
 FO_API int fo_fourier_gradient(fo_prop_plan plan, int kind, const void* param, const void* u_saved,

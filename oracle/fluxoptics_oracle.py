@@ -280,6 +280,32 @@ def asprop(u, dx, dy, lambdas, z, direction=FORWARD, n0=1.0, paraxial=False, til
     return out.reshape(shp)
 
 
+def asprop_z_gradient(u_in, du, dx, dy, lambdas, z, direction=FORWARD, n0=1.0):
+    """d loss / d z of ASPropZ as Zygote computes it through
+    ifft(fft(u) .* conj_direction(kernel)) (angular_spectrum.jl:325-344): with
+    U = FFT2(u_in), G = FFT2(du) (du the adjoint at the output) and
+    dH/dz = 2 pi i kz H (kz = sqrt(complex(n0^2/lambda^2 - f^2)), conj(kz) for z < 0),
+    dz = Re sum_b sum_k U conj(G) conj_direction(dH/dz) / (nx ny)."""
+    u = np.asarray(u_in, dtype=np.complex128)
+    g = np.asarray(du, dtype=np.complex128)
+    ny, nx = u.shape[-2:]
+    u = u.reshape(-1, ny, nx)
+    g = g.reshape(-1, ny, nx)
+    lam = _lams(lambdas, u.shape[0])
+    fx, fy = fftfreqs(nx, ny, dx, dy)
+    tot = 0.0
+    for b in range(u.shape[0]):
+        lm = lam[b] / n0
+        kz = np.sqrt((1.0 / lm ** 2 - fx[None, :] ** 2 - fy[:, None] ** 2).astype(np.complex128))
+        if z < 0:
+            kz = np.conj(kz)
+        dh = 2j * np.pi * kz * as_kernel(nx, ny, dx, dy, lam[b], z, n0)
+        if direction != FORWARD:
+            dh = np.conj(dh)
+        tot += float(np.real(np.sum(fft2(u[b]) * np.conj(fft2(g[b])) * dh))) / (nx * ny)
+    return tot
+
+
 def rsprop(u, dx, dy, lambdas, z, direction=FORWARD, pad=None):
     """RSProp: pad to (2n-1) (or ``pad``) at offset 0, FFT, * H_RS (conj for
     Backward), IFFT, crop the top-left n x n (rayleigh_sommerfeld.jl:128-169,

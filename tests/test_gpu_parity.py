@@ -289,6 +289,43 @@ def test_dot_product_power_coupling(fo, orc, selective):
 
 
 @pytest.mark.parametrize("d", [1, -1])
+def test_asprop_z_trainable_distance(fo, orc, d):
+    """ASPropZ with a trainable distance in Phase -> ASPropZ -> Mask -> ASProp -> SID:
+    the propagated field, dL/dz and the mask gradients against the oracle."""
+    rng = np.random.default_rng(29)
+    n, B = 256, 3
+    ds, lams = (0.5, 0.5), np.array([0.64, 0.538, 0.455])
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(10.0, x, y + b) for b in range(B)]) * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    phi = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    m1 = c64(0.5 + rng.uniform(0, 1, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+    target = f32(np.abs(orc.gaussian(8.0, x - 2, y)) ** 2)
+    z0 = 250.0
+    u = fo.ScalarField(u0, ds, lams)
+    ph = fo.Phase(u, phi, trainable=True)
+    pz = fo.ASPropZ(u, z0, trainable=True)
+    mk = fo.Mask(u, m1, trainable=True)
+    system = fo.OpticalSystem(fo.ScalarSource(u), [ph, pz, mk, fo.ASProp(u, 120.0)], direction=d)
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    a0 = orc.phase_forward(u0, phi, d)
+    a1 = orc.asprop(a0, ds[0], ds[1], lams, z0, d)
+    a2 = orc.mask_forward(a1, m1, d)
+    out = orc.asprop(a2, ds[0], ds[1], lams, 120.0, d)
+    assert orc.rel_l2(npy(system()["out"].electric).reshape(B, n, n), out) < FIELD_TOL
+    c_ref, _ = orc.sid_value(out, target)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    dv = orc.asprop(orc.sid_backward(out, target), ds[0], ds[1], lams, 120.0, -d)
+    dv, gm = orc.mask_backward(dv, m1, a1, d)
+    gz = orc.asprop_z_gradient(a0, dv, ds[0], ds[1], lams, z0, d)
+    dv = orc.asprop(dv, ds[0], ds[1], lams, z0, -d)
+    _, gphi = orc.phase_backward(dv, phi, u0, d)
+    assert orc.rel_l2(npy(grads[mk]["m"]), gm) < GRAD_TOL
+    assert abs(float(grads[pz]["z"].item()) - gz) < GRAD_TOL * abs(gz) + 1e-12, (float(grads[pz]["z"].item()), gz)
+    assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+
+@pytest.mark.parametrize("d", [1, -1])
 def test_fourier_phase_and_mask(fo, orc, d):
     """FourierPhase / FourierMask: a static Fourier filter fused into a chain as a
     propagator (AS -> FourierPhase -> Mask -> AS, one fused segment), and trainable

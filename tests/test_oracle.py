@@ -404,3 +404,19 @@ def test_fourier_phase_gradient_matches_finite_differences(orc):
         # the reference's spectra are unnormalised: its gradient is N times the
         # derivative of the normalised-IFFT loss
         assert abs(fd * u.shape[-1] * u.shape[-2] - g[i, j]) < 1e-6 * max(1.0, abs(g[i, j]))
+
+
+def test_asprop_z_gradient_matches_finite_differences(orc):
+    """dL/dz of ASPropZ for L = Re<w, asprop(u, z)> against central differences in z,
+    both directions and both signs of z (evanescent components included)."""
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((2, 16, 16)) + 1j * rng.standard_normal((2, 16, 16))
+    w = rng.standard_normal((2, 16, 16)) + 1j * rng.standard_normal((2, 16, 16))
+    lams = np.array([0.9, 1.3])
+    for z in (37.0, -22.0):
+        for d in (orc.FORWARD, orc.BACKWARD):
+            loss = lambda zz: float(np.real(np.vdot(w, orc.asprop(u, 0.5, 0.5, lams, zz, d))))
+            eps = 1e-5
+            fd = (loss(z + eps) - loss(z - eps)) / (2 * eps)
+            g = orc.asprop_z_gradient(u, w, 0.5, 0.5, lams, z, d)
+            assert abs(fd - g) < 1e-6 * max(1.0, abs(fd)), (z, d, fd, g)
