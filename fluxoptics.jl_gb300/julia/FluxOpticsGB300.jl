@@ -53,11 +53,15 @@ dims_of(u::ScalarField) = (size(u.electric, 1), size(u.electric, 2), div(length(
 dirsign(::Type{Forward}) = Cint(1)
 dirsign(::Type{Backward}) = Cint(-1)
 
-# one wavelength per field, in the column-major order of the trailing dims
-function lambdas_per_field(u::ScalarField)
-    lam = Array(FluxOptics.get_lambdas(u))
-    nx, ny, b = dims_of(u)
-    Float64.(vec(broadcast((l, _) -> l, lam, zeros(size(u.electric)[3:end]...))))
+# one value per field, in the column-major order of the trailing dims: `val` is the
+# reference's broadcastable (1, 1, d3, ...) array (Fields.jl:18-38)
+per_field(u::ScalarField, val) =
+    Float64.(vec(broadcast((l, _) -> l, Array(val), zeros(1, 1, size(u.electric)[3:end]...))))
+lambdas_per_field(u::ScalarField) = per_field(u, FluxOptics.get_lambdas(u))
+# (theta_x, theta_y) pairs per field, flattened as the C ABI takes them
+function tilts_per_field(u::ScalarField)
+    tx, ty = FluxOptics.get_tilts(u)
+    vec(permutedims(hcat(per_field(u, tx), per_field(u, ty))))
 end
 
 # ---------------------------------------------------------------------------
@@ -74,14 +78,35 @@ function _finalize(p::GB300Prop)
     p.plan = C_NULL
 end
 
-"""GB300ASProp(u, z; n0=1) -- angular-spectrum propagation on the GPU path."""
-function GB300ASProp(u::ScalarField, z::Real; n0::Real = 1)
+struct FoASOptions          # mirrors `fo_as_options` (no filter callback from Julia here)
+    paraxial::Cint
+    track_tilts::Cint
+    tilts::Ptr{Cdouble}
+    n_tilts::Cint
+    filter::Ptr{Cvoid}
+    filter_ctx::Ptr{Cvoid}
+end
+
+"""GB300ASProp(u, z; n0=1, paraxial=false, track_tilts=false) -- angular-spectrum
+propagation on the GPU path; tilted fields (u.tilts) select the tilted kernel."""
+function GB300ASProp(u::ScalarField, z::Real; n0::Real = 1, paraxial::Bool = false, track_tilts::Bool = false)
     nx, ny, b = dims_of(u)
     lam = lambdas_per_field(u)
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:fo_asprop_create, LIB), Cint,
-                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
-                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0, FO_FLAG_AUTOTUNE))
+    if !paraxial && !track_tilts && FluxOptics.is_on_axis(u)
+        check(ccall((:fo_asprop_create, LIB), Cint,
+                    (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
+                    h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0, FO_FLAG_AUTOTUNE))
+    else
+        th = tilts_per_field(u)
+        GC.@preserve th begin
+            opt = Ref(FoASOptions(Cint(paraxial), Cint(track_tilts), pointer(th), Cint(b), C_NULL, C_NULL))
+            check(ccall((:fo_asprop_create_ex, LIB), Cint,
+                        (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble,
+                         Ref{FoASOptions}, Cint),
+                        h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0, opt, FO_FLAG_AUTOTUNE))
+        end
+    end
     finalizer(_finalize, GB300Prop(h[], :AS, Float64(z)))
 end
 
@@ -295,6 +320,204 @@ end
 # the propagation distance is kept by the wrapped kernel component
 _convert_prop(c::ASProp, u) = GB300ASProp(u, c.optical_components[2].z; n0 = c.optical_components[2].n0)
 _convert_prop(c::RSProp, u) = GB300RSProp(u, c.optical_components[3].z)
+
+# ---------------------------------------------------------------------------
+# TeaDOE / TeaReflector: per-field {2 pi dn(lambda)/lambda, Re r, Im r, 0}
+# ---------------------------------------------------------------------------
+struct GB300TeaDOE{M, A, C, U} <: AbstractCustomComponent{M}
+    h::A
+    coef::C                   # CuArray{Float32} of 4 x batch
+    ∂p::Union{Nothing, @NamedTuple{h::A}}
+    u::Union{Nothing, U}
+end
+
+function GB300TeaDOE(p::TeaDOE, u::ScalarField)   # adopt a reference TeaDOE for fields like u
+    M = FluxOptics.OpticalComponents.get_trainability(p)
+    lam = lambdas_per_field(u)
+    c = zeros(Float32, 4, length(lam))
+    for (k, l) in enumerate(lam)
+        r = ComplexF64(p.r(l))
+        c[:, k] .= (2π * p.dn(l) / l, real(r), imag(r), 0)
+    end
+    cd = CuArray(c)
+    GB300TeaDOE{M, typeof(p.h), typeof(cd), typeof(p.u)}(p.h, cd, p.∂p, p.u)
+end
+
+Functors.@functor GB300TeaDOE (h,)
+get_data(p::GB300TeaDOE) = p.h
+trainable(p::GB300TeaDOE{<:Trainable}) = (; h = p.h)
+get_preallocated_gradient(p::GB300TeaDOE{Trainable{Buffered}}) = p.∂p
+get_saved_buffer(p::GB300TeaDOE{Trainable{Buffered}}) = p.u
+alloc_saved_buffer(u::ScalarField, p::GB300TeaDOE{Trainable{Unbuffered}}) = similar(u.electric)
+
+function _tea_fwd!(u::ScalarField, p::GB300TeaDOE, saved, dir)
+    nx, ny, b = dims_of(u)
+    check(ccall((:fo_tea_forward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(u.electric), dptr(p.h), dptr(p.coef), dptr(saved), nx, ny, b, dirsign(dir), cstream()))
+    u
+end
+
+propagate!(u::ScalarField, p::GB300TeaDOE, dir::Type{<:Direction}) = _tea_fwd!(u, p, nothing, dir)
+propagate_and_save!(u::ScalarField, p::GB300TeaDOE{Trainable{Buffered}}, dir::Type{<:Direction}) =
+    _tea_fwd!(u, p, p.u, dir)
+propagate_and_save!(u::ScalarField, u_saved::AbstractArray, p::GB300TeaDOE{Trainable{Unbuffered}},
+                    dir::Type{<:Direction}) = _tea_fwd!(u, p, u_saved, dir)
+
+function backpropagate!(∂v::ScalarField, p::GB300TeaDOE, dir::Type{<:Direction})
+    nx, ny, b = dims_of(∂v)
+    check(ccall((:fo_tea_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(∂v.electric), dptr(p.h), dptr(p.coef), C_NULL, C_NULL, nx, ny, b, dirsign(dir), cstream()))
+    ∂v
+end
+
+function backpropagate_with_gradient!(∂v::ScalarField, u_saved::AbstractArray, ∂p::NamedTuple,
+                                      p::GB300TeaDOE{<:Trainable}, dir::Type{<:Direction})
+    nx, ny, b = dims_of(∂v)
+    check(ccall((:fo_tea_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Cint, Cint, Ptr{Cvoid}),
+                dptr(∂v.electric), dptr(p.h), dptr(p.coef), dptr(u_saved), dptr(∂p.h), nx, ny, b, dirsign(dir),
+                cstream()))
+    (∂v, ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# FourierPhase / FourierMask: a propagator plan with the Fourier-domain multiplier
+# ---------------------------------------------------------------------------
+mutable struct GB300Fourier{M, A} <: AbstractCustomComponent{M}
+    plan::Ptr{Cvoid}
+    kind::Cint                # FO_MOD_PHASE or FO_MOD_MASK
+    p::A                      # ϕ or m on the FFT-ordered frequency grid
+    ∂p::Union{Nothing, NamedTuple}
+end
+
+function GB300Fourier(u::ScalarField, p::AbstractArray, kind::Cint; trainable::Bool = false)
+    nx, ny, b = dims_of(u)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_fourier_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cint),
+                h, nx, ny, b, FO_FLAG_AUTOTUNE | (trainable ? Cint(2) : Cint(0))))
+    M = trainable ? Trainable{Unbuffered} : Static
+    f = GB300Fourier{M, typeof(p)}(h[], kind, p, trainable ? NamedTuple{(:p,)}((similar(p),)) : nothing)
+    finalizer(x -> ccall((:fo_prop_destroy, LIB), Cint, (Ptr{Cvoid},), x.plan), f)
+end
+GB300FourierPhase(u::ScalarField, ϕ; trainable = false) = GB300Fourier(u, ϕ, FO_MOD_PHASE; trainable)
+GB300FourierMask(u::ScalarField, m; trainable = false) = GB300Fourier(u, m, FO_MOD_MASK; trainable)
+
+Functors.@functor GB300Fourier (p,)
+get_data(f::GB300Fourier) = f.p
+trainable(f::GB300Fourier{<:Trainable}) = (; p = f.p)
+alloc_saved_buffer(u::ScalarField, f::GB300Fourier{Trainable{Unbuffered}}) = similar(u.electric)
+
+function propagate!(u::ScalarField, f::GB300Fourier, dir::Type{<:Direction})
+    check(ccall((:fo_fourier_set, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
+                f.plan, f.kind, dptr(f.p), cstream()))
+    check(ccall((:fo_propagate, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                f.plan, dptr(u.electric), dirsign(dir), cstream()))
+    u
+end
+function propagate_and_save!(u::ScalarField, u_saved::AbstractArray, f::GB300Fourier{Trainable{Unbuffered}},
+                             dir::Type{<:Direction})
+    copyto!(u_saved, u.electric)
+    propagate!(u, f, dir)
+end
+function backpropagate!(∂v::ScalarField, f::GB300Fourier, dir::Type{<:Direction})
+    check(ccall((:fo_propagate, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                f.plan, dptr(∂v.electric), -dirsign(dir), cstream()))
+    ∂v
+end
+function backpropagate_with_gradient!(∂v::ScalarField, u_saved::AbstractArray, ∂p::NamedTuple,
+                                      f::GB300Fourier{<:Trainable}, dir::Type{<:Direction})
+    check(ccall((:fo_fourier_gradient, LIB), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                f.plan, f.kind, dptr(f.p), dptr(u_saved), dptr(∂v.electric), dptr(∂p.p), dirsign(dir), cstream()))
+    (backpropagate!(∂v, f, dir), ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# ASPropZ: trainable distance, z in device memory
+# ---------------------------------------------------------------------------
+mutable struct GB300ASPropZ{M, A} <: AbstractCustomComponent{M}
+    plan::Ptr{Cvoid}
+    z::A                      # CuArray{Float32}(1)
+end
+
+function GB300ASPropZ(u::ScalarField, z::Real; n0::Real = 1, trainable::Bool = false)
+    nx, ny, b = dims_of(u)
+    lam = lambdas_per_field(u)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_asprop_create, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
+                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0,
+                FO_FLAG_AUTOTUNE | (trainable ? Cint(2) : Cint(0))))
+    zd = CuArray(Float32[z])
+    M = trainable ? Trainable{Unbuffered} : Static
+    p = GB300ASPropZ{M, typeof(zd)}(h[], zd)
+    finalizer(x -> ccall((:fo_prop_destroy, LIB), Cint, (Ptr{Cvoid},), x.plan), p)
+end
+
+Functors.@functor GB300ASPropZ (z,)
+get_data(p::GB300ASPropZ) = p.z
+trainable(p::GB300ASPropZ{<:Trainable}) = (; z = p.z)
+alloc_saved_buffer(u::ScalarField, p::GB300ASPropZ{Trainable{Unbuffered}}) = similar(u.electric)
+
+function propagate!(u::ScalarField, p::GB300ASPropZ, dir::Type{<:Direction})
+    check(ccall((:fo_prop_set_z, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}), p.plan, dptr(p.z), cstream()))
+    check(ccall((:fo_propagate, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                p.plan, dptr(u.electric), dirsign(dir), cstream()))
+    u
+end
+function propagate_and_save!(u::ScalarField, u_saved::AbstractArray, p::GB300ASPropZ{Trainable{Unbuffered}},
+                             dir::Type{<:Direction})
+    copyto!(u_saved, u.electric)
+    propagate!(u, p, dir)
+end
+function backpropagate!(∂v::ScalarField, p::GB300ASPropZ, dir::Type{<:Direction})
+    check(ccall((:fo_propagate, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                p.plan, dptr(∂v.electric), -dirsign(dir), cstream()))
+    ∂v
+end
+function backpropagate_with_gradient!(∂v::ScalarField, u_saved::AbstractArray, ∂p::NamedTuple,
+                                      p::GB300ASPropZ{<:Trainable}, dir::Type{<:Direction})
+    check(ccall((:fo_prop_z_gradient, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
+                p.plan, dptr(p.z), dptr(u_saved), dptr(∂v.electric), dirsign(dir), dptr(∂p.z), cstream()))
+    (backpropagate!(∂v, p, dir), ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# DotProduct / PowerCoupling against reference fields v (same grid and batch)
+# ---------------------------------------------------------------------------
+mutable struct GB300Overlap
+    handle::Ptr{Cvoid}
+    out::Any                  # CuArray{ComplexF32} (DotProduct) or CuArray{Float32} (PowerCoupling)
+end
+
+function GB300Overlap(v::ScalarField; mode_selective::Bool = true, power::Bool = false)
+    nx, ny, b = dims_of(v)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_overlap_create, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cvoid}, Cint, Cint),
+                h, nx, ny, b, v.ds[1], v.ds[2], dptr(v.electric), Cint(mode_selective), Cint(power)))
+    n = mode_selective ? b : b * b
+    out = power ? CUDA.zeros(Float32, n) : CUDA.zeros(ComplexF32, n)
+    o = GB300Overlap(h[], out)
+    finalizer(x -> ccall((:fo_overlap_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), o)
+end
+GB300DotProduct(v::ScalarField; mode_selective = true) = GB300Overlap(v; mode_selective, power = false)
+GB300PowerCoupling(v::ScalarField; mode_selective = true) = GB300Overlap(v; mode_selective, power = true)
+
+# compute_metric / backpropagate_metric of dot_product.jl:70-100 and power_coupling.jl:59-66
+function (o::GB300Overlap)(u::ScalarField)
+    check(ccall((:fo_overlap_forward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                o.handle, dptr(u.electric), dptr(o.out), cstream()))
+    o.out
+end
+function pullback!(o::GB300Overlap, ∂c, ∂u::ScalarField)
+    check(ccall((:fo_overlap_backward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                o.handle, dptr(∂c), dptr(∂u.electric), cstream()))
+    ∂u
+end
 
 # ---------------------------------------------------------------------------
 # Ragged batch: independent Phase |> ASProp |> SquaredIntensityDifference problems
