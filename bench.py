@@ -619,7 +619,7 @@ def run_config5(args):
     build()
     fo = load_package()
     lib = fo.load_library()
-    probs = ragged_problems()
+    probs = ragged_problems(count=args.problems)
     rb = fo.RaggedBatch(ragged_specs(fo, probs))
     for _ in range(max(3, args.warmup)):
         rb.run()
@@ -637,7 +637,7 @@ def run_config5(args):
     pix = sum(p["n"] ** 2 for p in probs)
     info = rb.info()
     pass_ms = rb.pass_ms()
-    return {"config": "ragged batch: 64 ASProp problems, N in {256..4096}^2 (seeded), random lambda/z/waist/"
+    return {"config": f"ragged batch: {len(probs)} ASProp problems, N in {{256..4096}}^2 (seeded), random lambda/z/waist/"
                       "offset/phase mask, intensity loss, fwd + adjoint + phase gradient, one persistent "
                       f"cooperative launch per step ({info['grid_ctas']} CTAs, one per SM)",
             "props_per_step": 2 * len(probs), "ms_per_step": round(ms, 3),
@@ -659,6 +659,8 @@ def main():
                     help="3: the 2048^2 x 48 headline (default); 2 / 4 / 5: the other configurations")
     ap.add_argument("--modes", type=int, default=16,
                     help="modes per wavelength (default 16; smaller values only for profiler captures)")
+    ap.add_argument("--problems", type=int, default=64,
+                    help="problems of the ragged batch (--config 5; default 64, smaller only for profiler captures)")
     args = ap.parse_args()
     global N_MODES
     N_MODES = args.modes
