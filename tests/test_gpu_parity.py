@@ -453,6 +453,60 @@ def test_bpm_forward_and_gradient(fo, orc, every):
     assert orc.rel_l2(npy(grads[bpm]["dn"]), g) < GRAD_TOL
 
 
+def test_bpm_config_shape(fo, orc):
+    """AS_BPM at the benchmark's grid (1024^2, ds = 0.25 um, n0 = 1.45, smooth dn of
+    amplitude 5e-3), 16 slices with checkpoints every 4: field and d(dn) against the oracle."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(44)
+    n, ns, ds, lam, n0 = 1024, 16, (0.25, 0.25), 1.064, 1.45
+    dn = gaussian_filter(rng.standard_normal((ns, n, n)).astype(np.float32), (2.0, 4.0, 4.0))
+    dn = f32(dn * (5e-3 / np.max(np.abs(dn))))
+    x, y = orc.spatial_vectors((n, n), ds)
+    tilt = 0.02
+    u0 = c64(orc.gaussian(40.0, x, y) * np.exp(2j * np.pi * np.sin(tilt) / lam * x[None, :]))
+    target = f32(np.abs(orc.gaussian(35.0, x - 3, y)) ** 2)
+    u = fo.ScalarField(u0, ds, lam)
+    bpm = fo.AS_BPM(u, float(ns), n0, dn, trainable=True, checkpoint_every=4)
+    system = fo.ScalarSource(u) | bpm
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    out, saves = orc.bpm_forward(u0, ds[0], ds[1], lam, float(ns), n0, dn, 1, save=True)
+    assert orc.rel_l2(npy(system()["out"].electric), out) < FIELD_TOL
+    _, g = orc.bpm_backward(orc.sid_backward(out, target), ds[0], ds[1], lam, float(ns), n0, dn, saves, 1)
+    assert orc.rel_l2(npy(grads[bpm]["dn"]), g) < GRAD_TOL
+
+
+def test_rs_two_doe_config_shape(fo, orc):
+    """The two-DOE RSProp chain at the benchmark's shape (512^2 padded to 1024^2,
+    z = 1500 / 2000 / 1500 um): loss and both mask gradients against the oracle."""
+    rng = np.random.default_rng(45)
+    n, ds, lam = 512, (1.0, 1.0), 1.064
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = orc.gaussian(30.0, x, y)
+    u0 = c64(u0 / np.sqrt(orc.power(u0, ds)))
+    t = np.abs(orc.gaussian(30.0, x - 60.0, y) + orc.gaussian(30.0, x + 60.0, y)) ** 2
+    t = f32(t / (t.sum() * ds[0] * ds[1]))
+    p1 = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    p2 = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    u = fo.ScalarField(u0, ds, lam)
+    m1 = fo.Phase(u, p1, trainable=True)
+    m2 = fo.Phase(u, p2, trainable=True)
+    system = fo.ScalarSource(u) | fo.RSProp(u, 1500.0) | m1 | fo.RSProp(u, 2000.0) | m2 | fo.RSProp(u, 1500.0)
+    metric = fo.SquaredIntensityDifference((u, t))
+    loss, grads = fo.withgradient(metric, system)
+    a1 = orc.rsprop(u0, 1.0, 1.0, lam, 1500.0)
+    a2 = orc.rsprop(orc.phase_forward(a1, p1), 1.0, 1.0, lam, 2000.0)
+    out = orc.rsprop(orc.phase_forward(a2, p2), 1.0, 1.0, lam, 1500.0)
+    c_ref, _ = orc.sid_value(out, t)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    dv = orc.rsprop(orc.sid_backward(out, t), 1.0, 1.0, lam, 1500.0, orc.BACKWARD)
+    dv, g2 = orc.phase_backward(dv, p2, a2)
+    dv = orc.rsprop(dv, 1.0, 1.0, lam, 2000.0, orc.BACKWARD)
+    _, g1 = orc.phase_backward(dv, p1, a1)
+    assert orc.rel_l2(npy(grads[m2]["phi"]), g2) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[m1]["phi"]), g1) < GRAD_TOL
+
+
 def test_bpm_backward_direction(fo, orc):
     rng = np.random.default_rng(10)
     n, ns = 32, 6
