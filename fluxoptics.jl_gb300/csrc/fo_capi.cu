@@ -780,7 +780,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   for (int b = 0; b < batch; ++b) order[b] = b;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hidx[a] < hidx[b]; });
   // column-pass work items: runs of at most kFieldsPerItem fields sharing one table
-  const int kFieldsPerItem = 16;
+  const int kFieldsPerItem = std::max(1, std::min(64, env_int("FO_FIELDS_PER_ITEM", 16)));
   std::vector<int> items{0};
   for (int i = 1; i <= batch; ++i) {
     if (i == batch || hidx[order[i]] != hidx[order[i - 1]] || i - items.back() >= kFieldsPerItem)
