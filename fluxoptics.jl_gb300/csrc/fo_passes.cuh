@@ -742,7 +742,9 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
   constexpr int SLOTS = SmemSize<N>::value;
   constexpr int BOX = 256;
   extern __shared__ float4 dsm4[];
-  char* base = reinterpret_cast<char*>(((reinterpret_cast<unsigned long long>(dsm4) + 127) >> 7) << 7);
+  // 128-byte aligned start, formed by pointer arithmetic on the shared array itself
+  // so that every access below compiles to a shared-memory (not generic) access
+  char* base = reinterpret_cast<char*>(dsm4) + ((128u - (smem_u32(dsm4) & 127u)) & 127u);
   float2* stage = reinterpret_cast<float2*>(base);  // dense [N][W]
   float2* hs = stage + N * W;                         // dense [N][W]
   float2* ex = hs + N * W;                            // padded exchange [SLOTS][W]

@@ -393,7 +393,8 @@ __device__ bool col_pass(const RgArgs& a, float2* smem, unsigned* counter, bool 
 
 __global__ void __launch_bounds__(RG_THREADS, 1) ragged_kernel(const RgArgs a) {
   extern __shared__ float4 dsm4[];
-  float2* smem = reinterpret_cast<float2*>(((reinterpret_cast<unsigned long long>(dsm4) + 127) >> 7) << 7);
+  // 128-byte aligned, by pointer arithmetic on the shared array (keeps shared-memory accesses)
+  float2* smem = reinterpret_cast<float2*>(reinterpret_cast<char*>(dsm4) + ((128u - (smem_u32(dsm4) & 127u)) & 127u));
   __shared__ unsigned long long bar[2];
   __shared__ int s_next[2], s_abort, s_flag;
   __shared__ float s_red[RG_THREADS / 32];
