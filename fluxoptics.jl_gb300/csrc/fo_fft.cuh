@@ -406,12 +406,9 @@ __device__ __forceinline__ void stages_from_r(V (&v)[E], int t, const float2 (&w
   }
 }
 
-// fft_forward with register-resident twiddles (see TwRegs / load_twiddles).
-template <int N, int E, int PS, typename V>
-__device__ __forceinline__ void fft_forward_r(V (&v)[E], int t, const float2 (&w)[TwRegs<N, E>::size], V* sm,
-                                              int bar_id = 0, int bar_n = 0) {
-  Dft<E>::run(v, 0);
-  stages_from_r<N, E, 1, PS>(v, t, w, sm, bar_id, bar_n);
+// The last stage leaves X[t + r*T] in register out(r): rename into natural order.
+template <int E, typename V>
+__device__ __forceinline__ void fft_last_stage_order(V (&v)[E]) {
   if constexpr (Dft<E>::out(1) != 1) {
     V x[E];
 #pragma unroll
@@ -419,6 +416,15 @@ __device__ __forceinline__ void fft_forward_r(V (&v)[E], int t, const float2 (&w
 #pragma unroll
     for (int r = 0; r < E; ++r) v[r] = x[r];
   }
+}
+
+// fft_forward with register-resident twiddles (see TwRegs / load_twiddles).
+template <int N, int E, int PS, typename V>
+__device__ __forceinline__ void fft_forward_r(V (&v)[E], int t, const float2 (&w)[TwRegs<N, E>::size], V* sm,
+                                              int bar_id = 0, int bar_n = 0) {
+  Dft<E>::run(v, 0);
+  stages_from_r<N, E, 1, PS>(v, t, w, sm, bar_id, bar_n);
+  fft_last_stage_order<E>(v);
 }
 
 }  // namespace fo

@@ -815,8 +815,6 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       const int p = t + i * T;
       v[i] = (col_ok && p < y_in) ? stage[p * W + c] : make_float2(0.f, 0.f);
     }
-    // the previous field's result tile has been read out of `ex`
-    if (threadIdx.x == 0) bulk_wait_read_all();
     __syncthreads();  // the staging buffer is free again; abort decision is uniform
     if (s_abort) {
       if (threadIdx.x == 0) {
@@ -831,7 +829,16 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       fence_proxy_async();
       issue_tile(f + 1);
     }
-    fft(v);
+    // First transform.  Its radix-E stage runs in registers; only then does thread 0
+    // wait until the previous field's result tile has been read out of `ex` (the
+    // TMA store), and the first exchange's barrier publishes that to every thread.
+    Dft<E>::run(v, 0);
+    if (threadIdx.x == 0) bulk_wait_read_all();
+    if constexpr (TWR)
+      stages_from_r<N, E, 1, W>(v, t, wr, ex + c, 0, 0);
+    else
+      stages_from<N, E, 1, W>(v, t, tw, ex + c, 0, 0);
+    fft_last_stage_order<E>(v);
     if (!a.fft_only) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
