@@ -82,6 +82,7 @@ SIGNATURES = {
     "fo_chain_destroy": (_i, [_vp]),
     "fo_chain_forward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp]),
     "fo_chain_forward_from": (_i, [_vp, _vp, _vp, C.POINTER(fo_mod), _i, _vp]),
+    "fo_chain_forward_sid": (_i, [_vp, _vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _vp, _vp]),
     "fo_chain_backward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _vp]),
     "fo_chain_backward_ex": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _i, _vp]),
     "fo_bpm_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i, _d, _i]),

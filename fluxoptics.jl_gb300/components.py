@@ -785,12 +785,20 @@ class OpticalSystem:
             lib.fo_chain_destroy(h)
 
     # -- execution ----------------------------------------------------------------
-    def forward(self, u: ScalarField, tape=None, src: ScalarField = None):
+    def forward(self, u: ScalarField, tape=None, src: ScalarField = None, metric=None):
         """Runs the system in place on u (or from ``src`` into u).  With a tape,
         trainable components save their inputs and the tape records what the
-        adjoint sweep needs."""
+        adjoint sweep needs.  A trainable modulator that directly follows the
+        source of an out-of-place run saves nothing: the tape refers to ``src``,
+        which must stay unchanged until the adjoint sweep has run.
+
+        With ``metric``, the metric is evaluated on the result (its ``loss`` holds
+        the values afterwards); SquaredIntensityDifference is then computed inside
+        the last pass when the system ends with a fused chain."""
         d = self.direction
-        for i, seg in enumerate(self.segments(u)):
+        segs = self.segments(u)
+        metric_done = False
+        for i, seg in enumerate(segs):
             from_src = src is not None and i == 0
             if src is not None and i == 0 and not isinstance(seg, _Chain):
                 u.electric.copy_(src.electric)
@@ -801,15 +809,27 @@ class OpticalSystem:
                         p.refresh(u)
                 mods = (fo_mod * len(seg.mods))()
                 saved = []
+                # The first modulator of a chain that reads the system input out of place
+                # sees that input unchanged, so its adjoint reads it there: no copy is saved.
+                src_is_input = from_src and src.electric.data_ptr() != u.electric.data_ptr()
                 for k, m in enumerate(seg.mods):
                     if m is None:
                         mods[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0, None)
                         saved.append(None)
                         continue
+                    if tape is not None and m.trainable and k == 0 and src_is_input:
+                        mods[k] = m.fo_mod(saved=None, u=u)
+                        saved.append(src.electric)
+                        continue
                     sv = m.get_saved_buffer(u) if (tape is not None and m.trainable) else None
                     mods[k] = m.fo_mod(saved=sv, u=u)
                     saved.append(sv)
-                if from_src:
+                if metric is not None and getattr(metric, "fuses_into_chain", False) and i == len(segs) - 1:
+                    _capi.call("fo_chain_forward_sid", self._chain_handle(seg, u),
+                               _ptr(src.electric) if from_src else None, _ptr(u.electric), mods, int(d),
+                               metric.handle, _ptr(metric.target), _ptr(metric.loss), _stream())
+                    metric_done = True
+                elif from_src:
                     _capi.call("fo_chain_forward_from", self._chain_handle(seg, u), _ptr(src.electric),
                                _ptr(u.electric), mods, int(d), _stream())
                 else:
@@ -832,6 +852,8 @@ class OpticalSystem:
                         tape.append((c, None))
         if src is not None and not self.components:
             u.electric.copy_(src.electric)
+        if metric is not None and not metric_done:
+            metric(u)
         return u
 
     def backward(self, du: ScalarField, tape, seed=None, input_grad=None):

@@ -687,6 +687,11 @@ cudaError_t launch_mask_bwd(float2* dv, const float2* m, const float2* saved, fl
 
 int sid_partial_blocks(long long npix) { return (int)grid_for(npix); }
 
+cudaError_t launch_sid_finalize(const float* partials, int nblocks, int T, float* loss, cudaStream_t st) {
+  sid_finalize_kernel<<<T, kThreads, 0, st>>>(partials, nblocks, T, loss);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sid_fwd(const float2* u, const float* target, const int* order, const int* offsets,
                            int T, long long npix, float* resid, float* partials, float* loss,
                            cudaStream_t st) {

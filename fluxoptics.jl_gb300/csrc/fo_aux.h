@@ -36,6 +36,8 @@ cudaError_t launch_mask_bwd(float2* dv, const float2* m, const float2* saved, fl
                             long long npix, int batch, float s, cudaStream_t st);
 
 int sid_partial_blocks(long long npix);
+// loss[t] = fixed-order sum of partials[b * T + t] over b < nblocks
+cudaError_t launch_sid_finalize(const float* partials, int nblocks, int T, float* loss, cudaStream_t st);
 cudaError_t launch_sid_fwd(const float2* u, const float* target, const int* order, const int* offsets,
                            int T, long long npix, float* resid, float* partials, float* loss,
                            cudaStream_t st);

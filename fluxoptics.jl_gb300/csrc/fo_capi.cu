@@ -266,6 +266,17 @@ struct fo_prop_plan_s {
   size_t ws_bytes = 0;
 };
 
+struct fo_sid_s {
+  int nx = 0, ny = 0, batch = 0, T = 0;
+  int group = 0;           // fields per target slice when every slice has the same count, else 0
+  int* tidx = nullptr;     // device, per field
+  int* order = nullptr;    // device, fields grouped by target slice
+  int* offsets = nullptr;  // device, T+1
+  float* resid = nullptr;  // device, T x ny x nx
+  float* partials = nullptr;  // device, max(pixel blocks, ny) x T
+  float* ones = nullptr;   // device, T
+};
+
 namespace {
 
 void plan_free(fo_prop_plan p) {
@@ -348,6 +359,7 @@ Mod mod_from(const fo_mod* m) {
   return r;
 }
 
+
 struct SeedArgs {
   const float* resid = nullptr;
   const int* tidx = nullptr;
@@ -369,7 +381,7 @@ int validate_mod(const Mod& m, bool backward) {
 // selected by the inv/fwd flags.
 int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bool fwd_after,
              const Mod& mod, bool bwd, float s, const float* inv_lambda, const SeedArgs* seed,
-             const float2* tw, cudaStream_t st) {
+             const float2* tw, cudaStream_t st, const fo_sid_s* sid = nullptr, const float* target = nullptr) {
   RowPassArgs a;
   std::memset(&a, 0, sizeof(a));
   const long long real_bs = (long long)L.nx * L.ny, spec_bs = (long long)L.fx * L.ny;
@@ -413,9 +425,20 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
     a.tidx = seed->tidx;
     a.dc = seed->dc;
   }
+  if (sid) {  // the metric on this pass's output: one CTA per (target slice, rows)
+    a.field_list = sid->order;
+    a.fields_per_cta = sid->group;
+    a.tidx = sid->tidx;
+    a.resid_tstride = real_bs;
+    a.resid_ld = L.nx;
+    a.sid_target = target;
+    a.sid_resid = sid->resid;
+    a.sid_partials = sid->partials;
+    a.sid_T = sid->T;
+  }
   const int load_n = inv_first ? L.fx : L.nx;
   const bool pf = L.row_pf && load_n == L.fx && row_prefetch_fits(L.fx, L.row_v) &&
-                  !(grad && mod.kind == MOD_MASK);
+                  !(grad && mod.kind == MOD_MASK) && !sid;
   ProfScope prof(inv_first && fwd_after ? 1 : 0, st);
   FO_LAUNCH(launch_row_pass(L.fx, L.row_v, pf, a, tw, st));
   return FO_OK;
@@ -472,8 +495,12 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
 }
 
 // Forward sweep: mods[0] -> props[0] -> ... -> props[K-1] -> mods[K], in place on u.
+// Forward sweep.  With `sid` (fused form only: every target slice has the same
+// number of fields) the last pass also evaluates the metric on u against `target`
+// and loss[T] receives the per-slice sums.
 int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, const Mod* mods, int s,
-                cudaStream_t st, const float2* src = nullptr) {
+                cudaStream_t st, const float2* src = nullptr, const fo_sid_s* sid = nullptr,
+                const float* target = nullptr, float* loss = nullptr) {
   const int K = (int)props.size();
   const Layout L = layout_of(props[0]);
   const float* il = props[0]->inv_lambda;
@@ -484,8 +511,9 @@ int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, 
     if (k + 1 < K)
       FO_TRY(row_pass(L, buf, buf, true, true, mods[k + 1], false, sf, il, nullptr, props[0]->tw_x, st));
     else
-      FO_TRY(row_pass(L, buf, u, true, false, mods[K], false, sf, il, nullptr, props[0]->tw_x, st));
+      FO_TRY(row_pass(L, buf, u, true, false, mods[K], false, sf, il, nullptr, props[0]->tw_x, st, sid, target));
   }
+  if (sid) FO_LAUNCH(launch_sid_finalize(sid->partials, L.ny, sid->T, loss, st));
   return FO_OK;
 }
 
@@ -1201,16 +1229,6 @@ struct fo_chain_s {
   float2* scratch = nullptr;  // padded layouts only
 };
 
-struct fo_sid_s {
-  int nx = 0, ny = 0, batch = 0, T = 0;
-  int* tidx = nullptr;     // device, per field
-  int* order = nullptr;    // device, fields grouped by target slice
-  int* offsets = nullptr;  // device, T+1
-  float* resid = nullptr;  // device, T x ny x nx
-  float* partials = nullptr;
-  float* ones = nullptr;   // device, T
-};
-
 extern "C" {
 
 FO_API int fo_chain_create(fo_chain* chain, int n_props, const fo_prop_plan* props) {
@@ -1272,6 +1290,29 @@ FO_API int fo_chain_forward_from(fo_chain chain, const void* u_in, void* u, cons
   float2* buf = chain->scratch ? chain->scratch : uu;
   return run_forward(chain->props, buf, uu, m.data(), direction, S(stream),
                      reinterpret_cast<const float2*>(u_in));
+}
+
+FO_API int fo_chain_forward_sid(fo_chain chain, const void* u_in, void* u, const fo_mod* mods, int direction,
+                                fo_sid sid, const float* target, float* loss, void* stream) {
+  if (!chain || !u || !mods || !sid || !target || !loss)
+    return fail(FO_ERR_ARG, "chain, u, mods, sid, target and loss must not be NULL");
+  FO_TRY(check_dir(direction));
+  const int K = (int)chain->props.size();
+  const Layout L = layout_of(chain->props[0]);
+  if (sid->nx != L.nx || sid->ny != L.ny || sid->batch != L.batch)
+    return fail(FO_ERR_SHAPE, "metric and chain shapes differ");
+  std::vector<Mod> m(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    m[k] = mod_from(&mods[k]);
+    FO_TRY(validate_mod(m[k], false));
+  }
+  float2* uu = reinterpret_cast<float2*>(u);
+  float2* buf = chain->scratch ? chain->scratch : uu;
+  const float2* src = reinterpret_cast<const float2*>(u_in);
+  if (sid->group > 0) return run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src, sid, target, loss);
+  // slices with different field counts: the metric runs as its own pass
+  FO_TRY(run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src));
+  return fo_sid_forward(sid, u, target, loss, stream);
 }
 
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,
@@ -1535,6 +1576,9 @@ FO_API int fo_sid_create(fo_sid* sid, int nx, int ny, int batch, int n_targets, 
   }
   offsets[n_targets] = (int)order.size();
   fo_sid m = new fo_sid_s();
+  m->group = offsets[1];
+  for (int t = 0; t < n_targets; ++t)
+    if (offsets[t + 1] - offsets[t] != m->group) m->group = 0;
   m->nx = nx;
   m->ny = ny;
   m->batch = batch;
@@ -1546,7 +1590,8 @@ FO_API int fo_sid_create(fo_sid* sid, int nx, int ny, int batch, int n_targets, 
       (rc = dalloc(&m->order, batch, "metric order")) != FO_OK ||
       (rc = dalloc(&m->offsets, n_targets + 1, "metric offsets")) != FO_OK ||
       (rc = dalloc(&m->resid, (size_t)n_targets * npix, "metric residuals")) != FO_OK ||
-      (rc = dalloc(&m->partials, (size_t)sid_partial_blocks(npix) * n_targets, "metric partial sums")) != FO_OK ||
+      (rc = dalloc(&m->partials, (size_t)std::max(sid_partial_blocks(npix), ny) * n_targets,
+                   "metric partial sums")) != FO_OK ||
       (rc = dalloc(&m->ones, n_targets, "metric ones")) != FO_OK) {
     fo_sid_destroy(m);
     return rc;

@@ -62,6 +62,15 @@ struct RowPassArgs {
   int resid_ld;
   const int* tidx;
   const float* dc;
+  // SquaredIntensityDifference evaluated on the pass output (row kernel GK = 3):
+  // each CTA visits one target slice's fields (field_list grouped by slice,
+  // fields_per_cta fields per slice), sums their intensities, and writes
+  // sid_resid = I - sid_target (layout of resid_tstride / resid_ld) and the row's
+  // sum of squares to sid_partials[row * sid_T + slice]; tidx gives the slice.
+  const float* sid_target;
+  float* sid_resid;
+  float* sid_partials;
+  int sid_T;
 };
 
 // One column pass: forward FFT along y, multiply by the transfer function of the

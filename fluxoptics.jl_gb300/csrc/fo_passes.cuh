@@ -59,7 +59,9 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // --------------------------------------------------------------------------
-// Row pass.  GK: gradient accumulator (0 none, 1 real: phase / dn, 2 complex: mask).
+// Row pass.  GK: gradient accumulator (0 none, 1 real: phase / dn, 2 complex: mask,
+// 3: intensity of the output summed over the CTA's fields for the squared
+// intensity difference, see RowPassArgs::sid_target).
 // PF: stage the next field's row through cp.async (needs load_n == N).
 // Shared memory: 2 * LANES * SLOTS float2 (PF) or LANES * SLOTS float2.
 // --------------------------------------------------------------------------
@@ -83,7 +85,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
   const int n_valid = FULL ? N : a.n_valid;
   const int load_n = a.inv_first ? N : n_valid;
   const int store_n = a.fwd_after ? N : n_valid;
-  constexpr int GR = (GK == 1) ? E : 1;
+  constexpr int GR = (GK == 1 || GK == 3) ? E : 1;
   constexpr int GC = (GK == 2) ? E : 1;
   float gacc[GR];
   float2 gacc_c[GC];
@@ -264,6 +266,10 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
       }
     }
     if (a.fwd_after) fft(v, PF ? cur : buf0);
+    if constexpr (GK == 3) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) gacc[i] = fmaf(v[i].x, v[i].x, fmaf(v[i].y, v[i].y, gacc[i]));
+    }
     if (row_ok && a.dst) {  // a null destination discards the pass output (gradients only)
       float2* dst = a.dst + (long long)b * a.dst_bstride + (long long)y * a.dst_ld;
 #pragma unroll
@@ -274,7 +280,40 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
     }
     __syncthreads();  // `cur` is refilled by the prefetch of the next iteration
   }
-  if constexpr (GK != 0) {
+  if constexpr (GK == 3) {
+    // residual I - target of this row for the CTA's target slice, and the row's sum
+    // of squared residuals (fixed-order reduction)
+    const int ts = a.tidx[field_of(f0)];
+    float r2 = 0.f;
+    if (row_ok) {
+      const long long off = (long long)ts * a.resid_tstride + (long long)y * a.resid_ld;
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        if (p < n_valid) {
+          const float r = gacc[i] - a.sid_target[off + p];
+          a.sid_resid[off + p] = r;
+          r2 = fmaf(r, r, r2);
+        }
+      }
+    }
+    constexpr int G = T < 32 ? T : 32;  // lanes of one row within a warp
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    float* red = reinterpret_cast<float*>(buf0);  // this row's staging slots are free now
+    if constexpr (T > 32) {
+      if ((t & 31) == 0) red[t >> 5] = r2;
+      __syncthreads();
+      if (t == 0) {
+        float acc = 0.f;
+#pragma unroll
+        for (int w = 0; w < T / 32; ++w) acc += red[w];
+        r2 = acc;
+      }
+    }
+    if (t == 0 && row_ok) a.sid_partials[(long long)y * a.sid_T + ts] = r2;
+  }
+  if constexpr (GK == 1 || GK == 2) {
     if (row_ok) {
 #pragma unroll
       for (int i = 0; i < E; ++i) {
@@ -909,7 +948,8 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
   using SH = RowShape<N, E, LANES>;
   dim3 grid((a.batch + a.fields_per_cta - 1) / a.fields_per_cta, (a.nrows + LANES - 1) / LANES);
   const bool grad = a.mod_bwd && a.grad != nullptr && a.mod_kind != MOD_NONE;
-  const size_t smem = SH::smem(pf && !(grad && a.mod_kind == MOD_MASK), grad);
+  const bool sid = a.sid_partials != nullptr;  // GK 3 (no staging)
+  const size_t smem = SH::smem(pf && !sid && !(grad && a.mod_kind == MOD_MASK), grad || sid);
   const bool full = a.n_valid == N && a.nrows % LANES == 0;
   cudaError_t e = cudaSuccess;
 #define FO_ROW_GO(GK, PFV)                                                                        \
@@ -922,7 +962,9 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
       if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, false>, grid, dim3(SH::threads), smem, s, a, tw); \
     }                                                                                             \
   } while (0)
-  if (!grad) {
+  if (sid) {
+    FO_ROW_GO(3, false);
+  } else if (!grad) {
     if (pf) FO_ROW_GO(0, true); else FO_ROW_GO(0, false);
   } else if (a.mod_kind == MOD_MASK) {
     FO_ROW_GO(2, false);

@@ -22,6 +22,9 @@ class SquaredIntensityDifference:
     (nx, ny[, T]) target).  By default field b maps to slice b % T, the broadcast of an
     (nx, ny, T) target over (nx, ny, T, M) fields; ``target_index`` overrides it."""
 
+    # OpticalSystem.forward(..., metric=m) evaluates it inside the last fused pass
+    fuses_into_chain = True
+
     def __init__(self, pair, target_index=None):
         u0, target = pair
         t = torch.as_tensor(target.detach().cpu().numpy() if isinstance(target, torch.Tensor) else np.asarray(target),
@@ -117,8 +120,12 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     src = system.source.u0 if x is None else x
     u = src.similar()
     tape = []
-    system.forward(u, tape, src=src)
-    c = metric(u)
+    if isinstance(metric, SquaredIntensityDifference):
+        system.forward(u, tape, src=src, metric=metric)
+        c = metric.loss
+    else:
+        system.forward(u, tape, src=src)
+        c = metric(u)
     du = u.similar()
     if isinstance(metric, SquaredIntensityDifference) and dc is None:
         grads = system.backward(du, tape, seed=(metric, u))

@@ -318,6 +318,21 @@ typedef struct fo_sid_s* fo_sid;
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction,
                              fo_sid sid, const void* u_out, void* stream);
 
+/*
+ * Forward through the chain (from u_in when not NULL, else in place on u) with
+ * SquaredIntensityDifference evaluated on the result inside the last pass: the
+ * same outputs as fo_chain_forward[_from] followed by fo_sid_forward(sid, u,
+ * target, loss), without a separate read of u.  The residuals are kept in `sid`
+ * for a seeded fo_chain_backward_ex.  When the metric's target slices have
+ * different field counts the metric runs as its own pass instead.
+ * Replaces: the forward half of Zygote.withgradient(metric, system) for
+ * SquaredIntensityDifference -- system/optical_system.jl:189-214 followed by
+ * compute_metric, src/metrics/squared_intensity_difference.jl:78-83.
+ */
+FO_API int fo_chain_forward_sid(fo_chain chain, const void* u_in, void* u, const fo_mod* mods,
+                                int direction, fo_sid sid, const float* target, float* loss,
+                                void* stream);
+
 /* fo_chain_backward with flags.  FO_BWD_DISCARD_INPUT_GRAD: only the parameter
  * gradients are wanted (the chain's input is not trainable); the final write of
  * the input gradient is skipped and du is left holding scratch values. */

@@ -211,6 +211,59 @@ def test_chain_gradients(fo, orc, kind, d):
     assert orc.rel_l2(npy(grads[c0]["phi"]), g0) < GRAD_TOL
 
 
+@pytest.mark.parametrize("n", [16, 64, 256, 512])
+@pytest.mark.parametrize("kind", ["AS", "RS"])
+@pytest.mark.parametrize("uneven", [False, True])
+def test_metric_fused_into_last_pass(fo, orc, n, kind, uneven):
+    """SquaredIntensityDifference evaluated inside the chain's last pass (uniform
+    target slices) or as its own pass (uneven slices), the first modulator reading
+    its saved input from the source field, and the seeded adjoint after it."""
+    rng = np.random.default_rng(30 + n)
+    B = 6
+    ds = (1.0, 1.0)
+    lams = np.array([1.064, 0.8, 0.6, 1.064, 0.8, 0.6])
+    zs = [0.2 * n * n / 8, 0.15 * n * n / 8]
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(n / 6, x, y)] * B) * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    phi0 = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    m2 = c64(0.5 + rng.uniform(0, 1, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+    target = f32(rng.uniform(0, 2, (3, n, n)) * np.abs(orc.gaussian(n / 5, x, y)) ** 2)
+    tix = [0, 0, 0, 1, 2, 2] if uneven else None
+
+    u = fo.ScalarField(u0, ds, lams)
+    P = fo.ASProp if kind == "AS" else fo.RSProp
+    c0 = fo.Phase(u, phi0, trainable=True)
+    c2 = fo.Mask(u, m2, trainable=True)
+    props = [P(u, z) for z in zs]
+    system = fo.OpticalSystem(fo.ScalarSource(u), [c0, props[0], props[1], c2])
+    assert len(system.segments(u)) == 1
+    metric = fo.SquaredIntensityDifference((u, target), target_index=tix)
+    loss, grads = fo.withgradient(metric, system)
+
+    # the fused forward leaves the same field as the plain forward, and the same
+    # loss as the metric's own pass
+    a, b = u.similar(), u.similar()
+    system.forward(a, src=u, metric=metric)
+    l_fused = npy(metric.loss).astype(np.float64)
+    system.forward(b, src=u)
+    l_sep = npy(metric(b)).astype(np.float64)
+    assert np.array_equal(npy(a.electric), npy(b.electric))
+    assert np.max(np.abs(l_fused - l_sep) / np.abs(l_sep)) < 1e-5
+
+    out, saves, prop = _oracle_chain(orc, kind, u0, [("phase", phi0), None, ("mask", m2)], ds, lams, zs, 1)
+    assert orc.rel_l2(npy(a.electric), out) < FIELD_TOL
+    c_ref, _ = orc.sid_value(out, target, tix)
+    assert np.max(np.abs(l_fused - c_ref) / np.abs(c_ref)) < 1e-4
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    dv = orc.sid_backward(out, target, target_index=tix)
+    dv, g2 = orc.mask_backward(dv, m2, saves[2], 1)
+    dv = prop(dv, zs[1], -1)
+    dv = prop(dv, zs[0], -1)
+    _, g0 = orc.phase_backward(dv, phi0, saves[0], 1)
+    assert orc.rel_l2(npy(grads[c2]["m"]), g2) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[c0]["phi"]), g0) < GRAD_TOL
+
+
 @pytest.mark.parametrize("mode", ["paraxial", "tilted", "tilted_track", "filtered", "paraxial_tilted_track"])
 @pytest.mark.parametrize("d", [1, -1])
 def test_asprop_paraxial_tilted_filtered(fo, orc, mode, d):
