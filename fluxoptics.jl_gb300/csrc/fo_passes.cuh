@@ -27,10 +27,19 @@
 
 namespace fo {
 
+// Register cap per thread of the E = 16 row passes without a gradient, and whether
+// forward row passes keep their twiddles in registers (build-time settings).
+#ifndef FO_ROW_E16_REG_CAP
+#define FO_ROW_E16_REG_CAP 96
+#endif
+#ifndef FO_ROW_TWR
+#define FO_ROW_TWR 0
+#endif
+
 // Minimum resident CTAs per SM requested from the compiler: caps registers near
-// 96 per thread for E <= 8 and at 128 for E = 16.
-__host__ __device__ constexpr int min_blocks(int threads, int E) {
-  return (65536 / (threads * (E <= 8 ? 96 : 128))) > 0 ? 65536 / (threads * (E <= 8 ? 96 : 128)) : 1;
+// 96 per thread for E <= 8 and at 128 (cap16) for E = 16.
+__host__ __device__ constexpr int min_blocks(int threads, int E, int cap16 = 128) {
+  return (65536 / (threads * (E <= 8 ? 96 : cap16))) > 0 ? 65536 / (threads * (E <= 8 ? 96 : cap16)) : 1;
 }
 
 // Programmatic dependent launch: let the next pass be launched while this one
@@ -68,7 +77,8 @@ __device__ __forceinline__ void cp_async_wait() {
 // FULL: the row count is a multiple of LANES and n_valid == N, so no
 // per-element guards are needed.
 template <int N, int E, int LANES, int GK, bool PF, bool FULL>
-__global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
+__global__ void __launch_bounds__(LANES*(N / E),
+                                  min_blocks(LANES*(N / E), E, (GK == 0 || GK == 3) ? FO_ROW_E16_REG_CAP : 128))
     row_pass_kernel(const RowPassArgs a, const float2* __restrict__ tw) {
   pdl_prologue();
   constexpr int T = N / E;
@@ -117,7 +127,7 @@ __global__ void __launch_bounds__(LANES*(N / E), min_blocks(LANES*(N / E), E))
 
   // Passes without a gradient accumulator have the registers to keep this
   // thread's twiddles for all the CTA's fields.
-  constexpr bool TWR = (GK == 0) && (E == 16) && FULL && TwRegs<N, E>::total <= 24;
+  constexpr bool TWR = FO_ROW_TWR && (GK == 0) && (E == 16) && FULL && TwRegs<N, E>::total <= 24;
   float2 wr[TwRegs<N, E>::size];
   if constexpr (TWR) load_twiddles<N, E>(wr, t, tw);
   auto fft = [&](float2(&x)[E], float2* sm) {
