@@ -547,22 +547,31 @@ std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int, int>, std::tuple<int, bool, int, bool>> g_tune;
 
 
+// Best per-launch time of `reps` samples.  Launches shorter than about 0.25 ms are
+// timed in back-to-back runs of that length, so that event resolution and launch
+// latency do not decide between variants of a short pass.
 float time_launches(const std::function<cudaError_t()>& fn, int reps) {
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   float best = 1e30f;
   if (fn() != cudaSuccess) best = -1.f;  // warm-up (and a launch-failure probe)
-  for (int r = 0; r < reps && best >= 0.f; ++r) {
+  int runs = 1;
+  for (int r = 0; r < reps + 1 && best >= 0.f; ++r) {
     cudaEventRecord(a, 0);
-    if (fn() != cudaSuccess) {
-      best = -1.f;
-      break;
-    }
+    for (int i = 0; i < runs && best >= 0.f; ++i)
+      if (fn() != cudaSuccess) best = -1.f;
+    if (best < 0.f) break;
     cudaEventRecord(b, 0);
     cudaEventSynchronize(b);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
+    ms /= runs;
+    if (r == 0) {  // sizing sample
+      runs = std::max(1, std::min(64, (int)std::ceil(0.25f / std::max(ms, 1e-3f))));
+      if (runs == 1) best = ms;
+      continue;
+    }
     best = std::min(best, ms);
   }
   cudaEventDestroy(a);

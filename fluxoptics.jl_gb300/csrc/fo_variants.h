@@ -22,8 +22,8 @@
 #define FO_COL_VARIANTS_64(X) X(0, 8, 16, 1)
 #define FO_COL_VARIANTS_128(X) X(0, 8, 16, 1) X(1, 8, 16, 2)
 #define FO_COL_VARIANTS_256(X) X(0, 16, 16, 1) X(1, 8, 8, 1) X(2, 8, 8, 2)
-#define FO_COL_VARIANTS_512(X) X(0, 8, 8, 1) X(1, 16, 8, 1) X(2, 8, 4, 1) X(3, 8, 4, 2) X(4, 16, 4, 4) X(5, 8, 4, 4) X(6, 16, 2, 6)
-#define FO_COL_VARIANTS_1024(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 8, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6)
+#define FO_COL_VARIANTS_512(X) X(0, 8, 8, 1) X(1, 16, 8, 1) X(2, 8, 4, 1) X(3, 8, 4, 2) X(4, 16, 4, 4) X(5, 8, 4, 4) X(6, 16, 2, 6) X(7, 16, 4, 6) X(8, 16, 8, 6)
+#define FO_COL_VARIANTS_1024(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 8, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6) X(8, 16, 4, 6) X(9, 16, 8, 6)
 #define FO_COL_VARIANTS_2048(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 2, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6) X(8, 16, 4, 6)
 #define FO_COL_VARIANTS_4096(X) X(0, 16, 2, 1) X(1, 8, 2, 1) X(2, 16, 4, 1) X(3, 16, 2, 0) X(4, 16, 2, 4) X(5, 16, 2, 6)
 

@@ -704,7 +704,7 @@ def test_graph_capture_replays_iteration(fo, orc):
 # Every launch-shape variant of the passes (forced through the environment)
 # ---------------------------------------------------------------------------
 
-_VARIANTS = {512: (3, 7), 1024: (4, 8), 2048: (4, 9), 4096: (2, 6)}
+_VARIANTS = {512: (3, 9), 1024: (4, 10), 2048: (4, 9), 4096: (2, 6)}
 
 
 @pytest.mark.parametrize("n", sorted(_VARIANTS))
