@@ -179,9 +179,10 @@ __global__ void __launch_bounds__(LANES*(N / E),
         v[i] = a.inv_first ? cconj(x) : x;
       }
     }
-    // loads whose latency the inverse transform can hide
-    float2 sv[GK != 0 ? E : 1];
-    if constexpr (GK != 0) {
+    // the saved modulation input of the gradient passes, loaded where the inverse
+    // transform hides the latency
+    float2 sv[(GK == 1 || GK == 2) ? E : 1];
+    if constexpr (GK == 1 || GK == 2) {
       const float2* svp = a.saved + (long long)b * a.saved_bstride + (long long)y * a.saved_ld;
 #pragma unroll
       for (int i = 0; i < E; ++i) {
