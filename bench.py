@@ -303,22 +303,34 @@ def run_gb300(args, rank, world):
             ev_copied[0].record(copy_stream)
         # Step k is enqueued before the copy of step k+1: when the graph launch is
         # enqueued, the copy stream holds nothing later than the copy it waits for.
+        # Timing events bracket every step's compute on the compute stream.
+        ev_step = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(e2_steps)]
+        ev_copy = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(e2_steps)]
         for k in range(e2_steps):
             cur = k % 2
             stream.wait_event(ev_copied[cur])
+            ev_step[k][0].record(stream)
             fo._capi.check(lib.fo_graph_launch(graphs[cur], sp))
             host_loss[k].copy_(metric.loss, non_blocking=True)
+            ev_step[k][1].record(stream)
             ev_done[cur].record(stream)
             if k + 1 < e2_steps:
                 nxt = (k + 1) % 2
                 if k >= 1:
                     copy_stream.wait_event(ev_done[nxt])  # step k-1 has finished with this buffer
                 with torch.cuda.stream(copy_stream):
+                    ev_copy[k][0].record(copy_stream)
                     bufs[nxt].electric.copy_(host_in, non_blocking=True)
+                    ev_copy[k][1].record(copy_stream)
                     ev_copied[nxt].record(copy_stream)
         e3.record(stream)
         stream.synchronize()
         e2e_ms = e2.elapsed_time(e3) / e2_steps
+        e2e_compute_ms = statistics.median(a.elapsed_time(b) for a, b in ev_step)
+        # input copies made while a step computes (the last step has none)
+        e2e_copy_ms = statistics.median(a.elapsed_time(b) for a, b in ev_copy[:-1]) if e2_steps > 1 else None
         fo._capi.check(lib.fo_graph_destroy(g_b))
         fo._capi.check(lib.fo_graph_destroy(g))
 
@@ -330,8 +342,8 @@ def run_gb300(args, rank, world):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     achieved = col_pass_bytes(batch=batch) / (col_ms * 1e-3) / 1e9
-    # the committed DRAM-traffic capture is of the 48-field launch
-    traffic = read_traffic() if batch == N_MODES * len(LAMBDAS) else None
+    # the committed DRAM-traffic capture is of the full 48-field launch
+    traffic = read_traffic() if batch == 48 else None
     row_name, col_name = C.create_string_buffer(160), C.create_string_buffer(160)
     fo._capi.check(lib.fo_prop_variants(prop.plan_for(u0), None, None, row_name, col_name, 160))
     value = job_rate(props_per_step, world, ms)
@@ -358,6 +370,8 @@ def run_gb300(args, rank, world):
         "e2e": {"value": round(props_per_step / (e2e_ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": int(fields_np.nbytes), "d2h_bytes_per_step": int(len(LAMBDAS) * 4),
                 "overlap": "input copy of step k+1 on a copy stream overlaps the compute of step k",
+                "compute_ms_per_step": round(e2e_compute_ms, 4),
+                "copy_ms_per_step": round(e2e_copy_ms, 4) if e2e_copy_ms is not None else None,
                 "h2d_gbs_measured": round(h2d_gbs, 1)},
         "clocks": clk.summary(),
         "final_loss": final_loss,
@@ -663,11 +677,14 @@ def main():
                     help="3: the 2048^2 x 48 headline (default); 2 / 4 / 5: the other configurations")
     ap.add_argument("--modes", type=int, default=16,
                     help="modes per wavelength (default 16; smaller values only for profiler captures)")
+    ap.add_argument("--wavelengths", type=int, default=3, choices=[1, 2, 3],
+                    help="wavelengths of the batch (default 3; fewer only for profiler captures)")
     ap.add_argument("--problems", type=int, default=64,
                     help="problems of the ragged batch (--config 5; default 64, smaller only for profiler captures)")
     args = ap.parse_args()
-    global N_MODES
+    global N_MODES, LAMBDAS
     N_MODES = args.modes
+    LAMBDAS = LAMBDAS[:args.wavelengths]
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
 
