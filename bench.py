@@ -35,6 +35,10 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# Streams share the device's hardware work queues (8 by default). The e2e loop's copy
+# stream and compute stream must not share one, or the input copy of step k+1
+# waits behind the compute of step k. 32 queues for this process.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 N = 2048
 DS = (0.5, 0.5)

@@ -580,8 +580,16 @@ float time_launches(const std::function<cudaError_t()>& fn, int reps) {
   return best;
 }
 
+// Column-pass work items: runs of at most this many fields sharing one table.
+int fields_per_item() { return std::max(1, std::min(64, env_int("FO_FIELDS_PER_ITEM", 16))); }
+
 int autotune_plan(fo_prop_plan p) {
-  const int nb = std::min(p->batch, 16);
+  // Time the shapes on the plan's own batch (up to 2 GiB of fields) and with the
+  // plan's work-item length, so that the number of CTAs and the last partial wave
+  // are those of the real passes.
+  const size_t field_bytes = sizeof(float2) * (size_t)p->ny * p->fx;
+  const int cap = (int)std::max<size_t>(1, std::min<size_t>(64, (size_t(2) << 30) / field_bytes));
+  const int nb = std::min(p->batch, cap);
   const auto key = std::make_tuple(p->kind, p->fx, p->fy, p->ny, nb);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -599,10 +607,11 @@ int autotune_plan(fo_prop_plan p) {
     return FO_ERR_ALLOC;
   }
   std::vector<int> hidx(2 * nb + 2, 0);
-  for (int i = 0; i < nb; ++i) hidx[i] = i;                     // field list
-  hidx[nb] = 0;  // one run of nb fields
-  hidx[nb + 1] = nb;
-  const int n_items = 1;
+  for (int i = 0; i < nb; ++i) hidx[i] = i;  // field list
+  const int fpi = fields_per_item();
+  int n_items = 0;  // runs of fpi fields (all on table 0)
+  for (int f = 0; f < nb; f += fpi) hidx[nb + n_items++] = f;
+  hidx[nb + n_items] = nb;
   cudaMemcpy(idx, hidx.data(), sizeof(int) * hidx.size(), cudaMemcpyHostToDevice);
   cudaMemset(tmp, 0, sizeof(float2) * (size_t)nb * p->ny * p->fx);
   float best = 1e30f;
@@ -817,7 +826,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   for (int b = 0; b < batch; ++b) order[b] = b;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hidx[a] < hidx[b]; });
   // column-pass work items: runs of at most kFieldsPerItem fields sharing one table
-  const int kFieldsPerItem = std::max(1, std::min(64, env_int("FO_FIELDS_PER_ITEM", 16)));
+  const int kFieldsPerItem = fields_per_item();
   std::vector<int> items{0};
   for (int i = 1; i <= batch; ++i) {
     if (i == batch || hidx[order[i]] != hidx[order[i - 1]] || i - items.back() >= kFieldsPerItem)
