@@ -255,6 +255,9 @@ struct fo_prop_plan_s {
   int* sorted_fields = nullptr; // device, fields ordered by transfer-function table
   int* items = nullptr;         // device, n_items+1 offsets into sorted_fields (runs of one table)
   int n_items = 0;
+  std::vector<int> items_host;  // the same offsets on the host
+  int4* units = nullptr;        // device, balanced column work units of the TMA variants (or null)
+  int n_units = 0;
   int row_v = 0, col_v = 0;     // launch-shape variants (autotuned or default)
   bool row_pf = true, col_pf = true;
   unsigned int* err_word = nullptr;         // device error word (bounded waits)
@@ -284,6 +287,7 @@ void plan_free(fo_prop_plan p) {
   cudaFree(p->H);
   cudaFree(p->h_index);
   cudaFree(p->sorted_fields);
+  cudaFree(p->units);
   cudaFree(p->items);
   cudaFree(p->inv_lambda);
   cudaFree(p->scratch);
@@ -460,6 +464,8 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.fft_only = 0;
   a.batch = p->batch;
   a.field_list = p->sorted_fields;
+  a.units = p->units;
+  a.n_units = p->n_units;
   a.item_start = p->items;
   a.n_items = p->n_items;
   int v = p->col_v;
@@ -709,6 +715,55 @@ int autotune_plan(fo_prop_plan p) {
   return FO_OK;
 }
 
+// Work units of the TMA column variants.  The (strip, item) CTAs of the 2-D launch
+// come in rounds of `slots` (SMs x CTAs per SM); when the last round is only partly
+// filled, its units are cut into shorter runs of fields so that every slot takes
+// a share and the pass ends about when the full rounds do.
+int build_col_units(fo_prop_plan p) {
+  cudaFree(p->units);
+  p->units = nullptr;
+  p->n_units = 0;
+  if (!col_variant_uses_tma(p->fy, p->col_v) || env_int("FO_COL_UNITS", 1) == 0) return FO_OK;
+  const int W = col_variant(p->fy, p->col_v).lanes;
+  ColPassArgs q;
+  std::memset(&q, 0, sizeof(q));
+  int occ = 0;
+  q.occupancy_out = &occ;
+  int dev = 0, sms = 0;
+  if (launch_col_pass(p->fy, p->col_v, false, q, nullptr, 0) != cudaSuccess || occ < 1 ||
+      cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+    cudaGetLastError();
+    return FO_OK;  // keep the 2-D launch
+  }
+  const int slots = sms * occ;
+  const int strips = (p->fx + W - 1) / W;
+  std::vector<int4> units;
+  for (int st = 0; st < strips; ++st)
+    for (int i = 0; i < p->n_items; ++i) units.push_back(make_int4(p->items_host[i], p->items_host[i + 1], st, 0));
+  const int total = (int)units.size();
+  const int tail = total % slots;
+  if (total <= slots || tail == 0) return FO_OK;  // no partial last round
+  std::vector<int4> last(units.end() - tail, units.end());
+  units.resize(total - tail);
+  const int pieces = std::max(1, slots / tail);
+  for (const int4& u : last) {
+    const int len = u.y - u.x;
+    const int k = std::min(pieces, len);
+    for (int j = 0; j < k; ++j) units.push_back(make_int4(u.x + j * len / k, u.x + (j + 1) * len / k, u.z, 0));
+  }
+  int rc = dalloc(&p->units, units.size(), "column work units");
+  if (rc != FO_OK) return rc;
+  cudaError_t e = cudaMemcpy(p->units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(p->units);
+    p->units = nullptr;
+    return cuda_fail(e, "cudaMemcpy column work units");
+  }
+  p->n_units = (int)units.size();
+  return FO_OK;
+}
+
 void apply_overrides(fo_prop_plan p) {
   const int rv = env_int("FO_ROW_VARIANT", -1), cv = env_int("FO_COL_VARIANT", -1);
   if (rv >= 0 && rv < row_variant_count(p->fx)) p->row_v = rv;
@@ -833,6 +888,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
       items.push_back(i);
   }
   p->n_items = (int)items.size() - 1;
+  p->items_host = items;
   cudaError_t e = cudaMemcpy(p->h_index, hidx.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->sorted_fields, order.data(), sizeof(int) * batch, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -944,6 +1000,10 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   p->tw_x = twiddles(fx, row_variant(fx, p->row_v).E, &rc);
   p->tw_y = p->tw_x ? twiddles(fy, col_variant(fy, p->col_v).E, &rc) : nullptr;
   if (!p->tw_x || !p->tw_y) {
+    plan_free(p);
+    return rc;
+  }
+  if ((rc = build_col_units(p)) != FO_OK) {
     plan_free(p);
     return rc;
   }
@@ -1152,7 +1212,8 @@ FO_API int fo_prop_variants(fo_prop_plan plan, int* row_v, int* col_v, char* row
                      : cv.P == 0 ? "col_lane_kernel (lane-major)"
                                  : (plan->col_pf ? "col_pass_kernel (cp.async staging)" : "col_pass_kernel");
   put(col_kernel, std::string(form) + "<" + std::to_string(plan->fy) + ", E=" + std::to_string(cv.E) +
-                      ", columns/CTA=" + std::to_string(cv.lanes) + ">");
+                      ", columns/CTA=" + std::to_string(cv.lanes) + ">" +
+                      (plan->units ? " over " + std::to_string(plan->n_units) + " balanced work units" : ""));
   return FO_OK;
 }
 

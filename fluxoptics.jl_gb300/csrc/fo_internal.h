@@ -90,6 +90,11 @@ struct ColPassArgs {
   const int* field_list;  // fields ordered so that each work item shares one table
   const int* item_start;  // n_items+1 offsets into field_list (null: one field per item)
   int n_items;
+  // TMA variants: optional 1-D list of work units {first, end (positions in
+  // field_list), strip, 0}; the grid is then (n_units, 1)
+  const int4* units;
+  int n_units;
+  int* occupancy_out;     // when set, the launcher stores the variant's CTAs per SM and launches nothing
   // TMA variants: host addresses of the tensor maps (CUtensorMap) of the buffer,
   // viewed as fields x rows x ncols, and of the transfer functions, viewed as
   // (tables * N) x ncols; the device error word and the wait limit.

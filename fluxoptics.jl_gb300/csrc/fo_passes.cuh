@@ -803,12 +803,20 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
-  const int col0 = blockIdx.y * W;
+  int f0, f1, col0;
+  if (a.units) {  // balanced 1-D list of work units
+    const int4 u = a.units[blockIdx.x];
+    f0 = u.x;
+    f1 = u.y;
+    col0 = u.z * W;
+  } else {
+    f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
+    f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
+    col0 = blockIdx.y * W;
+  }
   const int col = col0 + c;
   const bool col_ok = col < a.ncols;
   const int y_in = a.y_in, y_out = a.y_out;
-  const int f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
-  const int f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
   auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
   const int nbox = (y_in + BOX - 1) / BOX;
   const unsigned tile_bytes = (unsigned)(nbox * BOX * W * sizeof(float2));
@@ -1020,8 +1028,15 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     constexpr size_t smem_t = 128 + sizeof(float2) * ((size_t)2 * N * W + (size_t)W * SmemSize<N>::value) + 16;
     static_assert(smem_t <= kMaxSmemPerCta, "TMA column variant does not fit");
     (void)pf;
-    if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
     e = set_smem(col_tma_kernel<N, E, W, TWR>, smem_t);
+    if (a.occupancy_out) {
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(a.occupancy_out, col_tma_kernel<N, E, W, TWR>, threads,
+                                                          smem_t);
+      return e;
+    }
+    if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
+    if (a.units) grid = dim3(a.n_units, 1);
     if (e == cudaSuccess)
       e = launch_pass(col_tma_kernel<N, E, W, TWR>, grid, dim3(threads), smem_t, s, a, tw,
                       *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),

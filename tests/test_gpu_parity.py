@@ -211,6 +211,42 @@ def test_chain_gradients(fo, orc, kind, d):
     assert orc.rel_l2(npy(grads[c0]["phi"]), g0) < GRAD_TOL
 
 
+def test_balanced_column_units(fo, orc, monkeypatch):
+    """A 2048^2 batch whose column CTAs leave the last round partly empty: the TMA
+    column pass runs over balanced work units (the last round's field runs cut
+    short).  Each field-strip is transformed the same way whichever CTA takes it, so
+    the result equals the plain 2-D launch bit for bit, and the oracle to FIELD_TOL."""
+    import ctypes as C
+    rng = np.random.default_rng(40)
+    n, B = 2048, 16
+    ds, lam, z = (0.5, 0.5), 0.64, 5000.0
+    x, y = orc.spatial_vectors((n, n), ds)
+    base = orc.gaussian(80.0, x, y)
+    u0 = c64(np.stack([base * np.exp(1j * 0.3 * k * x / 80.0) for k in range(B)])
+             * (1 + 0.05 * rng.standard_normal((1, n, n))))
+    lib = fo.load_library()
+
+    def run(units):
+        monkeypatch.setenv("FO_COL_UNITS", "1" if units else "0")
+        u = fo.ScalarField(u0, ds, lam)
+        prop = fo.ASProp(u, z)
+        plan = prop.plan_for(u)
+        name = C.create_string_buffer(200)
+        fo._capi.check(lib.fo_prop_variants(plan, None, None, None, name, 200))
+        prop.propagate_(u)
+        torch.cuda.synchronize()
+        return npy(u.electric), name.value.decode()
+
+    got, name = run(True)
+    ref, name0 = run(False)
+    if "balanced work units" not in name:
+        pytest.skip(f"this launch shape fills its last round: {name}")
+    assert "balanced" not in name0
+    assert np.array_equal(got, ref)
+    for b in (0, B - 1):
+        assert orc.rel_l2(got[b], orc.asprop(u0[b], ds[0], ds[1], lam, z, 1)) < FIELD_TOL
+
+
 @pytest.mark.parametrize("n", [16, 64, 256, 512])
 @pytest.mark.parametrize("kind", ["AS", "RS"])
 @pytest.mark.parametrize("uneven", [False, True])
