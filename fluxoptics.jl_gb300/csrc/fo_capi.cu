@@ -258,6 +258,7 @@ struct fo_prop_plan_s {
   std::vector<int> items_host;  // the same offsets on the host
   int4* units = nullptr;        // device, balanced column work units of the TMA variants (or null)
   int n_units = 0;
+  int col_ctas = 0;             // persistent column launch: CTAs taking every col_ctas-th unit (0: off)
   int row_v = 0, col_v = 0;     // launch-shape variants (autotuned or default)
   bool row_pf = true, col_pf = true;
   unsigned int* err_word = nullptr;         // device error word (bounded waits)
@@ -466,6 +467,7 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.field_list = p->sorted_fields;
   a.units = p->units;
   a.n_units = p->n_units;
+  a.persistent = p->col_ctas;
   a.item_start = p->items;
   a.n_items = p->n_items;
   int v = p->col_v;
@@ -723,6 +725,7 @@ int build_col_units(fo_prop_plan p) {
   cudaFree(p->units);
   p->units = nullptr;
   p->n_units = 0;
+  p->col_ctas = 0;
   if (!col_variant_uses_tma(p->fy, p->col_v) || env_int("FO_COL_UNITS", 1) == 0) return FO_OK;
   const int W = col_variant(p->fy, p->col_v).lanes;
   ColPassArgs q;
@@ -742,16 +745,20 @@ int build_col_units(fo_prop_plan p) {
   for (int st = 0; st < strips; ++st)
     for (int i = 0; i < p->n_items; ++i) units.push_back(make_int4(p->items_host[i], p->items_host[i + 1], st, 0));
   const int total = (int)units.size();
+  if (total <= slots) return FO_OK;  // a single round: the 2-D launch
   const int tail = total % slots;
-  if (total <= slots || tail == 0) return FO_OK;  // no partial last round
-  std::vector<int4> last(units.end() - tail, units.end());
-  units.resize(total - tail);
-  const int pieces = std::max(1, slots / tail);
-  for (const int4& u : last) {
-    const int len = u.y - u.x;
-    const int k = std::min(pieces, len);
-    for (int j = 0; j < k; ++j) units.push_back(make_int4(u.x + j * len / k, u.x + (j + 1) * len / k, u.z, 0));
+  if (tail != 0) {  // cut the partly filled last round into shorter runs
+    std::vector<int4> last(units.end() - tail, units.end());
+    units.resize(total - tail);
+    const int pieces = std::max(1, slots / tail);
+    for (const int4& u : last) {
+      const int len = u.y - u.x;
+      const int k = std::min(pieces, len);
+      for (int j = 0; j < k; ++j) units.push_back(make_int4(u.x + j * len / k, u.x + (j + 1) * len / k, u.z, 0));
+    }
   }
+  // one CTA per slot walks its share of the units, prefetching across unit boundaries
+  if (env_int("FO_COL_PERSIST", 1) != 0) p->col_ctas = slots;
   int rc = dalloc(&p->units, units.size(), "column work units");
   if (rc != FO_OK) return rc;
   cudaError_t e = cudaMemcpy(p->units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice);
@@ -1213,7 +1220,8 @@ FO_API int fo_prop_variants(fo_prop_plan plan, int* row_v, int* col_v, char* row
                                  : (plan->col_pf ? "col_pass_kernel (cp.async staging)" : "col_pass_kernel");
   put(col_kernel, std::string(form) + "<" + std::to_string(plan->fy) + ", E=" + std::to_string(cv.E) +
                       ", columns/CTA=" + std::to_string(cv.lanes) + ">" +
-                      (plan->units ? " over " + std::to_string(plan->n_units) + " balanced work units" : ""));
+                      (plan->units ? " over " + std::to_string(plan->n_units) + " balanced work units" : "") +
+                      (plan->col_ctas ? " in " + std::to_string(plan->col_ctas) + " persistent CTAs" : ""));
   return FO_OK;
 }
 

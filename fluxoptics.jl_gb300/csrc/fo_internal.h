@@ -94,6 +94,7 @@ struct ColPassArgs {
   // field_list), strip, 0}; the grid is then (n_units, 1)
   const int4* units;
   int n_units;
+  int persistent;         // with units: launch this many CTAs, each taking every persistent-th unit (0: one per unit)
   int* occupancy_out;     // when set, the launcher stores the variant's CTAs per SM and launches nothing
   // TMA variants: host addresses of the tensor maps (CUtensorMap) of the buffer,
   // viewed as fields x rows x ncols, and of the transfer functions, viewed as

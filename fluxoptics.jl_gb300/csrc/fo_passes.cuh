@@ -803,25 +803,32 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
-  int f0, f1, col0;
-  if (a.units) {  // balanced 1-D list of work units
-    const int4 u = a.units[blockIdx.x];
-    f0 = u.x;
-    f1 = u.y;
-    col0 = u.z * W;
+  // A unit is a run [f0, f1) of field_list positions on the strip starting at col0:
+  // the (item, strip) block of the 2-D launch, or entries of a.units.  With
+  // a.persistent the CTA takes units blockIdx.x, blockIdx.x + gridDim.x, ... and
+  // loads the next unit's first strip and H strip while it finishes the current one.
+  struct Unit {
+    int f0, f1, col0;
+  };
+  auto unit_at = [&](int k) -> Unit {
+    const int4 u = a.units[k];
+    return Unit{u.x, u.y, u.z * W};
+  };
+  Unit U;
+  if (a.units) {
+    U = unit_at(blockIdx.x);
   } else {
-    f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
-    f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
-    col0 = blockIdx.y * W;
+    U.f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
+    U.f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
+    U.col0 = blockIdx.y * W;
   }
-  const int col = col0 + c;
-  const bool col_ok = col < a.ncols;
+  int uk = blockIdx.x;
   const int y_in = a.y_in, y_out = a.y_out;
   auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
   const int nbox = (y_in + BOX - 1) / BOX;
   const unsigned tile_bytes = (unsigned)(nbox * BOX * W * sizeof(float2));
 
-  auto issue_tile = [&](int f) {  // one thread
+  auto issue_tile = [&](int f, int col0) {  // one thread
     mbar_expect_tx(&bar[0], tile_bytes);
     if (a.test_skip_copy) return;
     const int fz = field_of(f);
@@ -829,6 +836,14 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       tma_load_4d(stage, &tm_buf, col0, 0, 0, fz, &bar[0]);
     else
       for (int k = 0; k < nbox; ++k) tma_load_3d(stage + k * BOX * W, &tm_buf, col0, k * BOX, fz, &bar[0]);
+  };
+  auto issue_h = [&](const Unit& u) {  // one thread
+    mbar_expect_tx(&bar[1], (unsigned)(N * W * sizeof(float2)));
+    const int hz = a.h_index[field_of(u.f0)];
+    if (a.tile4d)
+      tma_load_4d(hs, &tm_h, u.col0, 0, 0, hz, &bar[1]);
+    else
+      for (int k = 0; k < N / BOX; ++k) tma_load_2d(hs + k * BOX * W, &tm_h, u.col0, hz * N + k * BOX, &bar[1]);
   };
   const int nbox_out = (y_out + BOX - 1) / BOX;
   if (threadIdx.x == 0) {
@@ -839,15 +854,8 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (!a.fft_only) {
-      mbar_expect_tx(&bar[1], (unsigned)(N * W * sizeof(float2)));
-      const int hy0 = a.h_index[field_of(f0)] * N;
-      if (a.tile4d)
-        tma_load_4d(hs, &tm_h, col0, 0, 0, a.h_index[field_of(f0)], &bar[1]);
-      else
-        for (int k = 0; k < N / BOX; ++k) tma_load_2d(hs + k * BOX * W, &tm_h, col0, hy0 + k * BOX, &bar[1]);
-    }
-    if (f0 < f1) issue_tile(f0);
+    if (!a.fft_only) issue_h(U);
+    if (U.f0 < U.f1) issue_tile(U.f0, U.col0);
   }
   float2 wr[TwRegs<N, E>::size];
   if constexpr (TWR) load_twiddles<N, E>(wr, t, tw);
@@ -858,69 +866,96 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
       fft_forward<N, E, W>(x, t, tw, ex + c);
   };
   bool ok = true;
-  if (!a.fft_only) ok = mbar_wait_bounded(&bar[1], 0, a.wait_ns);
-  unsigned phase = 0;
+  unsigned phase = 0, hphase = 0;
   const float hsign = a.conj_h ? -1.f : 1.f;
 
-  for (int f = f0; f < f1; ++f) {
-    const unsigned wait_phase = phase;
-    if (ok) ok = mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
-    phase ^= 1u;
-    if (!ok) s_abort = 1;
-    float2 v[E];
-#pragma unroll
-    for (int i = 0; i < E; ++i) {
-      const int p = t + i * T;
-      v[i] = (col_ok && p < y_in) ? stage[p * W + c] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();  // the staging buffer is free again; abort decision is uniform
-    if (s_abort) {
-      if (threadIdx.x == 0) {
-        atomicOr(a.err_word, 1u);
-        // let copies still in flight land (bounded) before the CTA's memory is released
-        if (!a.test_skip_copy) mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
-        bulk_wait_all();
-      }
-      return;
-    }
-    if (threadIdx.x == 0 && f + 1 < f1) {
-      fence_proxy_async();
-      issue_tile(f + 1);
-    }
-    // First transform.  Its radix-E stage runs in registers; only then does thread 0
-    // wait until the previous field's result tile has been read out of `ex` (the
-    // TMA store), and the first exchange's barrier publishes that to every thread.
-    Dft<E>::run(v, 0);
-    if (threadIdx.x == 0) bulk_wait_read_all();
-    if constexpr (TWR)
-      stages_from_r<N, E, 1, W>(v, t, wr, ex + c, 0, 0);
-    else
-      stages_from<N, E, 1, W>(v, t, tw, ex + c, 0, 0);
-    fft_last_stage_order<E>(v);
+  while (true) {
     if (!a.fft_only) {
+      if (ok) ok = mbar_wait_bounded(&bar[1], hphase, a.wait_ns);
+      hphase ^= 1u;
+    }
+    const bool col_ok = U.col0 + c < a.ncols;
+    const bool has_next = a.persistent && a.units && uk + (int)gridDim.x < a.n_units;
+    Unit Un = U;
+    if (has_next) Un = unit_at(uk + gridDim.x);
+
+    for (int f = U.f0; f < U.f1; ++f) {
+      const unsigned wait_phase = phase;
+      if (ok) ok = mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
+      phase ^= 1u;
+      if (!ok) s_abort = 1;
+      float2 v[E];
 #pragma unroll
       for (int i = 0; i < E; ++i) {
-        float2 hv = hs[(t + i * T) * W + c];
-        hv.y *= hsign;
-        // conj(X * H): the inverse transform runs as conj(FFT(conj(.)))
-        v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
+        const int p = t + i * T;
+        v[i] = (col_ok && p < y_in) ? stage[p * W + c] : make_float2(0.f, 0.f);
       }
-      fft(v);
-    }
-    const float osign = a.fft_only ? 1.f : -1.f;
-    __syncthreads();  // the last stage has read `ex`
-#pragma unroll
-    for (int i = 0; i < E; ++i) ex[(t + i * T) * W + c] = make_float2(v[i].x, osign * v[i].y);
-    fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0 && !a.test_skip_copy) {
-      const int fz = field_of(f);
-      if (a.tile4d)
-        tma_store_4d(&tm_buf, col0, 0, 0, fz, ex);
+      __syncthreads();  // the staging buffer is free again; abort decision is uniform
+      if (s_abort) {
+        if (threadIdx.x == 0) {
+          atomicOr(a.err_word, 1u);
+          // let copies still in flight land (bounded) before the CTA's memory is released:
+          // this field's strip and the current unit's H strip
+          if (!a.test_skip_copy) mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
+          if (!a.fft_only) mbar_wait_bounded(&bar[1], hphase ^ 1u, a.wait_ns);
+          bulk_wait_all();
+        }
+        return;
+      }
+      if (threadIdx.x == 0) {
+        if (f + 1 < U.f1) {
+          fence_proxy_async();
+          issue_tile(f + 1, U.col0);
+        } else if (has_next) {
+          fence_proxy_async();
+          issue_tile(Un.f0, Un.col0);
+        }
+      }
+      // First transform.  Its radix-E stage runs in registers; only then does thread 0
+      // wait until the previous field's result tile has been read out of `ex` (the
+      // TMA store), and the first exchange's barrier publishes that to every thread.
+      Dft<E>::run(v, 0);
+      if (threadIdx.x == 0) bulk_wait_read_all();
+      if constexpr (TWR)
+        stages_from_r<N, E, 1, W>(v, t, wr, ex + c, 0, 0);
       else
-        for (int k = 0; k < nbox_out; ++k) tma_store_3d(&tm_buf, col0, k * BOX, fz, ex + k * BOX * W);
-      bulk_commit();
+        stages_from<N, E, 1, W>(v, t, tw, ex + c, 0, 0);
+      fft_last_stage_order<E>(v);
+      if (!a.fft_only) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          float2 hv = hs[(t + i * T) * W + c];
+          hv.y *= hsign;
+          // conj(X * H): the inverse transform runs as conj(FFT(conj(.)))
+          v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
+        }
+        if (f + 1 == U.f1 && has_next) {
+          __syncthreads();  // every thread has read this unit's H strip
+          if (threadIdx.x == 0) {
+            fence_proxy_async();
+            issue_h(Un);
+          }
+        }
+        fft(v);
+      }
+      const float osign = a.fft_only ? 1.f : -1.f;
+      __syncthreads();  // the last stage has read `ex`
+#pragma unroll
+      for (int i = 0; i < E; ++i) ex[(t + i * T) * W + c] = make_float2(v[i].x, osign * v[i].y);
+      fence_proxy_async();
+      __syncthreads();
+      if (threadIdx.x == 0 && !a.test_skip_copy) {
+        const int fz = field_of(f);
+        if (a.tile4d)
+          tma_store_4d(&tm_buf, U.col0, 0, 0, fz, ex);
+        else
+          for (int k = 0; k < nbox_out; ++k) tma_store_3d(&tm_buf, U.col0, k * BOX, fz, ex + k * BOX * W);
+        bulk_commit();
+      }
     }
+    if (!has_next) break;
+    U = Un;
+    uk += gridDim.x;
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }
@@ -1036,7 +1071,7 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
       return e;
     }
     if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
-    if (a.units) grid = dim3(a.n_units, 1);
+    if (a.units) grid = dim3(a.persistent ? std::min(a.persistent, a.n_units) : a.n_units, 1);
     if (e == cudaSuccess)
       e = launch_pass(col_tma_kernel<N, E, W, TWR>, grid, dim3(threads), smem_t, s, a, tw,
                       *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
