@@ -434,18 +434,56 @@ __global__ void sid_bwd_kernel(const float2* u, const float* resid, const int* t
 // Fista / Clamp
 // ---------------------------------------------------------------------------
 
+// One Fista step, optionally followed by clamp(x, lo, hi).  beta comes from the FP64
+// t state once per block (FP64 is a slow pipe on this part); four floats per thread
+// and iteration where the arrays allow it.
+__device__ __forceinline__ float fista_one(float xv, float xkv, float dxv, float e, float beta, float* nd_out) {
+  const float nd = e * dxv - beta * (xv - xkv);
+  *nd_out = nd;
+  return xv - nd;
+}
+
 __global__ void fista_kernel(float* x, float* xk, float* newdx, const float* dx, long long n, float e,
-                             const double* t_state) {
-  const double t = *t_state;
-  const double tn = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
-  const float beta = (float)((t - 1.0) / tn);
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-       q += (long long)gridDim.x * blockDim.x) {
+                             const double* t_state, int clamp, float lo, float hi) {
+  __shared__ float s_beta;
+  if (threadIdx.x == 0) {
+    const double t = *t_state;
+    const double tn = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
+    s_beta = (float)((t - 1.0) / tn);
+  }
+  __syncthreads();
+  const float beta = s_beta;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const bool vec = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(xk) |
+                     reinterpret_cast<uintptr_t>(dx) | reinterpret_cast<uintptr_t>(newdx)) & 15) == 0;
+  const long long n4 = vec ? n / 4 : 0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n4; q += stride) {
+    const float4 xv = reinterpret_cast<const float4*>(x)[q];
+    const float4 kv = reinterpret_cast<const float4*>(xk)[q];
+    const float4 dv = reinterpret_cast<const float4*>(dx)[q];
+    float4 nd, xo;
+    xo.x = fista_one(xv.x, kv.x, dv.x, e, beta, &nd.x);
+    xo.y = fista_one(xv.y, kv.y, dv.y, e, beta, &nd.y);
+    xo.z = fista_one(xv.z, kv.z, dv.z, e, beta, &nd.z);
+    xo.w = fista_one(xv.w, kv.w, dv.w, e, beta, &nd.w);
+    if (clamp) {
+      xo.x = fminf(fmaxf(xo.x, lo), hi);
+      xo.y = fminf(fmaxf(xo.y, lo), hi);
+      xo.z = fminf(fmaxf(xo.z, lo), hi);
+      xo.w = fminf(fmaxf(xo.w, lo), hi);
+    }
+    if (newdx) reinterpret_cast<float4*>(newdx)[q] = nd;
+    reinterpret_cast<float4*>(xk)[q] = xv;
+    reinterpret_cast<float4*>(x)[q] = xo;
+  }
+  for (long long q = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += stride) {
     const float xv = x[q];
-    const float nd = e * dx[q] - beta * (xv - xk[q]);
+    float nd;
+    float xo = fista_one(xv, xk[q], dx[q], e, beta, &nd);
+    if (clamp) xo = fminf(fmaxf(xo, lo), hi);
     if (newdx) newdx[q] = nd;
     xk[q] = xv;
-    x[q] = xv - nd;
+    x[q] = xo;
   }
 }
 
@@ -710,8 +748,9 @@ cudaError_t launch_sid_bwd(const float2* u, const float* resid, const int* tidx,
 }
 
 cudaError_t launch_fista(float* x, float* xk, float* newdx, const float* dx, long long n, float e,
-                         double* t_state, cudaStream_t st) {
-  fista_kernel<<<capped_grid(n), kThreads, 0, st>>>(x, xk, newdx, dx, n, e, t_state);
+                         double* t_state, cudaStream_t st, int clamp,
+                         float lo, float hi) {
+  fista_kernel<<<capped_grid((n + 3) / 4), kThreads, 0, st>>>(x, xk, newdx, dx, n, e, t_state, clamp, lo, hi);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   fista_t_kernel<<<1, 1, 0, st>>>(t_state);

@@ -45,7 +45,8 @@ cudaError_t launch_sid_bwd(const float2* u, const float* resid, const int* tidx,
                            long long npix, int batch, float2* du, cudaStream_t st);
 
 cudaError_t launch_fista(float* x, float* xk, float* newdx, const float* dx, long long n, float e,
-                         double* t_state, cudaStream_t st);
+                         double* t_state, cudaStream_t st, int clamp = 0,
+                         float lo = 0.f, float hi = 0.f);
 cudaError_t launch_clamp(float* x, long long n, float lo, float hi, cudaStream_t st);
 
 size_t tv_state_bytes();

@@ -1734,6 +1734,15 @@ FO_API int fo_fista_step(float* x, float* xk, float* newdx, const float* dx, lon
   return FO_OK;
 }
 
+FO_API int fo_fista_clamp_step(float* x, float* xk, float* newdx, const float* dx, long long n, double eta,
+                               double* t_state, double lo, double hi, void* stream) {
+  if (!x || !xk || !dx || !t_state) return fail(FO_ERR_ARG, "x, xk, dx and t_state must not be NULL");
+  if (n <= 0) return fail(FO_ERR_SHAPE, "n must be positive");
+  if (!(lo <= hi)) return fail(FO_ERR_ARG, "lo must not exceed hi");
+  FO_LAUNCH(launch_fista(x, xk, newdx, dx, n, (float)(eta * eta), t_state, S(stream), 1, (float)lo, (float)hi));
+  return FO_OK;
+}
+
 FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream) {
   if (!x) return fail(FO_ERR_ARG, "x must not be NULL");
   if (n <= 0) return fail(FO_ERR_SHAPE, "n must be positive");

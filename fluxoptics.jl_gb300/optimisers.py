@@ -91,6 +91,12 @@ class ProxRule:
         return {"rule": self.rule.init(x), "prox": self.prox.init(x)}
 
     def apply_(self, state, x, dx):
+        if isinstance(self.rule, Fista) and isinstance(self.prox, ClampProx) and x.dtype == torch.float32:
+            # the clamp rides in the Fista pass (fo_fista_clamp_step)
+            r = state["rule"]
+            _capi.call("fo_fista_clamp_step", _ptr(x), _ptr(r["xk"]), _ptr(r["newdx"]), _ptr(dx), x.numel(),
+                       self.rule.eta, _ptr(r["t"]), self.prox.lo, self.prox.hi, _stream())
+            return
         self.rule.apply_(state["rule"], x, dx)
         self.prox.apply_(state["prox"], x)
 

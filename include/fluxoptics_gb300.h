@@ -430,6 +430,12 @@ FO_API int fo_sid_loss_noalloc(const void* u, const float* target, const int* ta
 FO_API int fo_fista_step(float* x, float* xk, float* newdx, const float* dx, long long n,
                          double eta, double* t_state, void* stream);
 
+/* fo_fista_step followed by x = clamp(x, lo, hi), in one pass over the arrays.
+ * Replaces: ProxRule(Fista(eta), ClampProx(lo, hi)) -- src/OptimisersExt.jl:222-244 with
+ * proximal_operators/clamp_prox.jl:35-37. */
+FO_API int fo_fista_clamp_step(float* x, float* xk, float* newdx, const float* dx, long long n,
+                               double eta, double* t_state, double lo, double hi, void* stream);
+
 /* x = clamp(x, lo, hi).  Replaces ClampProx (proximal_operators/clamp_prox.jl:35-37). */
 FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream);
 
