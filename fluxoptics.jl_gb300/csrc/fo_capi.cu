@@ -382,6 +382,13 @@ int validate_mod(const Mod& m, bool backward) {
   return FO_OK;
 }
 
+// Fields a CTA of a row pass without a gradient loops over (the gradient passes take
+// the whole batch): the per-pixel modulation factor is computed once per CTA.
+int row_fields_per_cta() {
+  static const int v = std::max(1, std::min(64, env_int("FO_ROW_FIELDS", 16)));
+  return v;
+}
+
 // One row pass.  `src`/`dst` are real-space (ld nx) or spectral (ld fx) arrays as
 // selected by the inv/fwd flags.
 int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bool fwd_after,
@@ -400,7 +407,7 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
   a.n_valid = L.nx;
   a.batch = L.batch;
   const bool grad = bwd && mod.kind != MOD_NONE && mod.grad != nullptr;
-  a.fields_per_cta = grad ? L.batch : std::min(L.batch, 8);
+  a.fields_per_cta = grad ? L.batch : std::min(L.batch, row_fields_per_cta());
   a.field_list = nullptr;
   a.inv_first = inv_first;
   a.fwd_after = fwd_after;
