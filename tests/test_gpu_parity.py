@@ -649,6 +649,28 @@ def test_fista_clamp_tv(fo, orc):
         orc.fista_apply(0.3, so, xo, g)
         orc.clamp_prox(xo, -0.5, 0.7)
         assert orc.rel_l2(npy(xs), xo) < 1e-5
+    # plain Fista (the float4 body and the scalar tail), and the clamp fused into the
+    # Fista pass equal to Fista followed by ClampProx
+    for shape in ((64, 48), (37, 53)):
+        x1 = f32(rng.standard_normal(shape))
+        a, b, c = (torch.tensor(x1, dtype=torch.float32, device="cuda") for _ in range(3))
+        fa, fb = fo.Fista(0.2), fo.Fista(0.2)
+        sa, sb = fa.init(a), fb.init(b)
+        clamp = fo.ClampProx(-0.4, 0.6)
+        fused = fo.ProxRule(fo.Fista(0.2), clamp)
+        sc = fused.init(c)
+        xo = x1.copy()
+        so = orc.FistaState(xo)
+        for it in range(4):
+            g = f32(rng.standard_normal(shape))
+            gt = torch.tensor(g, dtype=torch.float32, device="cuda")
+            fa.apply_(sa, a, gt)
+            orc.fista_apply(0.2, so, xo, g)
+            assert orc.rel_l2(npy(a), xo) < 1e-5
+            fb.apply_(sb, b, gt)
+            clamp.apply_(None, b)
+            fused.apply_(sc, c, gt)
+            assert np.array_equal(npy(b), npy(c))
     for iso in (True, False):
         y0 = f32(rng.standard_normal((40, 30)))
         yt = torch.tensor(y0, dtype=torch.float32, device="cuda")
