@@ -644,7 +644,7 @@ int autotune_plan(fo_prop_plan p) {
       a.nrows = p->ny;
       a.n_valid = p->nx;
       a.batch = nb;
-      a.fields_per_cta = std::min(nb, 8);
+      a.fields_per_cta = std::min(nb, row_fields_per_cta());
       a.inv_first = 1;
       a.fwd_after = 1;
       int trc = FO_OK;
