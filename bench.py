@@ -335,6 +335,10 @@ def run_gb300(args, rank, world):
         e2e_compute_ms = statistics.median(a.elapsed_time(b) for a, b in ev_step)
         # input copies made while a step computes (the last step has none)
         e2e_copy_ms = statistics.median(a.elapsed_time(b) for a, b in ev_copy[:-1]) if e2_steps > 1 else None
+        # start / end (ms from the start of the e2e region) of the first steps' compute
+        # and of the input copies made meanwhile: shows whether the copies overlapped
+        e2e_timeline = [[round(e2.elapsed_time(ev), 2) for ev in (*ev_step[k], *(ev_copy[k] if k + 1 < e2_steps else ()))]
+                        for k in range(min(4, e2_steps))]
         fo._capi.check(lib.fo_graph_destroy(g_b))
         fo._capi.check(lib.fo_graph_destroy(g))
 
@@ -376,6 +380,8 @@ def run_gb300(args, rank, world):
                 "overlap": "input copy of step k+1 on a copy stream overlaps the compute of step k",
                 "compute_ms_per_step": round(e2e_compute_ms, 4),
                 "copy_ms_per_step": round(e2e_copy_ms, 4) if e2e_copy_ms is not None else None,
+                "timeline_ms": {"steps": "[compute start, compute end, next input copy start, copy end]",
+                                "first_steps": e2e_timeline},
                 "h2d_gbs_measured": round(h2d_gbs, 1)},
         "clocks": clk.summary(),
         "final_loss": final_loss,
