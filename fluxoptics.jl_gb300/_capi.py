@@ -96,6 +96,7 @@ SIGNATURES = {
     "fo_sid_backward": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "fo_sid_loss_noalloc": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp]),
     "fo_fista_step": (_i, [_vp, _vp, _vp, _vp, _ll, _d, _vp, _vp]),
+    "fo_copy": (_i, [_vp, _vp, C.c_size_t, _vp]),
     "fo_fista_clamp_step": (_i, [_vp, _vp, _vp, _vp, _ll, _d, _vp, _d, _d, _vp]),
     "fo_clamp": (_i, [_vp, _ll, _d, _d, _vp]),
     "fo_tv_create": (_i, [C.POINTER(_vp), _i, _i, _d, _i, _i, _d]),

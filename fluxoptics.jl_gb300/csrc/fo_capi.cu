@@ -1826,6 +1826,13 @@ struct fo_graph_s {
 
 extern "C" {
 
+FO_API int fo_copy(void* dst, const void* src, size_t bytes, void* stream) {
+  if (bytes == 0) return FO_OK;
+  if (!dst || !src) return fail(FO_ERR_ARG, "dst and src must not be NULL");
+  FO_LAUNCH(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, S(stream)));
+  return FO_OK;
+}
+
 FO_API int fo_graph_begin(void* stream) {
   if (!stream) return fail(FO_ERR_ARG, "graph capture needs a non-default stream");
   FO_LAUNCH(cudaStreamBeginCapture(S(stream), cudaStreamCaptureModeThreadLocal));

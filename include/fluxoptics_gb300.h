@@ -455,6 +455,15 @@ FO_API int fo_tv_apply(fo_tv tv, float* x, void* stream);
 /* CUDA graphs of whole iterations                                         */
 /* ---------------------------------------------------------------------- */
 
+/*
+ * Stream-ordered copy of `bytes` between host and device memory, either
+ * direction (the pointers decide).  With page-locked host memory it is
+ * asynchronous and can be captured into a graph.  It lets a host without CUDA
+ * bindings upload fields and read results back through this library.
+ * No counterpart in the reference (Julia moves data with CuArray / Array).
+ */
+FO_API int fo_copy(void* dst, const void* src, size_t bytes, void* stream);
+
 typedef struct fo_graph_s* fo_graph;
 FO_API int fo_graph_begin(void* stream);
 FO_API int fo_graph_end(void* stream, fo_graph* graph);
