@@ -764,8 +764,11 @@ int build_col_units(fo_prop_plan p) {
       for (int j = 0; j < k; ++j) units.push_back(make_int4(u.x + j * len / k, u.x + (j + 1) * len / k, u.z, 0));
     }
   }
-  // one CTA per slot walks its share of the units, prefetching across unit boundaries
-  if (env_int("FO_COL_PERSIST", 1) != 0) p->col_ctas = slots;
+  // One CTA per SM walks its share of the units, prefetching across unit
+  // boundaries.  Only for shapes that fill an SM with one CTA: at 2048^2 with
+  // 2-column strips (two CTAs per SM) the persistent walk measured 1.96 vs 1.06 ms,
+  // while the hardware's own dispatch of the units is fine at any occupancy.
+  if (occ == 1 && env_int("FO_COL_PERSIST", 1) != 0) p->col_ctas = slots;
   int rc = dalloc(&p->units, units.size(), "column work units");
   if (rc != FO_OK) return rc;
   cudaError_t e = cudaMemcpy(p->units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice);
