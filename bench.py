@@ -372,6 +372,8 @@ def run_gb300(args, rank, world):
                 "overlap": "each step is one graph: the iteration, and on a parallel branch the "
                            "upload of the next step's input (fo_copy from pinned memory)",
                 "step_ms": round(e2e_step_ms, 4), "copy_alone_ms": round(copy_alone_ms, 4),
+                # the rate of the median step, for runs where a few uploads stalled on the host side
+                "median_step_value": round(props_per_step / (e2e_step_ms * 1e-3), 1),
                 "timeline_ms": {"steps": "[step start, step end]", "first_steps": e2e_timeline},
                 "h2d_gbs_measured": round(h2d_gbs, 1)},
         "clocks": clk.summary(),
