@@ -93,3 +93,10 @@ def test_bad_arguments_are_rejected(capi):
     assert "alias" in lib.fo_last_error().decode()
     assert lib.fo_ragged_create(C.byref(h), probs, 0, 0) == 1
     assert lib.fo_fista_step(None, None, None, None, 10, 0.1, None, None) == 1
+    assert lib.fo_fista_clamp_step(None, None, None, None, 10, 0.1, None, 0.0, 1.0, None) == 1
+    p = C.c_void_p(16)
+    assert lib.fo_fista_clamp_step(p, p, p, p, 10, 0.1, p, 1.0, 0.0, None) == 1
+    assert "lo must not exceed hi" in lib.fo_last_error().decode()
+    assert lib.fo_chain_forward_sid(None, None, None, None, 1, None, None, None, None) == 1
+    assert lib.fo_copy(None, None, 16, None) == 1
+    assert lib.fo_copy(None, None, 0, None) == 0  # nothing to copy
