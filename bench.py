@@ -326,7 +326,8 @@ def run_gb300(args, rank, world):
             ev_step[k][1].record(stream)
         e3.record(stream)
         stream.synchronize()
-        e2e_ms = e2.elapsed_time(e3) / e2_steps
+        # the slowest rank's time, as for the device-timed value (whole-job rate below)
+        e2e_ms = max_over_ranks(e2.elapsed_time(e3) / e2_steps)
         e2e_step_ms = statistics.median(a.elapsed_time(b) for a, b in ev_step)
         # start / end (ms from the start of the e2e region) of the first steps
         e2e_timeline = [[round(e2.elapsed_time(ev), 2) for ev in ev_step[k]] for k in range(min(4, e2_steps))]
@@ -367,13 +368,13 @@ def run_gb300(args, rank, world):
         "pass_share": {k: round(v, 3) for k, v in pass_share.items()},
         "gpu_launches": int(nk.value) * args.steps,
         "gpu_launches_per_step": int(nk.value),
-        "e2e": {"value": round(props_per_step / (e2e_ms * 1e-3), 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
+        "e2e": {"value": round(job_rate(props_per_step, world, e2e_ms), 1), "unit": UNIT, "ms_per_step": round(e2e_ms, 4),
                 "h2d_bytes_per_step": int(fields_np.nbytes), "d2h_bytes_per_step": int(len(LAMBDAS) * 4),
                 "overlap": "each step is one graph: the iteration, and on a parallel branch the "
                            "upload of the next step's input (fo_copy from pinned memory)",
                 "step_ms": round(e2e_step_ms, 4), "copy_alone_ms": round(copy_alone_ms, 4),
                 # the rate of the median step, for runs where a few uploads stalled on the host side
-                "median_step_value": round(props_per_step / (e2e_step_ms * 1e-3), 1),
+                "median_step_value": round(job_rate(props_per_step, world, e2e_step_ms), 1),
                 "timeline_ms": {"steps": "[step start, step end]", "first_steps": e2e_timeline},
                 "h2d_gbs_measured": round(h2d_gbs, 1)},
         "clocks": clk.summary(),
