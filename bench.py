@@ -189,6 +189,24 @@ def algorithmic_bytes_per_step(n=N, batch=None):
     return props + fwd_phase + adj_phase + h + fista
 
 
+def pass_bytes_per_step(n=N, batch=None):
+    """DRAM bytes the iteration's passes must move: each of the 2K+1 forward and
+    2K+1 adjoint passes reads and writes every field once, plus saves, saved reads,
+    masks, gradients, transfer functions, the metric's target and residual, and Fista.
+    The first mask's adjoint reads the source field (no save); the metric runs inside
+    the last forward pass."""
+    batch = batch or N_MODES * len(LAMBDAS)
+    n2 = n * n
+    fld = 8 * n2 * batch                                    # one c32 copy of the batch
+    col = 2 * fld + len(LAMBDAS) * 8 * n2                   # column pass: field in and out, one H per wavelength
+    fwd_rows = (2 * fld + 4 * n2) + (N_MASKS - 1) * (3 * fld + 4 * n2) \
+        + (2 * fld + 2 * len(LAMBDAS) * 4 * n2)            # source pass, mask passes with saves, last pass + metric
+    adj_rows = (2 * fld + len(LAMBDAS) * 4 * n2) + (N_MASKS - 1) * (3 * fld + 8 * n2) \
+        + (2 * fld + 8 * n2)                               # seed pass, gradient passes, last gradient pass
+    fista = N_MASKS * 6 * 4 * n2
+    return 2 * N_MASKS * col + fwd_rows + adj_rows + fista
+
+
 def col_pass_bytes(n=N, batch=None):
     batch = batch or N_MODES * len(LAMBDAS)
     # one column pass over the batch: every field read and written once, one
@@ -358,6 +376,8 @@ def run_gb300(args, rank, world):
                    "l2": "inputs larger than L2 (1.5 GiB field batch), no flush"},
         "algorithmic_gb_per_step": round(algorithmic_bytes_per_step() / 1e9, 3),
         "algorithmic_gbs": round(algorithmic_bytes_per_step() / (ms * 1e-3) / 1e9, 1),
+        "pass_gb_per_step": round(pass_bytes_per_step() / 1e9, 3),
+        "pass_gbs": round(pass_bytes_per_step() / (ms * 1e-3) / 1e9, 1),
         "roofline": {"bound": "hbm",
                      "kernel": f"column pass {col_name.value.decode()} (FFT_y * H * IFFT_y over {batch} fields)",
                      "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
