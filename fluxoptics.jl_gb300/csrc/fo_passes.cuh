@@ -72,7 +72,8 @@ __device__ __forceinline__ void cp_async_wait() {
 // 3: intensity of the output summed over the CTA's fields for the squared
 // intensity difference, see RowPassArgs::sid_target).
 // PF: stage the next field's row through cp.async (needs load_n == N).
-// Shared memory: 2 * LANES * SLOTS float2 (PF) or LANES * SLOTS float2.
+// Shared memory: 2 * LANES * SLOTS float2 (PF) or LANES * SLOTS float2, plus
+// LANES * N float2 for the modulation-factor cache when GK != 0.
 // --------------------------------------------------------------------------
 // FULL: the row count is a multiple of LANES and n_valid == N, so no
 // per-element guards are needed.
