@@ -23,6 +23,7 @@
 #include "fo_aux.h"
 #include "fo_fft.cuh"
 #include "fo_internal.h"
+#include "fo_units.h"
 
 // ---------------------------------------------------------------------------
 // Errors
@@ -748,27 +749,11 @@ int build_col_units(fo_prop_plan p) {
   }
   const int slots = sms * occ;
   const int strips = (p->fx + W - 1) / W;
+  const std::vector<ColUnit> list = balanced_col_units(p->items_host, strips, slots);
+  if (list.empty()) return FO_OK;  // a single round: the 2-D launch
   std::vector<int4> units;
-  for (int st = 0; st < strips; ++st)
-    for (int i = 0; i < p->n_items; ++i) units.push_back(make_int4(p->items_host[i], p->items_host[i + 1], st, 0));
-  const int total = (int)units.size();
-  if (total <= slots) return FO_OK;  // a single round: the 2-D launch
-  const int tail = total % slots;
-  if (tail != 0) {  // cut the partly filled last round into shorter runs
-    std::vector<int4> last(units.end() - tail, units.end());
-    units.resize(total - tail);
-    const int pieces = std::max(1, slots / tail);
-    for (const int4& u : last) {
-      const int len = u.y - u.x;
-      const int k = std::min(pieces, len);
-      for (int j = 0; j < k; ++j) units.push_back(make_int4(u.x + j * len / k, u.x + (j + 1) * len / k, u.z, 0));
-    }
-  }
-  // One CTA per SM walks its share of the units, prefetching across unit
-  // boundaries.  Only for shapes that fill an SM with one CTA: at 2048^2 with
-  // 2-column strips (two CTAs per SM) the persistent walk measured 1.96 vs 1.06 ms,
-  // while the hardware's own dispatch of the units is fine at any occupancy.
-  if (occ == 1 && env_int("FO_COL_PERSIST", 1) != 0) p->col_ctas = slots;
+  units.reserve(list.size());
+  for (const ColUnit& u : list) units.push_back(make_int4(u.first, u.end, u.strip, 0));
   int rc = dalloc(&p->units, units.size(), "column work units");
   if (rc != FO_OK) return rc;
   cudaError_t e = cudaMemcpy(p->units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice);
@@ -778,6 +763,11 @@ int build_col_units(fo_prop_plan p) {
     return cuda_fail(e, "cudaMemcpy column work units");
   }
   p->n_units = (int)units.size();
+  // One CTA per SM walks its share of the units, prefetching across unit
+  // boundaries.  Only for shapes that fill an SM with one CTA: at 2048^2 with
+  // 2-column strips (two CTAs per SM) the persistent walk measured 1.96 vs 1.06 ms,
+  // while the hardware's own dispatch of the units is fine at any occupancy.
+  if (occ == 1 && env_int("FO_COL_PERSIST", 1) != 0) p->col_ctas = slots;
   return FO_OK;
 }
 
