@@ -371,9 +371,7 @@ def run_gb300(args, rank, world):
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c32 (fp32 complex; fp64 transfer-function phase)",
         "data": "synthetic, seeded (HG modes, Gaussian-filtered random masks and targets)",
-        "config": {"workload": WORKLOAD.format(fields=batch), "grid": N, "fields": batch, "masks": N_MASKS,
-                   "props_per_step": props_per_step, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (1.5 GiB field batch), no flush"},
+        "config": headline_config(batch, world),
         "algorithmic_gb_per_step": round(algorithmic_bytes_per_step() / 1e9, 3),
         "algorithmic_gbs": round(algorithmic_bytes_per_step() / (ms * 1e-3) / 1e9, 1),
         "pass_gb_per_step": round(pass_bytes_per_step() / 1e9, 3),
@@ -484,11 +482,20 @@ def run_plain(steps=3, warmup=1):
 # ---------------------------------------------------------------------------
 # CPU baseline: the FP64 oracle (restatement of the reference path)
 # ---------------------------------------------------------------------------
-def run_cpu_sample(budget_s=12.0, threads=None):
+def headline_config(batch, world):
+    """The `config` object of the headline workload, shared by both bench arms."""
+    return {"workload": WORKLOAD.format(fields=batch), "grid": N, "fields": batch, "masks": N_MASKS,
+            "props_per_step": 2 * N_MASKS * batch, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (1.5 GiB field batch), no flush"}
+
+
+def run_cpu_sample(budget_s=12.0, threads=None, inputs=None):
+    """The FP64 oracle on the host cores: repetitions of one field of the batch through
+    the chain, forward + adjoint, until budget_s has passed (at least one)."""
     from oracle import fluxoptics_oracle as orc
     threads = threads or os.cpu_count() or 1
     orc.set_workers(threads)
-    fields_np, masks_np, targets_np = make_inputs()
+    fields_np, masks_np, targets_np = inputs if inputs is not None else make_inputs()
     u0 = fields_np[0, 0].astype(np.complex128)      # HG00 at lambda = 0.640 um
     lam = LAMBDAS[0]
     phis = [m.astype(np.float64) for m in masks_np]
@@ -509,6 +516,7 @@ def run_cpu_sample(budget_s=12.0, threads=None):
         if el > budget_s or reps >= 50:
             break
     return {"value": round(2 * N_MASKS * reps / el, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "seconds_per_rep": el / reps,
             "sample": f"{reps} x (1 of 48 fields, HG00 at 0.640 um, 2048^2) through the 3-mask chain, "
                       f"forward + adjoint, FP64 numpy/scipy.fft with {threads} workers, {el:.1f} s"}
 
@@ -715,24 +723,36 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        vals = []
-        run_cpu_sample(budget_s=0.0)  # warm-up: one repetition
-        samples = []
+        # One step = one sample: 1 of the 48 fields through the 3-mask chain, forward +
+        # adjoint (6 propagations).  Every propagation of the workload costs the same, so
+        # the per-propagation rate of the sample is the workload's rate.  `steps` counts
+        # the samples actually timed and `ms_per_step` is the median time of one sample.
+        inputs = make_inputs()
+        for _ in range(max(1, args.warmup)):
+            run_cpu_sample(budget_s=0.0, inputs=inputs)
+        samples, secs = [], []
         for _ in range(args.steps):
-            s = run_cpu_sample(budget_s=max(2.0, 60.0 / max(1, args.steps)))
-            samples.append(s)
-            vals.append(s["value"])
-        v = statistics.median(vals)
+            smp = run_cpu_sample(budget_s=0.0, inputs=inputs)
+            secs.append(smp.pop("seconds_per_rep"))  # the sample's own timed repetition
+            samples.append(smp)
+        props_per_sample = 2 * N_MASKS
+        sec = statistics.median(secs)
+        v = round(props_per_sample / sec, 3)
         cpu = dict(samples[0])
         cpu["value"] = v
+        cpu["sample"] = (f"per step: 1 of 48 fields (HG00 at 0.640 um, 2048^2) through the 3-mask chain, forward + "
+                         f"adjoint = {props_per_sample} propagations, FP64 numpy/scipy.fft with {cpu['cores']} workers")
+        config = headline_config(48, world)
+        config["sample"] = "1 of 48 fields per step (6 of the 288 propagations of the workload)"
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(2 * N_MASKS * 48 / v * 1e3, 1),
+                "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": round(sec * 1e3, 1),
+                "props_per_sample": props_per_sample, "total_timed_s": round(sum(secs), 2),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)",
-                "data": "synthetic, seeded", "config": {"workload": WORKLOAD.format(fields=48), "grid": N, "fields": 48},
+                "data": "synthetic, seeded", "config": config,
                 "cpu_baseline": cpu,
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "Julia is absent on this box: the reference arm is the FP64 oracle restatement of the "
-                        "reference's CPU path (FFTW replaced by pocketfft), timed on a bounded sample"}
+                        "reference's CPU path (FFTW replaced by pocketfft), one field of the batch per step"}
         print(json.dumps(line))
         return
 
@@ -751,6 +771,7 @@ def main():
             line["speedup_vs_plain_cufft"] = round(line["value"] / line["plain_cufft"]["value"] / world, 2)
         if not args.no_cpu and world == 1:
             line["cpu_baseline"] = run_cpu_sample()
+            line["cpu_baseline"].pop("seconds_per_rep", None)
             one = run_cpu_sample(budget_s=6.0, threads=1)
             line["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": one["unit"], "cores": 1,
                                                      "sample": one["sample"]}

@@ -1,9 +1,9 @@
 // SquaredIntensityDifference loss for callers that cannot allocate device memory.
 //
-// Some hosts of this library must not call cudaMalloc: code running inside a
-// CUDA-graph capture they do not control, plug-ins whose memory is owned by a
-// pool allocator of the host application, or real-time loops where a device
-// allocation (an implicit synchronisation) is not allowed.  fo_sid_loss_noalloc
+// Some hosts of this library must not call cudaMalloc: plug-ins whose device
+// memory is owned by a pool allocator of the host application, or real-time loops
+// where a device allocation (an implicit synchronisation) is not allowed.
+// fo_sid_loss_noalloc
 // gives them the metric's loss values without any allocation: the per-block
 // partial sums live in a fixed array compiled into this library.
 #include <cuda_runtime.h>
@@ -73,9 +73,10 @@ __global__ void sid_noalloc_finalize(const float* partials, int nblocks, int T, 
   if (threadIdx.x == 0) loss[t] = s;
 }
 
-// Device address of g_sid_partials, looked up once per device.  In host code the
-// symbol names a host-side stand-in, not device memory, so kernels must be given
-// the address returned by cudaGetSymbolAddress.
+// Device address of g_sid_partials, looked up once per device (the first call on
+// that device) and kept for the life of the process: a cudaDeviceReset after it is
+// not supported.  In host code the symbol names a host-side stand-in, not device
+// memory, so kernels must be given the address returned by cudaGetSymbolAddress.
 std::mutex g_mu;
 float* g_addr[64] = {nullptr};
 

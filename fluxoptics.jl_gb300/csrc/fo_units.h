@@ -19,13 +19,16 @@ struct ColUnit {
 
 // items: n_items+1 offsets into the field list (runs sharing one transfer function).
 // Returns the units in dispatch order, or an empty list when the launch fits in one
-// round (total <= slots) and the plain 2-D launch is kept.
+// round (total <= slots) and the plain 2-D launch is kept.  An empty item (two equal
+// offsets) yields no unit, so every unit holds at least one field: the persistent
+// kernel issues the next unit's first strip from inside the current unit's field loop.
 inline std::vector<ColUnit> balanced_col_units(const std::vector<int>& items, int strips, int slots) {
   std::vector<ColUnit> units;
   const int n_items = (int)items.size() - 1;
   if (n_items < 1 || strips < 1 || slots < 1) return units;
   for (int st = 0; st < strips; ++st)
-    for (int i = 0; i < n_items; ++i) units.push_back(ColUnit{items[i], items[i + 1], st});
+    for (int i = 0; i < n_items; ++i)
+      if (items[i + 1] > items[i]) units.push_back(ColUnit{items[i], items[i + 1], st});
   const int total = (int)units.size();
   if (total <= slots) return {};
   const int tail = total % slots;

@@ -11,9 +11,17 @@ Replaces, for CuArray fields:
 - ASProp / RSProp  (src/optical_components/freespace_propagators/angular_spectrum.jl:193-234,
                     rayleigh_sommerfeld.jl:128-169)
 - Phase / Mask     (src/optical_components/modulators/phasemask.jl:38-150, mask.jl:39-142)
-- AS_BPM           (src/optical_components/bulk_propagators/bpm.jl:130-142)
+- AS_BPM           (src/optical_components/bulk_propagators/bpm.jl:130-142, 244-321), with
+                   √N-slice checkpoints instead of every slice (GB300AS_BPM)
 - a fused run of the above (GB300Chain), the GPU counterpart of the merge rules
   (src/optical_components/system/merge_rules.jl:45-52)
+- TeaDOE / TeaReflector, FourierPhase / FourierMask, ASPropZ, DotProduct / PowerCoupling
+- SquaredIntensityDifference (src/metrics/squared_intensity_difference.jl:58-90), also
+  evaluated inside a chain's last forward pass (forward_with_metric!)
+- Fista, ProxRule(Fista, ClampProx) in one pass, ClampProx and TVProx
+  (src/OptimisersExt.jl:33-54, 222-244; src/proximal_operators/clamp_prox.jl:35-37,
+  tv_prox.jl:94-195) as in-place device steps (fista_step!, gb300_clamp!, tv_prox!)
+- the ragged batch of independent problems in one persistent launch (GB300Ragged)
 """
 module FluxOpticsGB300
 
@@ -483,6 +491,231 @@ function backpropagate_with_gradient!(∂v::ScalarField, u_saved::AbstractArray,
                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}, Ptr{Cvoid}),
                 p.plan, dptr(p.z), dptr(u_saved), dptr(∂v.electric), dirsign(dir), dptr(∂p.z), cstream()))
     (backpropagate!(∂v, p, dir), ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# AS_BPM: split-step march with sqrt(N) checkpoints kept inside the plan
+# ---------------------------------------------------------------------------
+mutable struct GB300BPM{M, A} <: AbstractCustomComponent{M}
+    plan::Ptr{Cvoid}
+    dn::A                     # CuArray{Float32, 3}: nx x ny x n_slices (the reference's layout)
+    ∂p::Union{Nothing, @NamedTuple{dn::A}}
+end
+
+# Token standing for the slice inputs of the last saving forward: the plan keeps
+# every checkpoint_every-th slice input itself and recomputes the others in the
+# adjoint, so no (nx, ny, batch, n_slices) buffer exists on the Julia side.
+struct GB300BPMSaved
+    plan::Ptr{Cvoid}
+end
+
+"""
+    GB300AS_BPM(u, thickness, n0, dn0; trainable=false, buffered=false, checkpoint_every=0)
+
+AS_BPM (bpm.jl:130-142) on the GPU path: the symmetric split-step march of
+`propagate!` (bpm.jl:244-260) and its adjoint with the ∂dn gradient
+(bpm.jl:275-321).  Instead of saving every slice input (bpm.jl:49, 2 GiB at
+1024² × 256) the plan keeps every `checkpoint_every`-th one (0: round(√n_slices))
+and recomputes each segment during the adjoint.  On-axis fields only (the
+reference's cos correction is 1 there); `dn0` is nx × ny × n_slices.
+"""
+function GB300AS_BPM(u::ScalarField, thickness::Real, n0::Real, dn0::AbstractArray{<:Real, 3};
+                     trainable::Bool = false, buffered::Bool = false, checkpoint_every::Integer = 0)
+    FluxOptics.is_on_axis(u) || error("GB300AS_BPM: tilted fields are not supported")
+    nx, ny, b = dims_of(u)
+    size(dn0, 1) == nx && size(dn0, 2) == ny || error("GB300AS_BPM: dn0 must be nx x ny x n_slices")
+    ns = size(dn0, 3)
+    ns >= 2 || error("GB300AS_BPM: at least 2 slices")
+    lam = lambdas_per_field(u)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_bpm_create, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble,
+                 Cint, Cint, Cdouble, Cint),
+                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), thickness, n0, ns, checkpoint_every, 1.0,
+                FO_FLAG_AUTOTUNE))
+    dn = CuArray{Float32}(dn0)
+    M = trainable ? (buffered ? Trainable{Buffered} : Trainable{Unbuffered}) : Static
+    ∂p = (trainable && buffered) ? (; dn = similar(dn)) : nothing
+    p = GB300BPM{M, typeof(dn)}(h[], dn, ∂p)
+    finalizer(x -> ccall((:fo_bpm_destroy, LIB), Cint, (Ptr{Cvoid},), x.plan), p)
+end
+
+Functors.@functor GB300BPM (dn,)
+get_data(p::GB300BPM) = p.dn
+trainable(p::GB300BPM{<:Trainable}) = (; dn = p.dn)
+get_preallocated_gradient(p::GB300BPM{Trainable{Buffered}}) = p.∂p
+get_saved_buffer(p::GB300BPM{Trainable{Buffered}}) = GB300BPMSaved(p.plan)
+alloc_saved_buffer(u::ScalarField, p::GB300BPM{Trainable{Unbuffered}}) = GB300BPMSaved(p.plan)
+
+function _bpm_fwd!(u::ScalarField, p::GB300BPM, save::Bool, dir)
+    check(ccall((:fo_bpm_forward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Ptr{Cvoid}),
+                p.plan, dptr(u.electric), dptr(p.dn), dirsign(dir), Cint(save), cstream()))
+    u
+end
+
+propagate!(u::ScalarField, p::GB300BPM, dir::Type{<:Direction}) = _bpm_fwd!(u, p, false, dir)
+propagate_and_save!(u::ScalarField, p::GB300BPM{Trainable{Buffered}}, dir::Type{<:Direction}) =
+    _bpm_fwd!(u, p, true, dir)
+propagate_and_save!(u::ScalarField, ::GB300BPMSaved, p::GB300BPM{Trainable{Unbuffered}},
+                    dir::Type{<:Direction}) = _bpm_fwd!(u, p, true, dir)
+
+# the adjoint march without a gradient still needs the saved slice inputs of the plan
+backpropagate!(∂v::ScalarField, p::GB300BPM, dir::Type{<:Direction}) =
+    error("GB300AS_BPM: use backpropagate_with_gradient! after propagate_and_save!")
+
+function backpropagate_with_gradient!(∂v::ScalarField, ::GB300BPMSaved, ∂p::NamedTuple,
+                                      p::GB300BPM{<:Trainable}, dir::Type{<:Direction})
+    check(ccall((:fo_bpm_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                p.plan, dptr(∂v.electric), dptr(p.dn), dptr(∂p.dn), dirsign(dir), cstream()))
+    (∂v, ∂p)
+end
+
+# ---------------------------------------------------------------------------
+# SquaredIntensityDifference: the metric, its pullback, and the metric fused
+# into a chain's last forward pass
+# ---------------------------------------------------------------------------
+mutable struct GB300SID{T}
+    handle::Ptr{Cvoid}
+    target::T                 # CuArray{Float32}: nx x ny x n_targets
+    loss::CuArray{Float32, 1}
+end
+
+"""
+    GB300SquaredIntensityDifference(u, target)
+
+SquaredIntensityDifference (squared_intensity_difference.jl:58-90) for fields
+like `u`: I_t = Σ|u_b|² over the fields b of target slice t (field b belongs to
+slice b mod n_targets, the broadcast of an nx × ny × T target over
+nx × ny × T × M fields), loss_t = Σ(I_t − target_t)².
+"""
+function GB300SquaredIntensityDifference(u::ScalarField, target::AbstractArray{<:Real})
+    nx, ny, b = dims_of(u)
+    t = CuArray{Float32}(target)
+    nt = div(length(t), nx * ny)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_sid_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cint, Ptr{Cint}),
+                h, nx, ny, b, nt, C_NULL))
+    m = GB300SID(h[], t, CUDA.zeros(Float32, nt))
+    finalizer(x -> ccall((:fo_sid_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), m)
+end
+
+# compute_metric: per-slice losses (device), residuals kept for the pullback
+function (m::GB300SID)(u::ScalarField)
+    check(ccall((:fo_sid_forward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                m.handle, dptr(u.electric), dptr(m.target), dptr(m.loss), cstream()))
+    m.loss
+end
+
+# backpropagate_metric: ∂u = 4 ∂c_t (I_t − target_t) u (∂c = nothing: all ones)
+function pullback!(m::GB300SID, ∂c, u::ScalarField, ∂u::ScalarField)
+    check(ccall((:fo_sid_backward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                m.handle, dptr(u.electric), ∂c === nothing ? C_NULL : dptr(∂c), dptr(∂u.electric), cstream()))
+    ∂u
+end
+
+"""
+    forward_with_metric!(u_out, c::GB300Chain, u_in, m::GB300SID; dir=Forward) -> losses
+
+The chain's saving forward from `u_in` into `u_out` with the metric evaluated
+inside the last pass (fo_chain_forward_sid); the device losses are returned and
+the residuals stay in `m` for [`backward_from_metric!`](@ref).
+"""
+function forward_with_metric!(u_out::ScalarField, c::GB300Chain, u_in::ScalarField, m::GB300SID;
+                              dir::Type{<:Direction} = Forward)
+    mods = [_fomod(x, _saved(x), nothing) for x in c.mods]
+    check(ccall((:fo_chain_forward_sid, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid},
+                 Ptr{Cvoid}),
+                c.chain, dptr(u_in.electric), dptr(u_out.electric), mods, dirsign(dir), m.handle,
+                dptr(m.target), dptr(m.loss), cstream()))
+    m.loss
+end
+
+"""
+    backward_from_metric!(∂u, c::GB300Chain, u_out, m::GB300SID; dir=Forward, input_grad=true)
+
+The chain's adjoint sweep seeded with the metric's pullback of the last
+[`forward_with_metric!`](@ref): every trainable modulator's gradient buffer is
+filled.  With `input_grad = false` the final write of the input gradient is
+skipped (FO_BWD_DISCARD_INPUT_GRAD) and `∂u` holds scratch values.
+"""
+function backward_from_metric!(∂u::ScalarField, c::GB300Chain, u_out::ScalarField, m::GB300SID;
+                               dir::Type{<:Direction} = Forward, input_grad::Bool = true)
+    mods = [_fomod(x, _saved(x), _grad(x)) for x in c.mods]
+    check(ccall((:fo_chain_backward_ex, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                c.chain, dptr(∂u.electric), mods, dirsign(dir), m.handle, dptr(u_out.electric),
+                input_grad ? Cint(0) : Cint(1), cstream()))
+    ∂u
+end
+
+# ---------------------------------------------------------------------------
+# Optimiser steps: Fista (η stored squared, OptimisersExt.jl:33-54), ProxRule(Fista,
+# ClampProx) in one pass (OptimisersExt.jl:222-244, clamp_prox.jl:35-37), TVProx
+# (tv_prox.jl:94-195).  Each call updates the parameter in place on the stream.
+# ---------------------------------------------------------------------------
+mutable struct GB300FistaState{A}
+    eta::Float64
+    xk::A                     # previous iterate
+    newdx::A                  # the step of the last update
+    t::CuArray{Float64, 1}    # Fista's t, advanced on the device
+end
+
+"""GB300FistaState(eta, x) -- the state Fista(eta) keeps for parameter x."""
+GB300FistaState(eta::Real, x::CuArray{Float32}) = GB300FistaState(Float64(eta), copy(x), similar(x), CuArray([1.0]))
+
+"""
+    fista_step!(st, x, dx; clamp=nothing)
+
+One Fista update of `x` with gradient `dx`; with `clamp = (lo, hi)` the
+ClampProx of ProxRule(Fista(eta), ClampProx(lo, hi)) runs in the same pass.
+"""
+function fista_step!(st::GB300FistaState, x::CuArray{Float32}, dx::CuArray{Float32}; clamp = nothing)
+    n = Clonglong(length(x))
+    if clamp === nothing
+        check(ccall((:fo_fista_step, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Clonglong, Cdouble, Ptr{Cvoid}, Ptr{Cvoid}),
+                    dptr(x), dptr(st.xk), dptr(st.newdx), dptr(dx), n, st.eta, dptr(st.t), cstream()))
+    else
+        check(ccall((:fo_fista_clamp_step, LIB), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Clonglong, Cdouble, Ptr{Cvoid}, Cdouble,
+                     Cdouble, Ptr{Cvoid}),
+                    dptr(x), dptr(st.xk), dptr(st.newdx), dptr(dx), n, st.eta, dptr(st.t),
+                    Float64(clamp[1]), Float64(clamp[2]), cstream()))
+    end
+    x
+end
+
+"""clamp!(x, lo, hi) on the device -- ClampProx (clamp_prox.jl:35-37)."""
+function gb300_clamp!(x::CuArray{Float32}, lo::Real, hi::Real)
+    check(ccall((:fo_clamp, LIB), Cint, (Ptr{Cvoid}, Clonglong, Cdouble, Cdouble, Ptr{Cvoid}),
+                dptr(x), Clonglong(length(x)), lo, hi, cstream()))
+    x
+end
+
+mutable struct GB300TV
+    handle::Ptr{Cvoid}
+end
+
+"""
+    GB300TVProx(nx, ny, λ; n_iter=50, isotropic=true, eta=0.25)
+
+TVProx(λ, n_iter; isotropic, rule = Fista(eta)) for nx × ny parameters; apply
+with `tv_prox!(tv, x)`.
+"""
+function GB300TVProx(nx::Integer, ny::Integer, λ::Real; n_iter::Integer = 50, isotropic::Bool = true,
+                     eta::Real = 0.25)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_tv_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Cint, Cint, Cdouble, Cint, Cint, Cdouble),
+                h, nx, ny, λ, n_iter, Cint(isotropic), eta))
+    tv = GB300TV(h[])
+    finalizer(x -> ccall((:fo_tv_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), tv)
+end
+
+function tv_prox!(tv::GB300TV, x::CuArray{Float32})
+    check(ccall((:fo_tv_apply, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}), tv.handle, dptr(x), cstream()))
+    x
 end
 
 # ---------------------------------------------------------------------------

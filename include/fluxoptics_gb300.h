@@ -398,8 +398,8 @@ FO_API int fo_sid_backward(fo_sid sid, const void* u, const float* dc, void* du,
 
 /*
  * The loss values of SquaredIntensityDifference (as fo_sid_forward's `loss`) for
- * callers that cannot allocate device memory: inside a CUDA-graph capture they do
- * not own, under a host application's pool allocator, or in a real-time loop
+ * callers that cannot allocate device memory: plug-ins whose host application
+ * owns all device memory through its own pool allocator, or real-time loops
  * where an allocation's implicit synchronisation is not allowed.  It allocates
  * nothing: the per-block partial sums live in a fixed 256 KiB array compiled into
  * the library (1024 blocks x 64 slices), which every GPU that loads the library
@@ -407,8 +407,10 @@ FO_API int fo_sid_backward(fo_sid sid, const void* u, const float* dc, void* du,
  * < n_targets); n_targets may not exceed FO_SID_NOALLOC_MAX_TARGETS, larger
  * values return FO_ERR_SHAPE.  The first call on a device looks the array's
  * device address up (cudaGetSymbolAddress), so make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * (different streams, no ordering between them) race and give wrong losses.
+ * stream capture.  The address is kept for the life of the process, so a
+ * cudaDeviceReset after that first call is not supported.  All calls share the
+ * array: calls that overlap on the GPU (different streams, no ordering between
+ * them) race and give wrong losses.
  * No counterpart in the reference (it allocates freely on the Julia side).
  */
 #define FO_SID_NOALLOC_MAX_TARGETS 64

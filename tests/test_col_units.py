@@ -67,3 +67,21 @@ def test_units_cover_every_field_strip_once(dump, batch, per_table, strips, slot
     if tail and min(items[i + 1] - items[i] for i in range(n_items)) > 1:
         assert len(units) - full > tail          # the last round was spread
         assert len(units) - full <= max(slots, tail)
+
+
+def test_empty_items_make_no_units(dump):
+    """An empty run of fields (equal offsets) must not become a unit: the
+    persistent column kernel loads the next unit's first strip from inside the
+    current unit's field loop, so a unit without fields would leave that load
+    unissued."""
+    items = [0, 16, 16, 32, 48, 48]  # two empty items among three full ones
+    strips, slots = 512, 152
+    units = dump(items, strips, slots)
+    assert units, "1536 non-empty blocks need units"
+    seen = set()
+    for first, end, strip in units:
+        assert first < end
+        for f in range(first, end):
+            assert (strip, f) not in seen
+            seen.add((strip, f))
+    assert len(seen) == 48 * strips
