@@ -579,25 +579,39 @@ def run_config2(args):
             "unit": UNIT, "gpu_launches_per_step": nk}
 
 
+CONFIG4 = {"n": 1024, "ds": (0.25, 0.25), "lam": 1.064, "n0": 1.45, "slices": 256}
+
+
+def config4_inputs(n=CONFIG4["n"], ns=CONFIG4["slices"]):
+    """AS_BPM workload inputs: dn (ns, n, n) float32 of seeded white noise filtered with
+    sigma = 8 slices axially and 4 px transversally, scaled to max |dn| = 5e-3; a plane
+    wave tilted by a seeded angle within 2 degrees (baked into the data) under a
+    Gaussian envelope of waist 150 um, unit power (complex64); an intensity target."""
+    from scipy.ndimage import gaussian_filter
+    ds, lam, n0 = CONFIG4["ds"], CONFIG4["lam"], CONFIG4["n0"]
+    rng = np.random.default_rng(SEED + 4)
+    dn = gaussian_filter(rng.standard_normal((ns, n, n)).astype(np.float32), (8.0, 4.0, 4.0))
+    dn *= 5e-3 / np.max(np.abs(dn))
+    x = (np.arange(n) - (n - 1) / 2) * ds[0]
+    y = (np.arange(n) - (n - 1) / 2) * ds[1]
+    th = np.deg2rad(rng.uniform(-2, 2))
+    env = np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 150.0 ** 2)
+    u0 = env * np.exp(1j * 2 * np.pi * n0 / lam * np.sin(th) * x[None, :])
+    u0 = (u0 / np.sqrt(np.sum(np.abs(u0) ** 2) * ds[0] * ds[1])).astype(np.complex64)
+    target = (np.abs(gaussian_filter(rng.standard_normal((n, n)), 16.0)) ** 2).astype(np.float32)
+    return u0, dn.astype(np.float32), target
+
+
 def run_config4(args):
     """AS_BPM 1024^2 x 256 slices, gradient w.r.t. dn with sqrt(N) checkpoints."""
     import torch
-    from scipy.ndimage import gaussian_filter
     from __graft_entry__ import build, load_package
     build()
     fo = load_package()
     lib = fo.load_library()
-    n, ds, lam, n0, ns = 1024, (0.25, 0.25), 1.064, 1.45, 256
-    rng = np.random.default_rng(SEED + 4)
-    dn = gaussian_filter(rng.standard_normal((ns, n, n)).astype(np.float32), (8.0, 4.0, 4.0))
-    dn *= 5e-3 / np.max(np.abs(dn))
-    x, y = fo.spatial_vectors((n, n), ds)
-    th = np.deg2rad(rng.uniform(-2, 2))
-    env = np.exp(-(x[None, :] ** 2 + y[:, None] ** 2) / 150.0 ** 2)
-    u0 = (env * np.exp(1j * 2 * np.pi * n0 / lam * np.sin(th) * x[None, :])).astype(np.complex64)
+    n, ds, lam, n0, ns = CONFIG4["n"], CONFIG4["ds"], CONFIG4["lam"], CONFIG4["n0"], CONFIG4["slices"]
+    u0, dn, target = config4_inputs()
     u = fo.ScalarField(u0, ds, lam)
-    fo.normalize_power_(u)
-    target = np.abs(gaussian_filter(rng.standard_normal((n, n)), 16.0)) ** 2
     bpm = fo.AS_BPM(u, float(ns), n0, dn, trainable=True, buffered=True)
     system = fo.ScalarSource(u) | bpm
     metric = fo.SquaredIntensityDifference((u, target))

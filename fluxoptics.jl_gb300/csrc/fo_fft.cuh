@@ -87,8 +87,27 @@ inline void for_each_stage_twiddle(int N, int E, F f) {  // f(index, numerator, 
   }
 }
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract as one paired-FP32 instruction each (sm_100 and later):
+// the (re, im) pair of a float2 is exactly the operand pair of FADD2 / FFMA2, and
+// each lane rounds like the scalar operation, so results are unchanged.  a - b is
+// formed as fma(b, -1, a), which is exact before its single rounding.
+#ifndef FO_F32X2
+#define FO_F32X2 1
+#endif
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+#if FO_F32X2
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+#if FO_F32X2
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
