@@ -214,6 +214,33 @@ def col_pass_bytes(n=N, batch=None):
     return batch * 16 * n * n + len(LAMBDAS) * 8 * n * n
 
 
+def numa_pages(addr, nbytes):
+    """Pages per NUMA node of the host mappings that overlap [addr, addr + nbytes)
+    ({"N0": pages, ...}), from /proc/self/numa_maps; empty where it does not exist."""
+    try:
+        with open("/proc/self/maps") as f:
+            spans = {}
+            for ln in f:
+                a, b = (int(v, 16) for v in ln.split()[0].split("-"))
+                spans[a] = b
+        with open("/proc/self/numa_maps") as f:
+            lines = f.readlines()
+    except OSError:
+        return {}
+    out = {}
+    for ln in lines:
+        parts = ln.split()
+        start = int(parts[0], 16)
+        end = spans.get(start)
+        if end is None or end <= addr or start >= addr + nbytes:
+            continue
+        for kv in parts[1:]:
+            k, _, v = kv.partition("=")
+            if k.startswith("N") and k[1:].isdigit() and v.isdigit():
+                out[k] = out.get(k, 0) + int(v)
+    return out
+
+
 def max_over_ranks(ms, device="cuda"):
     """The slowest rank's step time: every replica processed its own share, so the
     job took as long as the slowest one (barrier on both sides)."""
@@ -297,6 +324,7 @@ def run_gb300(args, rank, world):
         # uploaded before it, inside the timed region.
         host_in = torch.from_numpy(fields_np).pin_memory()
         in_bytes = host_in.numel() * host_in.element_size()
+        host_numa = numa_pages(host_in.data_ptr(), in_bytes)
         host_loss = torch.empty((len(LAMBDAS),), dtype=torch.float32).pin_memory()
         bufs = (src, src.similar())
         copy_stream = torch.cuda.Stream()
@@ -347,8 +375,10 @@ def run_gb300(args, rank, world):
         # the slowest rank's time, as for the device-timed value (whole-job rate below)
         e2e_ms = max_over_ranks(e2.elapsed_time(e3) / e2_steps)
         e2e_step_ms = statistics.median(a.elapsed_time(b) for a, b in ev_step)
-        # start / end (ms from the start of the e2e region) of the first steps
+        # start / end (ms from the start of the e2e region) of the first steps, and every
+        # step's duration (a step that waited for its input upload shows up here)
         e2e_timeline = [[round(e2.elapsed_time(ev), 2) for ev in ev_step[k]] for k in range(min(4, e2_steps))]
+        e2e_steps_ms = [round(a.elapsed_time(b), 3) for a, b in ev_step]
         for gg in step_graphs:
             fo._capi.check(lib.fo_graph_destroy(gg))
         fo._capi.check(lib.fo_graph_destroy(g))
@@ -393,8 +423,10 @@ def run_gb300(args, rank, world):
                 "step_ms": round(e2e_step_ms, 4), "copy_alone_ms": round(copy_alone_ms, 4),
                 # the rate of the median step, for runs where a few uploads stalled on the host side
                 "median_step_value": round(job_rate(props_per_step, world, e2e_step_ms), 1),
-                "timeline_ms": {"steps": "[step start, step end]", "first_steps": e2e_timeline},
-                "h2d_gbs_measured": round(h2d_gbs, 1)},
+                "timeline_ms": {"steps": "[step start, step end]", "first_steps": e2e_timeline,
+                                "every_step": e2e_steps_ms},
+                "h2d_gbs_measured": round(h2d_gbs, 1),
+                "host_buffer_numa": host_numa},
         "clocks": clk.summary(),
         "final_loss": final_loss,
     }
@@ -711,6 +743,52 @@ def run_config5(args):
                                 [round(v, 3) for v in pass_ms]))}
 
 
+def config_bytes(cfg, result):
+    """Algorithmic HBM bytes of one step of the other configurations: every propagation
+    reads and writes its unpadded field once (16 n^2), every modulation reads its
+    parameter once (4 n^2), saves and reads back its input (8 n^2 each way) and writes
+    its gradient (4 n^2); the optimiser step reads x, xk, dx and writes x, xk, newdx."""
+    if cfg == 2:          # 512^2 two-DOE RSProp chain: 3 + 3 propagations, 2 phase masks, Fista
+        n2 = 512 * 512
+        return 6 * 16 * n2 + 2 * (4 + 8 + 8 + 4) * n2 + 2 * 24 * n2
+    if cfg == 4:          # AS_BPM 1024^2 x 256 slices: 257 + 257 propagations, dn read twice,
+        n2, ns = CONFIG4["n"] ** 2, CONFIG4["slices"]   # slice inputs saved and read, d(dn) written, Fista on dn
+        return 2 * (ns + 1) * 16 * n2 + ns * (4 + 8 + 4 + 8 + 4) * n2 + 24 * ns * n2
+    if cfg == 5:          # ragged: one forward + one adjoint propagation per problem, the mask read in
+        pix = result["pixels_per_step"]   # both, the input read again by the gradient, target, gradient written
+        return pix * (2 * 16 + 2 * 4 + 8 + 4 + 4)
+    raise ValueError(cfg)
+
+
+def run_other_configs(args):
+    """Bounded runs of configurations 2, 4 and 5 (a few steps each) for the JSON line:
+    value, time per step and the whole step's algorithmic bandwidth against the
+    measured HBM peak."""
+    import torch
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except (OSError, ValueError):
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    sub = argparse.Namespace(steps=max(3, min(args.steps, 6)), warmup=max(3, min(args.warmup, 3)),
+                             problems=args.problems)
+    out = {}
+    for cfg, fn in ((2, run_config2), (4, run_config4), (5, run_config5)):
+        r = fn(sub)
+        torch.cuda.synchronize()
+        b = config_bytes(cfg, r)
+        gbs = b / (r["ms_per_step"] * 1e-3) / 1e9
+        out[str(cfg)] = {"config": r["config"], "value": r["value"], "unit": r["unit"],
+                         "ms_per_step": r["ms_per_step"], "props_per_step": r["props_per_step"],
+                         "steps": sub.steps, "gpu_launches_per_step": r.get("gpu_launches_per_step"),
+                         "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+                                      "frac": round(gbs / hbm, 4), "scope": "whole step, algorithmic bytes",
+                                      "algorithmic_bytes_per_step": int(b)}}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -719,6 +797,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain cuFFT comparison")
+    ap.add_argument("--no-configs", action="store_true", help="skip the bounded runs of configurations 2, 4 and 5")
     ap.add_argument("--config", type=int, default=3, choices=[2, 3, 4, 5],
                     help="3: the 2048^2 x 48 headline (default); 2 / 4 / 5: the other configurations")
     ap.add_argument("--modes", type=int, default=16,
@@ -789,6 +868,8 @@ def main():
             one = run_cpu_sample(budget_s=6.0, threads=1)
             line["cpu_baseline"]["single_thread"] = {"value": one["value"], "unit": one["unit"], "cores": 1,
                                                      "sample": one["sample"]}
+        if not args.no_configs and world == 1:
+            line["configs"] = run_other_configs(args)
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist

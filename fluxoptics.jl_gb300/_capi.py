@@ -13,6 +13,7 @@ FO_BACKWARD = -1
 FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = 0, 1, 2, 3, 4
 FO_FOURIER_TRAINABLE = 2
 FO_FLAG_GRAD_SPECTRA = 2
+FO_FLAG_DEVICE_Z = 4
 
 ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
                5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
@@ -81,6 +82,7 @@ SIGNATURES = {
     "fo_chain_create": (_i, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
     "fo_chain_destroy": (_i, [_vp]),
     "fo_chain_forward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp]),
+    "fo_chain_set_probes": (_i, [_vp, _vp, _vp]),
     "fo_chain_forward_from": (_i, [_vp, _vp, _vp, C.POINTER(fo_mod), _i, _vp]),
     "fo_chain_forward_sid": (_i, [_vp, _vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _vp, _vp]),
     "fo_chain_backward": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _vp]),

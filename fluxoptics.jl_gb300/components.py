@@ -162,28 +162,34 @@ class ASProp(_Propagator):
             _capi.call("fo_asprop_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
                        _capi.dvec(lam), len(lam), self.z, self.n0, int(self.autotune))
             return h
-        opt = _capi.fo_as_options()
-        opt.paraxial = int(self.paraxial)
-        opt.track_tilts = int(self.track_tilts)
-        tv = _capi.dvec(tilts.ravel())
-        opt.tilts = C.cast(tv, C.POINTER(C.c_double))
-        opt.n_tilts = len(tilts)
-        cb = None
-        if self.filter is not None:
-            flt = self.filter
-
-            def _eval(fx, fy, n, re, im, _ctx):
-                fxv = np.ctypeslib.as_array(fx, shape=(n,))
-                fyv = np.ctypeslib.as_array(fy, shape=(n,))
-                val = np.broadcast_to(np.asarray(flt(fxv, fyv), dtype=np.complex128), (n,))
-                np.ctypeslib.as_array(re, shape=(n,))[:] = val.real
-                np.ctypeslib.as_array(im, shape=(n,))[:] = val.imag
-
-            cb = _capi.fo_filter_fn(_eval)
-            opt.filter = cb
+        opt, keep = _as_options(self.paraxial, self.track_tilts, tilts, self.filter)
         _capi.call("fo_asprop_create_ex", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
                    _capi.dvec(lam), len(lam), self.z, self.n0, C.byref(opt), int(self.autotune))
+        del keep
         return h
+
+
+def _as_options(paraxial, track_tilts, tilts, filt):
+    """fo_as_options for fo_asprop_create_ex, and the objects that must stay alive
+    until the call returns (the tilt array and the filter callback)."""
+    opt = _capi.fo_as_options()
+    opt.paraxial = int(paraxial)
+    opt.track_tilts = int(track_tilts)
+    tv = _capi.dvec(np.asarray(tilts).ravel())
+    opt.tilts = C.cast(tv, C.POINTER(C.c_double))
+    opt.n_tilts = len(tilts)
+    cb = None
+    if filt is not None:
+        def _eval(fx, fy, n, re, im, _ctx):
+            fxv = np.ctypeslib.as_array(fx, shape=(n,))
+            fyv = np.ctypeslib.as_array(fy, shape=(n,))
+            val = np.broadcast_to(np.asarray(filt(fxv, fyv), dtype=np.complex128), (n,))
+            np.ctypeslib.as_array(re, shape=(n,))[:] = val.real
+            np.ctypeslib.as_array(im, shape=(n,))[:] = val.imag
+
+        cb = _capi.fo_filter_fn(_eval)
+        opt.filter = cb
+    return opt, (tv, cb)
 
 
 def ParaxialProp(u, z, ds=None, n0=1.0, filter=None, track_tilts=False, **kw):
@@ -384,18 +390,20 @@ def TeaReflector(u, f=None, ds=None, r=1.0, trainable=False, buffered=False):
 
 class ASPropZ(_Modulator):
     """Angular-spectrum propagation with a trainable distance z
-    (angular_spectrum.jl:236-344).  z lives in device memory; every forward rebuilds
-    the transfer functions from it in FP64, and the adjoint sweep gets dL/dz from
-    fo_prop_z_gradient.  On-axis, non-paraxial, unfiltered fields only."""
+    (angular_spectrum.jl:236-344), with the on-axis, tilted (fields with tilts,
+    ``track_tilts``) or ``paraxial`` kernel and an optional frequency ``filter``, like
+    the reference's.  z lives in device memory; every forward rebuilds the transfer
+    functions from it in FP64, and the adjoint sweep gets dL/dz from fo_prop_z_gradient."""
 
     pname = "z"
 
     def __init__(self, u, z, ds=None, n0=1.0, trainable=False, track_tilts=False, paraxial=False,
                  filter=None, double_precision_kernel=False):
-        if paraxial or track_tilts or filter is not None or not u.is_on_axis():
-            raise NotImplementedError("ASPropZ on the GB300 path is on-axis, non-paraxial and unfiltered")
         self.ds = tuple(float(d) for d in (ds if ds is not None else u.ds))
         self.n0 = float(n0)
+        self.paraxial = bool(paraxial)
+        self.track_tilts = bool(track_tilts)
+        self.filter = filter
         self.z = torch.tensor([float(z)], dtype=torch.float32, device="cuda")
         self.trainable = bool(trainable)
         self.buffered = False
@@ -406,13 +414,20 @@ class ASPropZ(_Modulator):
 
     def plan_for(self, u: ScalarField):
         lam = tuple(float(v) for v in u.lambdas_per_field())
-        key = (u.nx, u.ny, u.batch, lam)
+        tilts = u.tilts_per_field()
+        key = (u.nx, u.ny, u.batch, lam, tuple(tilts.ravel()))
         p = self._plans.get(key)
         if p is None:
             p = C.c_void_p()
-            flags = 1 | (_capi.FO_FLAG_GRAD_SPECTRA if self.trainable else 0)
-            _capi.call("fo_asprop_create", C.byref(p), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
-                       _capi.dvec(lam), len(lam), float(self.z.item()), self.n0, flags)
+            flags = 1 | _capi.FO_FLAG_DEVICE_Z | (_capi.FO_FLAG_GRAD_SPECTRA if self.trainable else 0)
+            if not (self.paraxial or self.track_tilts or self.filter is not None or np.any(tilts != 0.0)):
+                _capi.call("fo_asprop_create", C.byref(p), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                           _capi.dvec(lam), len(lam), float(self.z.item()), self.n0, flags)
+            else:
+                opt, keep = _as_options(self.paraxial, self.track_tilts, tilts, self.filter)
+                _capi.call("fo_asprop_create_ex", C.byref(p), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                           _capi.dvec(lam), len(lam), float(self.z.item()), self.n0, C.byref(opt), flags)
+                del keep
             self._plans[key] = p
         return p
 
@@ -686,7 +701,11 @@ class ScalarSource:
 
 
 class FieldProbe(Component):
-    """Records the field where it sits (system/field_probe.jl:31-43)."""
+    """Records the field where it sits (system/field_probe.jl:31-43): calling the
+    system returns a copy of the field at every probe in ``result["probes"][probe]``
+    (system/optical_system.jl:194-214).  Inside a fused chain the copy is written by
+    the row pass that produces that plane, so a probe costs no extra pass; the field
+    itself is unchanged."""
 
     def propagate_(self, u, direction=Forward):
         return u
@@ -701,9 +720,11 @@ def _is_prop(c):
 
 
 class _Chain:
-    def __init__(self, props, mods):
+    def __init__(self, props, mods, probes=()):
         self.props = props
         self.mods = mods  # len(props) + 1, entries None or modulators
+        # (("pre" | "post", slot k), FieldProbe): the plane entering / leaving modulation slot k
+        self.probes = list(probes)
 
 
 class OpticalSystem:
@@ -740,14 +761,24 @@ class OpticalSystem:
         i, n = 0, len(comps)
         fuse = self.merge_components
         while i < n:
-            if fuse and (_is_mod(comps[i]) or _is_prop(comps[i])):
+            if fuse and (_is_mod(comps[i]) or _is_prop(comps[i]) or isinstance(comps[i], FieldProbe)):
                 j = i
                 mods = [None]
                 props = []
+                probes = []
                 lay = None
-                if _is_mod(comps[j]):
+
+                def take_probes(plane):
+                    nonlocal j
+                    while j < n and isinstance(comps[j], FieldProbe):
+                        probes.append((plane, comps[j]))
+                        j += 1
+
+                take_probes(("pre", 0))
+                if j < n and _is_mod(comps[j]):
                     mods[0] = comps[j]
                     j += 1
+                    take_probes(("post", 0))
                 while j < n and _is_prop(comps[j]):
                     lj = comps[j].layout(u)
                     if lay is not None and lj != lay:
@@ -756,16 +787,44 @@ class OpticalSystem:
                     props.append(comps[j])
                     mods.append(None)
                     j += 1
+                    k = len(props)
+                    take_probes(("pre", k))
                     if j < n and _is_mod(comps[j]):
                         mods[-1] = comps[j]
                         j += 1
+                        take_probes(("post", k))
                 if props:
-                    segs.append(_Chain(props, mods))
+                    # a probe after the chain's last propagator or modulator stays in the chain;
+                    # one that is followed by a propagator the chain could not take is left out
+                    segs.append(_Chain(props, mods, probes))
                     i = j
                     continue
             segs.append(comps[i])
             i += 1
         return segs
+
+    def _set_chain_probes(self, seg: _Chain, u: ScalarField, probes):
+        """Points the chain's probe planes at fresh fields (collected into ``probes``)
+        or clears them."""
+        if not seg.probes:
+            return
+        h = self._chain_handle(seg, u)
+        if probes is None:
+            _capi.call("fo_chain_set_probes", h, None, None)
+            return
+        K = len(seg.props)
+        pre = (C.c_void_p * (K + 1))()
+        post = (C.c_void_p * (K + 1))()
+        by_plane = {}
+        for (side, k), pr in seg.probes:
+            f = by_plane.get((side, k))
+            if f is None:
+                f = u.similar()
+                by_plane[(side, k)] = f
+                (pre if side == "pre" else post)[k] = f.electric.data_ptr()
+            # several probes on one plane share one copy, like the reference's copies of one field
+            probes[pr] = f
+        _capi.call("fo_chain_set_probes", h, pre, post)
 
     def _chain_handle(self, ch: _Chain, u: ScalarField):
         plans = tuple(p.plan_for(u).value for p in ch.props)
@@ -785,7 +844,7 @@ class OpticalSystem:
             lib.fo_chain_destroy(h)
 
     # -- execution ----------------------------------------------------------------
-    def forward(self, u: ScalarField, tape=None, src: ScalarField = None, metric=None):
+    def forward(self, u: ScalarField, tape=None, src: ScalarField = None, metric=None, probes=None):
         """Runs the system in place on u (or from ``src`` into u).  With a tape,
         trainable components save their inputs and the tape records what the
         adjoint sweep needs.  A trainable modulator that directly follows the
@@ -794,7 +853,9 @@ class OpticalSystem:
 
         With ``metric``, the metric is evaluated on the result (its ``loss`` holds
         the values afterwards); SquaredIntensityDifference is then computed inside
-        the last pass when the system ends with a fused chain."""
+        the last pass when the system ends with a fused chain.
+
+        With a ``probes`` dict, every FieldProbe's copy of the field is stored in it."""
         d = self.direction
         segs = self.segments(u)
         metric_done = False
@@ -807,6 +868,7 @@ class OpticalSystem:
                 for p in seg.props:
                     if isinstance(p, _FourierModulator):
                         p.refresh(u)
+                self._set_chain_probes(seg, u, probes)
                 mods = (fo_mod * len(seg.mods))()
                 saved = []
                 # The first modulator of a chain that reads the system input out of place
@@ -846,6 +908,11 @@ class OpticalSystem:
                 elif tape is not None and c.trainable and isinstance(c, AS_BPM):
                     c.propagate_and_save_(u, None, d)
                     tape.append((c, None))
+                elif isinstance(c, FieldProbe):
+                    if probes is not None:
+                        probes[c] = u.copy()
+                    if tape is not None:
+                        tape.append((c, None))
                 else:
                     c.propagate_(u, d)
                     if tape is not None:
@@ -916,8 +983,9 @@ class OpticalSystem:
             raise ValueError("give exactly one of a source or an input field")
         src = self.source.u0 if x is None else x
         u = src.similar()
-        self.forward(u, src=src)
-        return {"out": u, "probes": {}}
+        probes = {}
+        self.forward(u, src=src, probes=probes)
+        return {"out": u, "probes": probes}
 
 
 def propagate(u, p, direction=Forward):

@@ -60,11 +60,14 @@ __global__ void as_h_kernel(float2* H, int fx_n, int fy_n, double dx, double dy,
 //   mode 1 tilted  : cis(2 pi z (sqrt(1/lm^2 - (fx+f0x)^2 - (fy+f0y)^2) + off)), off = track ? (f0x fx + f0y fy) lm : 0
 //   mode 2 paraxial: cis(-pi lm z ((fx+f0x)^2 + (fy+f0y)^2) - off + 2 pi z / lm), off = track ? 2 (f0x fx + f0y fy) : 0
 // with lm = lambda / n0 and f0 = sin(theta) / lm; complex square root (evanescent
-// components decay); modes 0 and 1 take conj(H(-z)) for z < 0.  Multiplied by the
-// optional filter values (same layout) and by `scale`.
+// components decay), times the optional filter values v (same layout) and `scale`.
+// Modes 0 and 1 take conj(H(-z) v) for z < 0 (angular_spectrum.jl:9-12, 55-60), so the
+// filter value is conjugated there too.  With zp the distance is read from device
+// memory (ASPropZ, a trainable z) instead of `z`.
 __global__ void as_h_general_kernel(float2* H, int fx_n, int fy_n, double dx, double dy, double lm, double z,
                                     double scale, int mode, double f0x, double f0y, int track,
-                                    const double2* filter) {
+                                    const double2* filter, const float* zp) {
+  if (zp) z = (double)*zp;
   const long long n = (long long)fx_n * fy_n;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
@@ -91,7 +94,8 @@ __global__ void as_h_general_kernel(float2* H, int fx_n, int fy_n, double dx, do
       if (z < 0.0) im = -im;
     }
     if (filter) {
-      const double2 f = filter[q];
+      double2 f = filter[q];
+      if (mode != 2 && z < 0.0) f.y = -f.y;
       const double r2 = re * f.x - im * f.y;
       im = re * f.y + im * f.x;
       re = r2;
@@ -125,12 +129,17 @@ __global__ void as_h_z_kernel(float2* H, int fx_n, int fy_n, double dx, double d
 }
 
 // d loss / d z of ASPropZ: per block, sum over its frequency pixels k and the fields
-// b of Re(U_b[k] conj(G_b[k]) dH_b[k]) with dH = 2 pi i kz H (z > 0) or 2 pi i conj(kz) H
-// (z < 0), conjugated for the Backward direction; U = FFT2(input), G = FFT2(adjoint
-// at the output), H the stored table (which carries the 1/N of the inverse transform).
+// b of Re(U_b[k] conj(G_b[k]) dH_b[k]), conjugated for the Backward direction; U =
+// FFT2(input), G = FFT2(adjoint at the output), H the stored table (which carries the
+// 1/N of the inverse transform and the filter, constant in z).  dH/dz = i R H with the
+// phase rate R of the table's kernel (mode as in as_h_general_kernel, g = f + f0):
+//   modes 0 / 1: R = 2 pi (sqrt(complex(1/lm^2 - |g|^2)) + off), conjugated for z < 0,
+//                off = track ? (f0x fx + f0y fy) lm : 0 (mode 1 only)
+//   mode 2     : R = -pi lm |g|^2 + 2 pi / lm (the offset does not depend on z).
+// par[b] = {1/lm, f0x, f0y, lm} of field b (f0 = 0 in mode 0).
 __global__ void as_z_grad_partial_kernel(const float2* U, const float2* G, const float2* H, const int* h_index,
-                                         const float* lam_eff, int fx_n, int fy_n, double dx, double dy,
-                                         const float* zp, int batch, int backward, double* partials) {
+                                         const float4* par, int mode, int track, int fx_n, int fy_n, double dx,
+                                         double dy, const float* zp, int batch, int backward, double* partials) {
   __shared__ double red[kThreads / 32];
   const long long npix = (long long)fx_n * fy_n;
   const bool zneg = *zp < 0.f;
@@ -141,14 +150,23 @@ __global__ void as_z_grad_partial_kernel(const float2* U, const float2* G, const
     const float fx = (float)fftfreq_d(kx, fx_n, dx), fy = (float)fftfreq_d(ky, fy_n, dy);
     float t = 0.f;
     for (int b = 0; b < batch; ++b) {
-      const float li = lam_eff[b];  // n0 / lambda
-      const float arg = li * li - fx * fx - fy * fy;
-      // kz = sqrt(complex(arg)); conj(kz) for z < 0
-      float2 kz = arg >= 0.f ? make_float2(sqrtf(arg), 0.f) : make_float2(0.f, sqrtf(-arg));
-      if (zneg) kz.y = -kz.y;
+      const float4 pb = par[b];
+      const float gx = fx + pb.y, gy = fy + pb.z;
+      const float g2 = gx * gx + gy * gy;
+      float2 rate;  // R
+      if (mode == 2) {
+        rate = make_float2(-3.14159265358979f * pb.w * g2 + 6.283185307179586f / pb.w, 0.f);
+      } else {
+        const float arg = pb.x * pb.x - g2;
+        // sqrt(complex(arg)); conj for z < 0
+        float2 kz = arg >= 0.f ? make_float2(sqrtf(arg), 0.f) : make_float2(0.f, sqrtf(-arg));
+        if (zneg) kz.y = -kz.y;
+        const float off = (mode == 1 && track) ? (pb.y * fx + pb.z * fy) * pb.w : 0.f;
+        rate = make_float2(6.283185307179586f * (kz.x + off), 6.283185307179586f * kz.y);
+      }
       float2 h = H[(long long)h_index[b] * npix + q];
-      // dH = 2 pi i kz H
-      float2 dh = cmul(make_float2(-6.283185307179586f * kz.y, 6.283185307179586f * kz.x), h);
+      // dH = i R H
+      float2 dh = cmul(make_float2(-rate.y, rate.x), h);
       if (backward) dh = cconj(dh);
       const long long o = (long long)b * npix + q;
       const float2 ug = cmul(U[o], cconj(G[o]));
@@ -641,10 +659,10 @@ cudaError_t launch_as_h(float2* H, int fx_n, int fy_n, double dx, double dy, dou
 
 cudaError_t launch_as_h_general(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
                                 double z, double scale, int mode, double theta_x, double theta_y, int track,
-                                const double2* filter, cudaStream_t s) {
+                                const double2* filter, cudaStream_t s, const float* zp) {
   const double lm = lambda / n0;
   as_h_general_kernel<<<capped_grid((long long)fx_n * fy_n), kThreads, 0, s>>>(
-      H, fx_n, fy_n, dx, dy, lm, z, scale, mode, sin(theta_x) / lm, sin(theta_y) / lm, track, filter);
+      H, fx_n, fy_n, dx, dy, lm, z, scale, mode, sin(theta_x) / lm, sin(theta_y) / lm, track, filter, zp);
   return cudaGetLastError();
 }
 
@@ -659,10 +677,10 @@ cudaError_t launch_as_h_z(float2* H, int fx_n, int fy_n, double dx, double dy, d
 int as_z_grad_blocks() { return 304; }
 
 cudaError_t launch_as_z_grad(const float2* U, const float2* G, const float2* H, const int* h_index,
-                             const float* lam_eff, int fx_n, int fy_n, double dx, double dy, const float* z, int batch,
-                             int backward, double* partials, float* dz, cudaStream_t st) {
-  as_z_grad_partial_kernel<<<as_z_grad_blocks(), kThreads, 0, st>>>(U, G, H, h_index, lam_eff, fx_n, fy_n, dx, dy, z,
-                                                                   batch, backward, partials);
+                             const float4* par, int mode, int track, int fx_n, int fy_n, double dx, double dy,
+                             const float* z, int batch, int backward, double* partials, float* dz, cudaStream_t st) {
+  as_z_grad_partial_kernel<<<as_z_grad_blocks(), kThreads, 0, st>>>(U, G, H, h_index, par, mode, track, fx_n, fy_n,
+                                                                   dx, dy, z, batch, backward, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   as_z_grad_final_kernel<<<1, 32, 0, st>>>(partials, as_z_grad_blocks(), dz);

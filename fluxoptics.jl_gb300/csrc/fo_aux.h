@@ -9,13 +9,13 @@ cudaError_t launch_as_h(float2* H, int fx_n, int fy_n, double dx, double dy, dou
                         double z, double scale, cudaStream_t s);
 cudaError_t launch_as_h_general(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
                                 double z, double scale, int mode, double theta_x, double theta_y, int track,
-                                const double2* filter, cudaStream_t s);
+                                const double2* filter, cudaStream_t s, const float* zp = nullptr);
 cudaError_t launch_as_h_z(float2* H, int fx_n, int fy_n, double dx, double dy, double lambda, double n0,
                           const float* z, double scale, cudaStream_t s);
 int as_z_grad_blocks();
 cudaError_t launch_as_z_grad(const float2* U, const float2* G, const float2* H, const int* h_index,
-                             const float* lam_eff, int fx_n, int fy_n, double dx, double dy, const float* z, int batch,
-                             int backward, double* partials, float* dz, cudaStream_t st);
+                             const float4* par, int mode, int track, int fx_n, int fy_n, double dx, double dy,
+                             const float* z, int batch, int backward, double* partials, float* dz, cudaStream_t st);
 cudaError_t launch_fourier_h(float2* H, int kind, const void* param, long long n, double scale, cudaStream_t s);
 cudaError_t launch_fourier_grad(int kind, const void* param, const float2* U, const float2* A, void* grad,
                                 long long npix, int batch, float s, cudaStream_t st);

@@ -249,7 +249,11 @@ struct fo_prop_plan_s {
   int h_mode = 0;                   // 0 on axis, 1 tilted, 2 paraxial
   std::vector<double> table_lambda; // wavelength of each transfer-function table
   double* zgrad_partials = nullptr; // ASPropZ gradient: block partial sums
-  float* lam_eff = nullptr;         // ASPropZ gradient: n0 / lambda per field
+  float4* zpar = nullptr;           // ASPropZ gradient: per field {n0 / lambda, f0x, f0y, lambda / n0}
+  std::vector<std::array<double, 2>> table_theta;  // tilts of each table (tilted / paraxial kernels)
+  int track = 0;                    // track_tilts of the tilted / paraxial kernels
+  bool has_filter = false;          // the tables carry a frequency filter
+  double2* filters = nullptr;       // n_tables x fy x fx filter values, kept for fo_prop_set_z
   int n_tables = 0;
   float2* H = nullptr;          // n_tables x fy x fx, scaled by 1/(fx*fy)
   int* h_index = nullptr;       // device, per field
@@ -296,7 +300,8 @@ void plan_free(fo_prop_plan p) {
   cudaFree(p->spec_a);
   cudaFree(p->spec_b);
   cudaFree(p->zgrad_partials);
-  cudaFree(p->lam_eff);
+  cudaFree(p->zpar);
+  cudaFree(p->filters);
   delete p;
 }
 
@@ -394,7 +399,8 @@ int row_fields_per_cta() {
 // selected by the inv/fwd flags.
 int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bool fwd_after,
              const Mod& mod, bool bwd, float s, const float* inv_lambda, const SeedArgs* seed,
-             const float2* tw, cudaStream_t st, const fo_sid_s* sid = nullptr, const float* target = nullptr) {
+             const float2* tw, cudaStream_t st, const fo_sid_s* sid = nullptr, const float* target = nullptr,
+             float2* probe_pre = nullptr, float2* probe_post = nullptr) {
   RowPassArgs a;
   std::memset(&a, 0, sizeof(a));
   const long long real_bs = (long long)L.nx * L.ny, spec_bs = (long long)L.fx * L.ny;
@@ -424,6 +430,8 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
     a.save = reinterpret_cast<float2*>(mod.saved);
     a.save_bstride = real_bs;
     a.save_ld = L.nx;
+    a.probe_pre = probe_pre;
+    a.probe_post = probe_post;
   } else {
     a.saved = reinterpret_cast<const float2*>(mod.saved);
     a.saved_bstride = real_bs;
@@ -480,9 +488,10 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.n_items = p->n_items;
   int v = p->col_v;
   const float2* tw = p->tw_y;
-  alignas(64) CUtensorMap tm_buf, tm_h;
+  alignas(64) CUtensorMap tm_buf, tm_h, tm_out;
   if (col_variant_uses_tma(p->fy, v)) {
     const int W = col_variant(p->fy, v).lanes;
+    const bool skew = col_variant(p->fy, v).P == 8;
     // whole tiles in one TMA instruction when the field height is a multiple of 256
     const bool t4 = p->ny % 256 == 0 && p->fy % 256 == 0 && env_int("FO_TILE4D", 1) != 0;
     int rc = t4 ? encode_tmap_4d(&tm_buf, buf, p->batch, p->ny, p->fx, p->fx, W)
@@ -490,6 +499,8 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
     if (rc == FO_OK)
       rc = t4 ? encode_tmap_4d(&tm_h, p->H, p->n_tables, p->fy, p->fx, p->fx, W)
               : encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256);
+    if (rc == FO_OK && skew) rc = t4 ? encode_tmap_4d(&tm_out, buf, p->batch, p->ny, p->fx, p->fx, 2) : FO_ERR_SHAPE;
+    if (rc == FO_OK && skew) a.tmap_out = &tm_out;
     a.tile4d = t4 ? 1 : 0;
     if (rc != FO_OK) {  // e.g. an unaligned caller buffer: use the cp.async variant
       v = 0;
@@ -514,20 +525,28 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
 // Forward sweep.  With `sid` (fused form only: every target slice has the same
 // number of fields) the last pass also evaluates the metric on u against `target`
 // and loss[T] receives the per-slice sums.
+// With `probes`, probes[0][k] / probes[1][k] (k = 0..K, NULL entries skipped) receive the
+// field before / after modulation slot k from the row pass that applies it.
 int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, const Mod* mods, int s,
                 cudaStream_t st, const float2* src = nullptr, const fo_sid_s* sid = nullptr,
-                const float* target = nullptr, float* loss = nullptr) {
+                const float* target = nullptr, float* loss = nullptr,
+                const std::vector<float2*>* probes = nullptr) {
   const int K = (int)props.size();
   const Layout L = layout_of(props[0]);
   const float* il = props[0]->inv_lambda;
   const float sf = (float)s;
-  FO_TRY(row_pass(L, src ? src : u, buf, false, true, mods[0], false, sf, il, nullptr, props[0]->tw_x, st));
+  auto pre = [&](int k) { return probes ? probes[0][k] : nullptr; };
+  auto post = [&](int k) { return probes ? probes[1][k] : nullptr; };
+  FO_TRY(row_pass(L, src ? src : u, buf, false, true, mods[0], false, sf, il, nullptr, props[0]->tw_x, st, nullptr,
+                  nullptr, pre(0), post(0)));
   for (int k = 0; k < K; ++k) {
     FO_TRY(col_pass(props[k], buf, s < 0, st));
     if (k + 1 < K)
-      FO_TRY(row_pass(L, buf, buf, true, true, mods[k + 1], false, sf, il, nullptr, props[0]->tw_x, st));
+      FO_TRY(row_pass(L, buf, buf, true, true, mods[k + 1], false, sf, il, nullptr, props[0]->tw_x, st, nullptr,
+                      nullptr, pre(k + 1), post(k + 1)));
     else
-      FO_TRY(row_pass(L, buf, u, true, false, mods[K], false, sf, il, nullptr, props[0]->tw_x, st, sid, target));
+      FO_TRY(row_pass(L, buf, u, true, false, mods[K], false, sf, il, nullptr, props[0]->tw_x, st, sid, target,
+                      pre(K), post(K)));
   }
   if (sid) FO_LAUNCH(launch_sid_finalize(sid->partials, L.ny, sid->T, loss, st));
   return FO_OK;
@@ -684,16 +703,19 @@ int autotune_plan(fo_prop_plan p) {
       a.field_list = idx;
       a.item_start = idx + nb;
       a.n_items = n_items;
-      alignas(64) CUtensorMap tm_buf, tm_h;
+      alignas(64) CUtensorMap tm_buf, tm_h, tm_out;
       if (col_variant_uses_tma(p->fy, v)) {
         if (pf) continue;  // staging is built in
         const int W = col_variant(p->fy, v).lanes;
+        const bool skew = col_variant(p->fy, v).P == 8;
         const bool t4 = p->ny % 256 == 0 && p->fy % 256 == 0 && env_int("FO_TILE4D", 1) != 0;
         if ((t4 ? encode_tmap_4d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W)
                 : encode_tmap_3d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W, 256)) != FO_OK ||
             (t4 ? encode_tmap_4d(&tm_h, p->H, p->n_tables, p->fy, p->fx, p->fx, W)
                 : encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256)) != FO_OK)
           continue;
+        if (skew && (!t4 || encode_tmap_4d(&tm_out, tmp, nb, p->ny, p->fx, p->fx, 2) != FO_OK)) continue;
+        if (skew) a.tmap_out = &tm_out;
         a.tile4d = t4 ? 1 : 0;
         a.tmap_buf = &tm_buf;
         a.tmap_h = &tm_h;
@@ -844,7 +866,11 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   }
   p->n_tables = (int)uniq.size();
   p->h_mode = h_mode;
-  for (const auto& k : uniq) p->table_lambda.push_back(k[0]);
+  for (const auto& k : uniq) {
+    p->table_lambda.push_back(k[0]);
+    p->table_theta.push_back({k[1], k[2]});
+  }
+  p->track = (opt && opt->track_tilts) ? 1 : 0;
   int rc = FO_OK;
   const size_t table = (size_t)fx * fy;
   if ((rc = dalloc(&p->H, table * p->n_tables, "transfer functions")) != FO_OK ||
@@ -907,8 +933,18 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
   }
   const double scale = 1.0 / ((double)fx * (double)fy);
   double2* d_filter = nullptr;
+  // plans whose distance is later set from device memory keep the filter values of
+  // every table (the rebuild needs them); others fill one scratch table per table
+  const bool keep_filter = kind == 0 && opt && opt->filter && (flags & (FO_FLAG_GRAD_SPECTRA | FO_FLAG_DEVICE_Z));
   if (kind == 0 && opt && opt->filter) {
-    if ((rc = dalloc(&d_filter, table, "filter values")) != FO_OK) {
+    p->has_filter = true;
+    if (keep_filter) {
+      if ((rc = dalloc(&p->filters, table * p->n_tables, "filter values")) != FO_OK) {
+        plan_free(p);
+        return rc;
+      }
+      p->ws_bytes += sizeof(double2) * table * p->n_tables;
+    } else if ((rc = dalloc(&d_filter, table, "filter values")) != FO_OK) {
       plan_free(p);
       return rc;
     }
@@ -920,7 +956,8 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     float2* Hi = p->H + table * i;
     if (kind == 0) {
       const double lam = uniq[i][0];
-      if (d_filter) {
+      double2* fl = p->filters ? p->filters + table * i : d_filter;
+      if (fl) {
         // the reference evaluates the filter at the (tilt-shifted for the tilted
         // kernel) frequencies: filter(fx + f0x, fy + f0y), f0 = sin(theta) n0 / lambda
         const double lm = lam / n0;
@@ -938,14 +975,14 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
         opt->filter(ffx.data(), ffy.data(), (long long)table, fre.data(), fim.data(), opt->filter_ctx);
         fval.resize(table);
         for (size_t q = 0; q < table; ++q) fval[q] = make_double2(fre[q], fim[q]);
-        e = cudaMemcpy(d_filter, fval.data(), sizeof(double2) * table, cudaMemcpyHostToDevice);
+        e = cudaMemcpy(fl, fval.data(), sizeof(double2) * table, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) break;
       }
-      if (h_mode == 0 && !d_filter)
+      if (h_mode == 0 && !fl)
         e = launch_as_h(Hi, fx, fy, dx, dy, lam, n0, z, scale, 0);
       else
         e = launch_as_h_general(Hi, fx, fy, dx, dy, lam, n0, z, scale, h_mode, uniq[i][1], uniq[i][2],
-                                opt && opt->track_tilts ? 1 : 0, d_filter, 0);
+                                opt && opt->track_tilts ? 1 : 0, fl, 0);
       if (d_filter && e == cudaSuccess) e = cudaDeviceSynchronize();  // d_filter is refilled next
     } else {
       e = launch_rs_h_spatial(Hi, nx, ny, fx, fy, dx, dy, uniq[i][0], z, scale, 0);
@@ -978,15 +1015,19 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
     if ((rc = dalloc(&p->spec_a, nf, "gradient spectra")) != FO_OK ||
         (rc = dalloc(&p->spec_b, nf, "gradient spectra")) != FO_OK ||
         (rc = dalloc(&p->zgrad_partials, (size_t)as_z_grad_blocks(), "z-gradient partials")) != FO_OK ||
-        (rc = dalloc(&p->lam_eff, batch, "n0 / lambda")) != FO_OK) {
+        (rc = dalloc(&p->zpar, batch, "z-gradient field parameters")) != FO_OK) {
       if (d_filter) cudaFree(d_filter);
       plan_free(p);
       return rc;
     }
     p->ws_bytes += 2 * sizeof(float2) * nf;
-    std::vector<float> le(batch);
-    for (int b = 0; b < batch; ++b) le[b] = (float)(n0 / p->lambdas[b]);
-    e = cudaMemcpy(p->lam_eff, le.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
+    std::vector<float4> zp(batch);
+    for (int b = 0; b < batch; ++b) {
+      const double lm = p->lambdas[b] / n0;
+      const double f0x = h_mode ? sin(tilt[b][0]) / lm : 0.0, f0y = h_mode ? sin(tilt[b][1]) / lm : 0.0;
+      zp[b] = make_float4((float)(1.0 / lm), (float)f0x, (float)f0y, (float)lm);
+    }
+    e = cudaMemcpy(p->zpar, zp.data(), sizeof(float4) * batch, cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (d_filter) cudaFree(d_filter);
@@ -1115,26 +1156,36 @@ static int fft2_into(const fo_prop_plan_s* p, const float2* src, float2* dst, cu
 
 FO_API int fo_prop_set_z(fo_prop_plan plan, const float* z, void* stream) {
   if (!plan || !z) return fail(FO_ERR_ARG, "plan and z must not be NULL");
-  if (plan->kind != 0 || plan->h_mode != 0) return fail(FO_ERR_ARG, "fo_prop_set_z needs an on-axis ASProp plan");
+  if (plan->kind != 0) return fail(FO_ERR_ARG, "fo_prop_set_z needs an ASProp plan");
+  if (plan->has_filter && !plan->filters)
+    return fail(FO_ERR_ARG, "a filtered plan needs FO_FLAG_DEVICE_Z (or FO_FLAG_GRAD_SPECTRA) for fo_prop_set_z");
   const double scale = 1.0 / ((double)plan->fx * (double)plan->fy);
   const size_t table = (size_t)plan->fx * plan->fy;
-  for (int i = 0; i < plan->n_tables; ++i)
-    FO_LAUNCH(launch_as_h_z(plan->H + table * i, plan->fx, plan->fy, plan->dx, plan->dy, plan->table_lambda[i],
-                            plan->n0, z, scale, S(stream)));
+  for (int i = 0; i < plan->n_tables; ++i) {
+    float2* Hi = plan->H + table * i;
+    if (plan->h_mode == 0 && !plan->filters)
+      FO_LAUNCH(launch_as_h_z(Hi, plan->fx, plan->fy, plan->dx, plan->dy, plan->table_lambda[i], plan->n0, z, scale,
+                              S(stream)));
+    else
+      FO_LAUNCH(launch_as_h_general(Hi, plan->fx, plan->fy, plan->dx, plan->dy, plan->table_lambda[i], plan->n0,
+                                    0.0, scale, plan->h_mode, plan->table_theta[i][0], plan->table_theta[i][1],
+                                    plan->track, plan->filters ? plan->filters + table * i : nullptr, S(stream), z));
+  }
   return FO_OK;
 }
 
 FO_API int fo_prop_z_gradient(fo_prop_plan plan, const float* z, const void* u_saved, const void* du, int direction,
                               float* dz, void* stream) {
   if (!plan || !z || !u_saved || !du || !dz) return fail(FO_ERR_ARG, "plan, z, u_saved, du and dz must not be NULL");
-  if (plan->kind != 0 || plan->h_mode != 0 || !plan->spec_a)
-    return fail(FO_ERR_ARG, "needs an on-axis ASProp plan created with FO_FLAG_GRAD_SPECTRA");
+  if (plan->kind != 0 || !plan->spec_a)
+    return fail(FO_ERR_ARG, "needs an ASProp plan created with FO_FLAG_GRAD_SPECTRA");
   FO_TRY(check_dir(direction));
   cudaStream_t st = S(stream);
   FO_TRY(fft2_into(plan, reinterpret_cast<const float2*>(u_saved), plan->spec_a, st));
   FO_TRY(fft2_into(plan, reinterpret_cast<const float2*>(du), plan->spec_b, st));
-  FO_LAUNCH(launch_as_z_grad(plan->spec_a, plan->spec_b, plan->H, plan->h_index, plan->lam_eff, plan->fx, plan->fy,
-                             plan->dx, plan->dy, z, plan->batch, direction < 0, plan->zgrad_partials, dz, st));
+  FO_LAUNCH(launch_as_z_grad(plan->spec_a, plan->spec_b, plan->H, plan->h_index, plan->zpar, plan->h_mode,
+                             plan->track, plan->fx, plan->fy, plan->dx, plan->dy, z, plan->batch, direction < 0,
+                             plan->zgrad_partials, dz, st));
   return FO_OK;
 }
 
@@ -1213,7 +1264,8 @@ FO_API int fo_prop_variants(fo_prop_plan plan, int* row_v, int* col_v, char* row
   const PassVariant cv = col_variant(plan->fy, plan->col_v);
   put(row_kernel, "row_pass_kernel<" + std::to_string(plan->fx) + ", E=" + std::to_string(rv.E) +
                       ", rows/CTA=" + std::to_string(rv.lanes) + (plan->row_pf ? ", cp.async staging>" : ">"));
-  const char* form = cv.P == 6   ? "col_tma_kernel (TMA load/store, register twiddles)"
+  const char* form = cv.P == 8   ? "col_tma_skew_kernel (TMA load/store, two halves one FFT stage apart)"
+                     : cv.P == 6   ? "col_tma_kernel (TMA load/store, register twiddles)"
                      : cv.P == 4 ? "col_tma_kernel (TMA load/store)"
                      : cv.P == 2 ? "col_pass2_kernel (paired columns)"
                      : cv.P == 0 ? "col_lane_kernel (lane-major)"
@@ -1314,6 +1366,8 @@ FO_API int fo_mask_backward(void* dv, const void* m, const void* u_saved, void* 
 struct fo_chain_s {
   std::vector<fo_prop_plan> props;
   float2* scratch = nullptr;  // padded layouts only
+  std::vector<float2*> probes[2];  // field probes before / after each modulation slot (empty: none)
+  const std::vector<float2*>* probe_ptr() const { return probes[0].empty() ? nullptr : probes; }
 };
 
 extern "C" {
@@ -1349,6 +1403,29 @@ FO_API int fo_chain_destroy(fo_chain chain) {
   return FO_OK;
 }
 
+FO_API int fo_chain_set_probes(fo_chain chain, void* const* pre, void* const* post) {
+  if (!chain) return fail(FO_ERR_ARG, "chain is NULL");
+  const int K = (int)chain->props.size();
+  bool any = false;
+  for (int k = 0; k <= K; ++k) any = any || (pre && pre[k]) || (post && post[k]);
+  for (int h = 0; h < 2; ++h) chain->probes[h].clear();
+  if (!any) return FO_OK;
+  for (int h = 0; h < 2; ++h) {
+    void* const* src = h == 0 ? pre : post;
+    chain->probes[h].assign(K + 1, nullptr);
+    for (int k = 0; k <= K; ++k) {
+      void* q = src ? src[k] : nullptr;
+      if (q && (reinterpret_cast<uintptr_t>(q) & 7) != 0) {
+        chain->probes[0].clear();
+        chain->probes[1].clear();
+        return fail(FO_ERR_ARG, "probe buffers must be 8-byte aligned");
+      }
+      chain->probes[h][k] = reinterpret_cast<float2*>(q);
+    }
+  }
+  return FO_OK;
+}
+
 FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int direction, void* stream) {
   if (!chain || !u || !mods) return fail(FO_ERR_ARG, "chain, u and mods must not be NULL");
   FO_TRY(check_dir(direction));
@@ -1360,7 +1437,8 @@ FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int dir
   }
   float2* uu = reinterpret_cast<float2*>(u);
   float2* buf = chain->scratch ? chain->scratch : uu;
-  return run_forward(chain->props, buf, uu, m.data(), direction, S(stream));
+  return run_forward(chain->props, buf, uu, m.data(), direction, S(stream), nullptr, nullptr, nullptr, nullptr,
+                     chain->probe_ptr());
 }
 
 FO_API int fo_chain_forward_from(fo_chain chain, const void* u_in, void* u, const fo_mod* mods,
@@ -1376,7 +1454,7 @@ FO_API int fo_chain_forward_from(fo_chain chain, const void* u_in, void* u, cons
   float2* uu = reinterpret_cast<float2*>(u);
   float2* buf = chain->scratch ? chain->scratch : uu;
   return run_forward(chain->props, buf, uu, m.data(), direction, S(stream),
-                     reinterpret_cast<const float2*>(u_in));
+                     reinterpret_cast<const float2*>(u_in), nullptr, nullptr, nullptr, chain->probe_ptr());
 }
 
 FO_API int fo_chain_forward_sid(fo_chain chain, const void* u_in, void* u, const fo_mod* mods, int direction,
@@ -1396,9 +1474,12 @@ FO_API int fo_chain_forward_sid(fo_chain chain, const void* u_in, void* u, const
   float2* uu = reinterpret_cast<float2*>(u);
   float2* buf = chain->scratch ? chain->scratch : uu;
   const float2* src = reinterpret_cast<const float2*>(u_in);
-  if (sid->group > 0) return run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src, sid, target, loss);
+  if (sid->group > 0)
+    return run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src, sid, target, loss,
+                       chain->probe_ptr());
   // slices with different field counts: the metric runs as its own pass
-  FO_TRY(run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src));
+  FO_TRY(run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src, nullptr, nullptr, nullptr,
+                     chain->probe_ptr()));
   return fo_sid_forward(sid, u, target, loss, stream);
 }
 

@@ -71,6 +71,10 @@ struct RowPassArgs {
   float* sid_resid;
   float* sid_partials;
   int sid_T;
+  // field probes of a forward pass (real-space layout of `save`): a copy of the field
+  // before (probe_pre) and after (probe_post) the modulation; either may be NULL
+  float2* probe_pre;
+  float2* probe_post;
 };
 
 // One column pass: forward FFT along y, multiply by the transfer function of the
@@ -101,6 +105,7 @@ struct ColPassArgs {
   // (tables * N) x ncols; the device error word and the wait limit.
   const void* tmap_buf;
   const void* tmap_h;
+  const void* tmap_out;  // skewed variant: the buffer's 4-D view with 2-column boxes (result stores)
   unsigned int* err_word;
   unsigned long long wait_ns;
   int test_skip_copy;  // test knob: arm the barrier but issue no copy (the wait must time out)

@@ -36,6 +36,8 @@ import FluxOptics.OpticalComponents: propagate!, backpropagate!, propagate_and_s
 
 const LIB = joinpath(@__DIR__, "..", "lib", "libfluxoptics_gb300.so")
 const FO_FLAG_AUTOTUNE = Cint(1)
+const FO_FLAG_GRAD_SPECTRA = Cint(2)
+const FO_FLAG_DEVICE_Z = Cint(4)
 const FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = Cint(0), Cint(1), Cint(2), Cint(3), Cint(4)
 
 struct FoMod            # mirrors `fo_mod`
@@ -450,14 +452,29 @@ mutable struct GB300ASPropZ{M, A} <: AbstractCustomComponent{M}
     z::A                      # CuArray{Float32}(1)
 end
 
-function GB300ASPropZ(u::ScalarField, z::Real; n0::Real = 1, trainable::Bool = false)
+"""GB300ASPropZ(u, z; n0=1, trainable=false, paraxial=false, track_tilts=false) -- ASPropZ
+(angular_spectrum.jl:274-344) with the on-axis, tilted (u.tilts) or paraxial kernel; the
+transfer functions are rebuilt from the device-resident z on every call."""
+function GB300ASPropZ(u::ScalarField, z::Real; n0::Real = 1, trainable::Bool = false, paraxial::Bool = false,
+                      track_tilts::Bool = false)
     nx, ny, b = dims_of(u)
     lam = lambdas_per_field(u)
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:fo_asprop_create, LIB), Cint,
-                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
-                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0,
-                FO_FLAG_AUTOTUNE | (trainable ? Cint(2) : Cint(0))))
+    flags = FO_FLAG_AUTOTUNE | FO_FLAG_DEVICE_Z | (trainable ? FO_FLAG_GRAD_SPECTRA : Cint(0))
+    if !paraxial && !track_tilts && FluxOptics.is_on_axis(u)
+        check(ccall((:fo_asprop_create, LIB), Cint,
+                    (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
+                    h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0, flags))
+    else
+        th = tilts_per_field(u)
+        GC.@preserve th begin
+            opt = Ref(FoASOptions(Cint(paraxial), Cint(track_tilts), pointer(th), Cint(b), C_NULL, C_NULL))
+            check(ccall((:fo_asprop_create_ex, LIB), Cint,
+                        (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble,
+                         Ref{FoASOptions}, Cint),
+                        h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), z, n0, opt, flags))
+        end
+    end
     zd = CuArray(Float32[z])
     M = trainable ? Trainable{Unbuffered} : Static
     p = GB300ASPropZ{M, typeof(zd)}(h[], zd)

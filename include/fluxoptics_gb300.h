@@ -52,6 +52,7 @@ extern "C" {
 #define FO_FLAG_AUTOTUNE 1 /* time every launch shape of the passes and keep the fastest */
 #define FO_FOURIER_TRAINABLE 2 /* fo_fourier_create: allocate the spectra of fo_fourier_gradient */
 #define FO_FLAG_GRAD_SPECTRA 2 /* fo_asprop_create(_ex): allocate the spectra of fo_prop_z_gradient */
+#define FO_FLAG_DEVICE_Z 4     /* fo_asprop_create_ex: keep what fo_prop_set_z needs to rebuild a filtered plan */
 
 /* Modulation kinds (fo_mod.kind) */
 #define FO_MOD_NONE 0
@@ -174,14 +175,18 @@ FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, doubl
  * fourier/fourier_operator.jl:37-83).
  */
 /*
- * ASPropZ (trainable distance) on an on-axis ASProp plan: fo_prop_set_z rebuilds the
- * transfer functions in FP64 from the distance held in device memory (float z, read
- * on the stream, so an iteration that updates z can be captured as one graph).
+ * ASPropZ (trainable distance) on an ASProp plan of any kernel (on axis, tilted or
+ * paraxial, with or without a filter): fo_prop_set_z rebuilds the transfer functions
+ * in FP64 from the distance held in device memory (float z, read on the stream, so an
+ * iteration that updates z can be captured as one graph).  A filtered plan must be
+ * created with FO_FLAG_DEVICE_Z or FO_FLAG_GRAD_SPECTRA, which keep its filter values.
  * fo_prop_z_gradient (plan created with FO_FLAG_GRAD_SPECTRA) writes to *dz the
  * derivative of the loss with respect to z, from the propagator's input u_saved and
  * the adjoint du at its output: Re sum_b sum_k U conj(G) dH/dz / N with U = FFT2(u_saved),
- * G = FFT2(du), dH/dz = 2 pi i kz H (kz = sqrt(complex(n0^2/lambda^2 - f^2)); conj(kz) for
- * z < 0), conjugated for the Backward direction -- what Zygote computes through the
+ * G = FFT2(du), dH/dz = i R H, conjugated for the Backward direction, where R is the
+ * kernel's phase rate: 2 pi (kz + off) for the on-axis and tilted kernels (kz =
+ * sqrt(complex(1/lm^2 - (f+f0)^2)), conj for z < 0, off the tilt-tracking term) and
+ * -pi lm (f+f0)^2 + 2 pi / lm for the paraxial one -- what Zygote computes through the
  * reference's propagate(u, ::ASPropZ) (angular_spectrum.jl:274-344).
  */
 FO_API int fo_prop_set_z(fo_prop_plan plan, const float* z, void* stream);
@@ -293,6 +298,20 @@ typedef struct fo_chain_s* fo_chain;
  */
 FO_API int fo_chain_create(fo_chain* chain, int n_props, const fo_prop_plan* props);
 FO_API int fo_chain_destroy(fo_chain chain);
+
+/*
+ * Field probes of the chain's forward calls: pre[k] receives the field entering
+ * modulation slot k (after propagator k-1; pre[0] is the chain input) and post[k]
+ * the field leaving it (before propagator k; post[n_props] is the chain output),
+ * k = 0..n_props.  Each non-NULL pointer is a caller-owned batch x ny x nx complex
+ * float array written by the row pass that applies slot k, so probes cost no extra
+ * pass.  The pointers stay set for every later fo_chain_forward[_from|_sid] until
+ * replaced; NULL arrays (or all-NULL entries) remove them.  Probes are not written
+ * by the adjoint sweep.
+ * Replaces: FieldProbe (system/field_probe.jl:31-43) collected into
+ * result.probes by OpticalSystem (system/optical_system.jl:194-214).
+ */
+FO_API int fo_chain_set_probes(fo_chain chain, void* const* pre, void* const* post);
 
 /* Forward through the chain, in place on u; mods has n_props+1 entries. */
 FO_API int fo_chain_forward(fo_chain chain, void* u, const fo_mod* mods, int direction,

@@ -185,11 +185,10 @@ def as_kernel_general(nx, ny, dx, dy, lam, z, n0=1.0, paraxial=False, theta=(0.0
     off = (f0x * FX + f0y * FY) * lm if (tilted and track_tilts) else 0.0
     za = abs(z)
     h = np.exp(1j * 2 * np.pi * za * (np.sqrt((1 / lm ** 2 - gx ** 2 - gy ** 2).astype(np.complex128)) + off))
-    if z < 0:
-        h = np.conj(h)
     if filt is not None:
         h = h * filt(gx, gy)
-    return h
+    # z < 0: conj of the z > 0 kernel, filter value included (angular_spectrum.jl:9-12, 55-60)
+    return np.conj(h) if z < 0 else h
 
 
 def rs_kernel_spatial(n_x, n_y, dx, dy, lam, z, m_x=None, m_y=None):
@@ -280,30 +279,59 @@ def asprop(u, dx, dy, lambdas, z, direction=FORWARD, n0=1.0, paraxial=False, til
     return out.reshape(shp)
 
 
-def asprop_z_gradient(u_in, du, dx, dy, lambdas, z, direction=FORWARD, n0=1.0):
+def asprop_z_gradient(u_in, du, dx, dy, lambdas, z, direction=FORWARD, n0=1.0, paraxial=False, tilts=None,
+                      track_tilts=False, filt=None, return_scale=False):
     """d loss / d z of ASPropZ as Zygote computes it through
     ifft(fft(u) .* conj_direction(kernel)) (angular_spectrum.jl:325-344): with
-    U = FFT2(u_in), G = FFT2(du) (du the adjoint at the output) and
-    dH/dz = 2 pi i kz H (kz = sqrt(complex(n0^2/lambda^2 - f^2)), conj(kz) for z < 0),
-    dz = Re sum_b sum_k U conj(G) conj_direction(dH/dz) / (nx ny)."""
+    U = FFT2(u_in), G = FFT2(du) (du the adjoint at the output) and dH/dz = i R H,
+    dz = Re sum_b sum_k U conj(G) conj_direction(dH/dz) / (nx ny).  R is the derivative
+    in z of the kernel's phase (lm = lambda / n0, g = f + f0, f0 = sin(theta) / lm;
+    angular_spectrum.jl:1-76): on axis and tilted, R = 2 pi (sqrt(complex(1/lm^2 - g^2))
+    + off) with off = track_tilts ? (f0x fx + f0y fy) lm : 0, conjugated for z < 0;
+    paraxial, R = -pi lm g^2 + 2 pi / lm.  The filter is constant in z.
+
+    With ``return_scale`` also returns the sum of the magnitudes of the summed terms,
+    sum |U conj(G) dH| / (nx ny): the sum nearly cancels for intensity losses (the
+    constant part of R is a global phase), and a float32 evaluation of it is accurate
+    to a few ulps of that scale, not of the result."""
     u = np.asarray(u_in, dtype=np.complex128)
     g = np.asarray(du, dtype=np.complex128)
     ny, nx = u.shape[-2:]
     u = u.reshape(-1, ny, nx)
     g = g.reshape(-1, ny, nx)
     lam = _lams(lambdas, u.shape[0])
+    th = np.zeros((u.shape[0], 2))
+    if tilts is not None:
+        th[:] = np.asarray(tilts, dtype=np.float64).reshape(-1, 2)
+    general = paraxial or filt is not None or bool(np.any(th != 0.0))
     fx, fy = fftfreqs(nx, ny, dx, dy)
+    FX, FY = fx[None, :] + 0 * fy[:, None], fy[:, None] + 0 * fx[None, :]
     tot = 0.0
+    scale = 0.0
     for b in range(u.shape[0]):
         lm = lam[b] / n0
-        kz = np.sqrt((1.0 / lm ** 2 - fx[None, :] ** 2 - fy[:, None] ** 2).astype(np.complex128))
-        if z < 0:
-            kz = np.conj(kz)
-        dh = 2j * np.pi * kz * as_kernel(nx, ny, dx, dy, lam[b], z, n0)
+        tilted = th[b, 0] != 0.0 or th[b, 1] != 0.0
+        f0x, f0y = (np.sin(th[b, 0]) / lm, np.sin(th[b, 1]) / lm) if (tilted or paraxial) else (0.0, 0.0)
+        gx, gy = FX + f0x, FY + f0y
+        if paraxial:
+            rate = -np.pi * lm * (gx ** 2 + gy ** 2) + 2 * np.pi / lm + 0j
+        else:
+            kz = np.sqrt((1.0 / lm ** 2 - gx ** 2 - gy ** 2).astype(np.complex128))
+            off = (f0x * FX + f0y * FY) * lm if (tilted and track_tilts) else 0.0
+            rate = 2 * np.pi * (kz + off)
+            if z < 0:
+                rate = np.conj(rate)
+        if general:
+            h = as_kernel_general(nx, ny, dx, dy, lam[b], z, n0, paraxial, tuple(th[b]), track_tilts, filt)
+        else:
+            h = as_kernel(nx, ny, dx, dy, lam[b], z, n0)
+        dh = 1j * rate * h
         if direction != FORWARD:
             dh = np.conj(dh)
-        tot += float(np.real(np.sum(fft2(u[b]) * np.conj(fft2(g[b])) * dh))) / (nx * ny)
-    return tot
+        terms = fft2(u[b]) * np.conj(fft2(g[b])) * dh
+        tot += float(np.real(np.sum(terms))) / (nx * ny)
+        scale += float(np.sum(np.abs(terms))) / (nx * ny)
+    return (tot, scale) if return_scale else tot
 
 
 def rsprop(u, dx, dy, lambdas, z, direction=FORWARD, pad=None):

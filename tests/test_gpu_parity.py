@@ -414,6 +414,50 @@ def test_asprop_z_trainable_distance(fo, orc, d):
     assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
 
 
+@pytest.mark.parametrize("mode", ["paraxial", "tilted", "tilted_track", "filtered", "paraxial_track_filtered"])
+@pytest.mark.parametrize("z0", [180.0, -140.0])
+def test_asprop_z_general_kernels(fo, orc, mode, z0):
+    """ASPropZ with the reference's other kernels (angular_spectrum.jl:274-344): the
+    paraxial kernel, the tilted kernel on fields with per-field tilts (with and without
+    tilt tracking) and a complex frequency filter, for both signs of z: the propagated
+    field after the distance was rebuilt from device memory, and dL/dz, against the
+    oracle; a later z set on the device moves the result accordingly.
+
+    dL/dz of an intensity loss is a sum over the spectra that nearly cancels: the
+    constant part of the kernel's phase rate, 2 pi n0 / lambda, is a global phase the
+    loss does not see, and it dominates every term (the terms' magnitudes add up to
+    1e3 - 1e5 times the result here).  Computed from float32 spectra, the sum is
+    accurate to about one float32 ulp of that magnitude, so dL/dz is held to 1e-4 of
+    its value plus float32 epsilon times the sum of magnitudes."""
+    rng = np.random.default_rng(33)
+    n, B = 128, 2
+    ds, lams, n0 = (0.5, 0.5), np.array([0.64, 0.455]), 1.1
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(6.0, x, y + b) for b in range(B)]) * (1 + 0.1 * rng.standard_normal((B, n, n))))
+    target = f32(np.abs(orc.gaussian(5.0, x - 1, y)) ** 2)
+    tilts = np.array([[0.04, -0.02], [0.01, 0.03]]) if "tilted" in mode or "track" in mode else None
+    filt = (lambda fx, fy: np.exp(-(fx ** 2 + fy ** 2) / 1.5) * np.exp(0.3j * fx)) if "filtered" in mode else None
+    kw = dict(paraxial="paraxial" in mode, track_tilts="track" in mode, filt=filt)
+    u = fo.ScalarField(u0, ds, lams, tilts=None if tilts is None else (tilts[:, 0], tilts[:, 1]))
+    pz = fo.ASPropZ(u, z0, n0=n0, trainable=True, paraxial=kw["paraxial"], track_tilts=kw["track_tilts"],
+                    filter=filt)
+    system = fo.ScalarSource(u) | pz
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    out = orc.asprop(u0, ds[0], ds[1], lams, z0, 1, n0=n0, tilts=tilts, **kw)
+    assert orc.rel_l2(npy(system()["out"].electric).reshape(B, n, n), out) < FIELD_TOL
+    c_ref, _ = orc.sid_value(out, target)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    gz, scale = orc.asprop_z_gradient(u0, orc.sid_backward(out, target), ds[0], ds[1], lams, z0, 1, n0=n0,
+                                      tilts=tilts, return_scale=True, **kw)
+    tol = GRAD_TOL * abs(gz) + float(np.finfo(np.float32).eps) * scale
+    assert abs(float(grads[pz]["z"].item()) - gz) < tol, (float(grads[pz]["z"].item()), gz, scale)
+    # move z on the device: the next forward rebuilds every table from it
+    pz.z.fill_(z0 + 30.0)
+    out2 = orc.asprop(u0, ds[0], ds[1], lams, z0 + 30.0, 1, n0=n0, tilts=tilts, **kw)
+    assert orc.rel_l2(npy(system()["out"].electric).reshape(B, n, n), out2) < FIELD_TOL
+
+
 @pytest.mark.parametrize("d", [1, -1])
 def test_fourier_phase_and_mask(fo, orc, d):
     """FourierPhase / FourierMask: a static Fourier filter fused into a chain as a
@@ -762,7 +806,7 @@ def test_graph_capture_replays_iteration(fo, orc):
 # Every launch-shape variant of the passes (forced through the environment)
 # ---------------------------------------------------------------------------
 
-_VARIANTS = {512: (3, 9), 1024: (4, 10), 2048: (4, 9), 4096: (2, 6)}
+_VARIANTS = {512: (3, 10), 1024: (4, 11), 2048: (4, 10), 4096: (2, 6)}
 
 
 @pytest.mark.parametrize("n", sorted(_VARIANTS))
@@ -786,6 +830,33 @@ def test_every_pass_variant(fo, orc, n, monkeypatch):
             got = npy(system()["out"].electric).reshape(B, n, n)
             err = orc.rel_l2(got, ref)
             assert err < FIELD_TOL, (rv, cv, pf, err)
+
+
+@pytest.mark.parametrize("n,tma,skew", [(2048, 8, 9), (1024, 8, 10), (512, 7, 9)])
+def test_skewed_column_pass_matches_tma_pass(fo, n, tma, skew, monkeypatch):
+    """The column pass split into two halves one FFT stage apart (col_tma_skew_kernel)
+    runs the same arithmetic as the one-CTA TMA pass with register twiddles: equal
+    results bit for bit, over balanced work units walked by persistent CTAs (48
+    fields of three wavelengths at 2048^2) and in the plain 2-D launch."""
+    rng = np.random.default_rng(n)
+    B = 48 if n == 2048 else 6
+    u0 = torch.tensor(rand_field(rng, (B // 3, 3, n, n)), dtype=torch.complex64, device="cuda")
+    outs = []
+    for cv in (tma, skew):
+        monkeypatch.setenv("FO_AUTOTUNE", "0")
+        monkeypatch.setenv("FO_COL_VARIANT", str(cv))
+        u = fo.ScalarField(u0, (0.5, 0.5), [0.64, 0.538, 0.455])
+        p = fo.ASProp(u, 5000.0)
+        v = u.copy()
+        p.propagate_(v)
+        p.propagate_(v, fo.Backward)
+        p.propagate_(v)
+        torch.cuda.synchronize()
+        outs.append(v.electric.clone())
+        del p
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert fo._capi.load().fo_device_status(stream) == 0
+    assert torch.equal(outs[0], outs[1])
 
 
 def test_ragged_batch_per_problem(fo, orc):
@@ -873,3 +944,55 @@ def test_bounded_wait_reports_timeout(fo, orc, monkeypatch):
     v = p.propagate(u)
     assert lib.fo_device_status(stream) == 0
     assert orc.rel_l2(npy(v.electric), orc.asprop(u0, 1.0, 1.0, 1.064, 300.0)) < FIELD_TOL
+
+
+# ---------------------------------------------------------------------------
+# Field probes
+# ---------------------------------------------------------------------------
+
+def test_field_probes_in_fused_chain(fo, orc):
+    """FieldProbe (system/field_probe.jl:31-43, collected by optical_system.jl:194-214)
+    at every kind of plane of a fused chain -- the input, after a modulator, between
+    two propagators, before and after the last modulator -- against the oracle's
+    planes; the output equals the same system without probes bit for bit."""
+    rng = np.random.default_rng(31)
+    n, ds, lams = 128, (1.0, 1.0), [1.064, 0.8]
+    u0 = rand_field(rng, (2, n, n))
+    phi1, phi2 = f32(rng.uniform(0, 6, (n, n))), f32(rng.uniform(0, 6, (n, n)))
+    u = fo.ScalarField(u0, ds, lams)
+    m1, m2 = fo.Phase(u, phi1), fo.Phase(u, phi2)
+    pa, pb = fo.ASProp(u, 300.0), fo.ASProp(u, 150.0)
+    pr = [fo.FieldProbe() for _ in range(6)]
+    system = fo.ScalarSource(u) | pr[0] | m1 | pr[1] | pa | pr[2] | pb | pr[3] | m2 | pr[4] | pr[5]
+    plain = fo.ScalarSource(u) | m1 | pa | pb | m2
+    segs = system.segments(u)
+    assert len(segs) == 1 and len(segs[0].probes) == 6  # one fused chain, probes inside it
+    res = system()
+    a1 = orc.phase_forward(u0, phi1)
+    a2 = orc.asprop(a1, 1.0, 1.0, lams, 300.0)
+    a3 = orc.asprop(a2, 1.0, 1.0, lams, 150.0)
+    a4 = orc.phase_forward(a3, phi2)
+    refs = [u0, a1, a2, a3, a4, a4]
+    for k, ref in enumerate(refs):
+        assert pr[k] in res["probes"], k
+        assert orc.rel_l2(npy(res["probes"][pr[k]].electric), ref) < FIELD_TOL, k
+    assert torch.equal(res["out"].electric, plain()["out"].electric)
+    # a later call without probes leaves earlier probe copies alone
+    keep = res["probes"][pr[2]].electric.clone()
+    system.forward(system.source.u0.similar(), src=system.source.u0)
+    assert torch.equal(keep, res["probes"][pr[2]].electric)
+
+
+def test_field_probes_standalone(fo):
+    """The reference's own probe test (test/optical_components_test.jl:212-236):
+    probes around a constant pi/2 Phase with no propagator capture the input and
+    the phase-shifted field."""
+    n = 64
+    u0 = np.ones((n, n), dtype=np.complex64)
+    u = fo.ScalarField(u0, (1.0, 1.0), 1.0)
+    p1, p2 = fo.FieldProbe(), fo.FieldProbe()
+    system = fo.ScalarSource(u) | p1 | fo.Phase(u, np.full((n, n), np.pi / 2, dtype=np.float32)) | p2
+    res = system()
+    assert torch.allclose(res["probes"][p1].electric, torch.tensor(u0, device="cuda"))
+    ang = torch.angle(res["probes"][p2].electric)
+    assert torch.allclose(ang, torch.full_like(ang, np.pi / 2), atol=1e-6)

@@ -420,3 +420,36 @@ def test_asprop_z_gradient_matches_finite_differences(orc):
             fd = (loss(z + eps) - loss(z - eps)) / (2 * eps)
             g = orc.asprop_z_gradient(u, w, 0.5, 0.5, lams, z, d)
             assert abs(fd - g) < 1e-6 * max(1.0, abs(fd)), (z, d, fd, g)
+
+
+def test_asprop_z_gradient_general_kernels(orc):
+    """dL/dz of ASPropZ with the paraxial kernel, the tilted kernel (per-field tilts,
+    with and without tilt tracking) and a complex frequency filter, against central
+    differences in z, both directions and both signs of z."""
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((2, 16, 16)) + 1j * rng.standard_normal((2, 16, 16))
+    w = rng.standard_normal((2, 16, 16)) + 1j * rng.standard_normal((2, 16, 16))
+    lams = np.array([0.9, 1.3])
+    tilts = np.array([[0.05, -0.02], [0.01, 0.03]])
+    filt = lambda fx, fy: np.exp(-(fx ** 2 + fy ** 2) / 0.3) * np.exp(0.4j * fx)
+    cases = [dict(paraxial=True), dict(paraxial=True, tilts=tilts, track_tilts=True),
+             dict(tilts=tilts), dict(tilts=tilts, track_tilts=True), dict(filt=filt),
+             dict(tilts=tilts, filt=filt), dict(paraxial=True, filt=filt)]
+    for kw in cases:
+        for z in (37.0, -22.0):
+            for d in (orc.FORWARD, orc.BACKWARD):
+                loss = lambda zz: float(np.real(np.vdot(w, orc.asprop(u, 0.5, 0.5, lams, zz, d, n0=1.2, **kw))))
+                eps = 1e-5
+                fd = (loss(z + eps) - loss(z - eps)) / (2 * eps)
+                g = orc.asprop_z_gradient(u, w, 0.5, 0.5, lams, z, d, n0=1.2, **kw)
+                assert abs(fd - g) < 1e-6 * max(1.0, abs(fd)), (kw.keys(), z, d, fd, g)
+
+
+def test_filtered_kernel_is_conjugated_for_negative_z(orc):
+    """For z < 0 the reference takes conj of the z > 0 kernel with its filter value
+    (angular_spectrum.jl:9-12, 55-60): a complex filter is conjugated too."""
+    filt = lambda fx, fy: np.exp(0.7j * fx) * (1 + 0 * fy)
+    for theta in ((0.0, 0.0), (0.03, -0.01)):
+        hp = orc.as_kernel_general(8, 8, 0.5, 0.5, 0.8, 30.0, 1.0, False, theta, False, filt)
+        hm = orc.as_kernel_general(8, 8, 0.5, 0.5, 0.8, -30.0, 1.0, False, theta, False, filt)
+        assert np.allclose(hm, np.conj(hp))
