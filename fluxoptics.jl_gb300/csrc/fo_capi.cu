@@ -488,10 +488,9 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
   a.n_items = p->n_items;
   int v = p->col_v;
   const float2* tw = p->tw_y;
-  alignas(64) CUtensorMap tm_buf, tm_h, tm_out;
+  alignas(64) CUtensorMap tm_buf, tm_h;
   if (col_variant_uses_tma(p->fy, v)) {
     const int W = col_variant(p->fy, v).lanes;
-    const bool skew = col_variant(p->fy, v).P == 8;
     // whole tiles in one TMA instruction when the field height is a multiple of 256
     const bool t4 = p->ny % 256 == 0 && p->fy % 256 == 0 && env_int("FO_TILE4D", 1) != 0;
     int rc = t4 ? encode_tmap_4d(&tm_buf, buf, p->batch, p->ny, p->fx, p->fx, W)
@@ -499,8 +498,6 @@ int col_pass(const fo_prop_plan_s* p, float2* buf, bool conj_h, cudaStream_t st)
     if (rc == FO_OK)
       rc = t4 ? encode_tmap_4d(&tm_h, p->H, p->n_tables, p->fy, p->fx, p->fx, W)
               : encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256);
-    if (rc == FO_OK && skew) rc = t4 ? encode_tmap_4d(&tm_out, buf, p->batch, p->ny, p->fx, p->fx, 2) : FO_ERR_SHAPE;
-    if (rc == FO_OK && skew) a.tmap_out = &tm_out;
     a.tile4d = t4 ? 1 : 0;
     if (rc != FO_OK) {  // e.g. an unaligned caller buffer: use the cp.async variant
       v = 0;
@@ -703,19 +700,16 @@ int autotune_plan(fo_prop_plan p) {
       a.field_list = idx;
       a.item_start = idx + nb;
       a.n_items = n_items;
-      alignas(64) CUtensorMap tm_buf, tm_h, tm_out;
+      alignas(64) CUtensorMap tm_buf, tm_h;
       if (col_variant_uses_tma(p->fy, v)) {
         if (pf) continue;  // staging is built in
         const int W = col_variant(p->fy, v).lanes;
-        const bool skew = col_variant(p->fy, v).P == 8;
         const bool t4 = p->ny % 256 == 0 && p->fy % 256 == 0 && env_int("FO_TILE4D", 1) != 0;
         if ((t4 ? encode_tmap_4d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W)
                 : encode_tmap_3d(&tm_buf, tmp, nb, p->ny, p->fx, p->fx, W, 256)) != FO_OK ||
             (t4 ? encode_tmap_4d(&tm_h, p->H, p->n_tables, p->fy, p->fx, p->fx, W)
                 : encode_tmap_2d(&tm_h, p->H, (long long)p->n_tables * p->fy, p->fx, p->fx, W, 256)) != FO_OK)
           continue;
-        if (skew && (!t4 || encode_tmap_4d(&tm_out, tmp, nb, p->ny, p->fx, p->fx, 2) != FO_OK)) continue;
-        if (skew) a.tmap_out = &tm_out;
         a.tile4d = t4 ? 1 : 0;
         a.tmap_buf = &tm_buf;
         a.tmap_h = &tm_h;
@@ -1264,8 +1258,7 @@ FO_API int fo_prop_variants(fo_prop_plan plan, int* row_v, int* col_v, char* row
   const PassVariant cv = col_variant(plan->fy, plan->col_v);
   put(row_kernel, "row_pass_kernel<" + std::to_string(plan->fx) + ", E=" + std::to_string(rv.E) +
                       ", rows/CTA=" + std::to_string(rv.lanes) + (plan->row_pf ? ", cp.async staging>" : ">"));
-  const char* form = cv.P == 8   ? "col_tma_skew_kernel (TMA load/store, two halves one FFT stage apart)"
-                     : cv.P == 6   ? "col_tma_kernel (TMA load/store, register twiddles)"
+  const char* form = cv.P == 6   ? "col_tma_kernel (TMA load/store, register twiddles)"
                      : cv.P == 4 ? "col_tma_kernel (TMA load/store)"
                      : cv.P == 2 ? "col_pass2_kernel (paired columns)"
                      : cv.P == 0 ? "col_lane_kernel (lane-major)"

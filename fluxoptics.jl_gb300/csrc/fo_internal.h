@@ -105,7 +105,6 @@ struct ColPassArgs {
   // (tables * N) x ncols; the device error word and the wait limit.
   const void* tmap_buf;
   const void* tmap_h;
-  const void* tmap_out;  // skewed variant: the buffer's 4-D view with 2-column boxes (result stores)
   unsigned int* err_word;
   unsigned long long wait_ns;
   int test_skip_copy;  // test knob: arm the barrier but issue no copy (the wait must time out)

@@ -973,183 +973,6 @@ __global__ void __launch_bounds__(W*(N / E), min_blocks(W*(N / E), E))
 }
 
 // --------------------------------------------------------------------------
-// TMA column pass with the CTA split into two halves that run one FFT phase apart.
-// In col_tma_kernel all 16 warps of the SM cross the same CTA barriers, so the
-// phases that load the FMA pipe (butterflies) and the phases that load shared
-// memory (exchanges) follow one another and never overlap.  Here half h (256
-// threads) transforms columns 2h and 2h+1 of the 4-column strip with its own named
-// barrier (id 1 + h), its own exchange region and its own 2-column TMA store; half 1
-// starts each field only after half 0 has run that field's first butterfly stage,
-// so while one half exchanges through shared memory the other computes.
-// The halves share the strip's TMA load (the second half to finish reading a strip
-// issues the next load) and the unit's H strip (likewise).  Every wait that depends
-// on the other half is a bounded mbarrier wait: a half that gives up sets bit 0 of
-// the device error word, lets its own copies land and returns, and the other half's
-// next wait then gives up too.  Rows: y_in == y_out == N (whole 256-row boxes).
-// Shared memory: 128 (alignment) + 2 N W float2 (strip, H strip) + 2 x SLOTS x 2
-// float2 (exchange regions) + 3 mbarriers.
-// --------------------------------------------------------------------------
-template <int N, int E, bool TWR>
-__global__ void __launch_bounds__(4 * (N / E), 1)
-    col_tma_skew_kernel(const ColPassArgs a, const float2* __restrict__ tw, const __grid_constant__ CUtensorMap tm_buf,
-                        const __grid_constant__ CUtensorMap tm_h, const __grid_constant__ CUtensorMap tm_out) {
-  pdl_prologue();
-  constexpr int W = 4;
-  constexpr int T = N / E;   // threads per column
-  constexpr int HT = 2 * T;  // threads per half
-  constexpr int SLOTS = SmemSize<N>::value;
-  extern __shared__ float4 dsm4[];
-  char* base = reinterpret_cast<char*>(dsm4) + ((128u - (smem_u32(dsm4) & 127u)) & 127u);
-  float2* stage = reinterpret_cast<float2*>(base);  // dense [N][4]
-  float2* hs = stage + N * W;                         // dense [N][4]
-  float2* exr = hs + N * W;                           // [2][SLOTS][2]
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(exr + 2 * SLOTS * 2);  // tile, H, skew
-  __shared__ int s_abort[2];
-  __shared__ int s_tile_cnt, s_h_cnt;
-
-  const int h = threadIdx.x / HT;
-  const int lt = threadIdx.x % HT;
-  const int cl = lt % 2;
-  const int t = lt / 2;
-  const int c = 2 * h + cl;
-  float2* ex = exr + h * (SLOTS * 2);
-  const bool leader = lt == 0;
-  const int bid = 1 + h;
-  auto hsync = [&]() { fft_sync(bid, HT); };
-
-  struct Unit {
-    int f0, f1, col0;
-  };
-  auto unit_at = [&](int k) -> Unit {
-    const int4 u = a.units[k];
-    return Unit{u.x, u.y, u.z * W};
-  };
-  Unit U;
-  if (a.units) {
-    U = unit_at(blockIdx.x);
-  } else {
-    U.f0 = a.item_start ? a.item_start[blockIdx.x] : blockIdx.x;
-    U.f1 = a.item_start ? a.item_start[blockIdx.x + 1] : blockIdx.x + 1;
-    U.col0 = blockIdx.y * W;
-  }
-  int uk = blockIdx.x;
-  auto field_of = [&](int f) { return a.field_list ? a.field_list[f] : f; };
-  const unsigned tile_bytes = (unsigned)(N * W * sizeof(float2));
-  auto issue_tile = [&](int f, int col0) {  // one thread
-    mbar_expect_tx(&bar[0], tile_bytes);
-    if (a.test_skip_copy) return;
-    tma_load_4d(stage, &tm_buf, col0, 0, 0, field_of(f), &bar[0]);
-  };
-  auto issue_h = [&](const Unit& u) {  // one thread
-    mbar_expect_tx(&bar[1], tile_bytes);
-    tma_load_4d(hs, &tm_h, u.col0, 0, 0, a.h_index[field_of(u.f0)], &bar[1]);
-  };
-  // The second of the two halves to call this with the same counter does `fn`: each
-  // round adds 2, so an odd previous value marks the second caller (no reset).
-  auto second_of_two = [&](int* cnt, auto fn) {  // one thread per half
-    __threadfence_block();
-    if (atomicAdd(cnt, 1) & 1) {
-      __threadfence_block();
-      fence_proxy_async();
-      fn();
-    }
-  };
-  if (threadIdx.x == 0) {
-    s_abort[0] = s_abort[1] = 0;
-    s_tile_cnt = s_h_cnt = 0;
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    mbar_init(&bar[2], 1);
-    fence_proxy_async();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    issue_h(U);
-    if (U.f0 < U.f1) issue_tile(U.f0, U.col0);
-  }
-  float2 wr[TwRegs<N, E>::size];
-  if constexpr (TWR) load_twiddles<N, E>(wr, t, tw);
-  bool ok = true;
-  unsigned phase = 0, hphase = 0, sphase = 0;
-  const float hsign = a.conj_h ? -1.f : 1.f;
-
-  while (true) {
-    if (ok) ok = mbar_wait_bounded(&bar[1], hphase, a.wait_ns);
-    hphase ^= 1u;
-    const bool has_next = a.persistent && a.units && uk + (int)gridDim.x < a.n_units;
-    Unit Un = U;
-    if (has_next) Un = unit_at(uk + gridDim.x);
-
-    for (int f = U.f0; f < U.f1; ++f) {
-      if (h == 1 && ok) ok = mbar_wait_bounded(&bar[2], sphase, a.wait_ns);  // half 0 is one stage ahead
-      sphase ^= 1u;
-      const unsigned wait_phase = phase;
-      if (ok) ok = mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
-      phase ^= 1u;
-      if (!ok) s_abort[h] = 1;
-      float2 v[E];
-#pragma unroll
-      for (int i = 0; i < E; ++i) v[i] = stage[(t + i * T) * W + c];
-      hsync();  // this half has read the strip; its abort decision is uniform
-      if (s_abort[h]) {
-        if (leader) {
-          atomicOr(a.err_word, 1u);
-          // let copies this half may have started land (bounded) before returning
-          if (!a.test_skip_copy) mbar_wait_bounded(&bar[0], wait_phase, a.wait_ns);
-          mbar_wait_bounded(&bar[1], hphase ^ 1u, a.wait_ns);
-          bulk_wait_all();
-        }
-        return;
-      }
-      if (leader)
-        second_of_two(&s_tile_cnt, [&] {
-          if (f + 1 < U.f1)
-            issue_tile(f + 1, U.col0);
-          else if (has_next)
-            issue_tile(Un.f0, Un.col0);
-        });
-      Dft<E>::run(v, 0);
-      if (h == 0 && leader) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&bar[2])) : "memory");
-      // this half's previous result has left its exchange region before the first exchange
-      if (leader) bulk_wait_read_all();
-      if constexpr (TWR)
-        stages_from_r<N, E, 1, 2>(v, t, wr, ex + cl, bid, HT);
-      else
-        stages_from<N, E, 1, 2>(v, t, tw, ex + cl, bid, HT);
-      fft_last_stage_order<E>(v);
-#pragma unroll
-      for (int i = 0; i < E; ++i) {
-        float2 hv = hs[(t + i * T) * W + c];
-        hv.y *= hsign;
-        // conj(X * H): the inverse transform runs as conj(FFT(conj(.)))
-        v[i] = make_float2(fmaf(v[i].x, hv.x, -v[i].y * hv.y), -fmaf(v[i].x, hv.y, v[i].y * hv.x));
-      }
-      if (f + 1 == U.f1 && has_next) {
-        hsync();  // this half has read the unit's H strip
-        if (leader) second_of_two(&s_h_cnt, [&] { issue_h(Un); });
-      }
-      if constexpr (TWR)
-        fft_forward_r<N, E, 2>(v, t, wr, ex + cl, bid, HT);
-      else
-        fft_forward<N, E, 2>(v, t, tw, ex + cl, bid, HT);
-      hsync();  // the last stage has read the exchange region
-#pragma unroll
-      for (int i = 0; i < E; ++i) ex[(t + i * T) * 2 + cl] = make_float2(v[i].x, -v[i].y);
-      fence_proxy_async();
-      hsync();
-      if (leader && !a.test_skip_copy) {
-        tma_store_4d(&tm_out, U.col0 + 2 * h, 0, 0, field_of(f), ex);
-        bulk_commit();
-      }
-    }
-    if (!has_next) break;
-    U = Un;
-    uk += gridDim.x;
-  }
-  if (leader) bulk_wait_all();
-}
-
-// --------------------------------------------------------------------------
 // Launch helpers used by the per-size translation units.
 // --------------------------------------------------------------------------
 template <int N, int E, int LANES>
@@ -1230,32 +1053,6 @@ constexpr size_t kMaxSmemPerCta = 227 * 1024;
 template <int N, int E, int W, int P>
 cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
   constexpr int threads = (W / (P == 2 ? 2 : 1)) * (N / E);
-  if constexpr (P == 8) {
-    // two skewed halves of 2 columns each (col_tma_skew_kernel): W == 4, TWR
-    static_assert(W == 4, "the skewed column pass takes 4-column strips");
-    constexpr size_t smem_k = 128 + sizeof(float2) * ((size_t)2 * N * W + (size_t)4 * SmemSize<N>::value) + 32;
-    static_assert(smem_k <= kMaxSmemPerCta, "skewed column variant does not fit");
-    (void)pf;
-    cudaError_t e = set_smem(col_tma_skew_kernel<N, E, true>, smem_k);
-    if (a.occupancy_out) {
-      if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(a.occupancy_out, col_tma_skew_kernel<N, E, true>, threads,
-                                                          smem_k);
-      return e;
-    }
-    if (!a.tmap_buf || !a.tmap_h || !a.tmap_out || !a.tile4d || a.fft_only || a.y_in != N || a.y_out != N ||
-        a.ncols % W != 0)
-      return cudaErrorInvalidValue;
-    dim3 grid(a.n_items, a.ncols / W);
-    if (a.units) grid = dim3(a.persistent ? std::min(a.persistent, a.n_units) : a.n_units, 1);
-    if (e == cudaSuccess)
-      e = launch_pass(col_tma_skew_kernel<N, E, true>, grid, dim3(threads), smem_k, s, a, tw,
-                      *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
-                      *reinterpret_cast<const CUtensorMap*>(a.tmap_h),
-                      *reinterpret_cast<const CUtensorMap*>(a.tmap_out));
-    if (e != cudaSuccess) return e;
-    return cudaGetLastError();
-  }
   dim3 grid(a.n_items, (a.ncols + W - 1) / W);
   const bool full = a.y_in == N && a.y_out == N && a.ncols % W == 0;
   cudaError_t e;

@@ -86,16 +86,12 @@ size_t row_smem_bytes(int N, int v, bool pf) {
 size_t col_smem_bytes(int N, int v, bool pf) {
   const PassVariant pv = col_variant(N, v);
   if (pv.P == 0) return sizeof(float2) * 2 * pv.lanes * (size_t)(N + N / 16 + 4);  // always staged
-  if (pv.P == 4 || pv.P == 6 || pv.P == 8)
-    return sizeof(float2) * pv.lanes * (size_t)(2 * N + N + N / 16);  // TMA staging
+  if (pv.P == 4 || pv.P == 6) return sizeof(float2) * pv.lanes * (size_t)(2 * N + N + N / 16);  // TMA staging
   return sizeof(float2) * (size_t)(pf ? 2 : 1) * pv.lanes * (size_t)(N + N / 16);  // staging only
 }
 bool row_prefetch_fits(int N, int v) { return row_smem_bytes(N, v, true) <= kMaxSmem; }
 bool col_prefetch_fits(int N, int v) { return col_smem_bytes(N, v, true) <= kMaxSmem; }
-bool col_variant_uses_tma(int N, int v) {
-  const int P = col_variant(N, v).P;
-  return P == 4 || P == 6 || P == 8;
-}
+bool col_variant_uses_tma(int N, int v) { return col_variant(N, v).P == 4 || col_variant(N, v).P == 6; }
 
 cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s) {
   switch (N) {

@@ -3,9 +3,7 @@
 // Column: X(index, E, W, P) with W columns per CTA; P = 1: one column per thread
 // (column-fastest mapping), P = 2: paired columns, P = 0: lane-major mapping
 // with a named barrier per column, P = 4: tiles staged by TMA (cp.async.bulk.tensor),
-// P = 6: TMA staging with the FFT twiddles held in registers for the CTA's lifetime,
-// P = 8: the same with the CTA split into two halves running one FFT phase apart
-// (col_tma_skew_kernel; 4-column strips).  The autotuner picks among them at plan creation;
+// P = 6: TMA staging with the FFT twiddles held in registers for the CTA's lifetime.  The autotuner picks among them at plan creation;
 // index 0 is the default.
 #pragma once
 
@@ -24,9 +22,9 @@
 #define FO_COL_VARIANTS_64(X) X(0, 8, 16, 1)
 #define FO_COL_VARIANTS_128(X) X(0, 8, 16, 1) X(1, 8, 16, 2)
 #define FO_COL_VARIANTS_256(X) X(0, 16, 16, 1) X(1, 8, 8, 1) X(2, 8, 8, 2)
-#define FO_COL_VARIANTS_512(X) X(0, 8, 8, 1) X(1, 16, 8, 1) X(2, 8, 4, 1) X(3, 8, 4, 2) X(4, 16, 4, 4) X(5, 8, 4, 4) X(6, 16, 2, 6) X(7, 16, 4, 6) X(8, 16, 8, 6) X(9, 16, 4, 8)
-#define FO_COL_VARIANTS_1024(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 8, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6) X(8, 16, 4, 6) X(9, 16, 8, 6) X(10, 16, 4, 8)
-#define FO_COL_VARIANTS_2048(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 2, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6) X(8, 16, 4, 6) X(9, 16, 4, 8)
+#define FO_COL_VARIANTS_512(X) X(0, 8, 8, 1) X(1, 16, 8, 1) X(2, 8, 4, 1) X(3, 8, 4, 2) X(4, 16, 4, 4) X(5, 8, 4, 4) X(6, 16, 2, 6) X(7, 16, 4, 6) X(8, 16, 8, 6)
+#define FO_COL_VARIANTS_1024(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 8, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6) X(8, 16, 4, 6) X(9, 16, 8, 6)
+#define FO_COL_VARIANTS_2048(X) X(0, 16, 4, 1) X(1, 8, 4, 1) X(2, 16, 2, 1) X(3, 8, 4, 2) X(4, 16, 4, 0) X(5, 16, 4, 4) X(6, 16, 2, 4) X(7, 16, 2, 6) X(8, 16, 4, 6)
 #define FO_COL_VARIANTS_4096(X) X(0, 16, 2, 1) X(1, 8, 2, 1) X(2, 16, 4, 1) X(3, 16, 2, 0) X(4, 16, 2, 4) X(5, 16, 2, 6)
 
 #define FO_FOR_EACH_N(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
