@@ -170,10 +170,15 @@ def build_system(fo, fields_np, masks_np, targets_np):
 
 
 def iteration(fo, system, metric, opt, x, du, src):
-    tape = []
-    system.forward(x, tape, src=src, metric=metric)  # the metric runs inside the last forward pass
+    """One optimisation step: forward, SquaredIntensityDifference and the seeded adjoint
+    sweep in one library call (the chain's last forward row pass and the adjoint's first
+    row pass share one pass; the output field is not written), then the optimiser."""
+    grads = system.forward_backward_sid(du, src, metric)
+    if grads is None:  # a system the fused call does not cover
+        tape = []
+        system.forward(x, tape, src=src, metric=metric)  # the metric runs inside the last forward pass
+        grads = system.backward(du, tape, seed=(metric, x))
     loss = metric.loss
-    grads = system.backward(du, tape, seed=(metric, x))
     fo.update_(opt, system, grads)
     return loss
 
@@ -190,21 +195,21 @@ def algorithmic_bytes_per_step(n=N, batch=None):
 
 
 def pass_bytes_per_step(n=N, batch=None):
-    """DRAM bytes the iteration's passes must move: each of the 2K+1 forward and
-    2K+1 adjoint passes reads and writes every field once, plus saves, saved reads,
-    masks, gradients, transfer functions, the metric's target and residual, and Fista.
-    The first mask's adjoint reads the source field (no save); the metric runs inside
-    the last forward pass."""
+    """DRAM bytes the iteration's passes must move: each of the 4K+1 passes (the
+    forward sweep's last row pass and the adjoint's first share one pass) reads and
+    writes every field once, plus saves, saved reads, masks, gradients, transfer
+    functions, the metric's target and residual, and Fista.  The first mask's adjoint
+    reads the source field (no save); the shared pass writes no output field, and its
+    second reading of the spectrum is not counted (it comes partly from L2)."""
     batch = batch or N_MODES * len(LAMBDAS)
     n2 = n * n
     fld = 8 * n2 * batch                                    # one c32 copy of the batch
     col = 2 * fld + len(LAMBDAS) * 8 * n2                   # column pass: field in and out, one H per wavelength
-    fwd_rows = (2 * fld + 4 * n2) + (N_MASKS - 1) * (3 * fld + 4 * n2) \
-        + (2 * fld + 2 * len(LAMBDAS) * 4 * n2)            # source pass, mask passes with saves, last pass + metric
-    adj_rows = (2 * fld + len(LAMBDAS) * 4 * n2) + (N_MASKS - 1) * (3 * fld + 8 * n2) \
-        + (2 * fld + 8 * n2)                               # seed pass, gradient passes, last gradient pass
+    fwd_rows = (2 * fld + 4 * n2) + (N_MASKS - 1) * (3 * fld + 4 * n2)  # source pass, mask passes with saves
+    shared = 2 * fld + 2 * len(LAMBDAS) * 4 * n2            # metric + seed: spectrum in, adjoint spectrum out
+    adj_rows = (N_MASKS - 1) * (3 * fld + 8 * n2) + (2 * fld + 8 * n2)  # gradient passes, last gradient pass
     fista = N_MASKS * 6 * 4 * n2
-    return 2 * N_MASKS * col + fwd_rows + adj_rows + fista
+    return 2 * N_MASKS * col + fwd_rows + shared + adj_rows + fista
 
 
 def col_pass_bytes(n=N, batch=None):

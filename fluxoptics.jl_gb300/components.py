@@ -923,6 +923,51 @@ class OpticalSystem:
             metric(u)
         return u
 
+    def forward_backward_sid(self, du: ScalarField, src: ScalarField, metric, u_out: ScalarField = None,
+                             input_grad=None):
+        """Forward sweep from ``src``, SquaredIntensityDifference and its seeded adjoint
+        sweep in one library call (fo_chain_withgradient_sid), for a system that is one
+        fused chain; when it ends in a propagator, the chain's last forward row pass and
+        the adjoint's first row pass run as one pass.  ``metric.loss`` holds the
+        per-slice losses afterwards; ``u_out`` (optional) receives the output field.
+        Returns {component: {name: grad}}, or None when the system has another shape
+        (callers then run forward and backward)."""
+        if not getattr(metric, "fuses_into_chain", False) or src is None:
+            return None
+        segs = self.segments(src)
+        if len(segs) != 1 or not isinstance(segs[0], _Chain):
+            return None
+        seg = segs[0]
+        if seg.probes or any(isinstance(p, _FourierModulator) for p in seg.props):
+            return None
+        if input_grad is None:
+            input_grad = self.source is None or getattr(self.source, "trainable", False)
+        n = len(seg.mods)
+        mf, mb = (fo_mod * n)(), (fo_mod * n)()
+        grads = {}
+        saves = []  # kept with the system until the next call: the stream may still use them
+        for k, m in enumerate(seg.mods):
+            if m is None:
+                mf[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0, None)
+                mb[k] = fo_mod(_capi.FO_MOD_NONE, None, None, None, 0.0, None)
+                continue
+            if not m.trainable:
+                mf[k] = m.fo_mod(saved=None, u=src)
+                mb[k] = m.fo_mod(saved=None, grad=None, u=src)
+                continue
+            # the first slot reads the unchanged input in the adjoint instead of a saved copy
+            sv = None if k == 0 else m.get_saved_buffer(src)
+            g = m.get_gradient_buffer()
+            saves.append(sv)
+            mf[k] = m.fo_mod(saved=sv, u=src)
+            mb[k] = m.fo_mod(saved=src.electric if k == 0 else sv, grad=g, u=src)
+            grads[m] = {m.pname: g}
+        _capi.call("fo_chain_withgradient_sid", self._chain_handle(seg, src), _ptr(src.electric),
+                   _ptr(u_out.electric) if u_out is not None else None, _ptr(du.electric), mf, mb, int(self.direction),
+                   metric.handle, _ptr(metric.target), _ptr(metric.loss), 0 if input_grad else 1, _stream())
+        self._fused_saves = saves
+        return grads
+
     def backward(self, du: ScalarField, tape, seed=None, input_grad=None):
         """Adjoint sweep over a tape; returns {component: {name: grad}}.
 

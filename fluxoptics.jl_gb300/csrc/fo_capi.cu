@@ -549,6 +549,77 @@ int run_forward(const std::vector<fo_prop_plan>& props, float2* buf, float2* u, 
   return FO_OK;
 }
 
+// The chain's last forward row pass, the metric and the adjoint sweep's first row pass
+// as one launch (row kernel GK = 4): the spectrum `spec` (after the last column pass)
+// is inverse-transformed along x, the metric's residuals and row partials are formed,
+// `u_out` (nullable) receives the output field, and the seeded adjoint spectrum
+// replaces `spec` field by field.  No modulation: the chain's last slot is empty.
+int row_pass_sid_seed(const Layout& L, float2* spec, float2* u_out, const fo_sid_s* sid, const float* target,
+                      const float2* tw, cudaStream_t st) {
+  RowPassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const long long real_bs = (long long)L.nx * L.ny, spec_bs = (long long)L.fx * L.ny;
+  a.src = spec;
+  a.src_bstride = spec_bs;
+  a.src_ld = L.fx;
+  a.dst = u_out;
+  a.dst_bstride = real_bs;
+  a.dst_ld = L.nx;
+  a.nrows = L.ny;
+  a.n_valid = L.nx;
+  a.batch = L.batch;
+  a.inv_first = 1;
+  a.fwd_after = 0;
+  a.mod_kind = MOD_NONE;
+  a.field_list = sid->order;
+  a.fields_per_cta = sid->group;
+  a.tidx = sid->tidx;
+  a.dc = sid->ones;
+  a.resid_tstride = real_bs;
+  a.resid_ld = L.nx;
+  a.sid_target = target;
+  a.sid_resid = sid->resid;
+  a.sid_partials = sid->partials;
+  a.sid_T = sid->T;
+  a.seed_dst = spec;
+  a.seed_bstride = spec_bs;
+  a.seed_ld = L.fx;
+  ProfScope prof(1, st);
+  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, false, a, tw, st));
+  return FO_OK;
+}
+
+// Forward sweep, SquaredIntensityDifference and the seeded adjoint sweep in one
+// sequence of passes on the working buffer `w` (the chain scratch for padded layouts,
+// else du): 2K + 1 forward passes and 2K + 1 adjoint passes share one row pass.
+// mods_f / mods_b are the forward and adjoint descriptions of the K + 1 slots; the last
+// slot must be empty and every target slice must hold the same number of fields.
+int run_withgradient_sid(const std::vector<fo_prop_plan>& props, float2* w, const float2* u_in, float2* u_out,
+                         float2* du, const Mod* mods_f, const Mod* mods_b, int s, const fo_sid_s* sid,
+                         const float* target, float* loss, cudaStream_t st, bool discard_input_grad) {
+  const int K = (int)props.size();
+  const Layout L = layout_of(props[0]);
+  const float* il = props[0]->inv_lambda;
+  const float sf = (float)s;
+  const float2* tw = props[0]->tw_x;
+  FO_TRY(row_pass(L, u_in, w, false, true, mods_f[0], false, sf, il, nullptr, tw, st));
+  for (int k = 0; k < K; ++k) {
+    FO_TRY(col_pass(props[k], w, s < 0, st));
+    if (k + 1 < K) FO_TRY(row_pass(L, w, w, true, true, mods_f[k + 1], false, sf, il, nullptr, tw, st));
+  }
+  FO_TRY(row_pass_sid_seed(L, w, u_out, sid, target, tw, st));
+  FO_LAUNCH(launch_sid_finalize(sid->partials, L.ny, sid->T, loss, st));
+  for (int k = K - 1; k >= 0; --k) {
+    FO_TRY(col_pass(props[k], w, s > 0, st));
+    if (k > 0)
+      FO_TRY(row_pass(L, w, w, true, true, mods_b[k], true, sf, il, nullptr, tw, st));
+    else
+      FO_TRY(row_pass(L, w, discard_input_grad ? nullptr : du, true, false, mods_b[0], true, sf, il, nullptr, tw,
+                      st));
+  }
+  return FO_OK;
+}
+
 // Adjoint sweep in reverse order, in place on du (src0 is du, or the forward
 // output when the sweep is seeded by the metric).
 int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du, const float2* src0,
@@ -1474,6 +1545,38 @@ FO_API int fo_chain_forward_sid(fo_chain chain, const void* u_in, void* u, const
   FO_TRY(run_forward(chain->props, buf, uu, m.data(), direction, S(stream), src, nullptr, nullptr, nullptr,
                      chain->probe_ptr()));
   return fo_sid_forward(sid, u, target, loss, stream);
+}
+
+FO_API int fo_chain_withgradient_sid(fo_chain chain, const void* u_in, void* u_out, void* du,
+                                     const fo_mod* mods_fwd, const fo_mod* mods_bwd, int direction, fo_sid sid,
+                                     const float* target, float* loss, int flags, void* stream) {
+  if (!chain || !u_in || !du || !mods_fwd || !mods_bwd || !sid || !target || !loss)
+    return fail(FO_ERR_ARG, "chain, u_in, du, mods_fwd, mods_bwd, sid, target and loss must not be NULL");
+  FO_TRY(check_dir(direction));
+  if (u_out == du) return fail(FO_ERR_ARG, "u_out and du must be different buffers");
+  const int K = (int)chain->props.size();
+  const Layout L = layout_of(chain->props[0]);
+  if (sid->nx != L.nx || sid->ny != L.ny || sid->batch != L.batch)
+    return fail(FO_ERR_SHAPE, "metric and chain shapes differ");
+  std::vector<Mod> mf(K + 1), mb(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    mf[k] = mod_from(&mods_fwd[k]);
+    mb[k] = mod_from(&mods_bwd[k]);
+    FO_TRY(validate_mod(mf[k], false));
+    FO_TRY(validate_mod(mb[k], true));
+  }
+  const bool discard = (flags & FO_BWD_DISCARD_INPUT_GRAD) != 0;
+  if (mf[K].kind != MOD_NONE || mb[K].kind != MOD_NONE || sid->group <= 0 || chain->probe_ptr()) {
+    // the shared pass does not apply: the separate forward and adjoint sweeps
+    void* out = u_out ? u_out : du;
+    FO_TRY(fo_chain_forward_sid(chain, u_in, out, mods_fwd, direction, sid, target, loss, stream));
+    return fo_chain_backward_ex(chain, du, mods_bwd, direction, sid, out, flags, stream);
+  }
+  float2* d = reinterpret_cast<float2*>(du);
+  float2* w = chain->scratch ? chain->scratch : d;
+  return run_withgradient_sid(chain->props, w, reinterpret_cast<const float2*>(u_in),
+                              reinterpret_cast<float2*>(u_out), d, mf.data(), mb.data(), direction, sid, target, loss,
+                              S(stream), discard);
 }
 
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,

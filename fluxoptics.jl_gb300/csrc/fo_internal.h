@@ -75,6 +75,13 @@ struct RowPassArgs {
   // before (probe_pre) and after (probe_post) the modulation; either may be NULL
   float2* probe_pre;
   float2* probe_post;
+  // With sid_partials: the adjoint sweep's first pass in the same launch (row kernel
+  // GK = 4), in place on the spectrum: seed_dst must equal src.  The seed
+  // 4 dc_t (I_t - target_t) u of every field, forward-transformed along x, replaces the
+  // spectrum; `dst` (nullable) receives the output field.  No modulation.
+  float2* seed_dst;
+  long long seed_bstride;
+  int seed_ld;
 };
 
 // One column pass: forward FFT along y, multiply by the transfer function of the

@@ -35,6 +35,11 @@ namespace fo {
 #ifndef FO_ROW_TWR
 #define FO_ROW_TWR 0
 #endif
+// Register cap per thread of the row pass that shares the metric and the adjoint's seed
+// (GK = 4) for E = 16 (build-time setting).
+#ifndef FO_ROW_SEED_REG_CAP
+#define FO_ROW_SEED_REG_CAP 128
+#endif
 
 // Minimum resident CTAs per SM requested from the compiler: caps registers near
 // 96 per thread for E <= 8 and at 128 (cap16) for E = 16.
@@ -70,7 +75,8 @@ __device__ __forceinline__ void cp_async_wait() {
 // --------------------------------------------------------------------------
 // Row pass.  GK: gradient accumulator (0 none, 1 real: phase / dn, 2 complex: mask,
 // 3: intensity of the output summed over the CTA's fields for the squared
-// intensity difference, see RowPassArgs::sid_target).
+// intensity difference, see RowPassArgs::sid_target; 4: the same followed by the
+// seeded first pass of the adjoint sweep, see RowPassArgs::seed_dst).
 // PF: stage the next field's row through cp.async (needs load_n == N).
 // Shared memory: 2 * LANES * SLOTS float2 (PF) or LANES * SLOTS float2, plus
 // LANES * N float2 for the modulation-factor cache when GK != 0.
@@ -79,7 +85,9 @@ __device__ __forceinline__ void cp_async_wait() {
 // per-element guards are needed.
 template <int N, int E, int LANES, int GK, bool PF, bool FULL>
 __global__ void __launch_bounds__(LANES*(N / E),
-                                  min_blocks(LANES*(N / E), E, (GK == 0 || GK == 3) ? FO_ROW_E16_REG_CAP : 128))
+                                  min_blocks(LANES*(N / E), E,
+                                             (GK == 0 || GK == 3) ? FO_ROW_E16_REG_CAP
+                                                                  : (GK == 4 ? FO_ROW_SEED_REG_CAP : 128)))
     row_pass_kernel(const RowPassArgs a, const float2* __restrict__ tw) {
   pdl_prologue();
   constexpr int T = N / E;
@@ -149,6 +157,93 @@ __global__ void __launch_bounds__(LANES*(N / E),
       cp_async8(dst + spad(p), src + p);
     }
   };
+  if constexpr (GK == 4) {
+    // The chain's last forward pass, SquaredIntensityDifference and the first pass of the
+    // seeded adjoint sweep in one launch.  Loop 1 inverse-transforms the rows of the
+    // CTA's fields (the fields of one target slice) along x, sums their intensities,
+    // writes the output field when a.dst is set, and puts each real-space row back in
+    // place of its spectrum row (a.seed_dst == a.src).  Loop 2 reads those rows back --
+    // newest field first, so that most of them are still in L2 and the adjoint row that
+    // overwrites each one leaves a single write to DRAM -- multiplies them by
+    // 4 dc_t (I - t) and forward-transforms them in place.  No other CTA touches these
+    // rows.  The arithmetic equals the GK = 3 pass followed by the seeded pass, so the
+    // results are the same bit for bit.
+    const int ts = a.tidx[field_of(f0)];
+    float r[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) r[i] = 0.f;
+    for (int f = f0; f < f1; ++f) {
+      const int b = field_of(f);
+      float2* row = a.seed_dst + (long long)b * a.seed_bstride + (long long)y * a.seed_ld;
+      float2 v[E];
+#pragma unroll
+      for (int i = 0; i < E; ++i) v[i] = row_ok ? cconj(row[t + i * T]) : make_float2(0.f, 0.f);
+      fft(v, buf0);
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        v[i] = (p < n_valid) ? cconj(v[i]) : make_float2(0.f, 0.f);  // crop / re-pad
+        r[i] = fmaf(v[i].x, v[i].x, fmaf(v[i].y, v[i].y, r[i]));
+      }
+      if (row_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) row[t + i * T] = v[i];
+        if (a.dst) {
+          float2* dst = a.dst + (long long)b * a.dst_bstride + (long long)y * a.dst_ld;
+#pragma unroll
+          for (int i = 0; i < E; ++i) {
+            const int p = t + i * T;
+            if (p < n_valid) dst[p] = v[i];
+          }
+        }
+      }
+    }
+    // residual I - target of this row and the row's sum of squares (as GK = 3)
+    float r2 = 0.f;
+    {
+      const long long off = (long long)ts * a.resid_tstride + (long long)y * a.resid_ld;
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        float rr = 0.f;
+        if (row_ok && p < n_valid) {
+          rr = r[i] - a.sid_target[off + p];
+          a.sid_resid[off + p] = rr;
+          r2 = fmaf(rr, rr, r2);
+        }
+        r[i] = rr;
+      }
+    }
+    constexpr int G = T < 32 ? T : 32;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    float* red = reinterpret_cast<float*>(buf0);
+    if constexpr (T > 32) {
+      if ((t & 31) == 0) red[t >> 5] = r2;
+      __syncthreads();
+      if (t == 0) {
+        float acc = 0.f;
+#pragma unroll
+        for (int w = 0; w < T / 32; ++w) acc += red[w];
+        r2 = acc;
+      }
+    }
+    if (t == 0 && row_ok) a.sid_partials[(long long)y * a.sid_T + ts] = r2;
+    const float k4 = 4.f * a.dc[ts];
+    for (int f = f1 - 1; f >= f0; --f) {
+      const int b = field_of(f);
+      float2* row = a.seed_dst + (long long)b * a.seed_bstride + (long long)y * a.seed_ld;
+      float2 v[E];
+#pragma unroll
+      for (int i = 0; i < E; ++i) v[i] = row_ok ? cscale(row[t + i * T], k4 * r[i]) : make_float2(0.f, 0.f);
+      fft(v, buf0);
+      if (row_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) row[t + i * T] = v[i];
+      }
+    }
+    return;
+  }
   if constexpr (PF) {
     if (row_ok && f0 < f1) prefetch(f0, buf0);
     cp_async_commit();
@@ -1028,7 +1123,9 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
       if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, false>, grid, dim3(SH::threads), smem, s, a, tw); \
     }                                                                                             \
   } while (0)
-  if (sid) {
+  if (sid && a.seed_dst) {
+    FO_ROW_GO(4, false);
+  } else if (sid) {
     FO_ROW_GO(3, false);
   } else if (!grad) {
     if (pf) FO_ROW_GO(0, true); else FO_ROW_GO(0, false);

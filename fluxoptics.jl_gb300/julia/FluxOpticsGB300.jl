@@ -667,6 +667,29 @@ function backward_from_metric!(∂u::ScalarField, c::GB300Chain, u_out::ScalarFi
     ∂u
 end
 
+"""
+    withgradient!(∂u, c::GB300Chain, u_in, m::GB300SID; u_out=nothing, input_grad=true) -> losses
+
+Zygote.withgradient(metric, system) for a chain ending in a propagator and
+SquaredIntensityDifference, in one call (fo_chain_withgradient_sid): the forward
+sweep from `u_in`, the metric and the seeded adjoint sweep, whose first row pass is
+shared with the forward's last.  Trainable modulators' gradient buffers are filled;
+`∂u` ends holding the gradient with respect to `u_in` (scratch with
+`input_grad=false`); `u_out` receives the output field when given.
+"""
+function withgradient!(∂u::ScalarField, c::GB300Chain, u_in::ScalarField, m::GB300SID;
+                       u_out = nothing, input_grad::Bool = true, dir::Type{<:Direction} = Forward)
+    mf = [_fomod(x, _saved(x), nothing) for x in c.mods]
+    mb = [_fomod(x, _saved(x), _grad(x)) for x in c.mods]
+    check(ccall((:fo_chain_withgradient_sid, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Ptr{FoMod}, Cint, Ptr{Cvoid},
+                 Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                c.chain, dptr(u_in.electric), u_out === nothing ? C_NULL : dptr(u_out.electric),
+                dptr(∂u.electric), mf, mb, dirsign(dir), m.handle, dptr(m.target), dptr(m.loss),
+                input_grad ? Cint(0) : Cint(1), cstream()))
+    m.loss
+end
+
 # ---------------------------------------------------------------------------
 # Optimiser steps: Fista (η stored squared, OptimisersExt.jl:33-54), ProxRule(Fista,
 # ClampProx) in one pass (OptimisersExt.jl:222-244, clamp_prox.jl:35-37), TVProx

@@ -118,6 +118,12 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     SquaredIntensityDifference seeds the adjoint inside the first fused pass; the
     overlap metrics write their pull-back first."""
     src = system.source.u0 if x is None else x
+    du = src.similar()
+    if isinstance(metric, SquaredIntensityDifference) and dc is None:
+        # one fused chain ending in a propagator: forward, metric and adjoint in one call
+        grads = system.forward_backward_sid(du, src, metric)
+        if grads is not None:
+            return metric.loss.sum(), grads
     u = src.similar()
     tape = []
     if isinstance(metric, SquaredIntensityDifference):
@@ -126,7 +132,6 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     else:
         system.forward(u, tape, src=src)
         c = metric(u)
-    du = u.similar()
     if isinstance(metric, SquaredIntensityDifference) and dc is None:
         grads = system.backward(du, tape, seed=(metric, u))
         return c.sum(), grads

@@ -359,6 +359,28 @@ FO_API int fo_chain_forward_sid(fo_chain chain, const void* u_in, void* u, const
 FO_API int fo_chain_backward_ex(fo_chain chain, void* du, const fo_mod* mods, int direction,
                                 fo_sid sid, const void* u_out, int flags, void* stream);
 
+/*
+ * Zygote.withgradient(metric, system) for a chain and SquaredIntensityDifference in
+ * one call: the forward sweep from u_in (left unchanged) with the metric (loss[T]
+ * receives the per-slice values), then the seeded adjoint sweep on du, which ends
+ * holding the gradient with respect to u_in unless flags has
+ * FO_BWD_DISCARD_INPUT_GRAD.  mods_fwd and mods_bwd describe the n_props + 1
+ * modulation slots for the two sweeps (what fo_chain_forward_sid and
+ * fo_chain_backward_ex would be given); trainable slots write their gradients.
+ * u_out (nullable, not du) receives the output field.  When the last slot is empty,
+ * every target slice holds the same number of fields and no probes are set, the
+ * forward sweep's last row pass and the adjoint sweep's first row pass run as one
+ * pass, so the iteration reads and writes the fields once less: 4K + 1 passes
+ * instead of 4K + 2.  Otherwise the result is that of the two separate calls.  The
+ * values are the same bit for bit either way.
+ * Replaces: Zygote.withgradient over the reference's rrules (src/ChainRulesCoreExt.jl:21-111)
+ * for a system ending in a propagator with SquaredIntensityDifference
+ * (src/metrics/squared_intensity_difference.jl:58-90) as the loss.
+ */
+FO_API int fo_chain_withgradient_sid(fo_chain chain, const void* u_in, void* u_out, void* du,
+                                     const fo_mod* mods_fwd, const fo_mod* mods_bwd, int direction, fo_sid sid,
+                                     const float* target, float* loss, int flags, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* AS_BPM                                                                  */
 /* ---------------------------------------------------------------------- */

@@ -54,6 +54,15 @@ def _chain_case(fo, orc, bench, monkeypatch, lambdas, modes):
     out_gpu = npy(x.electric)
     loss_gpu = npy(metric.loss)
     g_gpu = [npy(grads[ph]["phi"]) for ph in phases]
+    # the benchmark's own call (forward, metric and adjoint sharing one row pass) gives
+    # the same losses and gradients bit for bit
+    du2 = src.similar()
+    grads2 = system.forward_backward_sid(du2, src, metric)
+    torch.cuda.synchronize()
+    assert grads2 is not None
+    assert np.array_equal(npy(metric.loss), loss_gpu)
+    for k, ph in enumerate(phases):
+        assert np.array_equal(npy(grads2[ph]["phi"]), g_gpu[k]), k
     phi_before = [npy(ph.phi) for ph in phases]
     fo.update_(opt, system, grads)
     torch.cuda.synchronize()

@@ -969,3 +969,100 @@ def test_field_probes_standalone(fo):
     assert torch.allclose(res["probes"][p1].electric, torch.tensor(u0, device="cuda"))
     ang = torch.angle(res["probes"][p2].electric)
     assert torch.allclose(ang, torch.full_like(ang, np.pi / 2), atol=1e-6)
+
+
+# ---------------------------------------------------------------------------
+# Forward, metric and adjoint in one call (shared metric + seed pass)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("kind,d,with_out,last_mod", [("AS", 1, False, False), ("AS", -1, True, False),
+                                                     ("RS", 1, True, False), ("AS", 1, False, True)])
+def test_withgradient_sid_shared_pass(fo, orc, kind, d, with_out, last_mod):
+    """fo_chain_withgradient_sid: the chain's last forward row pass and the adjoint's
+    first row pass run as one pass (or, with a modulator in the last slot, as the two
+    separate sweeps).  Losses, output field and every gradient equal the separate
+    fo_chain_forward_sid + fo_chain_backward_ex calls bit for bit, and the oracle."""
+    rng = np.random.default_rng(41 if kind == "AS" else 42)
+    n = 256 if kind == "AS" else 200
+    lams = [0.64, 0.538, 0.455]
+    u0 = rand_field(rng, (2, 3, n, n))  # Julia (n, n, 3, 2): 3 target slices of 2 fields
+    target = f32(rng.uniform(0, 2, (3, n, n)))
+    phis = [f32(rng.uniform(0, 6, (n, n))) for _ in range(3)]
+    m_last = c64(rng.uniform(0.5, 1.0, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+
+    def build():
+        u = fo.ScalarField(u0, (0.5, 0.5) if kind == "AS" else (1.0, 1.0), lams)
+        P = (lambda zz: fo.ASProp(u, zz)) if kind == "AS" else (lambda zz: fo.RSProp(u, zz))
+        ph = [fo.Phase(u, p, trainable=True, buffered=True) for p in phis]
+        comps = [ph[0], P(300.0), ph[1], P(200.0), ph[2], P(250.0)]
+        mk = None
+        if last_mod:
+            mk = fo.Mask(u, m_last, trainable=True, buffered=True)
+            comps.append(mk)
+        system = fo.OpticalSystem(fo.ScalarSource(u), comps, direction=d)
+        return u, system, ph, mk
+
+    # separate sweeps
+    u, system, ph, mk = build()
+    metric = fo.SquaredIntensityDifference((u, target))
+    src = system.source.u0
+    x, du = src.similar(), src.similar()
+    tape = []
+    system.forward(x, tape, src=src, metric=metric)
+    grads = system.backward(du, tape, seed=(metric, x), input_grad=True)
+    torch.cuda.synchronize()
+    ref_loss = metric.loss.clone()
+    ref_out = x.electric.clone()
+    ref_du = du.electric.clone()
+    ref_g = {i: grads[p]["phi"].clone() for i, p in enumerate(ph)}
+    ref_gm = grads[mk]["m"].clone() if mk is not None else None
+
+    # one call
+    u2, system2, ph2, mk2 = build()
+    metric2 = fo.SquaredIntensityDifference((u2, target))
+    src2 = system2.source.u0
+    x2, du2 = src2.similar(), src2.similar()
+    x2.electric.zero_()
+    segs = system2.segments(src2)
+    n_ch = len(segs)
+    if last_mod:
+        assert segs[0].mods[-1] is not None
+    g2 = system2.forward_backward_sid(du2, src2, metric2, u_out=x2 if with_out else None, input_grad=True)
+    assert g2 is not None and n_ch == 1
+    torch.cuda.synchronize()
+    assert torch.equal(metric2.loss, ref_loss)
+    assert torch.equal(du2.electric, ref_du)
+    for i, p in enumerate(ph2):
+        assert torch.equal(g2[p]["phi"], ref_g[i]), i
+    if mk2 is not None:
+        assert torch.equal(g2[mk2]["m"], ref_gm)
+    if with_out:
+        assert torch.equal(x2.electric, ref_out)
+    else:
+        assert not torch.any(x2.electric != 0)  # the output field is not written
+
+    # and the oracle, for the phase of the first slot
+    prop = (lambda v, zz, dd: orc.asprop(v, 0.5, 0.5, np.tile(lams, 2), zz, dd)) if kind == "AS" else \
+        (lambda v, zz, dd: orc.rsprop(v, 1.0, 1.0, np.tile(lams, 2), zz, dd))
+    U = u0.reshape(6, n, n)
+    a0 = U
+    a1 = prop(orc.phase_forward(a0, phis[0], d), 300.0, d)
+    a2 = prop(orc.phase_forward(a1, phis[1], d), 200.0, d)
+    out = prop(orc.phase_forward(a2, phis[2], d), 250.0, d)
+    if last_mod:
+        a3 = out
+        out = orc.mask_forward(a3, m_last, d)
+    tidx = np.arange(6) % 3
+    c_ref, _ = orc.sid_value(out, target, tidx)
+    assert np.max(np.abs(npy(metric2.loss) - c_ref) / c_ref) < 1e-4
+    dv = orc.sid_backward(out, target, 1.0, tidx)
+    if last_mod:
+        dv, _ = orc.mask_backward(dv, m_last, a3, d)
+    dv = prop(dv, 250.0, -d)
+    dv, _ = orc.phase_backward(dv, phis[2], a2, d)
+    dv = prop(dv, 200.0, -d)
+    dv, _ = orc.phase_backward(dv, phis[1], a1, d)
+    dv = prop(dv, 300.0, -d)
+    dv, g0 = orc.phase_backward(dv, phis[0], a0, d)
+    assert orc.rel_l2(npy(g2[ph2[0]]["phi"]), g0) < GRAD_TOL
+    assert orc.rel_l2(npy(du2.electric).reshape(6, n, n), dv) < 1e-4
