@@ -265,7 +265,8 @@ struct fo_prop_plan_s {
   int n_units = 0;
   int col_ctas = 0;             // persistent column launch: CTAs taking every col_ctas-th unit (0: off)
   int row_v = 0, col_v = 0;     // launch-shape variants (autotuned or default)
-  bool row_pf = true, col_pf = true;
+  int row_pf = 1;                // row staging: 0 none, 1 cp.async, 2 register prefetch
+  bool col_pf = true;
   unsigned int* err_word = nullptr;         // device error word (bounded waits)
   unsigned long long wait_ns = 1000000000ull;  // limit of a bounded device wait
   float* inv_lambda = nullptr;  // device, per field
@@ -309,7 +310,7 @@ struct Layout {
   int nx, ny, batch, fx, fy;
   bool padded;
   int row_v;
-  bool row_pf;
+  int row_pf;
 };
 
 Layout layout_of(const fo_prop_plan_s* p) {
@@ -458,10 +459,11 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
     a.sid_T = sid->T;
   }
   const int load_n = inv_first ? L.fx : L.nx;
-  const bool pf = L.row_pf && load_n == L.fx && row_prefetch_fits(L.fx, L.row_v) &&
-                  !(grad && mod.kind == MOD_MASK) && !sid;
+  int staging = L.row_pf;
+  if (staging == 1 && !(load_n == L.fx && row_prefetch_fits(L.fx, L.row_v) && !(grad && mod.kind == MOD_MASK) && !sid))
+    staging = 0;
   ProfScope prof(inv_first && fwd_after ? 1 : 0, st);
-  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, pf, a, tw, st));
+  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, staging, a, tw, st));
   return FO_OK;
 }
 
@@ -585,7 +587,7 @@ int row_pass_sid_seed(const Layout& L, float2* spec, float2* u_out, const fo_sid
   a.seed_bstride = spec_bs;
   a.seed_ld = L.fx;
   ProfScope prof(1, st);
-  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, false, a, tw, st));
+  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, 0, a, tw, st));
   return FO_OK;
 }
 
@@ -647,7 +649,7 @@ int run_backward(const std::vector<fo_prop_plan>& props, float2* buf, float2* du
 // FO_ROW_VARIANT / FO_COL_VARIANT / FO_PREFETCH=0 override the choice.
 // ---------------------------------------------------------------------------
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int, int, int>, std::tuple<int, bool, int, bool>> g_tune;
+std::map<std::tuple<int, int, int, int, int>, std::tuple<int, int, int, bool>> g_tune;
 
 
 // Best per-launch time of `reps` samples.  Launches shorter than about 0.25 ms are
@@ -719,10 +721,10 @@ int autotune_plan(fo_prop_plan p) {
   cudaMemset(tmp, 0, sizeof(float2) * (size_t)nb * p->ny * p->fx);
   float best = 1e30f;
   int bv = 0;
-  bool bpf = false;
+  int brs = 0;
   for (int v = 0; v < row_variant_count(p->fx); ++v) {
-    for (int pf = 0; pf < 2; ++pf) {
-      if (pf && !row_prefetch_fits(p->fx, v)) continue;
+    for (int pf = 0; pf < 3; ++pf) {  // staging: none, cp.async, register prefetch
+      if (pf == 1 && !row_prefetch_fits(p->fx, v)) continue;
       RowPassArgs a;
       std::memset(&a, 0, sizeof(a));
       a.src = tmp;
@@ -738,22 +740,22 @@ int autotune_plan(fo_prop_plan p) {
       int trc = FO_OK;
       const float2* tw = twiddles(p->fx, row_variant(p->fx, v).E, &trc);
       if (!tw) continue;
-      const float ms = time_launches([&] { return launch_row_pass(p->fx, v, pf != 0, a, tw, 0); }, 3);
+      const float ms = time_launches([&] { return launch_row_pass(p->fx, v, pf, a, tw, 0); }, 3);
       if (env_int("FO_VERBOSE", 0) > 1)
         fprintf(stderr, "[fluxoptics_gb300] tune row N=%d v=%d (E=%d lanes=%d) pf=%d: %.4f ms\n", p->fx, v,
                 row_variant(p->fx, v).E, row_variant(p->fx, v).lanes, pf, ms);
       if (ms >= 0.f && ms < best) {
         best = ms;
         bv = v;
-        bpf = pf != 0;
+        brs = pf;
       }
     }
   }
   p->row_v = bv;
-  p->row_pf = bpf;
+  p->row_pf = brs;
   best = 1e30f;
   bv = 0;
-  bpf = false;
+  bool bpf = false;
   for (int v = 0; v < col_variant_count(p->fy); ++v) {
     for (int pf = 0; pf < 2; ++pf) {
       if (pf && !col_prefetch_fits(p->fy, v)) continue;
@@ -862,9 +864,12 @@ void apply_overrides(fo_prop_plan p) {
   const int rv = env_int("FO_ROW_VARIANT", -1), cv = env_int("FO_COL_VARIANT", -1);
   if (rv >= 0 && rv < row_variant_count(p->fx)) p->row_v = rv;
   if (cv >= 0 && cv < col_variant_count(p->fy)) p->col_v = cv;
-  if (env_int("FO_PREFETCH", 1) == 0) p->row_pf = p->col_pf = false;
+  if (env_int("FO_PREFETCH", 1) == 0) {
+    p->row_pf = 0;
+    p->col_pf = false;
+  }
   const int rpf = env_int("FO_ROW_PF", -1), cpf = env_int("FO_COL_PF", -1);
-  if (rpf >= 0) p->row_pf = rpf != 0;
+  if (rpf >= 0) p->row_pf = std::min(rpf, 2);
   if (cpf >= 0) p->col_pf = cpf != 0;
 }
 
@@ -1053,7 +1058,7 @@ int make_plan(fo_prop_plan* out, int kind, int nx, int ny, int batch, double dx,
       e = launch_rs_h_spatial(Hi, nx, ny, fx, fy, dx, dy, uniq[i][0], z, scale, 0);
       if (e == cudaSuccess) {
         // H_RS = FFT2(h): row transforms of all fy rows, then column transforms
-        Layout L{fx, fy, 1, fx, fy, false, 0, false};
+        Layout L{fx, fy, 1, fx, fy, false, 0, 0};
         Mod none;
         rc = row_pass(L, Hi, Hi, false, true, none, false, 1.f, nullptr, nullptr, p->tw_x, 0);
         if (rc != FO_OK) {
@@ -1328,7 +1333,9 @@ FO_API int fo_prop_variants(fo_prop_plan plan, int* row_v, int* col_v, char* row
   const PassVariant rv = row_variant(plan->fx, plan->row_v);
   const PassVariant cv = col_variant(plan->fy, plan->col_v);
   put(row_kernel, "row_pass_kernel<" + std::to_string(plan->fx) + ", E=" + std::to_string(rv.E) +
-                      ", rows/CTA=" + std::to_string(rv.lanes) + (plan->row_pf ? ", cp.async staging>" : ">"));
+                      ", rows/CTA=" + std::to_string(rv.lanes) + (plan->row_pf == 1   ? ", cp.async staging>"
+                       : plan->row_pf == 2 ? ", register prefetch>"
+                                           : ">"));
   const char* form = cv.P == 6   ? "col_tma_kernel (TMA load/store, register twiddles)"
                      : cv.P == 4 ? "col_tma_kernel (TMA load/store)"
                      : cv.P == 2 ? "col_pass2_kernel (paired columns)"

@@ -155,7 +155,9 @@ size_t col_smem_bytes(int N, int v, bool pf);
 bool row_prefetch_fits(int N, int v);
 bool col_prefetch_fits(int N, int v);
 bool col_variant_uses_tma(int N, int v);
-cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s);
+// staging of the row passes: 0 none, 1 cp.async staging in shared memory, 2 register
+// prefetch of the next field's row (passes without a gradient)
+cudaError_t launch_row_pass(int N, int v, int staging, const RowPassArgs& a, const float2* tw, cudaStream_t s);
 cudaError_t launch_col_pass(int N, int v, bool pf, const ColPassArgs& a, const float2* tw, cudaStream_t s);
 
 // Stage-major twiddle tables of the (N, E) schedule for the current device (cached).

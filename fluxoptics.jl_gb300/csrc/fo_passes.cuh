@@ -83,12 +83,17 @@ __device__ __forceinline__ void cp_async_wait() {
 // --------------------------------------------------------------------------
 // FULL: the row count is a multiple of LANES and n_valid == N, so no
 // per-element guards are needed.
-template <int N, int E, int LANES, int GK, bool PF, bool FULL>
+// RP (passes without a gradient only): the next field's row is loaded into a second
+// set of registers while the current one is transformed, so that every row keeps a
+// load in flight (128-register cap).
+template <int N, int E, int LANES, int GK, bool PF, bool FULL, bool RP = false>
 __global__ void __launch_bounds__(LANES*(N / E),
                                   min_blocks(LANES*(N / E), E,
-                                             (GK == 0 || GK == 3) ? FO_ROW_E16_REG_CAP
-                                                                  : (GK == 4 ? FO_ROW_SEED_REG_CAP : 128)))
+                                             RP                          ? 128
+                                             : (GK == 0 || GK == 3)      ? FO_ROW_E16_REG_CAP
+                                             : (GK == 4 ? FO_ROW_SEED_REG_CAP : 128)))
     row_pass_kernel(const RowPassArgs a, const float2* __restrict__ tw) {
+  static_assert(!RP || (GK == 0 && !PF), "register prefetch is for passes without a gradient or staging");
   pdl_prologue();
   constexpr int T = N / E;
   constexpr int SLOTS = SmemSize<N>::value;
@@ -248,6 +253,20 @@ __global__ void __launch_bounds__(LANES*(N / E),
     if (row_ok && f0 < f1) prefetch(f0, buf0);
     cp_async_commit();
   }
+  float2 nxt[RP ? E : 1];
+  auto load_next = [&](int f) {
+    if constexpr (RP) {
+      const float2* src = a.src + (long long)field_of(f) * a.src_bstride + (long long)y * a.src_ld;
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        nxt[i] = (row_ok && p < load_n) ? src[p] : make_float2(0.f, 0.f);
+      }
+    }
+  };
+  if constexpr (RP) {
+    if (f0 < f1) load_next(f0);
+  }
 
   for (int f = f0; f < f1; ++f) {
     const int b = field_of(f);
@@ -265,6 +284,10 @@ __global__ void __launch_bounds__(LANES*(N / E),
         const float2 x = row_ok ? cur[spad(p)] : make_float2(0.f, 0.f);
         v[i] = a.inv_first ? cconj(x) : x;
       }
+    } else if constexpr (RP) {
+#pragma unroll
+      for (int i = 0; i < E; ++i) v[i] = a.inv_first ? cconj(nxt[i]) : nxt[i];
+      if (f + 1 < f1) load_next(f + 1);  // another field's row: no overlap with this field's stores
     } else {
       const float2* src = a.src + (long long)b * a.src_bstride + (long long)y * a.src_ld;
 #pragma unroll
@@ -1104,12 +1127,16 @@ inline cudaError_t set_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// staging: 0 none, 1 cp.async staging of the next field's row in shared memory (PF),
+// 2 register prefetch of the next field's row (RP; passes without a gradient only,
+// otherwise as 0)
 template <int N, int E, int LANES>
-cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
+cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_t s, int staging) {
   using SH = RowShape<N, E, LANES>;
   dim3 grid((a.batch + a.fields_per_cta - 1) / a.fields_per_cta, (a.nrows + LANES - 1) / LANES);
   const bool grad = a.mod_bwd && a.grad != nullptr && a.mod_kind != MOD_NONE;
   const bool sid = a.sid_partials != nullptr;  // GK 3 (no staging)
+  const bool pf = staging == 1;
   const size_t smem = SH::smem(pf && !sid && !(grad && a.mod_kind == MOD_MASK), grad || sid);
   const bool full = a.n_valid == N && a.nrows % LANES == 0;
   cudaError_t e = cudaSuccess;
@@ -1127,6 +1154,16 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
     FO_ROW_GO(4, false);
   } else if (sid) {
     FO_ROW_GO(3, false);
+  } else if (!grad && staging == 2) {
+    if (full) {
+      e = set_smem(row_pass_kernel<N, E, LANES, 0, false, true, true>, smem);
+      if (e == cudaSuccess)
+        e = launch_pass(row_pass_kernel<N, E, LANES, 0, false, true, true>, grid, dim3(SH::threads), smem, s, a, tw);
+    } else {
+      e = set_smem(row_pass_kernel<N, E, LANES, 0, false, false, true>, smem);
+      if (e == cudaSuccess)
+        e = launch_pass(row_pass_kernel<N, E, LANES, 0, false, false, true>, grid, dim3(SH::threads), smem, s, a, tw);
+    }
   } else if (!grad) {
     if (pf) FO_ROW_GO(0, true); else FO_ROW_GO(0, false);
   } else if (a.mod_kind == MOD_MASK) {

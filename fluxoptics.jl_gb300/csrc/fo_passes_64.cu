@@ -4,7 +4,7 @@
 
 namespace fo {
 
-cudaError_t row_launch_64(int v, const RowPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
+cudaError_t row_launch_64(int v, const RowPassArgs& a, const float2* tw, cudaStream_t s, int pf) {
   switch (v) {
 #define X(I, E, L) \
   case I:          \

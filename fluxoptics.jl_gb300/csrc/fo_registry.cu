@@ -8,7 +8,7 @@
 namespace fo {
 
 #define FO_DECL(NN)                                                                                  \
-  cudaError_t row_launch_##NN(int v, const RowPassArgs& a, const float2* tw, cudaStream_t s, bool pf); \
+  cudaError_t row_launch_##NN(int v, const RowPassArgs& a, const float2* tw, cudaStream_t s, int pf); \
   cudaError_t col_launch_##NN(int v, const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf);
 FO_FOR_EACH_N(FO_DECL)
 #undef FO_DECL
@@ -93,11 +93,11 @@ bool row_prefetch_fits(int N, int v) { return row_smem_bytes(N, v, true) <= kMax
 bool col_prefetch_fits(int N, int v) { return col_smem_bytes(N, v, true) <= kMaxSmem; }
 bool col_variant_uses_tma(int N, int v) { return col_variant(N, v).P == 4 || col_variant(N, v).P == 6; }
 
-cudaError_t launch_row_pass(int N, int v, bool pf, const RowPassArgs& a, const float2* tw, cudaStream_t s) {
+cudaError_t launch_row_pass(int N, int v, int staging, const RowPassArgs& a, const float2* tw, cudaStream_t s) {
   switch (N) {
 #define FO_CASE(NN) \
   case NN:          \
-    return row_launch_##NN(v, a, tw, s, pf);
+    return row_launch_##NN(v, a, tw, s, staging);
     FO_FOR_EACH_N(FO_CASE)
 #undef FO_CASE
     default:

@@ -820,10 +820,11 @@ def test_every_pass_variant(fo, orc, n, monkeypatch):
     n_row, n_col = _VARIANTS[n]
     combos = [(r, 0) for r in range(n_row)] + [(0, c) for c in range(1, n_col)]
     for rv, cv in combos:
-        for pf in ("0", "1"):
+        for pf in ("0", "1", "2"):  # row staging: none, cp.async, register prefetch
             monkeypatch.setenv("FO_ROW_VARIANT", str(rv))
             monkeypatch.setenv("FO_COL_VARIANT", str(cv))
-            monkeypatch.setenv("FO_PREFETCH", pf)
+            monkeypatch.setenv("FO_PREFETCH", "0" if pf == "0" else "1")
+            monkeypatch.setenv("FO_ROW_PF", pf)
             monkeypatch.setenv("FO_AUTOTUNE", "0")
             u = fo.ScalarField(u0, (1.0, 1.0), lams)
             system = fo.ScalarSource(u) | fo.Phase(u, phi) | fo.ASProp(u, 400.0)
