@@ -56,6 +56,34 @@ __device__ __forceinline__ void pdl_prologue() {
   asm volatile("griddepcontrol.wait;\n" ::: "memory");
 }
 
+// L2 eviction priorities for data that one pass writes and reads back soon
+// (createpolicy / cache_hint, sm_80 and later).
+__device__ __forceinline__ unsigned long long l2_evict_last_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_hint(float2* ptr, float2 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(ptr), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ float2 ld_hint(const float2* ptr, unsigned long long pol) {
+  float2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;\n" : "=f"(v.x), "=f"(v.y) : "l"(ptr), "l"(pol)
+               : "memory");
+  return v;
+}
+// Whether the shared metric + seed pass marks the rows it writes back and reads again
+// as evict-last / evict-first in L2 (build-time setting).
+#ifndef FO_SEED_L2_HINTS
+#define FO_SEED_L2_HINTS 1
+#endif
+
 __device__ __forceinline__ float2 cis_f(float a) {
   float s, c;
   sincosf(a, &s, &c);
@@ -191,8 +219,14 @@ __global__ void __launch_bounds__(LANES*(N / E),
         r[i] = fmaf(v[i].x, v[i].x, fmaf(v[i].y, v[i].y, r[i]));
       }
       if (row_ok) {
+        if constexpr (FO_SEED_L2_HINTS) {
+          const unsigned long long keep = l2_evict_last_policy();
 #pragma unroll
-        for (int i = 0; i < E; ++i) row[t + i * T] = v[i];
+          for (int i = 0; i < E; ++i) st_hint(row + t + i * T, v[i], keep);
+        } else {
+#pragma unroll
+          for (int i = 0; i < E; ++i) row[t + i * T] = v[i];
+        }
         if (a.dst) {
           float2* dst = a.dst + (long long)b * a.dst_bstride + (long long)y * a.dst_ld;
 #pragma unroll
@@ -239,8 +273,15 @@ __global__ void __launch_bounds__(LANES*(N / E),
       const int b = field_of(f);
       float2* row = a.seed_dst + (long long)b * a.seed_bstride + (long long)y * a.seed_ld;
       float2 v[E];
+      if constexpr (FO_SEED_L2_HINTS) {
+        const unsigned long long last_use = l2_evict_first_policy();
 #pragma unroll
-      for (int i = 0; i < E; ++i) v[i] = row_ok ? cscale(row[t + i * T], k4 * r[i]) : make_float2(0.f, 0.f);
+        for (int i = 0; i < E; ++i)
+          v[i] = row_ok ? cscale(ld_hint(row + t + i * T, last_use), k4 * r[i]) : make_float2(0.f, 0.f);
+      } else {
+#pragma unroll
+        for (int i = 0; i < E; ++i) v[i] = row_ok ? cscale(row[t + i * T], k4 * r[i]) : make_float2(0.f, 0.f);
+      }
       fft(v, buf0);
       if (row_ok) {
 #pragma unroll
