@@ -14,17 +14,18 @@ from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierM
                          ScalarSource, TeaDOE, TeaReflector, backpropagate_, function_to_array, propagate, propagate_,
                          reverse, spatial_vectors)
 from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
-from .metrics import DotProduct, PowerCoupling, SquaredIntensityDifference, withgradient
+from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
 from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
-from .optimisers import ClampProx, Fista, NoDescent, ProxRule, TVProx, make_rules, setup, update_
+from .optimisers import (ClampProx, Fista, IstaProx, NoDescent, PositiveProx, ProxRule, TVProx, make_rules, setup,
+                         update_)
 from .ragged import RaggedBatch
 
 load_library = _capi.load
 
 __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierPhase",
-    "Forward", "Mask", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PowerCoupling", "ProxRule",
-    "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredIntensityDifference", "TVProx", "TeaDOE",
+    "Forward", "IstaProx", "Mask", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PositiveProx", "PowerCoupling", "ProxRule",
+    "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
     "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "update_",

@@ -103,6 +103,12 @@ SIGNATURES = {
     "fo_copy": (_i, [_vp, _vp, C.c_size_t, _vp]),
     "fo_fista_clamp_step": (_i, [_vp, _vp, _vp, _vp, _ll, _d, _vp, _d, _d, _vp]),
     "fo_clamp": (_i, [_vp, _ll, _d, _d, _vp]),
+    "fo_ista": (_i, [_vp, C.c_longlong, C.c_double, C.c_double, _vp]),
+    "fo_positive": (_i, [_vp, C.c_longlong, _vp]),
+    "fo_sfd_create": (_i, [C.POINTER(_vp), _i, _i, _i]),
+    "fo_sfd_forward": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "fo_sfd_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "fo_sfd_destroy": (_i, [_vp]),
     "fo_tv_create": (_i, [C.POINTER(_vp), _i, _i, _d, _i, _i, _d]),
     "fo_tv_destroy": (_i, [_vp]),
     "fo_tv_apply": (_i, [_vp, _vp, _vp]),

@@ -18,9 +18,11 @@ Replaces, for CuArray fields:
 - TeaDOE / TeaReflector, FourierPhase / FourierMask, ASPropZ, DotProduct / PowerCoupling
 - SquaredIntensityDifference (src/metrics/squared_intensity_difference.jl:58-90), also
   evaluated inside a chain's last forward pass (forward_with_metric!)
-- Fista, ProxRule(Fista, ClampProx) in one pass, ClampProx and TVProx
-  (src/OptimisersExt.jl:33-54, 222-244; src/proximal_operators/clamp_prox.jl:35-37,
-  tv_prox.jl:94-195) as in-place device steps (fista_step!, gb300_clamp!, tv_prox!)
+- SquaredFieldDifference (src/metrics/squared_field_difference.jl:35-61)
+- Fista, ProxRule(Fista, ClampProx) in one pass, ClampProx, IstaProx, PositiveProx and
+  TVProx (src/OptimisersExt.jl:33-54, 222-244; src/proximal_operators/clamp_prox.jl:35-37,
+  ista_prox.jl:1-56, positive_prox.jl:1-40, tv_prox.jl:94-195) as in-place device steps (fista_step!, gb300_clamp!, gb300_ista!,
+  gb300_positive!, tv_prox!)
 - the ragged batch of independent problems in one persistent launch (GB300Ragged)
 """
 module FluxOpticsGB300
@@ -732,6 +734,59 @@ function gb300_clamp!(x::CuArray{Float32}, lo::Real, hi::Real)
     check(ccall((:fo_clamp, LIB), Cint, (Ptr{Cvoid}, Clonglong, Cdouble, Cdouble, Ptr{Cvoid}),
                 dptr(x), Clonglong(length(x)), lo, hi, cstream()))
     x
+end
+
+# IstaProx(s, c) (ista_prox.jl:1-56): soft threshold towards c; a complex array is
+# passed as its interleaved real and imaginary parts, each shrunk towards c
+function gb300_ista!(x::Union{CuArray{Float32}, CuArray{ComplexF32}}, s::Real, c::Real = 0)
+    n = length(x) * (eltype(x) <: Complex ? 2 : 1)
+    check(ccall((:fo_ista, LIB), Cint, (Ptr{Cvoid}, Clonglong, Cdouble, Cdouble, Ptr{Cvoid}),
+                dptr(x), Clonglong(n), s, c, cstream()))
+    x
+end
+
+# PositiveProx (positive_prox.jl:1-40): x = max(x, 0)
+function gb300_positive!(x::CuArray{Float32})
+    check(ccall((:fo_positive, LIB), Cint, (Ptr{Cvoid}, Clonglong, Ptr{Cvoid}),
+                dptr(x), Clonglong(length(x)), cstream()))
+    x
+end
+
+# ---------------------------------------------------------------------------
+# SquaredFieldDifference (squared_field_difference.jl:35-61)
+# ---------------------------------------------------------------------------
+mutable struct GB300SFD{V}
+    handle::Ptr{Cvoid}
+    v::V                      # reference field
+    c::CuArray{Float32, 1}
+end
+
+"""
+    GB300SquaredFieldDifference(v::ScalarField)
+
+c_b = Σ|u_b − v_b|² per field over the pixels (no dx dy factor), and the pullback
+∂u = 2 ∂c_b (u_b − v_b).
+"""
+function GB300SquaredFieldDifference(v::ScalarField)
+    nx, ny, b = dims_of(v)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_sfd_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Cint, Cint, Cint), h, nx, ny, b))
+    m = GB300SFD(h[], v, CUDA.zeros(Float32, b))
+    finalizer(x -> ccall((:fo_sfd_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), m)
+end
+
+function (m::GB300SFD)(u::ScalarField)
+    check(ccall((:fo_sfd_forward, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                m.handle, dptr(u.electric), dptr(m.v.electric), dptr(m.c), cstream()))
+    m.c
+end
+
+function pullback!(m::GB300SFD, ∂c, u::ScalarField, ∂u::ScalarField)
+    check(ccall((:fo_sfd_backward, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+                m.handle, dptr(u.electric), dptr(m.v.electric), ∂c === nothing ? C_NULL : dptr(∂c),
+                dptr(∂u.electric), cstream()))
+    ∂u
 end
 
 mutable struct GB300TV

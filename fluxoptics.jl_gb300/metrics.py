@@ -1,5 +1,6 @@
 """Metrics on the GPU: SquaredIntensityDifference
-(metrics/squared_intensity_difference.jl:58-90), DotProduct (metrics/dot_product.jl:47-100)
+(metrics/squared_intensity_difference.jl:58-90), SquaredFieldDifference
+(metrics/squared_field_difference.jl:35-61), DotProduct (metrics/dot_product.jl:47-100)
 and PowerCoupling (metrics/power_coupling.jl:48-66)."""
 
 from __future__ import annotations
@@ -58,6 +59,47 @@ class SquaredIntensityDifference:
         lib = _capi._LIB
         if lib is not None and getattr(self, "handle", None):
             lib.fo_sid_destroy(self.handle)
+
+
+class SquaredFieldDifference:
+    """c_b = sum |u_b - v_b|^2 over the field's pixels (no dx dy factor), against
+    reference fields v of the same grid and batch; pull-back 2 dc_b (u_b - v_b)."""
+
+    def __init__(self, v: ScalarField):
+        self.v = v
+        self.nx, self.ny, self.batch = v.nx, v.ny, v.batch
+        self.handle = C.c_void_p()
+        _capi.call("fo_sfd_create", C.byref(self.handle), v.nx, v.ny, v.batch)
+        self.out = torch.zeros(self.batch, dtype=torch.float32, device="cuda")
+
+    def _check(self, u: ScalarField):
+        if (u.nx, u.ny, u.batch) != (self.nx, self.ny, self.batch):
+            raise ValueError("SquaredFieldDifference: the field's grid and batch must match the reference fields")
+
+    def __call__(self, u: ScalarField):
+        """Per-field values (device tensor of batch floats)."""
+        self._check(u)
+        _capi.call("fo_sfd_forward", self.handle, _ptr(u.electric), _ptr(self.v.electric), _ptr(self.out), _stream())
+        return self.out
+
+    def backpropagate_into(self, u: ScalarField, du: ScalarField, dc=None):
+        self._check(u)
+        if dc is not None:
+            dc = dc.to(torch.float32).reshape(-1).contiguous()
+            if dc.numel() != self.batch:
+                raise ValueError("dc must hold one value per field")
+        _capi.call("fo_sfd_backward", self.handle, _ptr(u.electric), _ptr(self.v.electric), _ptr(dc),
+                   _ptr(du.electric), _stream())
+        return du
+
+    def backpropagate(self, u: ScalarField, dc=None):
+        du = u.similar()
+        return self.backpropagate_into(u, du, dc)
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is not None and getattr(self, "handle", None):
+            lib.fo_sfd_destroy(self.handle)
 
 
 class _Overlap:

@@ -1,5 +1,5 @@
-"""Fista, ProxRule, ClampProx and TVProx on the GPU (src/OptimisersExt.jl,
-src/proximal_operators/*)."""
+"""Fista, ProxRule, ClampProx, IstaProx, PositiveProx and TVProx on the GPU
+(src/OptimisersExt.jl, src/proximal_operators/*)."""
 
 from __future__ import annotations
 
@@ -47,6 +47,47 @@ class ClampProx:
 
     def apply_(self, state, x):
         _capi.call("fo_clamp", _ptr(x), x.numel(), self.lo, self.hi, _stream())
+
+
+def _float_view(x):
+    """The float values of a float32 or complex64 parameter (a complex one as its
+    interleaved real and imaginary parts)."""
+    if x.dtype == torch.complex64:
+        return torch.view_as_real(x)
+    if x.dtype != torch.float32:
+        raise NotImplementedError("the GPU proximal operators update float32 or complex64 parameters")
+    return x
+
+
+class IstaProx:
+    """Soft threshold towards c (proximal_operators/ista_prox.jl:1-56); a complex
+    parameter has its real and imaginary parts shrunk separately, each towards c."""
+
+    def __init__(self, s, c=0.0):
+        if s < 0:
+            raise ValueError("IstaProx threshold must be non-negative")
+        self.s, self.c = float(s), float(c)
+
+    def init(self, x):
+        return None
+
+    def apply_(self, state, x):
+        f = _float_view(x)
+        _capi.call("fo_ista", _ptr(f), f.numel(), self.s, self.c, _stream())
+
+
+class PositiveProx:
+    """max(x, 0) (proximal_operators/positive_prox.jl:1-40); real parameters only, as
+    the reference's comparison x < 0 is defined for real values only."""
+
+    def init(self, x):
+        return None
+
+    def apply_(self, state, x):
+        if x.is_complex():
+            raise TypeError("PositiveProx applies to real parameters")
+        f = _float_view(x)
+        _capi.call("fo_positive", _ptr(f), f.numel(), _stream())
 
 
 class TVProx:

@@ -458,6 +458,19 @@ FO_API int fo_sid_backward(fo_sid sid, const void* u, const float* dc, void* du,
 FO_API int fo_sid_loss_noalloc(const void* u, const float* target, const int* target_index, int n_targets,
                                int nx, int ny, int batch, float* loss, void* stream);
 
+/*
+ * SquaredFieldDifference against reference fields v of the same grid and batch:
+ * c[b] = sum over the field's pixels of |u_b - v_b|^2 (device float[batch];
+ * fixed-order sums), and the pull-back du = 2 dc[b] (u_b - v_b) (dc: device
+ * float[batch], NULL: all ones).
+ * Replaces: SquaredFieldDifference -- src/metrics/squared_field_difference.jl:35-61.
+ */
+typedef struct fo_sfd_s* fo_sfd;
+FO_API int fo_sfd_create(fo_sfd* sfd, int nx, int ny, int batch);
+FO_API int fo_sfd_forward(fo_sfd sfd, const void* u, const void* v, float* c, void* stream);
+FO_API int fo_sfd_backward(fo_sfd sfd, const void* u, const void* v, const float* dc, void* du, void* stream);
+FO_API int fo_sfd_destroy(fo_sfd sfd);
+
 /* ---------------------------------------------------------------------- */
 /* Optimiser and proximal operators                                        */
 /* ---------------------------------------------------------------------- */
@@ -481,6 +494,16 @@ FO_API int fo_fista_clamp_step(float* x, float* xk, float* newdx, const float* d
 
 /* x = clamp(x, lo, hi).  Replaces ClampProx (proximal_operators/clamp_prox.jl:35-37). */
 FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream);
+
+/* Soft threshold of every value towards c: c where |x - c| <= s, else x -+ s.  A
+ * complex parameter is passed as its 2n floats (the reference shrinks the real and the
+ * imaginary part separately, each towards c).
+ * Replaces: IstaProx(s, c) -- proximal_operators/ista_prox.jl:1-56 with PointwiseProx
+ * (pointwise_prox.jl:31-46). */
+FO_API int fo_ista(float* x, long long n, double s, double c, void* stream);
+
+/* x = max(x, 0).  Replaces: PositiveProx -- proximal_operators/positive_prox.jl:1-40. */
+FO_API int fo_positive(float* x, long long n, void* stream);
 
 /*
  * TVProx(lambda, n_iter; isotropic, rule = Fista(eta)) on an ny x nx float

@@ -642,11 +642,30 @@ def positive_prox(x):
 
 
 def ista_prox(x, s, c=0.0):
-    """IstaProx soft threshold towards c (ista_prox.jl:1-19)."""
+    """IstaProx soft threshold towards c (ista_prox.jl:1-19); a complex array has its
+    real and imaginary parts shrunk separately, each towards the real c
+    (ista_prox.jl:13-15)."""
+    if np.iscomplexobj(x):
+        x.real = ista_prox(x.real.copy(), s, c)
+        x.imag = ista_prox(x.imag.copy(), s, c)
+        return x
     xc = x - c
     out = np.where(np.abs(xc) <= s, c, np.where(xc > s, x - s, x + s))
     x[...] = out
     return x
+
+
+def sfd_value(u, v):
+    """SquaredFieldDifference per field: sum over the last two axes of |u - v|^2, with
+    no dx dy factor (metrics/squared_field_difference.jl:50-54)."""
+    d = np.asarray(u) - np.asarray(v)
+    return np.sum(d.real ** 2 + d.imag ** 2, axis=(-2, -1))
+
+
+def sfd_backward(u, v, dc=1.0):
+    """du = 2 dc_b (u_b - v_b) (metrics/squared_field_difference.jl:56-61)."""
+    dc = np.asarray(dc, dtype=np.float64)
+    return 2.0 * dc[..., None, None] * (np.asarray(u) - np.asarray(v))
 
 
 def _d(p_out, a):

@@ -75,6 +75,14 @@ def test_bad_arguments_are_rejected(capi):
     assert "direction" in lib.fo_last_error().decode()
     assert lib.fo_phase_backward(C.c_void_p(16), C.c_void_p(16), None, C.c_void_p(16), 8, 8, 1, 1, None) == 1
     assert lib.fo_clamp(C.c_void_p(16), 10, 1.0, 0.0, None) == 1
+    assert lib.fo_ista(C.c_void_p(16), 10, -0.1, 0.0, None) == 1
+    assert "non-negative" in lib.fo_last_error().decode()
+    assert lib.fo_ista(None, 10, 0.1, 0.0, None) == 1
+    assert lib.fo_positive(C.c_void_p(16), 0, None) == 2
+    assert lib.fo_sfd_create(C.byref(C.c_void_p()), 8, 0, 2) == 2
+    assert lib.fo_sfd_forward(None, None, None, None, None) == 1
+    assert lib.fo_sfd_backward(None, None, None, None, None, None) == 1
+    assert lib.fo_sfd_destroy(None) == 0
     assert lib.fo_chain_create(C.byref(C.c_void_p()), 0, None) == 1
     assert lib.fo_sid_create(C.byref(C.c_void_p()), 8, 8, 2, 2, capi.ivec([0, 5])) == 1
     assert lib.fo_tv_create(C.byref(C.c_void_p()), 1, 8, 0.1, 10, 1, 0.25) == 2

@@ -724,6 +724,77 @@ def test_fista_clamp_tv(fo, orc):
         assert orc.rel_l2(npy(yt), ref) < 1e-5
 
 
+def test_ista_positive_prox(fo, orc):
+    """IstaProx on real and complex parameters and PositiveProx, bit-exact against the
+    oracle evaluated in float32 (thresholds exactly representable in float32), and
+    ProxRule(Fista, IstaProx) against Fista followed by the oracle's shrink."""
+    rng = np.random.default_rng(31)
+    x0 = f32(rng.standard_normal((37, 53)))
+    xs = torch.tensor(x0, device="cuda")
+    fo.IstaProx(0.25, 0.125).apply_(None, xs)
+    assert np.array_equal(npy(xs), orc.ista_prox(x0.copy(), 0.25, 0.125))
+    z0 = c64(rng.standard_normal((3, 40, 24)) + 1j * rng.standard_normal((3, 40, 24)))
+    zs = torch.tensor(z0, device="cuda")
+    fo.IstaProx(0.375, -0.5).apply_(None, zs)
+    ref = orc.ista_prox(z0.copy(), 0.375, -0.5)
+    assert ref.dtype == np.complex64 and np.array_equal(npy(zs), ref)
+    xs = torch.tensor(x0, device="cuda")
+    fo.PositiveProx().apply_(None, xs)
+    assert np.array_equal(npy(xs), orc.positive_prox(x0.copy()))
+    with pytest.raises(TypeError):
+        fo.PositiveProx().apply_(None, zs)
+    rule = fo.ProxRule(fo.Fista(0.3), fo.IstaProx(0.125))
+    xs = torch.tensor(x0, device="cuda")
+    st = rule.init(xs)
+    xo = x0.astype(np.float64)
+    so = orc.FistaState(xo)
+    for it in range(4):
+        g = f32(rng.standard_normal(x0.shape))
+        rule.apply_(st, xs, torch.tensor(g, device="cuda"))
+        orc.fista_apply(0.3, so, xo, g.astype(np.float64))
+        orc.ista_prox(xo, 0.125)
+        assert orc.rel_l2(npy(xs), xo) < 1e-5
+
+
+def test_squared_field_difference(fo, orc):
+    """SquaredFieldDifference values and pull-back against the oracle, the docstring's
+    16.0, and the gradient of a phase mask through Phase -> ASProp -> the metric."""
+    one = fo.ScalarField(np.ones((4, 4), np.complex64), (1.0, 1.0), 1.064)
+    zero = fo.ScalarField(np.zeros((4, 4), np.complex64), (1.0, 1.0), 1.064)
+    assert npy(fo.SquaredFieldDifference(one)(zero)).tolist() == [16.0]
+    rng = np.random.default_rng(32)
+    n, B = 256, 5
+    ds, lams = (0.8, 0.8), np.array([0.64, 0.538, 0.455, 0.64, 0.538])
+    u0 = rand_field(rng, (B, n, n))
+    v0 = rand_field(rng, (B, n, n))
+    u = fo.ScalarField(u0, ds, lams)
+    v = fo.ScalarField(v0, ds, lams)
+    m = fo.SquaredFieldDifference(v)
+    c = npy(m(u))
+    c_ref = orc.sfd_value(u0.astype(np.complex128), v0.astype(np.complex128))
+    assert np.max(np.abs(c - c_ref) / c_ref) < 1e-5
+    # repeated evaluation is bit-identical (fixed-order sums)
+    assert np.array_equal(npy(m(u)), c)
+    w = f32(rng.standard_normal(B))
+    du = m.backpropagate(u, torch.tensor(w, device="cuda"))
+    assert orc.rel_l2(npy(du.electric), orc.sfd_backward(u0, v0, w)) < 1e-6
+    du = m.backpropagate(u)
+    assert orc.rel_l2(npy(du.electric), orc.sfd_backward(u0, v0)) < 1e-6
+    with pytest.raises(ValueError):
+        m(fo.ScalarField(u0[:2], ds, lams[:2]))
+
+    phi = f32(rng.uniform(0, 2 * np.pi, (n, n)))
+    ph = fo.Phase(u, phi, trainable=True)
+    system = fo.ScalarSource(u) | ph | fo.ASProp(u, 300.0)
+    loss, grads = fo.withgradient(m, system)
+    a = orc.asprop(orc.phase_forward(u0, phi), ds[0], ds[1], lams, 300.0)
+    lr = orc.sfd_value(a, v0).sum()
+    assert abs(float(loss) - lr) / lr < 1e-5
+    g = orc.asprop(orc.sfd_backward(a, v0), ds[0], ds[1], lams, 300.0, orc.BACKWARD)
+    _, gphi = orc.phase_backward(g, phi, u0)
+    assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+
 # ---------------------------------------------------------------------------
 # Full-size properties (sizes where the FP64 oracle is too slow)
 # ---------------------------------------------------------------------------

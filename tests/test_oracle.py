@@ -119,6 +119,43 @@ def test_pointwise_prox():
     assert np.allclose(x, [0.0, 0.3, 1.0, 0.8])
 
 
+def test_prox_docstring_known_answers():
+    """The values printed in the reference's docstrings: IstaProx(0.01, 0.0)
+    (ista_prox.jl:35-49) and PositiveProx (positive_prox.jl:19-33)."""
+    x = np.array([-0.5, -0.005, 0.0, 0.003, 0.2])
+    orc.ista_prox(x, 0.01, 0.0)
+    assert np.allclose(x, [-0.49, 0.0, 0.0, 0.0, 0.19], rtol=0, atol=1e-15)
+    x = np.array([-0.1, 0.0, 0.5, -0.3, 1.2])
+    orc.positive_prox(x)
+    assert np.array_equal(x, [0.0, 0.0, 0.5, 0.0, 1.2])
+    # complex values: real and imaginary parts shrink separately towards the real centre
+    z = np.array([1.0 + 0.05j, 0.25 - 1.0j, 0.31 + 0.29j])
+    orc.ista_prox(z, 0.1, 0.3)
+    assert np.allclose(z, [0.9 + 0.15j, 0.3 - 0.9j, 0.3 + 0.3j])
+
+
+def test_sfd_known_answer_and_pullback():
+    """SquaredFieldDifference: the docstring's 16.0 for 4 x 4 ones against zeros
+    (squared_field_difference.jl:16-31), and its pull-back 2 dc (u - v) against
+    central differences of the real loss sum(w c)."""
+    assert orc.sfd_value(np.ones((4, 4), complex), np.zeros((4, 4), complex)) == 16.0
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal((3, 6, 5)) + 1j * rng.standard_normal((3, 6, 5))
+    v = rng.standard_normal((3, 6, 5)) + 1j * rng.standard_normal((3, 6, 5))
+    w = rng.standard_normal(3)
+    loss = lambda uu: float(np.sum(w * orc.sfd_value(uu, v)))
+    g = orc.sfd_backward(u, v, w)
+    eps = 1e-6
+    for (b, i, j) in [(0, 0, 0), (2, 3, 4), (1, 5, 2)]:
+        for part, unit in (("re", 1.0), ("im", 1j)):
+            up, um = u.copy(), u.copy()
+            up[b, i, j] += eps * unit
+            um[b, i, j] -= eps * unit
+            fd = (loss(up) - loss(um)) / (2 * eps)
+            ref = g[b, i, j].real if part == "re" else g[b, i, j].imag
+            assert abs(fd - ref) < 1e-6 * max(1.0, abs(fd)), (part, fd, ref)
+
+
 # --- analytic paraxial Gaussian beam (src/modes/gaussian_modes.jl:87-104) -----------
 def test_as_matches_paraxial_gaussian_beam():
     n, ds, lam, w0, z = 512, (1.0, 1.0), 1.064, 30.0, 1500.0
