@@ -729,11 +729,11 @@ def test_ista_positive_prox(fo, orc):
     oracle evaluated in float32 (thresholds exactly representable in float32), and
     ProxRule(Fista, IstaProx) against Fista followed by the oracle's shrink."""
     rng = np.random.default_rng(31)
-    x0 = f32(rng.standard_normal((37, 53)))
+    x0 = rng.standard_normal((37, 53)).astype(np.float32)
     xs = torch.tensor(x0, device="cuda")
     fo.IstaProx(0.25, 0.125).apply_(None, xs)
     assert np.array_equal(npy(xs), orc.ista_prox(x0.copy(), 0.25, 0.125))
-    z0 = c64(rng.standard_normal((3, 40, 24)) + 1j * rng.standard_normal((3, 40, 24)))
+    z0 = (rng.standard_normal((3, 40, 24)) + 1j * rng.standard_normal((3, 40, 24))).astype(np.complex64)
     zs = torch.tensor(z0, device="cuda")
     fo.IstaProx(0.375, -0.5).apply_(None, zs)
     ref = orc.ista_prox(z0.copy(), 0.375, -0.5)
@@ -749,7 +749,7 @@ def test_ista_positive_prox(fo, orc):
     xo = x0.astype(np.float64)
     so = orc.FistaState(xo)
     for it in range(4):
-        g = f32(rng.standard_normal(x0.shape))
+        g = rng.standard_normal(x0.shape).astype(np.float32)
         rule.apply_(st, xs, torch.tensor(g, device="cuda"))
         orc.fista_apply(0.3, so, xo, g.astype(np.float64))
         orc.ista_prox(xo, 0.125)
