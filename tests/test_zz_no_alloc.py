@@ -4,7 +4,8 @@ their own pool allocator, real-time loops where an allocation's implicit
 synchronisation is not allowed).  Its partial sums live in a fixed array inside
 the library.  These tests call it through the C ABI and check, on two
 consecutive calls, its losses against the allocating metric (fo_sid_forward)
-and against the FP64 oracle, including the largest accepted slice count (64).
+and against the FP64 oracle, including the largest accepted slice count (64), and
+that a call after the first leaves the device's free memory unchanged.
 
 The file name sorts last so that a run stopping at the first failure has
 already run every other test; it also passes when run alone.
@@ -38,12 +39,19 @@ def _run_case(fo, orc, B, T, ny, nx, seed):
     capi.check(lib.fo_sid_forward(sid, C.c_void_p(u.data_ptr()), C.c_void_p(target.data_ptr()),
                                   C.c_void_p(ref.data_ptr()), stream))
     try:
-        for _ in range(2):
+        free_before = None
+        for k in range(2):
             got = torch.full((T,), -1.0, dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            if k == 1:
+                free_before = torch.cuda.mem_get_info()[0]
             capi.check(lib.fo_sid_loss_noalloc(C.c_void_p(u.data_ptr()), C.c_void_p(target.data_ptr()),
                                                C.c_void_p(tidx.data_ptr()), T, nx, ny, B,
                                                C.c_void_p(got.data_ptr()), stream))
             torch.cuda.synchronize()
+            if k == 1:
+                # the second call allocates no device memory
+                assert torch.cuda.mem_get_info()[0] == free_before
             # same tolerance as the metric's oracle tests: 1e-4 relative per slice
             assert torch.allclose(got, ref, rtol=1e-5, atol=0.0), (got, ref)
             g = got.cpu().numpy().astype(np.float64)
