@@ -90,6 +90,8 @@ SIGNATURES = {
     "fo_chain_withgradient_sid": (_i, [_vp, _vp, _vp, _vp, C.POINTER(fo_mod), C.POINTER(fo_mod), _i, _vp, _vp, _vp,
                                        _i, _vp]),
     "fo_bpm_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i, _d, _i]),
+    "fo_bpm_create_ex": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i,
+                              C.POINTER(fo_as_options), _i]),
     "fo_bpm_destroy": (_i, [_vp]),
     "fo_bpm_info": (_i, [_vp, _pi, C.POINTER(C.c_size_t)]),
     "fo_bpm_forward": (_i, [_vp, _vp, _vp, _i, _i, _vp]),

@@ -608,12 +608,15 @@ class AS_BPM(Component):
 
     ``dn0`` has shape (n_slices, ny, nx) -- the C view of the reference's
     (nx, ny, n_slices) array.  The adjoint keeps every ``checkpoint_every``-th
-    slice input and recomputes the rest (0: round(sqrt(n_slices)); 1: keep all)."""
+    slice input and recomputes the rest (0: round(sqrt(n_slices)); 1: keep all).
+    ``paraxial`` selects the Fresnel steps; fields with tilts take the tilted steps
+    and the per-field kdz = 2 pi dz / (cos theta_x cos theta_y) (bpm.jl:3-6).  The
+    reference computes but never applies its ``aperture`` mask, so it is accepted
+    and ignored here too."""
 
     def __init__(self, u, thickness, n0, dn0, use_cache=True, paraxial=False, trainable=False,
                  buffered=False, aperture=None, double_precision_kernel=True, checkpoint_every=0):
-        if paraxial:
-            raise NotImplementedError("paraxial AS_BPM is not in the GB300 path")
+        self.paraxial = bool(paraxial)
         dn = dn0.detach().cpu().numpy() if isinstance(dn0, torch.Tensor) else np.asarray(dn0)
         if dn.ndim != 3 or dn.shape[1:] != (u.ny, u.nx):
             raise ValueError("dn0 must have shape (n_slices, ny, nx)")
@@ -633,13 +636,21 @@ class AS_BPM(Component):
 
     def handle(self, u):
         lam = tuple(float(v) for v in u.lambdas_per_field())
-        key = (u.nx, u.ny, u.batch, lam)
+        tilts = u.tilts_per_field()
+        key = (u.nx, u.ny, u.batch, lam, tuple(map(float, tilts.ravel())))
         h = self._bpms.get(key)
         if h is None:
             h = C.c_void_p()
-            _capi.call("fo_bpm_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
-                       _capi.dvec(lam), len(lam), self.thickness, self.n0, self.n_slices,
-                       self.checkpoint_every, 1.0, 1)
+            if self.paraxial or np.any(tilts != 0.0):
+                opt, keep = _as_options(self.paraxial, False, tilts, None)
+                _capi.call("fo_bpm_create_ex", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                           _capi.dvec(lam), len(lam), self.thickness, self.n0, self.n_slices,
+                           self.checkpoint_every, C.byref(opt), 1)
+                del keep
+            else:
+                _capi.call("fo_bpm_create", C.byref(h), u.nx, u.ny, u.batch, self.ds[0], self.ds[1],
+                           _capi.dvec(lam), len(lam), self.thickness, self.n0, self.n_slices,
+                           self.checkpoint_every, 1.0, 1)
             self._bpms[key] = h
         return h
 

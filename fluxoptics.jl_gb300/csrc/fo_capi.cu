@@ -1636,22 +1636,47 @@ struct fo_bpm_s {
   size_t ws_bytes = 0;
 };
 
-extern "C" {
+namespace {
 
-FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
-                         const double* lambdas, int n_lambdas, double thickness, double n0,
-                         int n_slices, int checkpoint_every, double cos_correction, int flags) {
+// AS_BPM with a scalar cos correction (opt == NULL) or with the options' tilts, whose
+// per-field cos correction cos(theta_x) cos(theta_y) is folded into the plans' per-field
+// inverse wavelengths (the dn phase of field b is kdz * dn / (lambda_b cos_b), with
+// kdz = 2 pi dz).
+int bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy, const double* lambdas, int n_lambdas,
+               double thickness, double n0, int n_slices, int checkpoint_every, double cos_correction,
+               const fo_as_options* opt, int flags) {
   if (!bpm) return fail(FO_ERR_ARG, "bpm output pointer is NULL");
   *bpm = nullptr;
   if (n_slices < 2) return fail(FO_ERR_SHAPE, "AS_BPM needs at least 2 slices");
   if (!(thickness > 0) || !(cos_correction > 0)) return fail(FO_ERR_ARG, "thickness and cos_correction must be positive");
   if (checkpoint_every < 0) return fail(FO_ERR_ARG, "checkpoint_every must be >= 0");
+  if (opt && opt->filter) return fail(FO_ERR_ARG, "AS_BPM takes no frequency filter");
+  if (opt && opt->tilts && opt->n_tilts != 1 && opt->n_tilts != batch)
+    return fail(FO_ERR_ARG, "tilts must hold 1 or batch pairs");
   const double dz = thickness / n_slices;
   fo_bpm b = new fo_bpm_s();
-  int rc = make_plan(&b->full, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz, n0, flags);
-  if (rc == FO_OK) rc = make_plan(&b->half, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz / 2, n0, flags);
+  int rc = make_plan(&b->full, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz, n0, flags, opt);
+  if (rc == FO_OK) rc = make_plan(&b->half, 0, nx, ny, batch, dx, dy, lambdas, n_lambdas, dz / 2, n0, flags, opt);
+  if (rc == FO_OK && opt && opt->tilts) {
+    std::vector<float> il(batch);
+    for (int i = 0; i < batch; ++i) {
+      const double* th = opt->tilts + 2 * (opt->n_tilts == 1 ? 0 : i);
+      const double c = cos(th[0]) * cos(th[1]);
+      if (!(c > 0)) {
+        rc = fail(FO_ERR_ARG, "tilts must be below pi/2");
+        break;
+      }
+      il[i] = (float)(1.0 / (lambdas[n_lambdas == 1 ? 0 : i] * c));
+    }
+    for (fo_prop_plan q : {b->full, b->half}) {
+      if (rc != FO_OK) break;
+      cudaError_t e = cudaMemcpy(q->inv_lambda, il.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) rc = cuda_fail(e, "cudaMemcpy BPM phase factors");
+    }
+  }
   if (rc != FO_OK) {
     plan_free(b->full);
+    plan_free(b->half);
     delete b;
     return rc;
   }
@@ -1691,6 +1716,24 @@ FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, doub
                 b->half->ws_bytes;
   *bpm = b;
   return FO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
+                         const double* lambdas, int n_lambdas, double thickness, double n0,
+                         int n_slices, int checkpoint_every, double cos_correction, int flags) {
+  return bpm_create(bpm, nx, ny, batch, dx, dy, lambdas, n_lambdas, thickness, n0, n_slices, checkpoint_every,
+                    cos_correction, nullptr, flags);
+}
+
+FO_API int fo_bpm_create_ex(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
+                            const double* lambdas, int n_lambdas, double thickness, double n0,
+                            int n_slices, int checkpoint_every, const fo_as_options* options, int flags) {
+  return bpm_create(bpm, nx, ny, batch, dx, dy, lambdas, n_lambdas, thickness, n0, n_slices, checkpoint_every,
+                    1.0, options, flags);
 }
 
 FO_API int fo_bpm_destroy(fo_bpm b) {

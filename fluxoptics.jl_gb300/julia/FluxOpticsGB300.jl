@@ -529,29 +529,43 @@ struct GB300BPMSaved
 end
 
 """
-    GB300AS_BPM(u, thickness, n0, dn0; trainable=false, buffered=false, checkpoint_every=0)
+    GB300AS_BPM(u, thickness, n0, dn0; paraxial=false, trainable=false, buffered=false, checkpoint_every=0)
 
 AS_BPM (bpm.jl:130-142) on the GPU path: the symmetric split-step march of
 `propagate!` (bpm.jl:244-260) and its adjoint with the ∂dn gradient
 (bpm.jl:275-321).  Instead of saving every slice input (bpm.jl:49, 2 GiB at
 1024² × 256) the plan keeps every `checkpoint_every`-th one (0: round(√n_slices))
-and recomputes each segment during the adjoint.  On-axis fields only (the
-reference's cos correction is 1 there); `dn0` is nx × ny × n_slices.
+and recomputes each segment during the adjoint.  `paraxial` selects Fresnel steps;
+fields with tilts take the tilted steps and kdz = 2π dz / (cos θx cos θy) per field
+(bpm.jl:3-6).  `dn0` is nx × ny × n_slices.
 """
 function GB300AS_BPM(u::ScalarField, thickness::Real, n0::Real, dn0::AbstractArray{<:Real, 3};
-                     trainable::Bool = false, buffered::Bool = false, checkpoint_every::Integer = 0)
-    FluxOptics.is_on_axis(u) || error("GB300AS_BPM: tilted fields are not supported")
+                     paraxial::Bool = false, trainable::Bool = false, buffered::Bool = false,
+                     checkpoint_every::Integer = 0)
     nx, ny, b = dims_of(u)
     size(dn0, 1) == nx && size(dn0, 2) == ny || error("GB300AS_BPM: dn0 must be nx x ny x n_slices")
     ns = size(dn0, 3)
     ns >= 2 || error("GB300AS_BPM: at least 2 slices")
     lam = lambdas_per_field(u)
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:fo_bpm_create, LIB), Cint,
-                (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble,
-                 Cint, Cint, Cdouble, Cint),
-                h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), thickness, n0, ns, checkpoint_every, 1.0,
-                FO_FLAG_AUTOTUNE))
+    if !paraxial && FluxOptics.is_on_axis(u)
+        check(ccall((:fo_bpm_create, LIB), Cint,
+                    (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble,
+                     Cint, Cint, Cdouble, Cint),
+                    h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), thickness, n0, ns, checkpoint_every, 1.0,
+                    FO_FLAG_AUTOTUNE))
+    else
+        # tilted steps and kdz = 2π dz / (cos θx cos θy) per field (bpm.jl:3-6)
+        th = tilts_per_field(u)
+        GC.@preserve th begin
+            opt = Ref(FoASOptions(Cint(paraxial), Cint(0), pointer(th), Cint(b), C_NULL, C_NULL))
+            check(ccall((:fo_bpm_create_ex, LIB), Cint,
+                        (Ref{Ptr{Cvoid}}, Cint, Cint, Cint, Cdouble, Cdouble, Ptr{Cdouble}, Cint, Cdouble, Cdouble,
+                         Cint, Cint, Ref{FoASOptions}, Cint),
+                        h, nx, ny, b, u.ds[1], u.ds[2], lam, length(lam), thickness, n0, ns, checkpoint_every,
+                        opt, FO_FLAG_AUTOTUNE))
+        end
+    end
     dn = CuArray{Float32}(dn0)
     M = trainable ? (buffered ? Trainable{Buffered} : Trainable{Unbuffered}) : Static
     ∂p = (trainable && buffered) ? (; dn = similar(dn)) : nothing

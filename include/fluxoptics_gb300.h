@@ -400,6 +400,16 @@ typedef struct fo_bpm_s* fo_bpm;
 FO_API int fo_bpm_create(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
                          const double* lambdas, int n_lambdas, double thickness, double n0,
                          int n_slices, int checkpoint_every, double cos_correction, int flags);
+/*
+ * AS_BPM with the propagators of fo_asprop_create_ex: `options` selects the paraxial
+ * and the tilted kernel (no filter), and the dn phase of field b uses
+ * kdz_b = 2 pi dz / (cos(theta_x,b) cos(theta_y,b)) from the field's tilts.
+ * Replaces: AS_BPM(u, thickness, n0, dn; paraxial) for fields with tilts --
+ * bulk_propagators/bpm.jl:3-6 (compute_cos_correction), :54-74, :130-142.
+ */
+FO_API int fo_bpm_create_ex(fo_bpm* bpm, int nx, int ny, int batch, double dx, double dy,
+                            const double* lambdas, int n_lambdas, double thickness, double n0,
+                            int n_slices, int checkpoint_every, const fo_as_options* options, int flags);
 FO_API int fo_bpm_destroy(fo_bpm bpm);
 FO_API int fo_bpm_info(fo_bpm bpm, int* checkpoint_every, size_t* workspace_bytes);
 

@@ -467,12 +467,22 @@ def mask_backward(dv, m, u_saved, direction=FORWARD):
 # AS_BPM
 # ---------------------------------------------------------------------------
 
-def bpm_forward(u, dx, dy, lambdas, thickness, n0, dn, direction=FORWARD, save=False):
+def _bpm_kdz(nb, dz, tilts):
+    """kdz per field: 2 pi dz / (cos theta_x cos theta_y) (bpm.jl:3-6, :67-70)."""
+    th = np.zeros((nb, 2))
+    if tilts is not None:
+        th[:] = np.asarray(tilts, dtype=np.float64).reshape(-1, 2)
+    return (2.0 * np.pi * dz / (np.cos(th[:, 0]) * np.cos(th[:, 1])))[:, None, None]
+
+
+def bpm_forward(u, dx, dy, lambdas, thickness, n0, dn, direction=FORWARD, save=False, paraxial=False, tilts=None):
     """Symmetric split-step AS_BPM march (bpm.jl:54-74, :130-142, :235-260).
 
-    dn has shape (n_slices, ny, nx).  dz = thickness/n_slices, props ASProp(dz; n0)
-    and ASProp(dz/2; n0), on-axis kdz = 2 pi dz.  Returns the output field and,
-    when ``save``, the list of slice inputs u_k (taken before the dn phase)."""
+    dn has shape (n_slices, ny, nx).  dz = thickness/n_slices, props ASProp(dz; n0,
+    paraxial) and ASProp(dz/2; n0, paraxial) -- the tilted kernel for fields with
+    ``tilts`` -- and kdz = 2 pi dz / (cos theta_x cos theta_y) per field.  Returns the
+    output field and, when ``save``, the list of slice inputs u_k (taken before the dn
+    phase)."""
     u = np.array(u, dtype=np.complex128)
     shp = u.shape
     ny, nx = shp[-2:]
@@ -480,23 +490,24 @@ def bpm_forward(u, dx, dy, lambdas, thickness, n0, dn, direction=FORWARD, save=F
     lam = _lams(lambdas, v.shape[0])[:, None, None]
     n_slices = dn.shape[0]
     dz = thickness / n_slices
-    kdz = 2.0 * np.pi * dz
+    kdz = _bpm_kdz(v.shape[0], dz, tilts)
+    prop = lambda w, zz: asprop(w, dx, dy, lam.ravel(), zz, direction, n0, paraxial, tilts)
     saves = []
-    v = asprop(v, dx, dy, lam.ravel(), dz / 2, direction, n0)
+    v = prop(v, dz / 2)
     for k in range(n_slices - 1):
         if save:
             saves.append(v.copy())
         v = v * np.exp(1j * direction * kdz / lam * dn[k][None])
-        v = asprop(v, dx, dy, lam.ravel(), dz, direction, n0)
+        v = prop(v, dz)
     if save:
         saves.append(v.copy())
     v = v * np.exp(1j * direction * kdz / lam * dn[-1][None])
-    v = asprop(v, dx, dy, lam.ravel(), dz / 2, direction, n0)
+    v = prop(v, dz / 2)
     return v.reshape(shp), saves
 
 
-def bpm_backward(dv, dx, dy, lambdas, thickness, n0, dn, saves, direction=FORWARD):
-    """Adjoint march with the dn gradient (bpm.jl:275-321).
+def bpm_backward(dv, dx, dy, lambdas, thickness, n0, dn, saves, direction=FORWARD, paraxial=False, tilts=None):
+    """Adjoint march with the dn gradient (bpm.jl:262-321).
 
     d_dn_k = s * kdz/lam * sum_batch Im(du * conj(u_k)), taken after the
     conjugate dn phase of slice k."""
@@ -507,17 +518,18 @@ def bpm_backward(dv, dx, dy, lambdas, thickness, n0, dn, saves, direction=FORWAR
     lam = _lams(lambdas, du.shape[0])[:, None, None]
     n_slices = dn.shape[0]
     dz = thickness / n_slices
-    kdz = 2.0 * np.pi * dz
+    kdz = _bpm_kdz(du.shape[0], dz, tilts)
     rev = -direction
+    prop = lambda w, zz: asprop(w, dx, dy, lam.ravel(), zz, rev, n0, paraxial, tilts)
     ddn = np.zeros_like(dn, dtype=np.float64)
-    du = asprop(du, dx, dy, lam.ravel(), dz / 2, rev, n0)
+    du = prop(du, dz / 2)
     for k in range(n_slices - 1, 0, -1):
         du = du * np.exp(1j * rev * kdz / lam * dn[k][None])
         ddn[k] = (direction * kdz / lam * np.imag(du * np.conj(saves[k].reshape(du.shape)))).sum(0)
-        du = asprop(du, dx, dy, lam.ravel(), dz, rev, n0)
+        du = prop(du, dz)
     du = du * np.exp(1j * rev * kdz / lam * dn[0][None])
     ddn[0] = (direction * kdz / lam * np.imag(du * np.conj(saves[0].reshape(du.shape)))).sum(0)
-    du = asprop(du, dx, dy, lam.ravel(), dz / 2, rev, n0)
+    du = prop(du, dz / 2)
     return du.reshape(shp), ddn
 
 

@@ -661,6 +661,33 @@ def test_bpm_backward_direction(fo, orc):
     assert orc.rel_l2(npy(g), g_ref) < GRAD_TOL
 
 
+@pytest.mark.parametrize("paraxial,tilted,d", [(True, False, 1), (False, True, 1), (True, True, -1)])
+def test_bpm_paraxial_and_tilted(fo, orc, paraxial, tilted, d):
+    """AS_BPM with Fresnel steps and with tilted fields (tilted kernel and the per-field
+    kdz = 2 pi dz / (cos theta_x cos theta_y), bpm.jl:3-6): output field and d(dn)
+    against the oracle, with recomputed segments (checkpoint_every=3)."""
+    rng = np.random.default_rng(12 if tilted else 13)
+    n, ns = 64, 8
+    ds, lams, n0, L = (0.5, 0.5), [1.064, 0.8], 1.45, 16.0
+    u0 = rand_field(rng, (2, n, n))
+    dv0 = rand_field(rng, (2, n, n))
+    dn = f32(5e-3 * rng.standard_normal((ns, n, n)))
+    tilts = ([0.05, -0.02], [-0.03, 0.04]) if tilted else None  # (theta_x per field, theta_y per field)
+    u = fo.ScalarField(u0, ds, lams, tilts=tilts)
+    bpm = fo.AS_BPM(u, L, n0, dn, paraxial=paraxial, trainable=True, checkpoint_every=3)
+    v = u.copy()
+    bpm.propagate_and_save_(v, None, d)
+    th = None if tilts is None else np.stack(tilts, axis=1)  # one (theta_x, theta_y) pair per field
+    out, saves = orc.bpm_forward(u0, ds[0], ds[1], lams, L, n0, dn, d, save=True, paraxial=paraxial, tilts=th)
+    assert orc.rel_l2(npy(v.electric), out) < FIELD_TOL
+    dv = fo.ScalarField(dv0, ds, lams, tilts=tilts)
+    g = torch.empty_like(bpm.dn)
+    bpm.backpropagate_with_gradient_(dv, None, g, d)
+    du_ref, g_ref = orc.bpm_backward(dv0, ds[0], ds[1], lams, L, n0, dn, saves, d, paraxial=paraxial, tilts=th)
+    assert orc.rel_l2(npy(dv.electric), du_ref) < FIELD_TOL
+    assert orc.rel_l2(npy(g), g_ref) < GRAD_TOL
+
+
 # ---------------------------------------------------------------------------
 # Metric and optimiser
 # ---------------------------------------------------------------------------

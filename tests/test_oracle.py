@@ -249,22 +249,34 @@ def test_fd_mask(direction):
     _fd_check(loss, lambda dd: np.real(np.sum(np.conj(gm) * dd)), m, d)
 
 
-@pytest.mark.parametrize("direction", [1, -1])
-def test_fd_bpm(direction):
+@pytest.mark.parametrize("direction,paraxial,tilted", [(1, False, False), (-1, False, False), (1, True, False),
+                                                       (1, False, True), (-1, True, True)])
+def test_fd_bpm(direction, paraxial, tilted):
+    """The AS_BPM adjoint's d(dn) against central differences, on axis and for the
+    paraxial and tilted propagators with the per-field cos correction of kdz
+    (bpm.jl:3-6)."""
     n, ds, lam, n0, L = 32, (0.5, 0.5), 1.064, 1.45, 12.0
     rng = np.random.default_rng(11)
-    u0 = gauss_field(n, ds, 4.0).astype(complex)
+    u0 = np.stack([gauss_field(n, ds, 4.0).astype(complex)] * 2)
+    tilts = [(0.05, -0.03), (-0.02, 0.04)] if tilted else None
+    lams = [lam, 0.8]
     dn = 5e-3 * rng.standard_normal((6, n, n))
     target = np.abs(gauss_field(n, ds, 3.0)) ** 2
 
     def loss(d):
-        v, _ = orc.bpm_forward(u0, ds[0], ds[1], lam, L, n0, d, direction)
+        v, _ = orc.bpm_forward(u0, ds[0], ds[1], lams, L, n0, d, direction, paraxial=paraxial, tilts=tilts)
         return orc.sid_value(v, target)[0].sum()
 
-    v, saves = orc.bpm_forward(u0, ds[0], ds[1], lam, L, n0, dn, direction, save=True)
-    _, g = orc.bpm_backward(orc.sid_backward(v, target), ds[0], ds[1], lam, L, n0, dn, saves, direction)
+    v, saves = orc.bpm_forward(u0, ds[0], ds[1], lams, L, n0, dn, direction, save=True, paraxial=paraxial,
+                               tilts=tilts)
+    _, g = orc.bpm_backward(orc.sid_backward(v, target), ds[0], ds[1], lams, L, n0, dn, saves, direction,
+                            paraxial=paraxial, tilts=tilts)
     d = rng.standard_normal(dn.shape)
     _fd_check(loss, lambda dd: np.sum(g * dd), dn, d, eps=1e-7)
+    if tilted:
+        # the tilted march differs from the on-axis one through both the kernel and kdz
+        v0, _ = orc.bpm_forward(u0, ds[0], ds[1], lams, L, n0, dn, direction, paraxial=paraxial)
+        assert orc.rel_l2(v, v0) > 1e-3
 
 
 # --- TVProx against a loop-by-loop restatement of tv_prox.jl:1-59 ---------------------
