@@ -9,7 +9,8 @@ fails loudly when the library cannot be loaded.
 from . import _capi
 from ._capi import FluxOpticsError
 from .build import build as build_library
-from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierPhase, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
+from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierOperator, FourierPhase,
+                         FourierWrapper, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
                          RSProp,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate_, function_to_array, propagate, propagate_,
                          reverse, spatial_vectors)
@@ -23,7 +24,7 @@ from .ragged import RaggedBatch
 load_library = _capi.load
 
 __all__ = [
-    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierPhase",
+    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
     "Forward", "IstaProx", "Mask", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",

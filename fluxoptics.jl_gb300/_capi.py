@@ -14,6 +14,7 @@ FO_MOD_NONE, FO_MOD_PHASE, FO_MOD_MASK, FO_MOD_DN, FO_MOD_TEA = 0, 1, 2, 3, 4
 FO_FOURIER_TRAINABLE = 2
 FO_FLAG_GRAD_SPECTRA = 2
 FO_FLAG_DEVICE_Z = 4
+FO_FFT_FORWARD, FO_FFT_INVERSE, FO_FFT_FORWARD_ADJOINT, FO_FFT_INVERSE_ADJOINT = 0, 1, 2, 3
 
 ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
                5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
@@ -73,6 +74,7 @@ SIGNATURES = {
     "fo_fourier_gradient": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _i, _vp]),
     "fo_asprop_create_ex": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d,
                                  C.POINTER(fo_as_options), _i]),
+    "fo_fft2": (_i, [_vp, _vp, _i, _vp]),
     "fo_prop_variants": (_i, [_vp, _pi, _pi, C.c_char_p, C.c_char_p, _i]),
     "fo_propagate": (_i, [_vp, _vp, _i, _vp]),
     "fo_phase_forward": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),

@@ -711,6 +711,53 @@ class ScalarSource:
         return OpticalSystem(self, []) | other
 
 
+class FourierOperator(Component):
+    """In-place 2-D FFT (``direct=True``) or inverse FFT (``direct=False``) of every
+    field, FFTW's unnormalised fft and 1/(nx ny)-normalised ifft; the Backward direction
+    swaps the two (fourier/fourier_operator.jl:37-83).  Its pull-back is the exact
+    adjoint of the transform it applied: F^H for the FFT, F / (nx ny) for the inverse."""
+
+    def __init__(self, u, direct):
+        self.direct = bool(direct)
+        self._plans = {}
+
+    def _plan(self, u):
+        key = (u.nx, u.ny, u.batch)
+        h = self._plans.get(key)
+        if h is None:
+            h = C.c_void_p()
+            # a z = 0 ASProp plan gives the grid's transform layout and twiddles
+            _capi.call("fo_asprop_create", C.byref(h), u.nx, u.ny, u.batch, u.ds[0], u.ds[1], _capi.dvec([1.0]), 1,
+                       0.0, 1.0, 0)
+            self._plans[key] = h
+        return h
+
+    def _is_fft(self, direction):
+        return self.direct == (int(direction) == int(Forward))
+
+    def propagate_(self, u, direction=Forward):
+        _capi.call("fo_fft2", self._plan(u), _ptr(u.electric),
+                   _capi.FO_FFT_FORWARD if self._is_fft(direction) else _capi.FO_FFT_INVERSE, _stream())
+        return u
+
+    def backpropagate_(self, dv, direction=Forward):
+        mode = _capi.FO_FFT_FORWARD_ADJOINT if self._is_fft(direction) else _capi.FO_FFT_INVERSE_ADJOINT
+        _capi.call("fo_fft2", self._plan(dv), _ptr(dv.electric), mode, _stream())
+        return dv
+
+    def __del__(self):
+        lib = _capi._LIB
+        if lib is not None:
+            for h in getattr(self, "_plans", {}).values():
+                lib.fo_prop_destroy(h)
+
+
+def FourierWrapper(u, *components):
+    """FFT, the components on the spectrum, inverse FFT (fourier/fourier_wrapper.jl:1-42),
+    as a source-less system to pipe into another."""
+    return OpticalSystem(None, [FourierOperator(u, True), *components, FourierOperator(u, False)])
+
+
 class FieldProbe(Component):
     """Records the field where it sits (system/field_probe.jl:31-43): calling the
     system returns a copy of the field at every probe in ``result["probes"][probe]``
@@ -1020,7 +1067,7 @@ class OpticalSystem:
                     g = c.get_gradient_buffer()
                     _, gd = c.backpropagate_with_gradient_(du, saved, g, d)
                     grads[c] = gd
-                elif _is_prop(c) or _is_mod(c) or isinstance(c, (ASPropZ, _FourierModulator)):
+                elif _is_prop(c) or _is_mod(c) or isinstance(c, (ASPropZ, _FourierModulator, FourierOperator)):
                     c.backpropagate_(du, d)
                 elif isinstance(c, AS_BPM):
                     c.backpropagate_with_gradient_(du, None, None, d)

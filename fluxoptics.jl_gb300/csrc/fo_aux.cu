@@ -516,6 +516,16 @@ __global__ void clamp_kernel(float* x, long long n, float lo, float hi) {
     x[q] = fminf(fmaxf(x[q], lo), hi);
 }
 
+// x <- s * conj(x) (conj != 0) or s * x
+__global__ void conj_scale_kernel(float2* x, long long n, float s, int conj) {
+  const float sy = conj ? -s : s;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float2 v = x[q];
+    x[q] = make_float2(s * v.x, sy * v.y);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // TVProx (2-D).  p holds two dual slices: p0 (differences along x) and p1 (along y).
 // The dual is used through a per-slice scale (the isotropic projection of the
@@ -777,6 +787,11 @@ cudaError_t launch_fista(float* x, float* xk, float* newdx, const float* dx, lon
 
 cudaError_t launch_clamp(float* x, long long n, float lo, float hi, cudaStream_t st) {
   clamp_kernel<<<capped_grid(n), kThreads, 0, st>>>(x, n, lo, hi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conj_scale(float2* x, long long n, float s, int conj, cudaStream_t st) {
+  conj_scale_kernel<<<capped_grid(n), kThreads, 0, st>>>(x, n, s, conj);
   return cudaGetLastError();
 }
 

@@ -48,6 +48,8 @@ cudaError_t launch_fista(float* x, float* xk, float* newdx, const float* dx, lon
                          double* t_state, cudaStream_t st, int clamp = 0,
                          float lo = 0.f, float hi = 0.f);
 cudaError_t launch_clamp(float* x, long long n, float lo, float hi, cudaStream_t st);
+// x <- s * conj(x) (conj != 0) or s * x, over n complex values
+cudaError_t launch_conj_scale(float2* x, long long n, float s, int conj, cudaStream_t st);
 
 size_t tv_state_bytes();
 int tv_partial_blocks(long long n);

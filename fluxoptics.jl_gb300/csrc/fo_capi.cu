@@ -1224,6 +1224,24 @@ static int fft2_into(const fo_prop_plan_s* p, const float2* src, float2* dst, cu
   return FO_OK;
 }
 
+FO_API int fo_fft2(fo_prop_plan plan, void* u, int mode, void* stream) {
+  if (!plan || !u) return fail(FO_ERR_ARG, "plan and u must not be NULL");
+  if (mode < FO_FFT_FORWARD || mode > FO_FFT_INVERSE_ADJOINT) return fail(FO_ERR_ARG, "unknown fo_fft2 mode");
+  if (plan->fx != plan->nx || plan->fy != plan->ny)
+    return fail(FO_ERR_ARG, "fo_fft2 needs a plan on the field's own grid (ASProp or Fourier), not a padded one");
+  float2* x = reinterpret_cast<float2*>(u);
+  cudaStream_t st = S(stream);
+  const long long n = (long long)plan->nx * plan->ny * plan->batch;
+  const float inv_n = (float)(1.0 / ((double)plan->nx * (double)plan->ny));
+  // the inverse directions run as conj(DFT(conj(x)))
+  const bool conj = mode == FO_FFT_INVERSE || mode == FO_FFT_FORWARD_ADJOINT;
+  if (conj) FO_LAUNCH(launch_conj_scale(x, n, 1.f, 1, st));
+  FO_TRY(fft2_into(plan, x, x, st));
+  if (conj || mode == FO_FFT_INVERSE_ADJOINT)
+    FO_LAUNCH(launch_conj_scale(x, n, mode == FO_FFT_FORWARD_ADJOINT ? 1.f : inv_n, conj ? 1 : 0, st));
+  return FO_OK;
+}
+
 FO_API int fo_prop_set_z(fo_prop_plan plan, const float* z, void* stream) {
   if (!plan || !z) return fail(FO_ERR_ARG, "plan and z must not be NULL");
   if (plan->kind != 0) return fail(FO_ERR_ARG, "fo_prop_set_z needs an ASProp plan");

@@ -145,6 +145,23 @@ FO_API int fo_asprop_create_ex(fo_prop_plan* plan, int nx, int ny, int batch, do
                                const fo_as_options* options, int flags);
 
 /*
+ * In-place 2-D DFT of every field on the plan's grid (an ASProp or Fourier plan; a
+ * padded RSProp plan is rejected).  FFTW's fft / ifft conventions, which the
+ * reference's compute_ft! / compute_ift! use, and their adjoints:
+ *   FO_FFT_FORWARD          F u     = sum_x u(x) e^{-2 pi i k.x / n} (unnormalised)
+ *   FO_FFT_INVERSE          F^H u / (nx ny)
+ *   FO_FFT_FORWARD_ADJOINT  F^H u   (the adjoint of FO_FFT_FORWARD)
+ *   FO_FFT_INVERSE_ADJOINT  F u / (nx ny)  (the adjoint of FO_FFT_INVERSE)
+ * Replaces: FourierOperator(u, direct) -- fourier/fourier_operator.jl:37-83 with
+ * FFTutils.jl:13-28; the adjoints are the pull-backs of its two transforms.
+ */
+#define FO_FFT_FORWARD 0
+#define FO_FFT_INVERSE 1
+#define FO_FFT_FORWARD_ADJOINT 2
+#define FO_FFT_INVERSE_ADJOINT 3
+FO_API int fo_fft2(fo_prop_plan plan, void* u, int mode, void* stream);
+
+/*
  * RSProp: zero-pad to (px, py) = the smallest powers of two >= (2nx-1, 2ny-1),
  * FFT, multiply by H_RS = FFT of the Rayleigh-Sommerfeld impulse response
  * h = dx dy/(2 pi) cis(k r)/r (z/r)(1/r - i k) sampled on the circular offset

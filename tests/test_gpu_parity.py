@@ -331,6 +331,51 @@ def test_asprop_paraxial_tilted_filtered(fo, orc, mode, d):
     assert orc.rel_l2(npy(v.electric).reshape(B, n, n), ref) < FIELD_TOL
 
 
+def test_fourier_operator_and_wrapper(fo, orc):
+    """fo_fft2's four modes against numpy's FFTs (FFTW's conventions), FourierOperator
+    with its direction swap, and FourierWrapper(u, Phase) inside a system: loss and
+    phase gradient against the oracle, where the adjoint of the inverse transform is
+    F / (nx ny) (fourier/fourier_operator.jl:37-83, fourier_wrapper.jl:1-42)."""
+    rng = np.random.default_rng(45)
+    B, ny, nx = 3, 64, 128
+    u0 = rand_field(rng, (B, ny, nx))
+    u = fo.ScalarField(u0, (0.5, 0.5), [0.64, 0.538, 0.455])
+    op = fo.FourierOperator(u, True)
+    N = nx * ny
+    F = lambda a: np.fft.fft2(a)
+    refs = {0: F(u0), 1: np.fft.ifft2(u0), 2: N * np.fft.ifft2(u0), 3: F(u0) / N}
+    for mode, ref in refs.items():
+        v = u.copy()
+        fo._capi.call("fo_fft2", op._plan(v), C.c_void_p(v.electric.data_ptr()), mode,
+                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert orc.rel_l2(npy(v.electric), ref) < 1e-6, mode
+    # the Backward direction swaps the transforms; FFT then IFFT is the identity
+    v = op.propagate(u, fo.Backward)
+    assert orc.rel_l2(npy(v.electric), np.fft.ifft2(u0)) < 1e-6
+    w = fo.FourierOperator(u, False).propagate(op.propagate(u))
+    assert orc.rel_l2(npy(w.electric), u0) < 1e-6
+
+    n = 128
+    lams = [0.64, 0.538]
+    v0 = rand_field(rng, (2, n, n))
+    target = f32(rng.uniform(0, 2, (2, n, n)))
+    phi = f32(rng.uniform(0, 6, (n, n)))
+    uu = fo.ScalarField(v0, (0.5, 0.5), lams)
+    ph = fo.Phase(uu, phi, trainable=True)
+    system = fo.ScalarSource(uu) | fo.FourierWrapper(uu, ph) | fo.ASProp(uu, 200.0)
+    metric = fo.SquaredIntensityDifference((uu, target))
+    loss, grads = fo.withgradient(metric, system)
+    U = np.fft.fft2(v0)
+    a = np.fft.ifft2(orc.phase_forward(U, phi))
+    out = orc.asprop(a, 0.5, 0.5, lams, 200.0)
+    c_ref, _ = orc.sid_value(out, target)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    g = orc.asprop(orc.sid_backward(out, target), 0.5, 0.5, lams, 200.0, orc.BACKWARD)
+    G = np.fft.fft2(g) / (n * n)  # adjoint of the inverse transform
+    _, gphi = orc.phase_backward(G, phi, U)
+    assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+
 @pytest.mark.parametrize("selective", [True, False])
 def test_dot_product_power_coupling(fo, orc, selective):
     """DotProduct and PowerCoupling (values and pull-backs) against the oracle, and
