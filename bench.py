@@ -523,7 +523,7 @@ def headline_config(batch, world):
     """The `config` object of the headline workload, shared by both bench arms."""
     return {"workload": WORKLOAD.format(fields=batch), "grid": N, "fields": batch, "masks": N_MASKS,
             "props_per_step": 2 * N_MASKS * batch, "parallelism": f"replicas x{world}",
-            "l2": "inputs larger than L2 (1.5 GiB field batch), no flush"}
+            "l2": f"inputs larger than L2 ({batch * N * N * 8 / 2**30:.1f} GiB field batch), no flush"}
 
 
 def run_cpu_sample(budget_s=12.0, threads=None, inputs=None):
