@@ -161,11 +161,19 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     overlap metrics write their pull-back first."""
     src = system.source.u0 if x is None else x
     du = src.similar()
+
+    def with_source(grads):
+        # a trainable source's gradient is the adjoint sweep's input gradient
+        # (trainable(::ScalarSource), sources/scalar_source.jl:65)
+        if system.source is not None and getattr(system.source, "trainable", False):
+            grads[system.source] = {"u0": du.electric}
+        return grads
+
     if isinstance(metric, SquaredIntensityDifference) and dc is None:
         # one fused chain ending in a propagator: forward, metric and adjoint in one call
         grads = system.forward_backward_sid(du, src, metric)
         if grads is not None:
-            return metric.loss.sum(), grads
+            return metric.loss.sum(), with_source(grads)
     u = src.similar()
     tape = []
     if isinstance(metric, SquaredIntensityDifference):
@@ -176,8 +184,8 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
         c = metric(u)
     if isinstance(metric, SquaredIntensityDifference) and dc is None:
         grads = system.backward(du, tape, seed=(metric, u))
-        return c.sum(), grads
+        return c.sum(), with_source(grads)
     metric.backpropagate_into(u, du, dc)
     grads = system.backward(du, tape)
     w = torch.ones_like(c) if dc is None else dc.to(c.dtype)
-    return (w * c).sum().real if c.is_complex() else (w * c).sum(), grads
+    return (w * c).sum().real if c.is_complex() else (w * c).sum(), with_source(grads)

@@ -22,10 +22,12 @@ class Fista:
                 "newdx": torch.zeros_like(x)}
 
     def apply_(self, state, x, dx):
-        if x.dtype != torch.float32:
-            raise NotImplementedError("Fista on the GPU path updates float32 parameters")
-        _capi.call("fo_fista_step", _ptr(x), _ptr(state["xk"]), _ptr(state["newdx"]), _ptr(dx), x.numel(),
-                   self.eta, _ptr(state["t"]), _stream())
+        # the update is real-linear in x and dx, so a complex parameter (a trainable
+        # source field) is updated as its interleaved real and imaginary parts
+        xf, xk, nd = _float_view(x), _float_view(state["xk"]), _float_view(state["newdx"])
+        d = _float_view(dx.to(x.dtype).contiguous())
+        _capi.call("fo_fista_step", _ptr(xf), _ptr(xk), _ptr(nd), _ptr(d), xf.numel(), self.eta, _ptr(state["t"]),
+                   _stream())
 
 
 class NoDescent:

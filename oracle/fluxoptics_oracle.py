@@ -584,7 +584,8 @@ class FistaState:
 
     def __init__(self, x):
         self.t = 1.0
-        self.xk = np.array(x, dtype=np.float64, copy=True)
+        # FP64 copy of the parameter, complex for a complex parameter (a source field)
+        self.xk = np.array(x, dtype=np.result_type(np.asarray(x).dtype, np.float64), copy=True)
         self.newdx = np.zeros_like(self.xk)
 
 

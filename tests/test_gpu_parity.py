@@ -828,6 +828,52 @@ def test_ista_positive_prox(fo, orc):
         assert orc.rel_l2(npy(xs), xo) < 1e-5
 
 
+def test_trainable_source(fo, orc):
+    """A trainable ScalarSource (sources/scalar_source.jl:39-106): withgradient returns
+    the input-field gradient as its "u0" gradient, through the shared metric + seed
+    pass and through the separate sweeps (a DotProduct loss), and one Fista step
+    updates the complex source field like the oracle's Fista on complex values."""
+    rng = np.random.default_rng(46)
+    n = 128
+    lams = [0.64, 0.538]
+    u0 = rand_field(rng, (2, n, n))
+    target = f32(rng.uniform(0, 2, (2, n, n)))
+    phi = f32(rng.uniform(0, 6, (n, n)))
+    u = fo.ScalarField(u0, (0.5, 0.5), lams)
+    src = fo.ScalarSource(u, trainable=True)
+    ph = fo.Phase(u, phi, trainable=True)
+    system = src | ph | fo.ASProp(u, 200.0)
+    metric = fo.SquaredIntensityDifference((u, target))
+    loss, grads = fo.withgradient(metric, system)
+    out = orc.asprop(orc.phase_forward(u0, phi), 0.5, 0.5, lams, 200.0)
+    g = orc.asprop(orc.sid_backward(out, target), 0.5, 0.5, lams, 200.0, orc.BACKWARD)
+    du_ref, gphi = orc.phase_backward(g, phi, u0)
+    assert orc.rel_l2(npy(grads[src]["u0"]), du_ref) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+    # two Fista steps, so that the momentum term (x - x_k) of the complex field counts
+    opt = fo.setup(fo.Fista(0.1), system)
+    so = orc.FistaState(u0.copy())
+    x_ref = u0.copy()
+    for it in range(2):
+        g_src = npy(grads[src]["u0"])
+        fo.update_(opt, system, grads)
+        orc.fista_apply(0.1, so, x_ref, g_src)
+        assert orc.rel_l2(npy(src.u0.electric), x_ref) < 1e-6, it
+        if it == 0:
+            _, grads = fo.withgradient(metric, system)
+
+    v0 = rand_field(rng, (2, n, n))
+    dp = fo.DotProduct(fo.ScalarField(v0, (0.5, 0.5), lams))
+    _, grads = fo.withgradient(dp, system)
+    uu = npy(src.u0.electric)
+    out = orc.asprop(orc.phase_forward(uu, npy(ph.phi)), 0.5, 0.5, lams, 200.0)
+    g = orc.dot_product_backward(v0, np.ones(2))
+    g = orc.asprop(g, 0.5, 0.5, lams, 200.0, orc.BACKWARD)
+    du_ref, _ = orc.phase_backward(g, npy(ph.phi), uu)
+    assert orc.rel_l2(npy(grads[src]["u0"]), du_ref) < GRAD_TOL
+
+
 def test_squared_field_difference(fo, orc):
     """SquaredFieldDifference values and pull-back against the oracle, the docstring's
     16.0, and the gradient of a phase mask through Phase -> ASProp -> the metric."""
