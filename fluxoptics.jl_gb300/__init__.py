@@ -17,15 +17,15 @@ from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierM
 from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
 from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
 from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
-from .optimisers import (ClampProx, Fista, IstaProx, NoDescent, PositiveProx, ProxRule, TVProx, make_rules, setup,
-                         update_)
+from .optimisers import (ClampProx, Descent, Fista, IstaProx, Momentum, Nesterov, NoDescent, PositiveProx, ProxRule,
+                         TVProx, make_rules, setup, update_)
 from .ragged import RaggedBatch
 
 load_library = _capi.load
 
 __all__ = [
-    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
-    "Forward", "IstaProx", "Mask", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PositiveProx", "PowerCoupling", "ProxRule",
+    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
+    "Forward", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",

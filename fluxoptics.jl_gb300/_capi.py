@@ -15,6 +15,7 @@ FO_FOURIER_TRAINABLE = 2
 FO_FLAG_GRAD_SPECTRA = 2
 FO_FLAG_DEVICE_Z = 4
 FO_FFT_FORWARD, FO_FFT_INVERSE, FO_FFT_FORWARD_ADJOINT, FO_FFT_INVERSE_ADJOINT = 0, 1, 2, 3
+FO_RULE_DESCENT, FO_RULE_MOMENTUM, FO_RULE_NESTEROV = 0, 1, 2
 
 ERROR_NAMES = {1: "FO_ERR_ARG", 2: "FO_ERR_SHAPE", 3: "FO_ERR_ALLOC", 4: "FO_ERR_CUDA",
                5: "FO_ERR_TIMEOUT", 6: "FO_ERR_UNSUPPORTED"}
@@ -109,6 +110,7 @@ SIGNATURES = {
     "fo_clamp": (_i, [_vp, _ll, _d, _d, _vp]),
     "fo_ista": (_i, [_vp, C.c_longlong, C.c_double, C.c_double, _vp]),
     "fo_positive": (_i, [_vp, C.c_longlong, _vp]),
+    "fo_rule_step": (_i, [_vp, _vp, _vp, C.c_longlong, _i, C.c_double, C.c_double, _vp]),
     "fo_sfd_create": (_i, [C.POINTER(_vp), _i, _i, _i]),
     "fo_sfd_forward": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "fo_sfd_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),

@@ -1,5 +1,5 @@
-// Pointwise proximal operators IstaProx / PositiveProx and the SquaredFieldDifference
-// metric.
+// Pointwise proximal operators IstaProx / PositiveProx, the gradient rules Descent /
+// Momentum / Nesterov, and the SquaredFieldDifference metric.
 //
 // IstaProx(s, c) soft-thresholds every value towards c (ista_prox.jl:1-19, applied
 // pointwise by PointwiseProx, pointwise_prox.jl:40-42); for complex parameters the
@@ -42,6 +42,32 @@ __global__ void positive_kernel(float* x, long long n) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x)
     if (x[q] < 0.f) x[q] = 0.f;
+}
+
+// One step of Optimisers.jl's Descent / Momentum / Nesterov (Optimisers.jl 0.4, the
+// version the reference pins; re-exported by OptimisersExt.jl:9), x <- x - newdx, in
+// FP32 with the rule's operation order and no contraction into FMAs:
+//   Descent:  newdx = eta dx
+//   Momentum: v = rho v + eta dx;                      newdx = v
+//   Nesterov: newdx = (-rho^2) v + ((1 + rho) eta) dx; v = rho v - eta dx
+__global__ void rule_kernel(float* x, float* v, const float* dx, long long n, int rule, float eta, float rho) {
+  const float a = -__fmul_rn(rho, rho), b = __fmul_rn(__fadd_rn(1.f, rho), eta);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float g = dx[q];
+    float nd;
+    if (rule == FO_RULE_DESCENT) {
+      nd = __fmul_rn(eta, g);
+    } else if (rule == FO_RULE_MOMENTUM) {
+      nd = __fadd_rn(__fmul_rn(rho, v[q]), __fmul_rn(eta, g));
+      v[q] = nd;
+    } else {
+      const float vq = v[q];
+      nd = __fadd_rn(__fmul_rn(a, vq), __fmul_rn(b, g));
+      v[q] = __fsub_rn(__fmul_rn(rho, vq), __fmul_rn(eta, g));
+    }
+    x[q] = __fsub_rn(x[q], nd);
+  }
 }
 
 // partial[b * kSfdBlocks + blk] = sum over this block's pixels of |u_b - v_b|^2
@@ -113,6 +139,19 @@ FO_API int fo_positive(float* x, long long n, void* stream) {
   positive_kernel<<<pm_grid(n), kPmThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(x, n);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FO_OK : cuda_fail(e, "positive_kernel launch");
+}
+
+FO_API int fo_rule_step(float* x, float* state, const float* dx, long long n, int rule, double eta, double rho,
+                        void* stream) {
+  if (!x || !dx) return fail(FO_ERR_ARG, "x and dx must not be NULL");
+  if (n <= 0) return fail(FO_ERR_SHAPE, "n must be positive");
+  if (rule != FO_RULE_DESCENT && rule != FO_RULE_MOMENTUM && rule != FO_RULE_NESTEROV)
+    return fail(FO_ERR_ARG, "unknown rule");
+  if (rule != FO_RULE_DESCENT && !state) return fail(FO_ERR_ARG, "Momentum and Nesterov need a velocity state");
+  rule_kernel<<<pm_grid(n), kPmThreads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(x, state, dx, n, rule, (float)eta,
+                                                                                      (float)rho);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FO_OK : cuda_fail(e, "rule_kernel launch");
 }
 
 FO_API int fo_sfd_create(fo_sfd* sfd, int nx, int ny, int batch) {

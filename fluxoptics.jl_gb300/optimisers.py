@@ -1,5 +1,5 @@
-"""Fista, ProxRule, ClampProx, IstaProx, PositiveProx and TVProx on the GPU
-(src/OptimisersExt.jl, src/proximal_operators/*)."""
+"""Fista, Descent, Momentum, Nesterov, ProxRule, ClampProx, IstaProx, PositiveProx and
+TVProx on the GPU (src/OptimisersExt.jl, src/proximal_operators/*)."""
 
 from __future__ import annotations
 
@@ -28,6 +28,49 @@ class Fista:
         d = _float_view(dx.to(x.dtype).contiguous())
         _capi.call("fo_fista_step", _ptr(xf), _ptr(xk), _ptr(nd), _ptr(d), xf.numel(), self.eta, _ptr(state["t"]),
                    _stream())
+
+
+class _PlainRule:
+    """Descent / Momentum / Nesterov of Optimisers.jl 0.4 (re-exported by the reference,
+    OptimisersExt.jl:9) as one elementwise FP32 kernel (fo_rule_step)."""
+
+    kind = _capi.FO_RULE_DESCENT
+    eta = 0.1
+    rho = 0.0
+
+    def init(self, x):
+        return None if self.kind == _capi.FO_RULE_DESCENT else torch.zeros_like(x)
+
+    def apply_(self, state, x, dx):
+        xf = _float_view(x)
+        d = _float_view(dx.to(x.dtype).contiguous())
+        v = None if state is None else _float_view(state)
+        _capi.call("fo_rule_step", _ptr(xf), _ptr(v), _ptr(d), xf.numel(), self.kind, self.eta, self.rho, _stream())
+
+
+class Descent(_PlainRule):
+    """x <- x - eta dx."""
+
+    def __init__(self, eta=0.1):
+        self.eta = float(eta)
+
+
+class Momentum(_PlainRule):
+    """v <- rho v + eta dx; x <- x - v."""
+
+    kind = _capi.FO_RULE_MOMENTUM
+
+    def __init__(self, eta=0.01, rho=0.9):
+        self.eta, self.rho = float(eta), float(rho)
+
+
+class Nesterov(_PlainRule):
+    """newdx = -rho^2 v + (1 + rho) eta dx; v <- rho v - eta dx; x <- x - newdx."""
+
+    kind = _capi.FO_RULE_NESTEROV
+
+    def __init__(self, eta=0.001, rho=0.9):
+        self.eta, self.rho = float(eta), float(rho)
 
 
 class NoDescent:

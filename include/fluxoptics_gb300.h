@@ -533,6 +533,24 @@ FO_API int fo_ista(float* x, long long n, double s, double c, void* stream);
 FO_API int fo_positive(float* x, long long n, void* stream);
 
 /*
+ * One step x <- x - newdx of a plain gradient rule, in FP32 with the rule's own
+ * operation order (no fused multiply-adds):
+ *   FO_RULE_DESCENT  : newdx = eta dx (state unused, may be NULL)
+ *   FO_RULE_MOMENTUM : v = rho v + eta dx; newdx = v
+ *   FO_RULE_NESTEROV : newdx = (-rho^2) v + ((1 + rho) eta) dx; v = rho v - eta dx
+ * state is the velocity v (n floats, zero at init).  A complex parameter is passed as
+ * its 2n floats.
+ * Replaces: Descent / Momentum / Nesterov of Optimisers.jl 0.4 (the version the
+ * reference's Project.toml pins), re-exported by the reference (src/OptimisersExt.jl:9)
+ * and used with make_rules / ProxRule (OptimisersExt.jl:195-244).
+ */
+#define FO_RULE_DESCENT 0
+#define FO_RULE_MOMENTUM 1
+#define FO_RULE_NESTEROV 2
+FO_API int fo_rule_step(float* x, float* state, const float* dx, long long n, int rule, double eta, double rho,
+                        void* stream);
+
+/*
  * TVProx(lambda, n_iter; isotropic, rule = Fista(eta)) on an ny x nx float
  * array, in place: n_iter dual Fista iterations with the reference's D / D^T
  * boundary handling and per-slice normalisation.

@@ -642,6 +642,29 @@ def fista_apply(eta, state, x, dx):
     return x
 
 
+def rule_step(rule, x, v, dx, eta, rho=0.0):
+    """One step of Descent / Momentum / Nesterov as Optimisers.jl 0.4 defines them (a
+    third-party dependency of the reference, pinned in its Project.toml and re-exported
+    by OptimisersExt.jl:9), in place on x (and the velocity v), in the arrays' own
+    precision with the rules' operation order:
+    Descent newdx = eta dx; Momentum v = rho v + eta dx, newdx = v;
+    Nesterov newdx = (-rho^2) v + ((1 + rho) eta) dx, v = rho v - eta dx; x -= newdx."""
+    t = x.dtype.type
+    eta, rho = t(eta), t(rho)
+    if rule == "descent":
+        nd = eta * dx
+    elif rule == "momentum":
+        v[...] = rho * v + eta * dx
+        nd = v.copy()
+    elif rule == "nesterov":
+        nd = (-(rho * rho)) * v + ((t(1) + rho) * eta) * dx
+        v[...] = rho * v - eta * dx
+    else:
+        raise ValueError(rule)
+    x -= nd
+    return x
+
+
 def clamp_prox(x, lo, hi):
     """ClampProx (clamp_prox.jl:35-37)."""
     np.clip(x, lo, hi, out=x)

@@ -83,6 +83,11 @@ def test_bad_arguments_are_rejected(capi):
     assert lib.fo_sfd_forward(None, None, None, None, None) == 1
     assert lib.fo_sfd_backward(None, None, None, None, None, None) == 1
     assert lib.fo_sfd_destroy(None) == 0
+    p16 = C.c_void_p(16)
+    assert lib.fo_rule_step(p16, None, p16, 10, 1, 0.1, 0.9, None) == 1
+    assert "velocity" in lib.fo_last_error().decode()
+    assert lib.fo_rule_step(p16, p16, p16, 10, 7, 0.1, 0.9, None) == 1
+    assert lib.fo_fft2(None, None, 0, None) == 1
     assert lib.fo_chain_create(C.byref(C.c_void_p()), 0, None) == 1
     assert lib.fo_sid_create(C.byref(C.c_void_p()), 8, 8, 2, 2, capi.ivec([0, 5])) == 1
     assert lib.fo_tv_create(C.byref(C.c_void_p()), 1, 8, 0.1, 10, 1, 0.25) == 2

@@ -874,6 +874,45 @@ def test_trainable_source(fo, orc):
     assert orc.rel_l2(npy(grads[src]["u0"]), du_ref) < GRAD_TOL
 
 
+def test_plain_rules(fo, orc):
+    """Descent / Momentum / Nesterov (Optimisers.jl 0.4, re-exported by the reference):
+    three steps on a float32 parameter and on a complex64 one, bit-exact against the
+    oracle evaluated in float32 with the rules' operation order, and ProxRule(Momentum,
+    ClampProx)."""
+    rng = np.random.default_rng(47)
+    cases = [(fo.Descent(0.1), "descent", 0.1, 0.0), (fo.Momentum(0.05, 0.9), "momentum", 0.05, 0.9),
+             (fo.Nesterov(0.01, 0.8), "nesterov", 0.01, 0.8)]
+    for rule, name, eta, rho in cases:
+        for cplx in (False, True):
+            shape = (37, 53)
+            x0 = rng.standard_normal(shape).astype(np.float32)
+            if cplx:
+                x0 = (x0 + 1j * rng.standard_normal(shape)).astype(np.complex64)
+            xs = torch.tensor(x0, device="cuda")
+            st = rule.init(xs)
+            xo = x0.view(np.float32).copy() if cplx else x0.copy()
+            vo = np.zeros_like(xo)
+            for it in range(3):
+                g = rng.standard_normal(shape).astype(np.float32)
+                if cplx:
+                    g = (g + 1j * rng.standard_normal(shape)).astype(np.complex64)
+                rule.apply_(st, xs, torch.tensor(g, device="cuda"))
+                orc.rule_step(name, xo, vo, g.view(np.float32) if cplx else g, eta, rho)
+                got = xs.detach().cpu().numpy()
+                got = got.view(np.float32) if cplx else got
+                assert np.array_equal(got, xo), (name, cplx, it)
+    pr = fo.ProxRule(fo.Momentum(0.05, 0.9), fo.ClampProx(-0.5, 0.5))
+    x0 = rng.standard_normal((16, 24)).astype(np.float32)
+    xs = torch.tensor(x0, device="cuda")
+    st = pr.init(xs)
+    xo, vo = x0.copy(), np.zeros_like(x0)
+    for it in range(2):
+        g = rng.standard_normal(x0.shape).astype(np.float32)
+        pr.apply_(st, xs, torch.tensor(g, device="cuda"))
+        orc.clamp_prox(orc.rule_step("momentum", xo, vo, g, 0.05, 0.9), -0.5, 0.5)
+        assert np.array_equal(xs.cpu().numpy(), xo)
+
+
 def test_squared_field_difference(fo, orc):
     """SquaredFieldDifference values and pull-back against the oracle, the docstring's
     16.0, and the gradient of a phase mask through Phase -> ASProp -> the metric."""

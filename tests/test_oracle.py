@@ -134,6 +134,17 @@ def test_prox_docstring_known_answers():
     assert np.allclose(z, [0.9 + 0.15j, 0.3 - 0.9j, 0.3 + 0.3j])
 
 
+def test_plain_rules_known_answers():
+    """Two steps of Descent(0.1), Momentum(0.1, 0.9) and Nesterov(0.1, 0.9) on x = 1 with
+    dx = 1, worked by hand from Optimisers.jl 0.4's update rules."""
+    expect = {"descent": [0.9, 0.8], "momentum": [0.9, 0.71], "nesterov": [0.81, 0.539]}
+    for rule, xs in expect.items():
+        x, v = np.array([1.0]), np.zeros(1)
+        for k in range(2):
+            orc.rule_step(rule, x, v, np.array([1.0]), 0.1, 0.0 if rule == "descent" else 0.9)
+            assert abs(x[0] - xs[k]) < 1e-12, (rule, k, x[0])
+
+
 def test_sfd_known_answer_and_pullback():
     """SquaredFieldDifference: the docstring's 16.0 for 4 x 4 ones against zeros
     (squared_field_difference.jl:16-31), and its pull-back 2 dc (u - v) against
