@@ -18,7 +18,7 @@ from .fields import ScalarField, coupling_efficiency, intensity, normalize_power
 from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
 from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
 from .optimisers import (ClampProx, Descent, Fista, IstaProx, Momentum, Nesterov, NoDescent, PositiveProx, ProxRule,
-                         TVProx, make_rules, setup, update_)
+                         TVProx, make_rules, setup, tv_denoise_, update_)
 from .ragged import RaggedBatch
 
 load_library = _capi.load
@@ -29,6 +29,6 @@ __all__ = [
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
-    "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "update_",
+    "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "tv_denoise_", "update_",
     "withgradient",
 ]

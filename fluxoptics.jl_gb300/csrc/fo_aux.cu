@@ -536,6 +536,7 @@ struct TvState {  // device-resident scalars
   double t;        // Fista t of the dual iteration
   float beta;      // Fista beta of the next update
   float scale[2];  // per-slice projection factor of the current dual
+  int done;        // the tolerance was met: the remaining iterations do nothing
 };
 
 __global__ void tv_init_kernel(float* p, float* xk, long long n2, TvState* st) {
@@ -550,6 +551,7 @@ __global__ void tv_init_kernel(float* p, float* xk, long long n2, TvState* st) {
     st->beta = (float)((1.0 - 1.0) / tn);
     st->scale[0] = 1.f;
     st->scale[1] = 1.f;
+    st->done = 0;
   }
 }
 
@@ -562,15 +564,52 @@ __device__ __forceinline__ float tv_dt(const float* p0, const float* p1, float s
   return s0 * (p0[q - 1] - p0[q]) + s1 * (p1[q - nx] - p1[q]);
 }
 
-// y = lam * D^T(p) - y0
+// y = lam * D^T(p) - y0.  With a tolerance (yprev != NULL): per-block maxima of
+// |y - y_prev| (y_prev: the previous iteration's y, zero before the first), and
+// y_prev <- y.
 __global__ void tv_dt_kernel(const float* p, const float* y0, float* yv, int nx, int ny, float lam,
-                             const TvState* st) {
+                             const TvState* st, float* yprev, float* maxima) {
+  __shared__ float red[kThreads / 32];
+  if (st->done) return;
   const long long n = (long long)nx * ny;
   const float s0 = st->scale[0], s1 = st->scale[1];
+  float mx = 0.f;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(q % nx), y = (int)(q / nx);
-    yv[q] = lam * tv_dt(p, p + n, s0, s1, x, y, nx) - y0[q];
+    const float v = lam * tv_dt(p, p + n, s0, s1, x, y, nx) - y0[q];
+    yv[q] = v;
+    if (yprev) {
+      mx = fmaxf(mx, fabsf(yprev[q] - v));
+      yprev[q] = v;
+    }
+  }
+  if (yprev) {
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float m = 0.f;
+      for (int w = 0; w < kThreads / 32; ++w) m = fmaxf(m, red[w]);
+      maxima[blockIdx.x] = m;
+    }
+  }
+}
+
+// The tolerance test of the iteration: max |y - y_prev| < tol stops it before its
+// dual update (tv_prox.jl:158-166).
+__global__ void tv_check_kernel(const float* maxima, int nblocks, double tol, TvState* st) {
+  __shared__ float red[kThreads / 32];
+  if (st->done) return;
+  float mx = 0.f;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) mx = fmaxf(mx, maxima[b]);
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int w = 0; w < kThreads / 32; ++w) m = fmaxf(m, red[w]);
+    if ((double)m < tol) st->done = 1;
   }
 }
 
@@ -579,6 +618,7 @@ __global__ void tv_dt_kernel(const float* p, const float* y0, float* yv, int nx,
 __global__ void tv_step_kernel(float* p, float* xk, const float* yv, int nx, int ny, float e,
                                const TvState* st, int isotropic, float* partials) {
   __shared__ float red[kThreads / 32];
+  if (st->done) return;
   const long long n = (long long)nx * ny;
   const float beta = st->beta;
   float ss[2] = {0.f, 0.f};
@@ -613,6 +653,7 @@ __global__ void tv_step_kernel(float* p, float* xk, const float* yv, int nx, int
 // Per-slice norms -> projection scale; Fista t/beta for the next update.
 __global__ void tv_norm_kernel(const float* partials, int nblocks, int isotropic, TvState* st) {
   __shared__ float red[kThreads / 32];
+  if (st->done) return;
   float sc[2] = {1.f, 1.f};
   if (isotropic) {
 #pragma unroll
@@ -799,13 +840,20 @@ size_t tv_state_bytes() { return sizeof(TvState); }
 int tv_partial_blocks(long long n) { return (int)capped_grid(n); }
 
 cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nx,
-                      int ny, float lam, int n_iter, int isotropic, float e, cudaStream_t st) {
+                      int ny, float lam, int n_iter, int isotropic, float e, cudaStream_t st, double tol,
+                      float* yprev, float* maxima) {
   const long long n = (long long)nx * ny;
   TvState* s = reinterpret_cast<TvState*>(state);
   const unsigned g = capped_grid(n);
+  const bool use_tol = tol > 0.0 && yprev && maxima;
   tv_init_kernel<<<capped_grid(2 * n), kThreads, 0, st>>>(p, xk, 2 * n, s);
+  if (use_tol) {
+    cudaError_t e0 = cudaMemsetAsync(yprev, 0, sizeof(float) * n, st);
+    if (e0 != cudaSuccess) return e0;
+  }
   for (int it = 0; it < n_iter; ++it) {
-    tv_dt_kernel<<<g, kThreads, 0, st>>>(p, x, yv, nx, ny, lam, s);
+    tv_dt_kernel<<<g, kThreads, 0, st>>>(p, x, yv, nx, ny, lam, s, use_tol ? yprev : nullptr, maxima);
+    if (use_tol) tv_check_kernel<<<1, kThreads, 0, st>>>(maxima, (int)g, tol, s);
     tv_step_kernel<<<g, kThreads, 0, st>>>(p, xk, yv, nx, ny, e, s, isotropic, partials);
     tv_norm_kernel<<<1, kThreads, 0, st>>>(partials, (int)g, isotropic, s);
   }

@@ -2000,18 +2000,21 @@ FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream) {
 
 struct fo_tv_s {
   int nx = 0, ny = 0, n_iter = 0, isotropic = 1;
-  double lambda = 0, eta = 0;
+  double lambda = 0, eta = 0, tol = 0;
   float *p = nullptr, *xk = nullptr, *y = nullptr, *partials = nullptr;
+  float *yprev = nullptr, *maxima = nullptr;  // with a tolerance
   void* state = nullptr;
 };
 
 extern "C" {
 
-FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta) {
+FO_API int fo_tv_create_ex(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta,
+                           double tol) {
   if (!tv) return fail(FO_ERR_ARG, "tv output pointer is NULL");
   *tv = nullptr;
   if (nx < 2 || ny < 2) return fail(FO_ERR_SHAPE, "TVProx needs at least 2 x 2 samples");
   if (n_iter < 0) return fail(FO_ERR_ARG, "n_iter must be >= 0");
+  if (!(tol >= 0)) return fail(FO_ERR_ARG, "tol must be >= 0 (0: none)");
   fo_tv t = new fo_tv_s();
   t->nx = nx;
   t->ny = ny;
@@ -2019,11 +2022,15 @@ FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, in
   t->isotropic = isotropic ? 1 : 0;
   t->lambda = lambda;
   t->eta = eta;
+  t->tol = tol;
   const size_t n = (size_t)nx * ny;
+  const size_t blocks = (size_t)tv_partial_blocks((long long)n);
   int rc;
   if ((rc = dalloc(&t->p, 2 * n, "TV dual")) != FO_OK || (rc = dalloc(&t->xk, 2 * n, "TV state")) != FO_OK ||
       (rc = dalloc(&t->y, n, "TV primal")) != FO_OK ||
-      (rc = dalloc(&t->partials, (size_t)tv_partial_blocks((long long)n) * 2, "TV partials")) != FO_OK ||
+      (rc = dalloc(&t->partials, blocks * 2, "TV partials")) != FO_OK ||
+      (tol > 0 && (rc = dalloc(&t->yprev, n, "TV previous primal")) != FO_OK) ||
+      (tol > 0 && (rc = dalloc(&t->maxima, blocks, "TV block maxima")) != FO_OK) ||
       (rc = dalloc(reinterpret_cast<char**>(&t->state), tv_state_bytes(), "TV scalars")) != FO_OK) {
     fo_tv_destroy(t);
     return rc;
@@ -2032,12 +2039,18 @@ FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, in
   return FO_OK;
 }
 
+FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta) {
+  return fo_tv_create_ex(tv, nx, ny, lambda, n_iter, isotropic, eta, 0.0);
+}
+
 FO_API int fo_tv_destroy(fo_tv t) {
   if (!t) return FO_OK;
   cudaFree(t->p);
   cudaFree(t->xk);
   cudaFree(t->y);
   cudaFree(t->partials);
+  cudaFree(t->yprev);
+  cudaFree(t->maxima);
   cudaFree(t->state);
   delete t;
   return FO_OK;
@@ -2047,7 +2060,7 @@ FO_API int fo_tv_apply(fo_tv t, float* x, void* stream) {
   if (!t || !x) return fail(FO_ERR_ARG, "tv and x must not be NULL");
   const double lam = t->isotropic ? t->lambda : t->lambda / 100.0;
   FO_LAUNCH(launch_tv(x, t->p, t->xk, t->y, t->partials, t->state, t->nx, t->ny, (float)lam, t->n_iter,
-                      t->isotropic, (float)(t->eta * t->eta), S(stream)));
+                      t->isotropic, (float)(t->eta * t->eta), S(stream), t->tol, t->yprev, t->maxima));
   return FO_OK;
 }
 

@@ -136,24 +136,47 @@ class PositiveProx:
 
 
 class TVProx:
-    """TVProx(lambda, n_iter; isotropic, rule=Fista(eta)) (tv_prox.jl:94-195), 2-D."""
+    """TVProx(lambda, n_iter; tol, isotropic, rule=Fista(eta)) (tv_prox.jl:94-195), 2-D.
+    ``tol`` stops the dual iterations once the primal iterate changes by less than tol
+    (tested on the device); a complex parameter has its real and imaginary parts
+    denoised separately, each with its own dual state, as the reference does."""
 
-    def __init__(self, lam, n_iter=50, isotropic=True, eta=None):
+    def __init__(self, lam, n_iter=50, tol=None, isotropic=True, eta=None):
         self.lam = float(lam)
         self.n_iter = int(n_iter)
+        self.tol = None if tol is None else float(tol)
         self.isotropic = bool(isotropic)
         self.eta = float(eta if eta is not None else (0.25 if isotropic else 2.5))
+
+    def _handle(self, x):
+        h = C.c_void_p()
+        _capi.call("fo_tv_create_ex", C.byref(h), x.shape[1], x.shape[0], self.lam, self.n_iter,
+                   int(self.isotropic), self.eta, 0.0 if self.tol is None else self.tol)
+        return _TvHandle(h)
 
     def init(self, x):
         if x.dim() != 2:
             raise NotImplementedError("TVProx on the GPU path is 2-D")
-        h = C.c_void_p()
-        _capi.call("fo_tv_create", C.byref(h), x.shape[1], x.shape[0], self.lam, self.n_iter,
-                   int(self.isotropic), self.eta)
-        return _TvHandle(h)
+        if x.is_complex():
+            return (self._handle(x), self._handle(x))
+        return self._handle(x)
 
     def apply_(self, state, x):
+        if x.is_complex():
+            re, im = x.real.contiguous(), x.imag.contiguous()
+            _capi.call("fo_tv_apply", state[0].h, _ptr(re), _stream())
+            _capi.call("fo_tv_apply", state[1].h, _ptr(im), _stream())
+            x.copy_(torch.complex(re, im))
+            return
         _capi.call("fo_tv_apply", state.h, _ptr(x), _stream())
+
+
+def tv_denoise_(x, lam, n_iter=50, tol=None, isotropic=True, eta=None):
+    """TV_denoise!(x, lambda, n_iter; tol, isotropic) (tv_prox.jl:197-258): TVProx applied
+    once, in place."""
+    tv = TVProx(lam, n_iter, tol=tol, isotropic=isotropic, eta=eta)
+    tv.apply_(tv.init(x), x)
+    return x
 
 
 class _TvHandle:

@@ -553,12 +553,17 @@ FO_API int fo_rule_step(float* x, float* state, const float* dx, long long n, in
 /*
  * TVProx(lambda, n_iter; isotropic, rule = Fista(eta)) on an ny x nx float
  * array, in place: n_iter dual Fista iterations with the reference's D / D^T
- * boundary handling and per-slice normalisation.
- * Replaces: TVProx -- src/proximal_operators/tv_prox.jl:1-195.
+ * boundary handling and per-slice normalisation.  fo_tv_create_ex adds `tol`
+ * (0: none): the iterations stop, before their dual update, once the largest change
+ * of the primal iterate from the previous iteration is below tol (tested on the
+ * device; the remaining launches do nothing, so the call stays graph-capturable).
+ * Replaces: TVProx / TV_denoise! -- src/proximal_operators/tv_prox.jl:1-258.
  */
 typedef struct fo_tv_s* fo_tv;
 FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic,
                         double eta);
+FO_API int fo_tv_create_ex(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic,
+                           double eta, double tol);
 FO_API int fo_tv_destroy(fo_tv tv);
 FO_API int fo_tv_apply(fo_tv tv, float* x, void* stream);
 

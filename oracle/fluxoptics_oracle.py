@@ -741,13 +741,22 @@ def _dt(a, p):
     return a
 
 
-def tv_prox(y0, lam, n_iter=50, isotropic=True, eta=None):
+def tv_prox(y0, lam, n_iter=50, isotropic=True, eta=None, tol=None):
     """TVProx: dual FISTA on p (tv_prox.jl:94-195), in place on y0.
 
     Default inner rule Fista(0.25) (isotropic) / Fista(2.5) (anisotropic); the
     isotropic projection divides each dual slice by its global norm when > 1;
-    anisotropic uses lam/100 and clamps to [-1, 1]."""
+    anisotropic uses lam/100 and clamps to [-1, 1].  With ``tol`` the loop stops,
+    before the dual update, once max |y - y_prev| < tol, y_prev starting at zero
+    (tv_prox.jl:150-166).  A complex y0 has its real and imaginary parts denoised
+    separately (tv_prox.jl:177-195)."""
     y0 = np.asarray(y0)
+    if np.iscomplexobj(y0):
+        re, im = y0.real.copy(), y0.imag.copy()
+        tv_prox(re, lam, n_iter, isotropic, eta, tol)
+        tv_prox(im, lam, n_iter, isotropic, eta, tol)
+        y0[...] = re + 1j * im
+        return y0
     if eta is None:
         eta = 0.25 if isotropic else 2.5
     nd = y0.ndim
@@ -755,10 +764,15 @@ def tv_prox(y0, lam, n_iter=50, isotropic=True, eta=None):
     p = np.zeros((nd,) + y0.shape)
     dp = np.zeros_like(p)
     y = np.zeros_like(y0, dtype=np.float64)
+    y_prev = np.zeros_like(y)
     st = FistaState(p)
     for _ in range(n_iter):
         _dt(y, p)
         y = lam_eff * y - y0
+        if tol is not None:
+            if np.max(np.abs(y_prev - y)) < tol:
+                break
+            y_prev = y.copy()
         _d(dp, y)
         fista_apply(eta, st, p, dp)
         for i in range(nd):

@@ -794,6 +794,19 @@ def test_fista_clamp_tv(fo, orc):
         tv.apply_(tv.init(yt), yt)
         ref = orc.tv_prox(y0.copy(), 0.2, 25, isotropic=iso)
         assert orc.rel_l2(npy(yt), ref) < 1e-5
+    # tol: the device-side test stops after two dual updates here (changes 3.3, 0.32,
+    # then 7.8e-3 < 1e-2), like the oracle; TV_denoise! and a complex parameter
+    y0 = np.random.default_rng(3).standard_normal((40, 30))
+    yt = torch.tensor(f32(y0), dtype=torch.float32, device="cuda")
+    fo.tv_denoise_(yt, 1.0, 25, tol=1e-2)
+    ref = orc.tv_prox(f32(y0), 1.0, 25, tol=1e-2)
+    assert orc.rel_l2(npy(yt), ref) < 1e-5
+    assert orc.rel_l2(ref, orc.tv_prox(f32(y0), 1.0, 25)) > 1e-4
+    z0 = c64(rng.standard_normal((40, 30)) + 1j * rng.standard_normal((40, 30)))
+    zt = torch.tensor(z0, dtype=torch.complex64, device="cuda")
+    tvc = fo.TVProx(0.2, 25)
+    tvc.apply_(tvc.init(zt), zt)
+    assert orc.rel_l2(npy(zt), orc.tv_prox(z0.copy(), 0.2, 25)) < 1e-5
 
 
 def test_ista_positive_prox(fo, orc):

@@ -342,6 +342,22 @@ def test_tv_prox_matches_loops():
     assert np.max(np.abs(got - ref)) < 1e-12
 
 
+def test_tv_prox_tolerance_and_complex():
+    """TVProx's tol stops the dual iterations before their update once the primal
+    iterate changes by less than tol (tv_prox.jl:150-166): here after two updates, the
+    same as n_iter = 2 (changes 3.3, 0.32, then 7.8e-3 < 1e-2).  A complex array is
+    denoised as its real and imaginary parts (tv_prox.jl:177-195)."""
+    rng = np.random.default_rng(3)
+    y0 = rng.standard_normal((40, 30))
+    a = orc.tv_prox(y0.copy(), 1.0, 25, tol=1e-2)
+    assert np.array_equal(a, orc.tv_prox(y0.copy(), 1.0, 2))
+    assert orc.rel_l2(a, orc.tv_prox(y0.copy(), 1.0, 25)) > 1e-4
+    z0 = y0 + 1j * rng.standard_normal((40, 30))
+    z = orc.tv_prox(z0.copy(), 0.2, 10)
+    assert np.array_equal(z.real, orc.tv_prox(z0.real.copy(), 0.2, 10))
+    assert np.array_equal(z.imag, orc.tv_prox(z0.imag.copy(), 0.2, 10))
+
+
 def test_tv_prox_smooths():
     rng = np.random.default_rng(4)
     x = np.outer(np.sin(0.1 * np.arange(64)), np.sin(0.1 * np.arange(64))) * 5 + rng.standard_normal((64, 64))
