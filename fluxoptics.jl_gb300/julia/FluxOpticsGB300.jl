@@ -808,16 +808,17 @@ mutable struct GB300TV
 end
 
 """
-    GB300TVProx(nx, ny, λ; n_iter=50, isotropic=true, eta=0.25)
+    GB300TVProx(nx, ny, λ; n_iter=50, tol=nothing, isotropic=true, eta=0.25)
 
-TVProx(λ, n_iter; isotropic, rule = Fista(eta)) for nx × ny parameters; apply
-with `tv_prox!(tv, x)`.
+TVProx(λ, n_iter; tol, isotropic, rule = Fista(eta)) for nx × ny parameters; apply
+with `tv_prox!(tv, x)`.  `tol` stops the iterations on the device (tv_prox.jl:150-166).
 """
-function GB300TVProx(nx::Integer, ny::Integer, λ::Real; n_iter::Integer = 50, isotropic::Bool = true,
-                     eta::Real = 0.25)
+function GB300TVProx(nx::Integer, ny::Integer, λ::Real; n_iter::Integer = 50, tol = nothing,
+                     isotropic::Bool = true, eta::Real = 0.25)
     h = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:fo_tv_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Cint, Cint, Cdouble, Cint, Cint, Cdouble),
-                h, nx, ny, λ, n_iter, Cint(isotropic), eta))
+    check(ccall((:fo_tv_create_ex, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Cint, Cdouble, Cint, Cint, Cdouble, Cdouble),
+                h, nx, ny, λ, n_iter, Cint(isotropic), eta, tol === nothing ? 0.0 : Float64(tol)))
     tv = GB300TV(h[])
     finalizer(x -> ccall((:fo_tv_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), tv)
 end
