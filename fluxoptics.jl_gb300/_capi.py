@@ -117,6 +117,7 @@ SIGNATURES = {
     "fo_sfd_destroy": (_i, [_vp]),
     "fo_tv_create": (_i, [C.POINTER(_vp), _i, _i, _d, _i, _i, _d]),
     "fo_tv_create_ex": (_i, [C.POINTER(_vp), _i, _i, _d, _i, _i, _d, _d]),
+    "fo_tv_create_nd": (_i, [C.POINTER(_vp), _i, _pi, _d, _i, _i, _d, _d]),
     "fo_tv_destroy": (_i, [_vp]),
     "fo_tv_apply": (_i, [_vp, _vp, _vp]),
     "fo_graph_begin": (_i, [_vp]),

@@ -527,20 +527,28 @@ __global__ void conj_scale_kernel(float2* x, long long n, float s, int conj) {
 }
 
 // ---------------------------------------------------------------------------
-// TVProx (2-D).  p holds two dual slices: p0 (differences along x) and p1 (along y).
-// The dual is used through a per-slice scale (the isotropic projection of the
-// previous iteration), applied on read.
+// TVProx on 1-, 2- or 3-D arrays (x fastest, then y, then z).  p holds one dual
+// slice per dimension (the forward differences along it).  The dual is used through
+// a per-slice scale (the isotropic projection of the previous iteration), applied
+// on read.
 // ---------------------------------------------------------------------------
+
+struct TvGrid {
+  int nd;       // 1, 2 or 3
+  int n[3];     // extents (x, y, z); unused ones are 1
+  long long s[3];  // strides
+  long long total;
+};
 
 struct TvState {  // device-resident scalars
   double t;        // Fista t of the dual iteration
   float beta;      // Fista beta of the next update
-  float scale[2];  // per-slice projection factor of the current dual
+  float scale[3];  // per-slice projection factor of the current dual
   int done;        // the tolerance was met: the remaining iterations do nothing
 };
 
-__global__ void tv_init_kernel(float* p, float* xk, long long n2, TvState* st) {
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n2;
+__global__ void tv_init_kernel(float* p, float* xk, long long np, TvState* st) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < np;
        q += (long long)gridDim.x * blockDim.x) {
     p[q] = 0.f;
     xk[q] = 0.f;
@@ -549,35 +557,48 @@ __global__ void tv_init_kernel(float* p, float* xk, long long n2, TvState* st) {
     st->t = 1.0;
     const double tn = (1.0 + sqrt(5.0)) / 2.0;
     st->beta = (float)((1.0 - 1.0) / tn);
-    st->scale[0] = 1.f;
-    st->scale[1] = 1.f;
+    st->scale[0] = st->scale[1] = st->scale[2] = 1.f;
     st->done = 0;
   }
 }
 
-// D^T of the reference (tv_prox.jl:43-59), on the scaled dual.
-__device__ __forceinline__ float tv_dt(const float* p0, const float* p1, float s0, float s1, int x, int y,
-                                       int nx) {
-  const long long q = (long long)y * nx + x;
-  if (y == 0) return -s1 * p1[q];
-  if (x == 0) return -s0 * p0[q];
-  return s0 * (p0[q - 1] - p0[q]) + s1 * (p1[q - nx] - p1[q]);
+__device__ __forceinline__ void tv_coords(const TvGrid& g, long long q, int (&c)[3]) {
+  c[0] = (int)(q % g.n[0]);
+  const long long r = q / g.n[0];
+  c[1] = (int)(r % g.n[1]);
+  c[2] = (int)(r / g.n[1]);
+}
+
+// D^T of the reference (tv_prox.jl:43-59), on the scaled dual: the sum over the
+// dimensions of p_i[c - e_i] - p_i[c], except that a point on the first plane of some
+// dimension takes -p_J[c] of the highest such dimension J (the reference's boundary
+// assignments, made in dimension order, overwrite one another).
+__device__ __forceinline__ float tv_dt(const float* p, const float (&sc)[3], const TvGrid& g, long long q,
+                                       const int (&c)[3]) {
+  for (int i = g.nd - 1; i >= 0; --i)
+    if (c[i] == 0) return -sc[i] * p[i * g.total + q];
+  float v = 0.f;
+  for (int i = 0; i < g.nd; ++i) {
+    const float* pi = p + i * g.total;
+    v += sc[i] * (pi[q - g.s[i]] - pi[q]);
+  }
+  return v;
 }
 
 // y = lam * D^T(p) - y0.  With a tolerance (yprev != NULL): per-block maxima of
 // |y - y_prev| (y_prev: the previous iteration's y, zero before the first), and
 // y_prev <- y.
-__global__ void tv_dt_kernel(const float* p, const float* y0, float* yv, int nx, int ny, float lam,
-                             const TvState* st, float* yprev, float* maxima) {
+__global__ void tv_dt_kernel(const float* p, const float* y0, float* yv, TvGrid g, float lam, const TvState* st,
+                             float* yprev, float* maxima) {
   __shared__ float red[kThreads / 32];
   if (st->done) return;
-  const long long n = (long long)nx * ny;
-  const float s0 = st->scale[0], s1 = st->scale[1];
+  const float sc[3] = {st->scale[0], st->scale[1], st->scale[2]};
   float mx = 0.f;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.total;
        q += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(q % nx), y = (int)(q / nx);
-    const float v = lam * tv_dt(p, p + n, s0, s1, x, y, nx) - y0[q];
+    int c[3];
+    tv_coords(g, q, c);
+    const float v = lam * tv_dt(p, sc, g, q, c) - y0[q];
     yv[q] = v;
     if (yprev) {
       mx = fmaxf(mx, fabsf(yprev[q] - v));
@@ -615,25 +636,24 @@ __global__ void tv_check_kernel(const float* maxima, int nblocks, double tol, Tv
 
 // dp = D(y); Fista on the (scaled) dual; per-block partial sums of p^2 per slice
 // (isotropic) or clamp to [-1, 1] (anisotropic).
-__global__ void tv_step_kernel(float* p, float* xk, const float* yv, int nx, int ny, float e,
-                               const TvState* st, int isotropic, float* partials) {
+__global__ void tv_step_kernel(float* p, float* xk, const float* yv, TvGrid g, float e, const TvState* st,
+                               int isotropic, float* partials) {
   __shared__ float red[kThreads / 32];
   if (st->done) return;
-  const long long n = (long long)nx * ny;
   const float beta = st->beta;
-  float ss[2] = {0.f, 0.f};
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+  float ss[3] = {0.f, 0.f, 0.f};
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.total;
        q += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(q % nx), y = (int)(q / nx);
+    int c[3];
+    tv_coords(g, q, c);
     const float yc = yv[q];
-    float d[2];
-    d[0] = (x < nx - 1) ? yv[q + 1] - yc : 0.f;
-    d[1] = (y < ny - 1) ? yv[q + nx] - yc : 0.f;
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const long long qi = q + i * n;
+    for (int i = 0; i < 3; ++i) {
+      if (i >= g.nd) break;
+      const float d = (c[i] < g.n[i] - 1) ? yv[q + g.s[i]] - yc : 0.f;
+      const long long qi = q + i * g.total;
       const float pv = p[qi] * st->scale[i];
-      const float nd = e * d[i] - beta * (pv - xk[qi]);
+      const float nd = e * d - beta * (pv - xk[qi]);
       xk[qi] = pv;
       float pn = pv - nd;
       if (!isotropic) pn = fminf(fmaxf(pn, -1.f), 1.f);
@@ -643,23 +663,23 @@ __global__ void tv_step_kernel(float* p, float* xk, const float* yv, int nx, int
   }
   if (isotropic) {
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
+      if (i >= g.nd) break;
       const float b = block_sum<kThreads>(ss[i], red);
-      if (threadIdx.x == 0) partials[blockIdx.x * 2 + i] = b;
+      if (threadIdx.x == 0) partials[blockIdx.x * 3 + i] = b;
     }
   }
 }
 
 // Per-slice norms -> projection scale; Fista t/beta for the next update.
-__global__ void tv_norm_kernel(const float* partials, int nblocks, int isotropic, TvState* st) {
+__global__ void tv_norm_kernel(const float* partials, int nblocks, int nd, int isotropic, TvState* st) {
   __shared__ float red[kThreads / 32];
   if (st->done) return;
-  float sc[2] = {1.f, 1.f};
+  float sc[3] = {1.f, 1.f, 1.f};
   if (isotropic) {
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < nd; ++i) {
       double acc = 0.0;
-      for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[b * 2 + i];
+      for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[b * 3 + i];
       const float s = block_sum<kThreads>((float)acc, red);
       if (threadIdx.x == 0) {
         const float nrm = sqrtf(s);
@@ -670,6 +690,7 @@ __global__ void tv_norm_kernel(const float* partials, int nblocks, int isotropic
   if (threadIdx.x == 0) {
     st->scale[0] = sc[0];
     st->scale[1] = sc[1];
+    st->scale[2] = sc[2];
     const double t = (1.0 + sqrt(1.0 + 4.0 * st->t * st->t)) / 2.0;  // t after this update
     const double tn = (1.0 + sqrt(1.0 + 4.0 * t * t)) / 2.0;
     st->t = t;
@@ -678,13 +699,13 @@ __global__ void tv_norm_kernel(const float* partials, int nblocks, int isotropic
 }
 
 // y0 -= lam * D^T(p)
-__global__ void tv_final_kernel(const float* p, float* y0, int nx, int ny, float lam, const TvState* st) {
-  const long long n = (long long)nx * ny;
-  const float s0 = st->scale[0], s1 = st->scale[1];
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+__global__ void tv_final_kernel(const float* p, float* y0, TvGrid g, float lam, const TvState* st) {
+  const float sc[3] = {st->scale[0], st->scale[1], st->scale[2]};
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < g.total;
        q += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(q % nx), y = (int)(q / nx);
-    y0[q] -= lam * tv_dt(p, p + n, s0, s1, x, y, nx);
+    int c[3];
+    tv_coords(g, q, c);
+    y0[q] -= lam * tv_dt(p, sc, g, q, c);
   }
 }
 
@@ -839,25 +860,33 @@ cudaError_t launch_conj_scale(float2* x, long long n, float s, int conj, cudaStr
 size_t tv_state_bytes() { return sizeof(TvState); }
 int tv_partial_blocks(long long n) { return (int)capped_grid(n); }
 
-cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nx,
-                      int ny, float lam, int n_iter, int isotropic, float e, cudaStream_t st, double tol,
+cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nd,
+                      const int* dims, float lam, int n_iter, int isotropic, float e, cudaStream_t st, double tol,
                       float* yprev, float* maxima) {
-  const long long n = (long long)nx * ny;
+  TvGrid g;
+  g.nd = nd;
+  g.total = 1;
+  for (int i = 0; i < 3; ++i) {
+    g.n[i] = i < nd ? dims[i] : 1;
+    g.s[i] = g.total;
+    g.total *= g.n[i];
+  }
+  const long long n = g.total;
   TvState* s = reinterpret_cast<TvState*>(state);
-  const unsigned g = capped_grid(n);
+  const unsigned blocks = capped_grid(n);
   const bool use_tol = tol > 0.0 && yprev && maxima;
-  tv_init_kernel<<<capped_grid(2 * n), kThreads, 0, st>>>(p, xk, 2 * n, s);
+  tv_init_kernel<<<capped_grid(nd * n), kThreads, 0, st>>>(p, xk, nd * n, s);
   if (use_tol) {
     cudaError_t e0 = cudaMemsetAsync(yprev, 0, sizeof(float) * n, st);
     if (e0 != cudaSuccess) return e0;
   }
   for (int it = 0; it < n_iter; ++it) {
-    tv_dt_kernel<<<g, kThreads, 0, st>>>(p, x, yv, nx, ny, lam, s, use_tol ? yprev : nullptr, maxima);
-    if (use_tol) tv_check_kernel<<<1, kThreads, 0, st>>>(maxima, (int)g, tol, s);
-    tv_step_kernel<<<g, kThreads, 0, st>>>(p, xk, yv, nx, ny, e, s, isotropic, partials);
-    tv_norm_kernel<<<1, kThreads, 0, st>>>(partials, (int)g, isotropic, s);
+    tv_dt_kernel<<<blocks, kThreads, 0, st>>>(p, x, yv, g, lam, s, use_tol ? yprev : nullptr, maxima);
+    if (use_tol) tv_check_kernel<<<1, kThreads, 0, st>>>(maxima, (int)blocks, tol, s);
+    tv_step_kernel<<<blocks, kThreads, 0, st>>>(p, xk, yv, g, e, s, isotropic, partials);
+    tv_norm_kernel<<<1, kThreads, 0, st>>>(partials, (int)blocks, nd, isotropic, s);
   }
-  tv_final_kernel<<<g, kThreads, 0, st>>>(p, x, nx, ny, lam, s);
+  tv_final_kernel<<<blocks, kThreads, 0, st>>>(p, x, g, lam, s);
   return cudaGetLastError();
 }
 

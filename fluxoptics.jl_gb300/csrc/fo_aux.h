@@ -53,8 +53,9 @@ cudaError_t launch_conj_scale(float2* x, long long n, float s, int conj, cudaStr
 
 size_t tv_state_bytes();
 int tv_partial_blocks(long long n);
-cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nx,
-                      int ny, float lam, int n_iter, int isotropic, float e, cudaStream_t st, double tol = 0.0,
-                      float* yprev = nullptr, float* maxima = nullptr);
+// TVProx on an nd-dimensional array (nd = 1..3, dims x fastest).
+cudaError_t launch_tv(float* x, float* p, float* xk, float* yv, float* partials, void* state, int nd,
+                      const int* dims, float lam, int n_iter, int isotropic, float e, cudaStream_t st,
+                      double tol = 0.0, float* yprev = nullptr, float* maxima = nullptr);
 
 }  // namespace fo

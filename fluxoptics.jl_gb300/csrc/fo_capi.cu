@@ -1999,7 +1999,7 @@ FO_API int fo_clamp(float* x, long long n, double lo, double hi, void* stream) {
 }  // extern "C"
 
 struct fo_tv_s {
-  int nx = 0, ny = 0, n_iter = 0, isotropic = 1;
+  int nd = 2, dims[3] = {1, 1, 1}, n_iter = 0, isotropic = 1;
   double lambda = 0, eta = 0, tol = 0;
   float *p = nullptr, *xk = nullptr, *y = nullptr, *partials = nullptr;
   float *yprev = nullptr, *maxima = nullptr;  // with a tolerance
@@ -2008,27 +2008,31 @@ struct fo_tv_s {
 
 extern "C" {
 
-FO_API int fo_tv_create_ex(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta,
-                           double tol) {
+FO_API int fo_tv_create_nd(fo_tv* tv, int ndims, const int* dims, double lambda, int n_iter, int isotropic,
+                           double eta, double tol) {
   if (!tv) return fail(FO_ERR_ARG, "tv output pointer is NULL");
   *tv = nullptr;
-  if (nx < 2 || ny < 2) return fail(FO_ERR_SHAPE, "TVProx needs at least 2 x 2 samples");
+  if (ndims < 1 || ndims > 3 || !dims) return fail(FO_ERR_SHAPE, "TVProx takes 1-, 2- or 3-D arrays");
+  size_t n = 1;
+  for (int i = 0; i < ndims; ++i) {
+    if (dims[i] < 2) return fail(FO_ERR_SHAPE, "TVProx needs at least 2 samples along every dimension");
+    n *= (size_t)dims[i];
+  }
   if (n_iter < 0) return fail(FO_ERR_ARG, "n_iter must be >= 0");
   if (!(tol >= 0)) return fail(FO_ERR_ARG, "tol must be >= 0 (0: none)");
   fo_tv t = new fo_tv_s();
-  t->nx = nx;
-  t->ny = ny;
+  t->nd = ndims;
+  for (int i = 0; i < ndims; ++i) t->dims[i] = dims[i];
   t->n_iter = n_iter;
   t->isotropic = isotropic ? 1 : 0;
   t->lambda = lambda;
   t->eta = eta;
   t->tol = tol;
-  const size_t n = (size_t)nx * ny;
   const size_t blocks = (size_t)tv_partial_blocks((long long)n);
   int rc;
-  if ((rc = dalloc(&t->p, 2 * n, "TV dual")) != FO_OK || (rc = dalloc(&t->xk, 2 * n, "TV state")) != FO_OK ||
+  if ((rc = dalloc(&t->p, ndims * n, "TV dual")) != FO_OK || (rc = dalloc(&t->xk, ndims * n, "TV state")) != FO_OK ||
       (rc = dalloc(&t->y, n, "TV primal")) != FO_OK ||
-      (rc = dalloc(&t->partials, blocks * 2, "TV partials")) != FO_OK ||
+      (rc = dalloc(&t->partials, blocks * 3, "TV partials")) != FO_OK ||
       (tol > 0 && (rc = dalloc(&t->yprev, n, "TV previous primal")) != FO_OK) ||
       (tol > 0 && (rc = dalloc(&t->maxima, blocks, "TV block maxima")) != FO_OK) ||
       (rc = dalloc(reinterpret_cast<char**>(&t->state), tv_state_bytes(), "TV scalars")) != FO_OK) {
@@ -2037,6 +2041,12 @@ FO_API int fo_tv_create_ex(fo_tv* tv, int nx, int ny, double lambda, int n_iter,
   }
   *tv = t;
   return FO_OK;
+}
+
+FO_API int fo_tv_create_ex(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta,
+                           double tol) {
+  const int dims[2] = {nx, ny};
+  return fo_tv_create_nd(tv, 2, dims, lambda, n_iter, isotropic, eta, tol);
 }
 
 FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic, double eta) {
@@ -2059,7 +2069,7 @@ FO_API int fo_tv_destroy(fo_tv t) {
 FO_API int fo_tv_apply(fo_tv t, float* x, void* stream) {
   if (!t || !x) return fail(FO_ERR_ARG, "tv and x must not be NULL");
   const double lam = t->isotropic ? t->lambda : t->lambda / 100.0;
-  FO_LAUNCH(launch_tv(x, t->p, t->xk, t->y, t->partials, t->state, t->nx, t->ny, (float)lam, t->n_iter,
+  FO_LAUNCH(launch_tv(x, t->p, t->xk, t->y, t->partials, t->state, t->nd, t->dims, (float)lam, t->n_iter,
                       t->isotropic, (float)(t->eta * t->eta), S(stream), t->tol, t->yprev, t->maxima));
   return FO_OK;
 }

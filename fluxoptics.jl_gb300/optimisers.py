@@ -136,7 +136,8 @@ class PositiveProx:
 
 
 class TVProx:
-    """TVProx(lambda, n_iter; tol, isotropic, rule=Fista(eta)) (tv_prox.jl:94-195), 2-D.
+    """TVProx(lambda, n_iter; tol, isotropic, rule=Fista(eta)) (tv_prox.jl:94-195) on 1-, 2-
+    or 3-D parameters.
     ``tol`` stops the dual iterations once the primal iterate changes by less than tol
     (tested on the device); a complex parameter has its real and imaginary parts
     denoised separately, each with its own dual state, as the reference does."""
@@ -150,13 +151,14 @@ class TVProx:
 
     def _handle(self, x):
         h = C.c_void_p()
-        _capi.call("fo_tv_create_ex", C.byref(h), x.shape[1], x.shape[0], self.lam, self.n_iter,
+        dims = list(reversed(x.shape))  # x (the last axis) fastest, as in the reference's arrays
+        _capi.call("fo_tv_create_nd", C.byref(h), len(dims), _capi.ivec(dims), self.lam, self.n_iter,
                    int(self.isotropic), self.eta, 0.0 if self.tol is None else self.tol)
         return _TvHandle(h)
 
     def init(self, x):
-        if x.dim() != 2:
-            raise NotImplementedError("TVProx on the GPU path is 2-D")
+        if x.dim() not in (1, 2, 3):
+            raise NotImplementedError("TVProx on the GPU path takes 1-, 2- or 3-D parameters")
         if x.is_complex():
             return (self._handle(x), self._handle(x))
         return self._handle(x)

@@ -552,7 +552,7 @@ FO_API int fo_rule_step(float* x, float* state, const float* dx, long long n, in
 
 /*
  * TVProx(lambda, n_iter; isotropic, rule = Fista(eta)) on an ny x nx float
- * array, in place: n_iter dual Fista iterations with the reference's D / D^T
+ * array (fo_tv_create_nd: 1- to 3-D), in place: n_iter dual Fista iterations with the reference's D / D^T
  * boundary handling and per-slice normalisation.  fo_tv_create_ex adds `tol`
  * (0: none): the iterations stop, before their dual update, once the largest change
  * of the primal iterate from the previous iteration is below tol (tested on the
@@ -563,6 +563,10 @@ typedef struct fo_tv_s* fo_tv;
 FO_API int fo_tv_create(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic,
                         double eta);
 FO_API int fo_tv_create_ex(fo_tv* tv, int nx, int ny, double lambda, int n_iter, int isotropic,
+                           double eta, double tol);
+/* The same on a 1-, 2- or 3-D array of dims[0] x dims[1] x dims[2] (x fastest), with
+ * one dual slice per dimension (the reference's n-dimensional D / D^T). */
+FO_API int fo_tv_create_nd(fo_tv* tv, int ndims, const int* dims, double lambda, int n_iter, int isotropic,
                            double eta, double tol);
 FO_API int fo_tv_destroy(fo_tv tv);
 FO_API int fo_tv_apply(fo_tv tv, float* x, void* stream);

@@ -807,6 +807,13 @@ def test_fista_clamp_tv(fo, orc):
     tvc = fo.TVProx(0.2, 25)
     tvc.apply_(tvc.init(zt), zt)
     assert orc.rel_l2(npy(zt), orc.tv_prox(z0.copy(), 0.2, 25)) < 1e-5
+    # 1-D and 3-D parameters (a dn volume of AS_BPM is 3-D): the reference's n-D D / D^T
+    for shape in ((50,), (6, 10, 12)):
+        for iso in (True, False):
+            a0 = f32(rng.standard_normal(shape))
+            at = torch.tensor(a0, dtype=torch.float32, device="cuda")
+            fo.tv_denoise_(at, 0.3, 20, isotropic=iso)
+            assert orc.rel_l2(npy(at), orc.tv_prox(a0.copy(), 0.3, 20, isotropic=iso)) < 1e-5, (shape, iso)
 
 
 def test_ista_positive_prox(fo, orc):
