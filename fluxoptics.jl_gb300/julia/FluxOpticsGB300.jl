@@ -823,6 +823,18 @@ function GB300TVProx(nx::Integer, ny::Integer, λ::Real; n_iter::Integer = 50, t
     finalizer(x -> ccall((:fo_tv_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), tv)
 end
 
+# the same for a 1-, 2- or 3-D parameter of size `dims` (Julia order, x fastest)
+function GB300TVProx(dims::NTuple{N, Integer}, λ::Real; n_iter::Integer = 50, tol = nothing,
+                     isotropic::Bool = true, eta::Real = 0.25) where {N}
+    d = Cint[dims...]
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:fo_tv_create_nd, LIB), Cint,
+                (Ref{Ptr{Cvoid}}, Cint, Ptr{Cint}, Cdouble, Cint, Cint, Cdouble, Cdouble),
+                h, Cint(N), d, λ, n_iter, Cint(isotropic), eta, tol === nothing ? 0.0 : Float64(tol)))
+    tv = GB300TV(h[])
+    finalizer(x -> ccall((:fo_tv_destroy, LIB), Cint, (Ptr{Cvoid},), x.handle), tv)
+end
+
 function tv_prox!(tv::GB300TV, x::CuArray{Float32})
     check(ccall((:fo_tv_apply, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}), tv.handle, dptr(x), cstream()))
     x
