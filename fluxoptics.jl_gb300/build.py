@@ -8,6 +8,7 @@ rebuilt when a source or header is newer than it.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import glob
 import os
 import shutil
@@ -53,11 +54,24 @@ def is_stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
-    """Compile the library if needed and return its path."""
+    """Compile the library if needed and return its path.  Processes that build at the
+    same time (the ranks of a multi-GPU run) take turns through a file lock, and the
+    ones that find the library fresh once they hold it do not rebuild."""
     if not force and not is_stale():
         return LIB_PATH
-    nvcc = nvcc_path()
     os.makedirs(LIB_DIR, exist_ok=True)
+    with open(os.path.join(LIB_DIR, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            if not force and not is_stale():
+                return LIB_PATH
+            return _build_locked(verbose, extra_flags)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(verbose, extra_flags) -> str:
+    nvcc = nvcc_path()
     os.makedirs(OBJ_DIR, exist_ok=True)
     flags = COMMON_FLAGS + ARCH_FLAGS + list(extra_flags or [])
 
@@ -74,7 +88,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB_PATH + ".tmp"
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
     cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
