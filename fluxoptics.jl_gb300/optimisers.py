@@ -104,6 +104,22 @@ def _float_view(x):
     return x
 
 
+class PointwiseProx:
+    """PointwiseProx(f) (proximal_operators/pointwise_prox.jl:1-46): x <- f.(x) for a
+    user function of the parameter tensor (a torch expression evaluated on the device,
+    e.g. ``lambda x: torch.where(x < 0, 0, x)``).  The built-in operators below are
+    PointwiseProx of fixed functions with their own kernels."""
+
+    def __init__(self, f):
+        self.f = f
+
+    def init(self, x):
+        return None
+
+    def apply_(self, state, x):
+        x.copy_(self.f(x))
+
+
 class IstaProx:
     """Soft threshold towards c (proximal_operators/ista_prox.jl:1-56); a complex
     parameter has its real and imaginary parts shrunk separately, each towards c."""

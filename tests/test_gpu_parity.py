@@ -835,6 +835,11 @@ def test_ista_positive_prox(fo, orc):
     assert np.array_equal(npy(xs), orc.positive_prox(x0.copy()))
     with pytest.raises(TypeError):
         fo.PositiveProx().apply_(None, zs)
+    # PointwiseProx of a device expression equals the built-in operator it spells out
+    xa, xb = (torch.tensor(x0, device="cuda") for _ in range(2))
+    fo.PointwiseProx(lambda v: torch.clamp(v, min=0.0)).apply_(None, xa)
+    fo.PositiveProx().apply_(None, xb)
+    assert torch.equal(xa, xb)
     rule = fo.ProxRule(fo.Fista(0.3), fo.IstaProx(0.125))
     xs = torch.tensor(x0, device="cuda")
     st = rule.init(xs)
