@@ -785,6 +785,28 @@ class _Chain:
         self.probes = list(probes)
 
 
+def _merge_pair(a, b, u):
+    """The merge of two adjacent components (system/merge_rules.jl:1-80), or None."""
+    if getattr(a, "trainable", False) or getattr(b, "trainable", False):
+        return None
+    if type(a) is ASProp and type(b) is ASProp:
+        # one ASProp over z1 + z2 is the product of the two kernels when the distances
+        # have the same sign (for opposite signs the evanescent parts of the reference's
+        # kernels, conjugated for z < 0, do not combine that way)
+        if (a.filter is None and b.filter is None and a.n0 == b.n0 and a.paraxial == b.paraxial
+                and a.track_tilts == b.track_tilts and a.ds == b.ds and (a.z >= 0) == (b.z >= 0)):
+            return ASProp(u, a.z + b.z, ds=a.ds, n0=a.n0, paraxial=a.paraxial, track_tilts=a.track_tilts)
+        return None
+    if type(a) is Phase and type(b) is Phase and a.phi.shape == b.phi.shape:
+        return Phase(u, a.phi + b.phi)
+    if type(a) in (Phase, Mask) and type(b) in (Phase, Mask) and (Mask in (type(a), type(b))):
+        fa = a.m if type(a) is Mask else torch.polar(torch.ones_like(a.phi), a.phi)
+        fb = b.m if type(b) is Mask else torch.polar(torch.ones_like(b.phi), b.phi)
+        if fa.shape == fb.shape:
+            return Mask(u, fa * fb)
+    return None
+
+
 class OpticalSystem:
     """Source + pipe components (system/optical_system.jl:60-214)."""
 
@@ -812,9 +834,33 @@ class OpticalSystem:
         return list(self.components)
 
     # -- planning ---------------------------------------------------------------
+    def merged_components(self, u: ScalarField):
+        """The components after the reference's merge rules (system/merge_rules.jl:1-80),
+        applied to directly adjacent static components: two ASProps with the same
+        options and no filter become one ASProp over the summed distance (the product of
+        their transfer functions, so the FFT pair between them cancels as ift * ft does);
+        two phases add; masks and phases multiply into one mask.  Merged components are
+        new objects; the caller's own components are left unchanged.  The list is cached
+        per field shape."""
+        key = (u.nx, u.ny, u.batch, tuple(float(v) for v in u.lambdas_per_field()),
+               tuple(map(float, u.tilts_per_field().ravel())))
+        cache = self.__dict__.setdefault("_merged", {})
+        if key in cache:
+            return cache[key]
+        out = []
+        for c in self.components:
+            prev = out[-1] if out else None
+            m = _merge_pair(prev, c, u) if prev is not None else None
+            if m is not None:
+                out[-1] = m
+            else:
+                out.append(c)
+        cache[key] = out
+        return out
+
     def segments(self, u: ScalarField):
         """Split the components into fused chains and single components."""
-        comps = self.components
+        comps = self.merged_components(u) if self.merge_components else self.components
         segs = []
         i, n = 0, len(comps)
         fuse = self.merge_components
