@@ -390,10 +390,15 @@ int validate_mod(const Mod& m, bool backward) {
 }
 
 // Fields a CTA of a row pass without a gradient loops over (the gradient passes take
-// the whole batch): the per-pixel modulation factor is computed once per CTA.
-int row_fields_per_cta() {
-  static const int v = std::max(1, std::min(64, env_int("FO_ROW_FIELDS", 16)));
-  return v;
+// the whole batch): the per-pixel modulation factor is computed once per CTA.  The
+// batch is cut into the fewest equal groups of at most FO_ROW_FIELDS fields (default
+// 24): at 2048^2 x 48 fields, two groups of 24 measured 10.46 ms per iteration
+// against 10.51 ms for three of 16, 10.59 ms for 32 + 16 and 10.50 ms for one of 48.
+int row_fields_per_cta(int batch) {
+  static const int cap = std::max(1, std::min(64, env_int("FO_ROW_FIELDS", 24)));
+  if (batch <= cap) return std::max(1, batch);
+  const int groups = (batch + cap - 1) / cap;
+  return (batch + groups - 1) / groups;
 }
 
 // One row pass.  `src`/`dst` are real-space (ld nx) or spectral (ld fx) arrays as
@@ -415,7 +420,7 @@ int row_pass(const Layout& L, const float2* src, float2* dst, bool inv_first, bo
   a.n_valid = L.nx;
   a.batch = L.batch;
   const bool grad = bwd && mod.kind != MOD_NONE && mod.grad != nullptr;
-  a.fields_per_cta = grad ? L.batch : std::min(L.batch, row_fields_per_cta());
+  a.fields_per_cta = grad ? L.batch : row_fields_per_cta(L.batch);
   a.field_list = nullptr;
   a.inv_first = inv_first;
   a.fwd_after = fwd_after;
@@ -734,7 +739,7 @@ int autotune_plan(fo_prop_plan p) {
       a.nrows = p->ny;
       a.n_valid = p->nx;
       a.batch = nb;
-      a.fields_per_cta = std::min(nb, row_fields_per_cta());
+      a.fields_per_cta = row_fields_per_cta(nb);
       a.inv_first = 1;
       a.fwd_after = 1;
       int trc = FO_OK;
