@@ -92,6 +92,8 @@ SIGNATURES = {
     "fo_chain_backward_ex": (_i, [_vp, _vp, C.POINTER(fo_mod), _i, _vp, _vp, _i, _vp]),
     "fo_chain_withgradient_sid": (_i, [_vp, _vp, _vp, _vp, C.POINTER(fo_mod), C.POINTER(fo_mod), _i, _vp, _vp, _vp,
                                        _i, _vp]),
+    "fo_chain_withgradient_sfd": (_i, [_vp, _vp, _vp, _vp, C.POINTER(fo_mod), C.POINTER(fo_mod), _i, _vp, _vp, _vp,
+                                       _vp, _i, _vp]),
     "fo_bpm_create": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i, _d, _i]),
     "fo_bpm_create_ex": (_i, [C.POINTER(_vp), _i, _i, _i, _d, _d, _pd, _i, _d, _d, _i, _i,
                               C.POINTER(fo_as_options), _i]),

@@ -1027,16 +1027,11 @@ class OpticalSystem:
             metric(u)
         return u
 
-    def forward_backward_sid(self, du: ScalarField, src: ScalarField, metric, u_out: ScalarField = None,
-                             input_grad=None):
-        """Forward sweep from ``src``, SquaredIntensityDifference and its seeded adjoint
-        sweep in one library call (fo_chain_withgradient_sid), for a system that is one
-        fused chain; when it ends in a propagator, the chain's last forward row pass and
-        the adjoint's first row pass run as one pass.  ``metric.loss`` holds the
-        per-slice losses afterwards; ``u_out`` (optional) receives the output field.
-        Returns {component: {name: grad}}, or None when the system has another shape
-        (callers then run forward and backward)."""
-        if not getattr(metric, "fuses_into_chain", False) or src is None:
+    def _fused_chain_mods(self, src: ScalarField, input_grad):
+        """The single fused chain of a system for the withgradient entry points, with its
+        forward and adjoint modulation slots and gradient buffers; None when the system
+        has another shape."""
+        if src is None:
             return None
         segs = self.segments(src)
         if len(segs) != 1 or not isinstance(segs[0], _Chain):
@@ -1066,10 +1061,49 @@ class OpticalSystem:
             mf[k] = m.fo_mod(saved=sv, u=src)
             mb[k] = m.fo_mod(saved=src.electric if k == 0 else sv, grad=g, u=src)
             grads[m] = {m.pname: g}
+        return seg, mf, mb, grads, saves, (0 if input_grad else 1)
+
+    def forward_backward_sid(self, du: ScalarField, src: ScalarField, metric, u_out: ScalarField = None,
+                             input_grad=None):
+        """Forward sweep from ``src``, SquaredIntensityDifference and its seeded adjoint
+        sweep in one library call (fo_chain_withgradient_sid), for a system that is one
+        fused chain; when it ends in a propagator, the chain's last forward row pass and
+        the adjoint's first row pass run as one pass.  ``metric.loss`` holds the
+        per-slice losses afterwards; ``u_out`` (optional) receives the output field.
+        Returns {component: {name: grad}}, or None when the system has another shape
+        (callers then run forward and backward)."""
+        if not getattr(metric, "fuses_into_chain", False):
+            return None
+        fm = self._fused_chain_mods(src, input_grad)
+        if fm is None:
+            return None
+        seg, mf, mb, grads, saves, flags = fm
         _capi.call("fo_chain_withgradient_sid", self._chain_handle(seg, src), _ptr(src.electric),
                    _ptr(u_out.electric) if u_out is not None else None, _ptr(du.electric), mf, mb, int(self.direction),
-                   metric.handle, _ptr(metric.target), _ptr(metric.loss), 0 if input_grad else 1, _stream())
+                   metric.handle, _ptr(metric.target), _ptr(metric.loss), flags, _stream())
         self._fused_saves = saves
+        return grads
+
+    def forward_backward_sfd(self, du: ScalarField, src: ScalarField, metric, dc=None, u_out: ScalarField = None,
+                             input_grad=None):
+        """The same for SquaredFieldDifference (fo_chain_withgradient_sfd): ``metric.out``
+        holds the per-field values c afterwards and ``du`` the gradient of sum(dc * c)
+        (dc: one value per field, or None for ones).  Returns
+        {component: {name: grad}}, or None when the system is not one fused chain."""
+        if (src.nx, src.ny, src.batch) != (metric.nx, metric.ny, metric.batch):
+            return None
+        if dc is not None:
+            dc = dc.to(device=metric.out.device, dtype=torch.float32).reshape(-1).contiguous()
+            if dc.numel() != metric.batch:
+                raise ValueError("dc must hold one value per field")
+        fm = self._fused_chain_mods(src, input_grad)
+        if fm is None:
+            return None
+        seg, mf, mb, grads, saves, flags = fm
+        _capi.call("fo_chain_withgradient_sfd", self._chain_handle(seg, src), _ptr(src.electric),
+                   _ptr(u_out.electric) if u_out is not None else None, _ptr(du.electric), mf, mb, int(self.direction),
+                   metric.handle, _ptr(metric.v.electric), _ptr(dc), _ptr(metric.out), flags, _stream())
+        self._fused_saves = (saves, dc)
         return grads
 
     def backward(self, du: ScalarField, tape, seed=None, input_grad=None):

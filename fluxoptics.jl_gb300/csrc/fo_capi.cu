@@ -596,6 +596,66 @@ int row_pass_sid_seed(const Layout& L, float2* spec, float2* u_out, const fo_sid
   return FO_OK;
 }
 
+// The chain's last forward row pass, SquaredFieldDifference against `v` and the adjoint
+// sweep's first row pass as one launch (row kernel GK = 5), in place on the spectrum
+// `spec`; the per-row sums go to sfd->rows and `c` receives the per-field values.
+int row_pass_sfd_seed(const Layout& L, float2* spec, float2* u_out, const fo_sfd_s* sfd, const float2* v,
+                      const float* dc, float* c, const float2* tw, cudaStream_t st) {
+  RowPassArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const long long real_bs = (long long)L.nx * L.ny, spec_bs = (long long)L.fx * L.ny;
+  a.src = spec;
+  a.src_bstride = spec_bs;
+  a.src_ld = L.fx;
+  a.dst = u_out;
+  a.dst_bstride = real_bs;
+  a.dst_ld = L.nx;
+  a.nrows = L.ny;
+  a.n_valid = L.nx;
+  a.batch = L.batch;
+  a.inv_first = 1;
+  a.fwd_after = 0;
+  a.mod_kind = MOD_NONE;
+  a.fields_per_cta = row_fields_per_cta(L.batch);
+  a.seed_dst = spec;
+  a.seed_bstride = spec_bs;
+  a.seed_ld = L.fx;
+  a.sfd_v = v;
+  a.sfd_rows = sfd->rows;
+  a.sfd_dc = dc;
+  ProfScope prof(1, st);
+  FO_LAUNCH(launch_row_pass(L.fx, L.row_v, 0, a, tw, st));
+  FO_LAUNCH(launch_sid_finalize(sfd->rows, L.ny, L.batch, c, st));
+  return FO_OK;
+}
+
+// Forward sweep, SquaredFieldDifference and the seeded adjoint sweep: as
+// run_withgradient_sid, with the per-field metric of row_pass_sfd_seed.
+int run_withgradient_sfd(const std::vector<fo_prop_plan>& props, float2* w, const float2* u_in, float2* u_out,
+                         float2* du, const Mod* mods_f, const Mod* mods_b, int s, const fo_sfd_s* sfd,
+                         const float2* v, const float* dc, float* c, cudaStream_t st, bool discard_input_grad) {
+  const int K = (int)props.size();
+  const Layout L = layout_of(props[0]);
+  const float* il = props[0]->inv_lambda;
+  const float sf = (float)s;
+  const float2* tw = props[0]->tw_x;
+  FO_TRY(row_pass(L, u_in, w, false, true, mods_f[0], false, sf, il, nullptr, tw, st));
+  for (int k = 0; k < K; ++k) {
+    FO_TRY(col_pass(props[k], w, s < 0, st));
+    if (k + 1 < K) FO_TRY(row_pass(L, w, w, true, true, mods_f[k + 1], false, sf, il, nullptr, tw, st));
+  }
+  FO_TRY(row_pass_sfd_seed(L, w, u_out, sfd, v, dc, c, tw, st));
+  for (int k = K - 1; k >= 0; --k) {
+    FO_TRY(col_pass(props[k], w, s > 0, st));
+    if (k > 0)
+      FO_TRY(row_pass(L, w, w, true, true, mods_b[k], true, sf, il, nullptr, tw, st));
+    else
+      FO_TRY(row_pass(L, w, discard_input_grad ? nullptr : du, true, false, mods_b[0], true, sf, il, nullptr, tw,
+                      st));
+  }
+  return FO_OK;
+}
+
 // Forward sweep, SquaredIntensityDifference and the seeded adjoint sweep in one
 // sequence of passes on the working buffer `w` (the chain scratch for padded layouts,
 // else du): 2K + 1 forward passes and 2K + 1 adjoint passes share one row pass.
@@ -1607,6 +1667,40 @@ FO_API int fo_chain_withgradient_sid(fo_chain chain, const void* u_in, void* u_o
   return run_withgradient_sid(chain->props, w, reinterpret_cast<const float2*>(u_in),
                               reinterpret_cast<float2*>(u_out), d, mf.data(), mb.data(), direction, sid, target, loss,
                               S(stream), discard);
+}
+
+FO_API int fo_chain_withgradient_sfd(fo_chain chain, const void* u_in, void* u_out, void* du,
+                                     const fo_mod* mods_fwd, const fo_mod* mods_bwd, int direction, fo_sfd sfd,
+                                     const void* v, const float* dc, float* c, int flags, void* stream) {
+  if (!chain || !u_in || !du || !mods_fwd || !mods_bwd || !sfd || !v || !c)
+    return fail(FO_ERR_ARG, "chain, u_in, du, mods_fwd, mods_bwd, sfd, v and c must not be NULL");
+  FO_TRY(check_dir(direction));
+  if (u_out == du) return fail(FO_ERR_ARG, "u_out and du must be different buffers");
+  const int K = (int)chain->props.size();
+  const Layout L = layout_of(chain->props[0]);
+  if (sfd->nx != L.nx || sfd->ny != L.ny || sfd->batch != L.batch)
+    return fail(FO_ERR_SHAPE, "metric and chain shapes differ");
+  std::vector<Mod> mf(K + 1), mb(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    mf[k] = mod_from(&mods_fwd[k]);
+    mb[k] = mod_from(&mods_bwd[k]);
+    FO_TRY(validate_mod(mf[k], false));
+    FO_TRY(validate_mod(mb[k], true));
+  }
+  if (mf[K].kind != MOD_NONE || mb[K].kind != MOD_NONE || chain->probe_ptr()) {
+    // the shared pass does not apply: forward sweep, metric, pull-back, adjoint sweep
+    void* out = u_out ? u_out : du;
+    FO_TRY(fo_chain_forward_from(chain, u_in, out, mods_fwd, direction, stream));
+    FO_TRY(fo_sfd_forward(sfd, out, v, c, stream));
+    FO_TRY(fo_sfd_backward(sfd, out, v, dc, du, stream));
+    return fo_chain_backward_ex(chain, du, mods_bwd, direction, nullptr, nullptr, flags, stream);
+  }
+  float2* d = reinterpret_cast<float2*>(du);
+  float2* w = chain->scratch ? chain->scratch : d;
+  return run_withgradient_sfd(chain->props, w, reinterpret_cast<const float2*>(u_in),
+                              reinterpret_cast<float2*>(u_out), d, mf.data(), mb.data(), direction, sfd,
+                              reinterpret_cast<const float2*>(v), dc, c, S(stream),
+                              (flags & FO_BWD_DISCARD_INPUT_GRAD) != 0);
 }
 
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,

@@ -6,6 +6,15 @@
 
 #include <string>
 
+// SquaredFieldDifference handle (fo_sfd_*): fixed-order per-field sums in `partial`
+// (batch x kSfdBlocks) for the standalone metric, and per-row sums in `rows`
+// (ny x batch) for the metric fused into a chain's last pass.
+struct fo_sfd_s {
+  int nx = 0, ny = 0, batch = 0;
+  double* partial = nullptr;
+  float* rows = nullptr;
+};
+
 namespace fo {
 
 // ---------------------------------------------------------------------------
@@ -82,6 +91,14 @@ struct RowPassArgs {
   float2* seed_dst;
   long long seed_bstride;
   int seed_ld;
+  // With sfd_rows (row kernel GK = 5): the chain's last forward pass, SquaredFieldDifference
+  // against sfd_v (real-space layout of dst) and the adjoint sweep's first pass, in place on
+  // the spectrum (seed_dst == src): per field, the output row u (to dst when set), the
+  // row's sum |u - v|^2 to sfd_rows[row * batch + field], and the seed 2 dc_b (u - v)
+  // (sfd_dc: per field, NULL: ones) forward-transformed along x over the spectrum row.
+  const float2* sfd_v;
+  float* sfd_rows;
+  const float* sfd_dc;
 };
 
 // One column pass: forward FFT along y, multiply by the transfer function of the

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(LANES*(N / E),
                                   min_blocks(LANES*(N / E), E,
                                              RP                          ? 128
                                              : (GK == 0 || GK == 3)      ? FO_ROW_E16_REG_CAP
-                                             : (GK == 4 ? FO_ROW_SEED_REG_CAP : 128)))
+                                             : ((GK == 4 || GK == 5) ? FO_ROW_SEED_REG_CAP : 128)))
     row_pass_kernel(const RowPassArgs a, const float2* __restrict__ tw) {
   static_assert(!RP || (GK == 0 && !PF), "register prefetch is for passes without a gradient or staging");
   pdl_prologue();
@@ -190,6 +190,62 @@ __global__ void __launch_bounds__(LANES*(N / E),
       cp_async8(dst + spad(p), src + p);
     }
   };
+  if constexpr (GK == 5) {
+    // The chain's last forward pass, SquaredFieldDifference and the first pass of the
+    // adjoint sweep in one launch.  Each field is independent: its spectrum row is
+    // inverse-transformed along x (the output row, written to a.dst when set), the
+    // difference d = u - v to the reference field gives the row's sum of |d|^2
+    // (fixed-order reduction) and the seed 2 dc_b d, which is forward-transformed and
+    // written over the spectrum row.  The same arithmetic as the forward pass, the
+    // metric's pull-back (fo_sfd_backward) and the adjoint's first pass, so the seeds
+    // and the gradients are the same bit for bit.
+    float* red = reinterpret_cast<float*>(dsm + LANES * SLOTS) + lane * 32;  // past the exchange tiles
+    for (int f = f0; f < f1; ++f) {
+      const int b = field_of(f);
+      float2* row = a.seed_dst + (long long)b * a.seed_bstride + (long long)y * a.seed_ld;
+      float2 v[E];
+#pragma unroll
+      for (int i = 0; i < E; ++i) v[i] = row_ok ? cconj(row[t + i * T]) : make_float2(0.f, 0.f);
+      fft(v, buf0);
+      const float2* vr = a.sfd_v + (long long)b * a.dst_bstride + (long long)y * a.dst_ld;
+      float2* dst = a.dst ? a.dst + (long long)b * a.dst_bstride + (long long)y * a.dst_ld : nullptr;
+      const float k2 = 2.f * (a.sfd_dc ? a.sfd_dc[b] : 1.f);
+      float r2 = 0.f;
+#pragma unroll
+      for (int i = 0; i < E; ++i) {
+        const int p = t + i * T;
+        float2 d = make_float2(0.f, 0.f);
+        if (row_ok && p < n_valid) {
+          const float2 uo = cconj(v[i]);
+          if (dst) dst[p] = uo;
+          const float2 w = vr[p];
+          d = make_float2(uo.x - w.x, uo.y - w.y);
+          r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, r2));
+        }
+        v[i] = make_float2(k2 * d.x, k2 * d.y);
+      }
+      constexpr int G = T < 32 ? T : 32;
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+      if constexpr (T > 32) {
+        if ((t & 31) == 0) red[t >> 5] = r2;
+        __syncthreads();
+        if (t == 0) {
+          float acc = 0.f;
+#pragma unroll
+          for (int w = 0; w < T / 32; ++w) acc += red[w];
+          r2 = acc;
+        }
+      }
+      if (t == 0 && row_ok) a.sfd_rows[(long long)y * a.batch + b] = r2;
+      fft(v, buf0);  // its first barrier also ends this field's reads of `red`
+      if (row_ok) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) row[t + i * T] = v[i];
+      }
+    }
+    return;
+  }
   if constexpr (GK == 4) {
     // The chain's last forward pass, SquaredIntensityDifference and the first pass of the
     // seeded adjoint sweep in one launch.  Loop 1 inverse-transforms the rows of the
@@ -258,6 +314,7 @@ __global__ void __launch_bounds__(LANES*(N / E),
     for (int o = G / 2; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
     float* red = reinterpret_cast<float*>(buf0);
     if constexpr (T > 32) {
+      __syncthreads();  // every warp is done with the last transform's reads of buf0
       if ((t & 31) == 0) red[t >> 5] = r2;
       __syncthreads();
       if (t == 0) {
@@ -1191,7 +1248,19 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
       if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, false>, grid, dim3(SH::threads), smem, s, a, tw); \
     }                                                                                             \
   } while (0)
-  if (sid && a.seed_dst) {
+  if (a.sfd_rows) {
+    // the exchange tiles and 32 floats of reduction scratch per row
+    const size_t smem5 = SH::smem(false, false) + sizeof(float) * 32 * LANES;
+    if (full) {
+      e = set_smem(row_pass_kernel<N, E, LANES, 5, false, true>, smem5);
+      if (e == cudaSuccess)
+        e = launch_pass(row_pass_kernel<N, E, LANES, 5, false, true>, grid, dim3(SH::threads), smem5, s, a, tw);
+    } else {
+      e = set_smem(row_pass_kernel<N, E, LANES, 5, false, false>, smem5);
+      if (e == cudaSuccess)
+        e = launch_pass(row_pass_kernel<N, E, LANES, 5, false, false>, grid, dim3(SH::threads), smem5, s, a, tw);
+    }
+  } else if (sid && a.seed_dst) {
     FO_ROW_GO(4, false);
   } else if (sid) {
     FO_ROW_GO(3, false);

@@ -117,10 +117,6 @@ __global__ void sfd_backward_kernel(const float2* u, const float2* v, const floa
 
 using namespace fo;
 
-struct fo_sfd_s {
-  int nx = 0, ny = 0, batch = 0;
-  double* partial = nullptr;  // batch x kSfdBlocks
-};
 
 extern "C" {
 
@@ -163,7 +159,9 @@ FO_API int fo_sfd_create(fo_sfd* sfd, int nx, int ny, int batch) {
   h->ny = ny;
   h->batch = batch;
   cudaError_t e = cudaMalloc(&h->partial, sizeof(double) * (size_t)batch * kSfdBlocks);
+  if (e == cudaSuccess) e = cudaMalloc(&h->rows, sizeof(float) * (size_t)ny * batch);
   if (e != cudaSuccess) {
+    cudaFree(h->partial);
     delete h;
     return fail(FO_ERR_ALLOC, "SquaredFieldDifference partials: " + std::string(cudaGetErrorString(e)));
   }
@@ -174,6 +172,7 @@ FO_API int fo_sfd_create(fo_sfd* sfd, int nx, int ny, int batch) {
 FO_API int fo_sfd_destroy(fo_sfd sfd) {
   if (sfd) {
     cudaFree(sfd->partial);
+    cudaFree(sfd->rows);
     delete sfd;
   }
   return FO_OK;

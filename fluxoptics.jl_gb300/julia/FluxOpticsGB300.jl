@@ -803,6 +803,27 @@ function pullback!(m::GB300SFD, ∂c, u::ScalarField, ∂u::ScalarField)
     ∂u
 end
 
+"""
+    withgradient!(∂u, c::GB300Chain, u_in, m::GB300SFD; ∂c=nothing, u_out=nothing, input_grad=true) -> c
+
+Zygote.withgradient for a chain with SquaredFieldDifference as the loss
+(fo_chain_withgradient_sfd): forward sweep, metric, its pullback 2 ∂c_b (u_b − v_b)
+and the adjoint sweep, the forward's last row pass and the adjoint's first shared
+when the chain ends in a propagator.  Returns the per-field values `m.c`.
+"""
+function withgradient!(∂u::ScalarField, c::GB300Chain, u_in::ScalarField, m::GB300SFD;
+                       ∂c = nothing, u_out = nothing, input_grad::Bool = true, dir::Type{<:Direction} = Forward)
+    mf = [_fomod(x, _saved(x), nothing) for x in c.mods]
+    mb = [_fomod(x, _saved(x), _grad(x)) for x in c.mods]
+    check(ccall((:fo_chain_withgradient_sfd, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{FoMod}, Ptr{FoMod}, Cint, Ptr{Cvoid},
+                 Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Cvoid}),
+                c.chain, dptr(u_in.electric), u_out === nothing ? C_NULL : dptr(u_out.electric),
+                dptr(∂u.electric), mf, mb, dirsign(dir), m.handle, dptr(m.v.electric),
+                ∂c === nothing ? C_NULL : dptr(∂c), dptr(m.c), input_grad ? Cint(0) : Cint(1), cstream()))
+    m.c
+end
+
 mutable struct GB300TV
     handle::Ptr{Cvoid}
 end

@@ -157,8 +157,8 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     """Loss sum(dc * c) (dc = 1 by default) and the gradients of every trainable
     component, through the hand-written adjoint (the GPU counterpart of
     Zygote.withgradient over the reference's rrules, src/ChainRulesCoreExt.jl:21-111).
-    SquaredIntensityDifference seeds the adjoint inside the first fused pass; the
-    overlap metrics write their pull-back first."""
+    SquaredIntensityDifference and SquaredFieldDifference seed the adjoint inside the
+    first fused pass; the overlap metrics write their pull-back first."""
     src = system.source.u0 if x is None else x
     du = src.similar()
 
@@ -174,6 +174,13 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
         grads = system.forward_backward_sid(du, src, metric)
         if grads is not None:
             return metric.loss.sum(), with_source(grads)
+    if isinstance(metric, SquaredFieldDifference):
+        w = None if dc is None else dc.to(device=metric.out.device, dtype=torch.float32).reshape(-1).contiguous()
+        # one fused chain: forward, metric, pull-back and adjoint in one call
+        grads = system.forward_backward_sfd(du, src, metric, dc=w)
+        if grads is not None:
+            c = metric.out
+            return (c.sum() if w is None else (w * c).sum()), with_source(grads)
     u = src.similar()
     tape = []
     if isinstance(metric, SquaredIntensityDifference):

@@ -498,6 +498,22 @@ FO_API int fo_sfd_forward(fo_sfd sfd, const void* u, const void* v, float* c, vo
 FO_API int fo_sfd_backward(fo_sfd sfd, const void* u, const void* v, const float* dc, void* du, void* stream);
 FO_API int fo_sfd_destroy(fo_sfd sfd);
 
+/*
+ * fo_chain_withgradient_sid for SquaredFieldDifference against the reference fields v:
+ * c[b] (device float[batch]) receives the per-field values and du the gradient of
+ * sum_b dc[b] c[b] (dc: device float[batch], NULL: ones).  When the last slot is empty
+ * and no probes are set, the forward sweep's last row pass, the metric, its pull-back
+ * 2 dc_b (u_b - v_b) and the adjoint sweep's first row pass are one pass (4K + 1
+ * passes); the gradients equal those of the separate calls bit for bit, and the values
+ * c differ from fo_sfd_forward's only in the order of the per-field sums.
+ * Replaces: Zygote.withgradient over the reference's rrules for a system ending in a
+ * propagator with SquaredFieldDifference (src/metrics/squared_field_difference.jl:35-61)
+ * as the loss.
+ */
+FO_API int fo_chain_withgradient_sfd(fo_chain chain, const void* u_in, void* u_out, void* du,
+                                     const fo_mod* mods_fwd, const fo_mod* mods_bwd, int direction, fo_sfd sfd,
+                                     const void* v, const float* dc, float* c, int flags, void* stream);
+
 /* ---------------------------------------------------------------------- */
 /* Optimiser and proximal operators                                        */
 /* ---------------------------------------------------------------------- */

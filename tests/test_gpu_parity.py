@@ -1352,3 +1352,104 @@ def test_withgradient_sid_shared_pass(fo, orc, kind, d, with_out, last_mod):
     dv, g0 = orc.phase_backward(dv, phis[0], a0, d)
     assert orc.rel_l2(npy(g2[ph2[0]]["phi"]), g0) < GRAD_TOL
     assert orc.rel_l2(npy(du2.electric).reshape(6, n, n), dv) < 1e-4
+
+
+@pytest.mark.parametrize("kind,d,with_out,weighted,last_mod", [
+    ("AS", 1, False, False, False), ("AS", -1, True, True, False), ("RS", 1, True, True, False),
+    ("AS", 1, True, False, True)])
+def test_withgradient_sfd_shared_pass(fo, orc, kind, d, with_out, weighted, last_mod):
+    """fo_chain_withgradient_sfd: the chain's last forward row pass, SquaredFieldDifference,
+    its pull-back and the adjoint's first row pass as one pass (or, with a modulator in
+    the last slot, as the separate calls).  Gradients and the output field equal the
+    separate forward + fo_sfd_forward + fo_sfd_backward + backward calls bit for bit;
+    the values c differ only in the order of the sums; both match the oracle."""
+    rng = np.random.default_rng(51 if kind == "AS" else 52)
+    n = 256 if kind == "AS" else 200
+    lams = [0.64, 0.538, 0.455, 0.64]
+    B = len(lams)
+    ds = (0.5, 0.5) if kind == "AS" else (1.0, 1.0)
+    u0 = rand_field(rng, (B, n, n))
+    v0 = rand_field(rng, (B, n, n))
+    phis = [f32(rng.uniform(0, 6, (n, n))) for _ in range(2)]
+    m_last = c64(rng.uniform(0.5, 1.0, (n, n)) * np.exp(1j * rng.uniform(0, 6, (n, n))))
+    w = f32(rng.uniform(0.5, 2.0, B)) if weighted else None
+
+    def build():
+        u = fo.ScalarField(u0, ds, lams)
+        P = (lambda zz: fo.ASProp(u, zz)) if kind == "AS" else (lambda zz: fo.RSProp(u, zz))
+        ph = [fo.Phase(u, p, trainable=True, buffered=True) for p in phis]
+        comps = [ph[0], P(300.0), ph[1], P(200.0)]
+        mk = None
+        if last_mod:
+            mk = fo.Mask(u, m_last, trainable=True, buffered=True)
+            comps.append(mk)
+        system = fo.OpticalSystem(fo.ScalarSource(u), comps, direction=d)
+        return u, system, ph, mk
+
+    dc = torch.tensor(w, dtype=torch.float32, device="cuda") if weighted else None
+    # separate calls
+    u, system, ph, mk = build()
+    metric = fo.SquaredFieldDifference(fo.ScalarField(v0, ds, lams))
+    src = system.source.u0
+    x, du = src.similar(), src.similar()
+    tape = []
+    system.forward(x, tape, src=src)
+    c_sep = metric(x).clone()
+    metric.backpropagate_into(x, du, dc)
+    grads = system.backward(du, tape, input_grad=True)
+    torch.cuda.synchronize()
+    ref_out, ref_du = x.electric.clone(), du.electric.clone()
+    ref_g = [grads[p]["phi"].clone() for p in ph]
+    ref_gm = grads[mk]["m"].clone() if mk is not None else None
+
+    # one call
+    u2, system2, ph2, mk2 = build()
+    metric2 = fo.SquaredFieldDifference(fo.ScalarField(v0, ds, lams))
+    src2 = system2.source.u0
+    x2, du2 = src2.similar(), src2.similar()
+    x2.electric.zero_()
+    g2 = system2.forward_backward_sfd(du2, src2, metric2, dc=dc, u_out=x2 if with_out else None, input_grad=True)
+    assert g2 is not None
+    torch.cuda.synchronize()
+    c2 = metric2.out.clone()
+    assert torch.max(torch.abs(c2 - c_sep) / c_sep).item() < 1e-5
+    assert torch.equal(du2.electric, ref_du)
+    for i, p in enumerate(ph2):
+        assert torch.equal(g2[p]["phi"], ref_g[i]), i
+    if mk2 is not None:
+        assert torch.equal(g2[mk2]["m"], ref_gm)
+    if with_out:
+        assert torch.equal(x2.electric, ref_out)
+    elif not last_mod:
+        assert not torch.any(x2.electric != 0)  # the output field is not written
+    # the fused values are fixed-order too
+    system2.forward_backward_sfd(du2, src2, metric2, dc=dc, input_grad=True)
+    assert torch.equal(metric2.out, c2)
+
+    # withgradient dispatches to the fused call and returns sum(dc * c); dc of another
+    # dtype is converted
+    loss, g3 = fo.withgradient(metric2, system2, dc=None if dc is None else dc.double())
+    wsum = (c2 if dc is None else dc * c2).sum()
+    assert torch.equal(loss, wsum)
+    assert torch.equal(g3[ph2[0]]["phi"], ref_g[0])
+
+    # the oracle
+    prop = (lambda a, zz, dd: orc.asprop(a, ds[0], ds[1], lams, zz, dd)) if kind == "AS" else \
+        (lambda a, zz, dd: orc.rsprop(a, ds[0], ds[1], lams, zz, dd))
+    a0 = u0
+    a1 = prop(orc.phase_forward(a0, phis[0], d), 300.0, d)
+    out = prop(orc.phase_forward(a1, phis[1], d), 200.0, d)
+    a2 = out
+    if last_mod:
+        out = orc.mask_forward(a2, m_last, d)
+    c_ref = orc.sfd_value(out, v0)
+    assert np.max(np.abs(npy(c2) - c_ref) / c_ref) < 1e-4
+    dv = orc.sfd_backward(out, v0, 1.0 if w is None else w)
+    if last_mod:
+        dv, _ = orc.mask_backward(dv, m_last, a2, d)
+    dv = prop(dv, 200.0, -d)
+    dv, _ = orc.phase_backward(dv, phis[1], a1, d)
+    dv = prop(dv, 300.0, -d)
+    dv, g0 = orc.phase_backward(dv, phis[0], a0, d)
+    assert orc.rel_l2(npy(g2[ph2[0]]["phi"]), g0) < GRAD_TOL
+    assert orc.rel_l2(npy(du2.electric), dv) < 1e-4

@@ -108,7 +108,7 @@ def test_shim_binds_declared_entry_points():
 @pytest.mark.parametrize("sym", [
     "fo_bpm_create", "fo_bpm_forward", "fo_bpm_backward", "fo_bpm_destroy",
     "fo_sid_create", "fo_sid_forward", "fo_sid_backward", "fo_sid_destroy",
-    "fo_chain_forward_sid", "fo_chain_backward_ex", "fo_chain_withgradient_sid",
+    "fo_chain_forward_sid", "fo_chain_backward_ex", "fo_chain_withgradient_sid", "fo_chain_withgradient_sfd",
     "fo_fista_step", "fo_fista_clamp_step", "fo_clamp", "fo_tv_create_ex", "fo_tv_apply", "fo_tv_destroy",
 ])
 def test_shim_covers_the_hot_path(sym):
