@@ -1644,6 +1644,8 @@ FO_API int fo_chain_withgradient_sid(fo_chain chain, const void* u_in, void* u_o
     return fail(FO_ERR_ARG, "chain, u_in, du, mods_fwd, mods_bwd, sid, target and loss must not be NULL");
   FO_TRY(check_dir(direction));
   if (u_out == du) return fail(FO_ERR_ARG, "u_out and du must be different buffers");
+  if (u_in == du || u_in == u_out)
+    return fail(FO_ERR_ARG, "u_in must not alias u_out or du: the adjoint sweep reads it");
   const int K = (int)chain->props.size();
   const Layout L = layout_of(chain->props[0]);
   if (sid->nx != L.nx || sid->ny != L.ny || sid->batch != L.batch)
@@ -1676,6 +1678,9 @@ FO_API int fo_chain_withgradient_sfd(fo_chain chain, const void* u_in, void* u_o
     return fail(FO_ERR_ARG, "chain, u_in, du, mods_fwd, mods_bwd, sfd, v and c must not be NULL");
   FO_TRY(check_dir(direction));
   if (u_out == du) return fail(FO_ERR_ARG, "u_out and du must be different buffers");
+  if (u_in == du || u_in == u_out)
+    return fail(FO_ERR_ARG, "u_in must not alias u_out or du: the adjoint sweep reads it");
+  if (v == du || v == u_out) return fail(FO_ERR_ARG, "v must not alias u_out or du");
   const int K = (int)chain->props.size();
   const Layout L = layout_of(chain->props[0]);
   if (sfd->nx != L.nx || sfd->ny != L.ny || sfd->batch != L.batch)

@@ -384,7 +384,8 @@ FO_API int fo_chain_backward_ex(fo_chain chain, void* du, const fo_mod* mods, in
  * FO_BWD_DISCARD_INPUT_GRAD.  mods_fwd and mods_bwd describe the n_props + 1
  * modulation slots for the two sweeps (what fo_chain_forward_sid and
  * fo_chain_backward_ex would be given); trainable slots write their gradients.
- * u_out (nullable, not du) receives the output field.  When the last slot is empty,
+ * u_out (nullable, not du) receives the output field.  u_in must not alias u_out or du
+ * (the adjoint sweep reads it).  When the last slot is empty,
  * every target slice holds the same number of fields and no probes are set, the
  * forward sweep's last row pass and the adjoint sweep's first row pass run as one
  * pass, so the iteration reads and writes the fields once less: 4K + 1 passes
@@ -505,7 +506,8 @@ FO_API int fo_sfd_destroy(fo_sfd sfd);
  * and no probes are set, the forward sweep's last row pass, the metric, its pull-back
  * 2 dc_b (u_b - v_b) and the adjoint sweep's first row pass are one pass (4K + 1
  * passes); the gradients equal those of the separate calls bit for bit, and the values
- * c differ from fo_sfd_forward's only in the order of the per-field sums.
+ * c differ from fo_sfd_forward's only in the order of the per-field sums.  Neither u_in
+ * nor v may alias u_out or du.
  * Replaces: Zygote.withgradient over the reference's rrules for a system ending in a
  * propagator with SquaredFieldDifference (src/metrics/squared_field_difference.jl:35-61)
  * as the loss.

@@ -111,5 +111,15 @@ def test_bad_arguments_are_rejected(capi):
     assert lib.fo_fista_clamp_step(p, p, p, p, 10, 0.1, p, 1.0, 0.0, None) == 1
     assert "lo must not exceed hi" in lib.fo_last_error().decode()
     assert lib.fo_chain_forward_sid(None, None, None, None, 1, None, None, None, None) == 1
+    # the fused withgradient calls reject aliased fields before touching the chain
+    m = (capi.fo_mod * 1)()
+    p32, p48 = C.c_void_p(32), C.c_void_p(48)
+    assert lib.fo_chain_withgradient_sid(p, p, p32, p32, m, m, 1, p, p, p, 0, None) == 1
+    assert lib.fo_chain_withgradient_sid(p, p32, p32, p48, m, m, 1, p, p, p, 0, None) == 1
+    assert "alias" in lib.fo_last_error().decode()
+    assert lib.fo_chain_withgradient_sfd(p, p32, None, p32, m, m, 1, p, p48, None, p, 0, None) == 1
+    assert "alias" in lib.fo_last_error().decode()
+    assert lib.fo_chain_withgradient_sfd(p, p32, None, p48, m, m, 1, p, p48, None, p, 0, None) == 1
+    assert "v must not alias" in lib.fo_last_error().decode()
     assert lib.fo_copy(None, None, 16, None) == 1
     assert lib.fo_copy(None, None, 0, None) == 0  # nothing to copy

@@ -1354,17 +1354,16 @@ def test_withgradient_sid_shared_pass(fo, orc, kind, d, with_out, last_mod):
     assert orc.rel_l2(npy(du2.electric).reshape(6, n, n), dv) < 1e-4
 
 
-@pytest.mark.parametrize("kind,d,with_out,weighted,last_mod", [
-    ("AS", 1, False, False, False), ("AS", -1, True, True, False), ("RS", 1, True, True, False),
-    ("AS", 1, True, False, True)])
-def test_withgradient_sfd_shared_pass(fo, orc, kind, d, with_out, weighted, last_mod):
+@pytest.mark.parametrize("kind,n,d,with_out,weighted,last_mod", [
+    ("AS", 256, 1, False, False, False), ("AS", 256, -1, True, True, False), ("RS", 200, 1, True, True, False),
+    ("AS", 256, 1, True, False, True), ("AS", 32, 1, True, True, False), ("AS", 2048, -1, False, True, False)])
+def test_withgradient_sfd_shared_pass(fo, orc, kind, n, d, with_out, weighted, last_mod):
     """fo_chain_withgradient_sfd: the chain's last forward row pass, SquaredFieldDifference,
     its pull-back and the adjoint's first row pass as one pass (or, with a modulator in
     the last slot, as the separate calls).  Gradients and the output field equal the
     separate forward + fo_sfd_forward + fo_sfd_backward + backward calls bit for bit;
     the values c differ only in the order of the sums; both match the oracle."""
     rng = np.random.default_rng(51 if kind == "AS" else 52)
-    n = 256 if kind == "AS" else 200
     lams = [0.64, 0.538, 0.455, 0.64]
     B = len(lams)
     ds = (0.5, 0.5) if kind == "AS" else (1.0, 1.0)
