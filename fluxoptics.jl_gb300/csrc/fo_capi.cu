@@ -629,11 +629,16 @@ int row_pass_sfd_seed(const Layout& L, float2* spec, float2* u_out, const fo_sfd
   return FO_OK;
 }
 
-// Forward sweep, SquaredFieldDifference and the seeded adjoint sweep: as
-// run_withgradient_sid, with the per-field metric of row_pass_sfd_seed.
-int run_withgradient_sfd(const std::vector<fo_prop_plan>& props, float2* w, const float2* u_in, float2* u_out,
-                         float2* du, const Mod* mods_f, const Mod* mods_b, int s, const fo_sfd_s* sfd,
-                         const float2* v, const float* dc, float* c, cudaStream_t st, bool discard_input_grad) {
+// Forward sweep, metric and seeded adjoint sweep in one sequence of passes on the
+// working buffer `w` (the chain scratch for padded layouts, else du): 2K + 1 forward
+// passes and 2K + 1 adjoint passes share one row pass, `shared_pass(w)`, which ends the
+// forward sweep with the metric and starts the adjoint sweep with its seed.  mods_f /
+// mods_b are the forward and adjoint descriptions of the K + 1 slots; the last slot
+// must be empty.
+template <typename SharedPass>
+int run_withgradient(const std::vector<fo_prop_plan>& props, float2* w, const float2* u_in, float2* du,
+                     const Mod* mods_f, const Mod* mods_b, int s, cudaStream_t st, bool discard_input_grad,
+                     SharedPass&& shared_pass) {
   const int K = (int)props.size();
   const Layout L = layout_of(props[0]);
   const float* il = props[0]->inv_lambda;
@@ -644,38 +649,7 @@ int run_withgradient_sfd(const std::vector<fo_prop_plan>& props, float2* w, cons
     FO_TRY(col_pass(props[k], w, s < 0, st));
     if (k + 1 < K) FO_TRY(row_pass(L, w, w, true, true, mods_f[k + 1], false, sf, il, nullptr, tw, st));
   }
-  FO_TRY(row_pass_sfd_seed(L, w, u_out, sfd, v, dc, c, tw, st));
-  for (int k = K - 1; k >= 0; --k) {
-    FO_TRY(col_pass(props[k], w, s > 0, st));
-    if (k > 0)
-      FO_TRY(row_pass(L, w, w, true, true, mods_b[k], true, sf, il, nullptr, tw, st));
-    else
-      FO_TRY(row_pass(L, w, discard_input_grad ? nullptr : du, true, false, mods_b[0], true, sf, il, nullptr, tw,
-                      st));
-  }
-  return FO_OK;
-}
-
-// Forward sweep, SquaredIntensityDifference and the seeded adjoint sweep in one
-// sequence of passes on the working buffer `w` (the chain scratch for padded layouts,
-// else du): 2K + 1 forward passes and 2K + 1 adjoint passes share one row pass.
-// mods_f / mods_b are the forward and adjoint descriptions of the K + 1 slots; the last
-// slot must be empty and every target slice must hold the same number of fields.
-int run_withgradient_sid(const std::vector<fo_prop_plan>& props, float2* w, const float2* u_in, float2* u_out,
-                         float2* du, const Mod* mods_f, const Mod* mods_b, int s, const fo_sid_s* sid,
-                         const float* target, float* loss, cudaStream_t st, bool discard_input_grad) {
-  const int K = (int)props.size();
-  const Layout L = layout_of(props[0]);
-  const float* il = props[0]->inv_lambda;
-  const float sf = (float)s;
-  const float2* tw = props[0]->tw_x;
-  FO_TRY(row_pass(L, u_in, w, false, true, mods_f[0], false, sf, il, nullptr, tw, st));
-  for (int k = 0; k < K; ++k) {
-    FO_TRY(col_pass(props[k], w, s < 0, st));
-    if (k + 1 < K) FO_TRY(row_pass(L, w, w, true, true, mods_f[k + 1], false, sf, il, nullptr, tw, st));
-  }
-  FO_TRY(row_pass_sid_seed(L, w, u_out, sid, target, tw, st));
-  FO_LAUNCH(launch_sid_finalize(sid->partials, L.ny, sid->T, loss, st));
+  FO_TRY(shared_pass(L, tw));
   for (int k = K - 1; k >= 0; --k) {
     FO_TRY(col_pass(props[k], w, s > 0, st));
     if (k > 0)
@@ -1666,9 +1640,13 @@ FO_API int fo_chain_withgradient_sid(fo_chain chain, const void* u_in, void* u_o
   }
   float2* d = reinterpret_cast<float2*>(du);
   float2* w = chain->scratch ? chain->scratch : d;
-  return run_withgradient_sid(chain->props, w, reinterpret_cast<const float2*>(u_in),
-                              reinterpret_cast<float2*>(u_out), d, mf.data(), mb.data(), direction, sid, target, loss,
-                              S(stream), discard);
+  cudaStream_t st = S(stream);
+  return run_withgradient(chain->props, w, reinterpret_cast<const float2*>(u_in), d, mf.data(), mb.data(), direction,
+                          st, discard, [&](const Layout& L, const float2* tw) {
+                            FO_TRY(row_pass_sid_seed(L, w, reinterpret_cast<float2*>(u_out), sid, target, tw, st));
+                            FO_LAUNCH(launch_sid_finalize(sid->partials, L.ny, sid->T, loss, st));
+                            return FO_OK;
+                          });
 }
 
 FO_API int fo_chain_withgradient_sfd(fo_chain chain, const void* u_in, void* u_out, void* du,
@@ -1702,10 +1680,12 @@ FO_API int fo_chain_withgradient_sfd(fo_chain chain, const void* u_in, void* u_o
   }
   float2* d = reinterpret_cast<float2*>(du);
   float2* w = chain->scratch ? chain->scratch : d;
-  return run_withgradient_sfd(chain->props, w, reinterpret_cast<const float2*>(u_in),
-                              reinterpret_cast<float2*>(u_out), d, mf.data(), mb.data(), direction, sfd,
-                              reinterpret_cast<const float2*>(v), dc, c, S(stream),
-                              (flags & FO_BWD_DISCARD_INPUT_GRAD) != 0);
+  cudaStream_t st = S(stream);
+  return run_withgradient(chain->props, w, reinterpret_cast<const float2*>(u_in), d, mf.data(), mb.data(), direction,
+                          st, (flags & FO_BWD_DISCARD_INPUT_GRAD) != 0, [&](const Layout& L, const float2* tw) {
+                            return row_pass_sfd_seed(L, w, reinterpret_cast<float2*>(u_out), sfd,
+                                                     reinterpret_cast<const float2*>(v), dc, c, tw, st);
+                          });
 }
 
 FO_API int fo_chain_backward(fo_chain chain, void* du, const fo_mod* mods, int direction, fo_sid sid,
