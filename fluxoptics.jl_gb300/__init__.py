@@ -16,7 +16,8 @@ from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierM
                          reverse, spatial_vectors)
 from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
 from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
-from .modes import gaussian, hermite_gaussian, hermite_gaussian_groups
+from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, gaussian, hermite_gaussian,
+                    hermite_gaussian_groups)
 from .optimisers import (ClampProx, Descent, Fista, IstaProx, Momentum, Nesterov, NoDescent, PointwiseProx,
                          PositiveProx, ProxRule,
                          TVProx, make_rules, setup, tv_denoise_, update_)
@@ -26,7 +27,7 @@ load_library = _capi.load
 
 __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
-    "Forward", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
+    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
