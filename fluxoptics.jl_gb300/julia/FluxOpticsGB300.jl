@@ -18,7 +18,8 @@ Replaces, for CuArray fields:
 - TeaDOE / TeaReflector, FourierPhase / FourierMask, ASPropZ, DotProduct / PowerCoupling
 - SquaredIntensityDifference (src/metrics/squared_intensity_difference.jl:58-90), also
   evaluated inside a chain's last forward pass (forward_with_metric!)
-- SquaredFieldDifference (src/metrics/squared_field_difference.jl:35-61)
+- SquaredFieldDifference (src/metrics/squared_field_difference.jl:35-61), also with the
+  forward sweep, the metric and the adjoint sweep in one call (withgradient!)
 - Fista, ProxRule(Fista, ClampProx) in one pass, ClampProx, IstaProx, PositiveProx and
   TVProx (src/OptimisersExt.jl:33-54, 222-244; src/proximal_operators/clamp_prox.jl:35-37,
   ista_prox.jl:1-56, positive_prox.jl:1-40, tv_prox.jl:94-195) as in-place device steps (fista_step!, gb300_clamp!, gb300_ista!,
