@@ -12,8 +12,9 @@ from .build import build as build_library
 from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierOperator, FourierPhase,
                          FourierWrapper, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
                          RSProp,
-                         ScalarSource, TeaDOE, TeaReflector, backpropagate_, function_to_array, propagate, propagate_,
-                         reverse, spatial_vectors)
+                         ScalarSource, TeaDOE, TeaReflector, backpropagate, backpropagate_, function_to_array,
+                         get_components, get_data, get_source, isbuffered, istrainable, propagate, propagate_,
+                         reverse, spatial_vectors, trainable)
 from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
 from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
 from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, gaussian, hermite_gaussian,
@@ -29,7 +30,8 @@ __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
     "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
-    "TeaReflector", "backpropagate_", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
+    "TeaReflector", "backpropagate", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
+    "istrainable", "trainable", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
     "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "tv_denoise_", "update_",
     "withgradient",

@@ -1183,3 +1183,44 @@ def propagate_(u, p, direction=Forward):
 
 def backpropagate_(dv, p, direction=Forward):
     return p.backpropagate_(dv, direction)
+
+
+def backpropagate(dv, p, direction=Forward):
+    """Out-of-place adjoint (the reference's ``backpropagate``): a new field."""
+    out = dv.copy()
+    p.backpropagate_(out, direction)
+    return out
+
+
+# Accessors of the reference's component API (OpticalComponents.jl:277-340,
+# system/optical_system.jl), as free functions over the objects above.
+
+def trainable(p):
+    """The trainable arrays of a component, {name: tensor} ({} when static); of a
+    system, {component: {name: tensor}} over its source and components."""
+    if isinstance(p, OpticalSystem):
+        parts = ([p.source] if p.source is not None else []) + list(p.components)
+        return {c: c.params() for c in parts if c.params()}
+    return p.params()
+
+
+def istrainable(p):
+    return bool(getattr(p, "trainable", False))
+
+
+def isbuffered(p):
+    return bool(getattr(p, "trainable", False) and getattr(p, "buffered", False))
+
+
+def get_data(p):
+    """A component's parameter array (Phase: phi, Mask: m, TeaDOE: h, AS_BPM: dn, ...)."""
+    return p.get_data()
+
+
+def get_source(p):
+    """The system's ScalarSource, or a source's field."""
+    return p.source if isinstance(p, OpticalSystem) else p.get_source()
+
+
+def get_components(system):
+    return system.get_components()

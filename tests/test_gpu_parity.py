@@ -1452,3 +1452,33 @@ def test_withgradient_sfd_shared_pass(fo, orc, kind, n, d, with_out, weighted, l
     dv, g0 = orc.phase_backward(dv, phis[0], a0, d)
     assert orc.rel_l2(npy(g2[ph2[0]]["phi"]), g0) < GRAD_TOL
     assert orc.rel_l2(npy(du2.electric), dv) < 1e-4
+
+
+def test_component_accessors(fo, orc):
+    """trainable / istrainable / isbuffered / get_data / get_source / get_components and
+    the out-of-place backpropagate (OpticalComponents.jl:277-340)."""
+    rng = np.random.default_rng(61)
+    n = 64
+    u0 = rand_field(rng, (2, n, n))
+    u = fo.ScalarField(u0, (1.0, 1.0), [0.64, 0.455])
+    phi = f32(rng.uniform(0, 6, (n, n)))
+    ph = fo.Phase(u, phi, trainable=True, buffered=True)
+    mk = fo.Mask(u, c64(np.ones((n, n))))
+    p = fo.ASProp(u, 300.0)
+    src = fo.ScalarSource(u)
+    system = src | ph | p | mk
+    assert fo.istrainable(ph) and fo.isbuffered(ph) and not fo.istrainable(mk) and not fo.isbuffered(p)
+    assert set(fo.trainable(ph)) == {"phi"} and fo.trainable(mk) == {}
+    tr = fo.trainable(system)
+    assert list(tr) == [ph] and tr[ph]["phi"] is fo.get_data(ph)
+    assert fo.get_source(system) is src and fo.get_components(system) == [ph, p, mk]
+    assert np.allclose(npy(fo.get_data(ph)), phi)
+    # out-of-place adjoint leaves its input alone and equals the in-place one
+    dv = fo.ScalarField(rand_field(rng, (2, n, n)), (1.0, 1.0), [0.64, 0.455])
+    keep = dv.electric.clone()
+    out = fo.backpropagate(dv, p)
+    assert torch.equal(dv.electric, keep)
+    fo.backpropagate_(dv, p)
+    assert torch.equal(out.electric, dv.electric)
+    ref = orc.asprop(npy(keep), 1.0, 1.0, [0.64, 0.455], 300.0, orc.BACKWARD)
+    assert orc.rel_l2(npy(out.electric), ref) < FIELD_TOL
