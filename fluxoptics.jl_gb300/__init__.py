@@ -10,8 +10,8 @@ from . import _capi
 from ._capi import FluxOpticsError
 from .build import build as build_library
 from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierOperator, FourierPhase,
-                         FourierWrapper, Forward, Mask, OpticalSystem, ParaxialProp, Phase,
-                         RSProp,
+                         FourierWrapper, Forward, Mask, OpticalSystem, PadCropOperator, ParaxialProp, Phase,
+                         RSProp, adjoint, crop, pad,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate, backpropagate_, function_to_array,
                          get_components, get_data, get_source, isbuffered, istrainable, propagate, propagate_,
                          reverse, spatial_vectors, trainable)
@@ -28,9 +28,9 @@ load_library = _capi.load
 
 __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
-    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
+    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
-    "TeaReflector", "backpropagate", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
+    "TeaReflector", "adjoint", "backpropagate", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
     "istrainable", "trainable", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
     "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "tv_denoise_", "update_",

@@ -113,6 +113,8 @@ SIGNATURES = {
     "fo_ista": (_i, [_vp, C.c_longlong, C.c_double, C.c_double, _vp]),
     "fo_positive": (_i, [_vp, C.c_longlong, _vp]),
     "fo_rule_step": (_i, [_vp, _vp, _vp, C.c_longlong, _i, C.c_double, C.c_double, _vp]),
+    "fo_pad": (_i, [_vp, _i, _i, _vp, _i, _i, _i, _i, _i, C.c_double, C.c_double, _vp]),
+    "fo_crop": (_i, [_vp, _i, _i, _vp, _i, _i, _i, _i, _i, _vp]),
     "fo_sfd_create": (_i, [C.POINTER(_vp), _i, _i, _i]),
     "fo_sfd_forward": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "fo_sfd_backward": (_i, [_vp, _vp, _vp, _vp, _vp, _vp]),

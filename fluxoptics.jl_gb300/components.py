@@ -769,6 +769,163 @@ class FieldProbe(Component):
         return u
 
 
+# ---------------------------------------------------------------------------
+# Padding and cropping
+# ---------------------------------------------------------------------------
+
+def _grid_of(u):
+    """(tensor, rebuild) for a ScalarField or a CUDA complex tensor of shape (..., ny, nx)."""
+    if isinstance(u, ScalarField):
+        return u.electric, lambda t: u.set_field_data(t)
+    if isinstance(u, torch.Tensor) and u.is_cuda and u.dtype == torch.complex64:
+        return u.contiguous(), lambda t: t
+    raise TypeError("pad / crop take a ScalarField or a CUDA complex64 tensor")
+
+
+def _pad_into(src, dst, offset, fill):
+    ny, nx = src.shape[-2:]
+    py, px = dst.shape[-2:]
+    batch = src.numel() // (nx * ny)
+    fill = complex(fill)
+    _capi.call("fo_pad", _ptr(src), nx, ny, _ptr(dst), px, py, batch, int(offset[0]), int(offset[1]), fill.real,
+               fill.imag, _stream())
+
+
+def _crop_into(src, dst, offset):
+    py, px = src.shape[-2:]
+    ny, nx = dst.shape[-2:]
+    batch = dst.numel() // (nx * ny)
+    _capi.call("fo_crop", _ptr(src), px, py, _ptr(dst), nx, ny, batch, int(offset[0]), int(offset[1]), _stream())
+
+
+def pad(u, ns, offset=(0, 0), pad_val=0):
+    """A new field of size ns = (px, py) (Julia order) holding pad_val, with u placed at
+    the 0-based offset (ox, oy) (utilities/pad_crop_operators.jl:18-59)."""
+    t, rebuild = _grid_of(u)
+    out = torch.empty(tuple(t.shape[:-2]) + (int(ns[1]), int(ns[0])), dtype=torch.complex64, device=t.device)
+    _pad_into(t, out, offset, pad_val)
+    return rebuild(out)
+
+
+def crop(u, ns, offset=(0, 0)):
+    """The block of size ns = (nx, ny) at the 0-based offset (ox, oy) of u
+    (utilities/pad_crop_operators.jl:81-120)."""
+    t, rebuild = _grid_of(u)
+    out = torch.empty(tuple(t.shape[:-2]) + (int(ns[1]), int(ns[0])), dtype=torch.complex64, device=t.device)
+    _crop_into(t, out, offset)
+    return rebuild(out)
+
+
+def _padded_size(u_tmp):
+    if isinstance(u_tmp, ScalarField):
+        return (u_tmp.nx, u_tmp.ny)
+    if isinstance(u_tmp, (tuple, list)) and len(u_tmp) == 2 and all(isinstance(v, (int, np.integer)) for v in u_tmp):
+        return (int(u_tmp[0]), int(u_tmp[1]))
+    shape = tuple(u_tmp.shape)
+    if len(shape) < 2:
+        raise ValueError("the padded template needs two spatial dims")
+    return (int(shape[-1]), int(shape[-2]))
+
+
+class PadCropOperator(Component):
+    """Reversible padding of a field into a larger grid (pad_crop_operators.jl:224-356).
+
+    ``PadCropOperator(u, u_tmp; offset, pad_val)`` pads fields of u's grid to the grid of
+    ``u_tmp`` (a ScalarField, an array of shape (..., py, px), or (px, py)) with u at the
+    0-based ``offset`` (ox, oy); ``adjoint()`` gives the operator that crops back.  In the
+    Backward direction the two swap roles, and the pull-back of either is the operation
+    of the reversed direction, as in the reference (for pad_val = 0 this is the exact
+    adjoint).  Inside an OpticalSystem, the components between a padding operator and
+    its cropping partner run on the padded grid (they are built on it, as the reference's
+    ``ASProp(set_field_data(u, u_tmp), z)``).  ``store_ref`` is accepted for the
+    reference's signature; the padded buffers are owned by the system either way."""
+
+    def __init__(self, u, u_tmp, offset=(0, 0), pad_val=0, store_ref=False):
+        self.n = (u.nx, u.ny)
+        self.p = _padded_size(u_tmp)
+        self.offset = (int(offset[0]), int(offset[1]))
+        self.pad_val = complex(pad_val)
+        self.store_ref = bool(store_ref)
+        self.ispad = True
+        if min(self.offset) < 0:
+            raise ValueError("offsets must be non-negative")
+        if self.offset[0] + self.n[0] > self.p[0] or self.offset[1] + self.n[1] > self.p[1]:
+            raise ValueError(f"a {self.n} field at offset {self.offset} does not fit in {self.p}")
+
+    def adjoint(self):
+        c = PadCropOperator.__new__(PadCropOperator)
+        c.__dict__.update(self.__dict__)
+        c.ispad = not self.ispad
+        return c
+
+    def pads(self, direction=Forward):
+        return self.ispad == (int(direction) == int(Forward))
+
+    def pairs_with(self, other):
+        return isinstance(other, PadCropOperator) and (self.n, self.p, self.offset) == (other.n, other.p,
+                                                                                         other.offset)
+
+    def _apply(self, u, padding):
+        want = self.n if padding else self.p
+        if (u.nx, u.ny) != want:
+            raise ValueError(f"PadCropOperator: a {'padding' if padding else 'cropping'} step takes a {want} grid, "
+                             f"got {(u.nx, u.ny)}")
+        return pad(u, self.p, self.offset, self.pad_val) if padding else crop(u, self.n, self.offset)
+
+    def propagate(self, u, direction=Forward):
+        return self._apply(u, self.pads(direction))
+
+    def propagate_(self, u, direction=Forward):
+        raise TypeError("PadCropOperator changes the grid: use propagate, or place it in an OpticalSystem")
+
+    def backpropagate(self, dv, direction=Forward):
+        return self._apply(dv, not self.pads(direction))
+
+
+def adjoint(p):
+    """The reference's ``adjoint(p)`` / ``p'`` for PadCropOperator."""
+    return p.adjoint()
+
+
+class _PaddedSpan:
+    """The components between a padding PadCropOperator and its cropping partner, run
+    as a system on the padded grid: pad u into a padded buffer, run the components in
+    place there, crop back into u.  The adjoint pads the incoming gradient (the crop's
+    pull-back), runs the components' adjoint sweep and crops (the pad's pull-back)."""
+
+    trainable = False
+
+    def __init__(self, pad_op, inner, crop_op, direction, merge):
+        self.pad_op, self.crop_op = pad_op, crop_op
+        self.inner = OpticalSystem(None, inner, direction=direction, merge_components=merge)
+        self._bufs = {}
+
+    def _buf(self, u, key):
+        px, py = self.pad_op.p
+        shape = tuple(u.electric.shape[:-2]) + (py, px)
+        t = self._bufs.get((key, shape))
+        if t is None:
+            t = torch.empty(shape, dtype=torch.complex64, device=u.electric.device)
+            self._bufs[(key, shape)] = t
+        return u.set_field_data(t)
+
+    def forward(self, u, tape, probes):
+        w = self._buf(u, "fwd")
+        _pad_into(u.electric, w.electric, self.pad_op.offset, self.pad_op.pad_val)
+        inner_tape = [] if tape is not None else None
+        self.inner.forward(w, inner_tape, probes=probes)
+        _crop_into(w.electric, u.electric, self.crop_op.offset)
+        if tape is not None:
+            tape.append((self, inner_tape))
+
+    def backward(self, du, inner_tape):
+        dw = self._buf(du, "bwd")
+        _pad_into(du.electric, dw.electric, self.crop_op.offset, self.crop_op.pad_val)
+        grads = self.inner.backward(dw, inner_tape, input_grad=True)
+        _crop_into(dw.electric, du.electric, self.pad_op.offset)
+        return grads
+
+
 def _is_mod(c):
     return isinstance(c, (Phase, Mask, TeaDOE))
 
@@ -848,15 +1005,40 @@ class OpticalSystem:
         if key in cache:
             return cache[key]
         out = []
+        depth = 0  # inside a padded span the components live on another grid: not merged here
         for c in self.components:
+            if isinstance(c, PadCropOperator):
+                depth += 1 if c.pads(self.direction) else -1
+                out.append(c)
+                continue
             prev = out[-1] if out else None
-            m = _merge_pair(prev, c, u) if prev is not None else None
+            m = _merge_pair(prev, c, u) if (prev is not None and depth == 0) else None
             if m is not None:
                 out[-1] = m
             else:
                 out.append(c)
         cache[key] = out
         return out
+
+    def _padded_span(self, comps, i):
+        """The span that starts with the padding operator comps[i]: (span, index of its
+        cropping partner).  Spans nest; each is built once and kept with the system."""
+        depth = 0
+        for k in range(i, len(comps)):
+            c = comps[k]
+            if isinstance(c, PadCropOperator):
+                depth += 1 if c.pads(self.direction) else -1
+                if depth == 0:
+                    if not comps[i].pairs_with(c):
+                        raise ValueError("a PadCropOperator span must end with the operator that undoes its pad")
+                    spans = self.__dict__.setdefault("_spans", {})
+                    key = tuple(id(x) for x in comps[i:k + 1])
+                    sp = spans.get(key)
+                    if sp is None:
+                        sp = _PaddedSpan(comps[i], comps[i + 1:k], c, self.direction, self.merge_components)
+                        spans[key] = sp
+                    return sp, k
+        raise ValueError("a padding PadCropOperator has no cropping partner later in the system")
 
     def segments(self, u: ScalarField):
         """Split the components into fused chains and single components."""
@@ -865,6 +1047,13 @@ class OpticalSystem:
         i, n = 0, len(comps)
         fuse = self.merge_components
         while i < n:
+            if isinstance(comps[i], PadCropOperator):
+                if not comps[i].pads(self.direction):
+                    raise ValueError("a cropping PadCropOperator without a padding one before it")
+                sp, k = self._padded_span(comps, i)
+                segs.append(sp)
+                i = k + 1
+                continue
             if fuse and (_is_mod(comps[i]) or _is_prop(comps[i]) or isinstance(comps[i], FieldProbe)):
                 j = i
                 mods = [None]
@@ -1003,6 +1192,8 @@ class OpticalSystem:
                                _stream())
                 if tape is not None:
                     tape.append((seg, saved))
+            elif isinstance(seg, _PaddedSpan):
+                seg.forward(u, tape, probes)
             else:
                 c = seg
                 if tape is not None and c.trainable and isinstance(c, _Modulator):
@@ -1143,7 +1334,9 @@ class OpticalSystem:
                     sid, u_out = seed
                     sid.backpropagate_into(u_out, du)
                 c = seg
-                if c.trainable and hasattr(c, "backpropagate_with_gradient_"):
+                if isinstance(c, _PaddedSpan):
+                    grads.update(c.backward(du, saved))
+                elif c.trainable and hasattr(c, "backpropagate_with_gradient_"):
                     g = c.get_gradient_buffer()
                     _, gd = c.backpropagate_with_gradient_(du, saved, g, d)
                     grads[c] = gd
@@ -1187,6 +1380,8 @@ def backpropagate_(dv, p, direction=Forward):
 
 def backpropagate(dv, p, direction=Forward):
     """Out-of-place adjoint (the reference's ``backpropagate``): a new field."""
+    if isinstance(p, PadCropOperator):
+        return p.backpropagate(dv, direction)
     out = dv.copy()
     p.backpropagate_(out, direction)
     return out

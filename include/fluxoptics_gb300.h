@@ -176,6 +176,20 @@ FO_API int fo_rsprop_create(fo_prop_plan* plan, int nx, int ny, int batch, doubl
                             const double* lambdas, int n_lambdas, double z, int flags);
 
 /*
+ * Padding and cropping of `batch` fields.  fo_pad writes px x py fields whose values
+ * are pad_re + i pad_im except the nx x ny block whose first element is at column ox,
+ * row oy, which holds the src field; fo_crop writes the nx x ny block at (ox, oy) of
+ * each px x py src field.  The offsets are 0-based (the reference's `offset`).  src and
+ * dst must not overlap.
+ * Replaces: pad! / crop! (src/optical_components/utilities/pad_crop_operators.jl:1-16,
+ * :61-79) as PadOperator / CropOperator and PadCropOperator (:122-356) apply them.
+ */
+FO_API int fo_pad(const void* src, int nx, int ny, void* dst, int px, int py, int batch, int ox, int oy,
+                  double pad_re, double pad_im, void* stream);
+FO_API int fo_crop(const void* src, int px, int py, void* dst, int nx, int ny, int batch, int ox, int oy,
+                   void* stream);
+
+/*
  * Fourier-domain modulators (FourierPhase / FourierMask): u <- IFFT2(w . FFT2(u)) with
  * w = cis(phi) (kind FO_MOD_PHASE) or m (FO_MOD_MASK), the parameter given on the
  * FFT-ordered frequency grid (fftfreq, function_to_array(f, ns, ds, true)); conj(w)

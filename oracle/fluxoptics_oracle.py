@@ -691,6 +691,22 @@ def ista_prox(x, s, c=0.0):
     return x
 
 
+def pad(u, ns, offset=(0, 0), pad_val=0.0):
+    """pad (utilities/pad_crop_operators.jl:1-16, :55-59): an array of size ns = (px, py)
+    (Julia order) filled with pad_val, u copied to the 0-based offset (ox, oy)."""
+    u = np.asarray(u)
+    out = np.full(u.shape[:-2] + (ns[1], ns[0]), pad_val, dtype=np.result_type(u, np.complex128))
+    ny, nx = u.shape[-2:]
+    out[..., offset[1]:offset[1] + ny, offset[0]:offset[0] + nx] = u
+    return out
+
+
+def crop(u, ns, offset=(0, 0)):
+    """crop (pad_crop_operators.jl:61-79, :114-120): the ns = (nx, ny) block at offset."""
+    u = np.asarray(u)
+    return u[..., offset[1]:offset[1] + ns[1], offset[0]:offset[0] + ns[0]].copy()
+
+
 def sfd_value(u, v):
     """SquaredFieldDifference per field: sum over the last two axes of |u - v|^2, with
     no dx dy factor (metrics/squared_field_difference.jl:50-54)."""
