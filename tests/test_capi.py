@@ -111,9 +111,16 @@ def test_bad_arguments_are_rejected(capi):
     assert lib.fo_fista_clamp_step(p, p, p, p, 10, 0.1, p, 1.0, 0.0, None) == 1
     assert "lo must not exceed hi" in lib.fo_last_error().decode()
     assert lib.fo_chain_forward_sid(None, None, None, None, 1, None, None, None, None) == 1
-    # the fused withgradient calls reject aliased fields before touching the chain
     m = (capi.fo_mod * 1)()
     p32, p48 = C.c_void_p(32), C.c_void_p(48)
+    # pad / crop: NULL, aliasing, a block that does not fit, negative offsets
+    assert lib.fo_pad(None, 8, 8, p32, 16, 16, 1, 0, 0, 0.0, 0.0, None) == 1
+    assert lib.fo_pad(p32, 8, 8, p32, 16, 16, 1, 0, 0, 0.0, 0.0, None) == 1
+    assert lib.fo_pad(p, 8, 8, p32, 16, 16, 1, 9, 0, 0.0, 0.0, None) == 2
+    assert "does not fit" in lib.fo_last_error().decode()
+    assert lib.fo_crop(p, 16, 16, p32, 8, 8, 1, -1, 0, None) == 1
+    assert lib.fo_crop(p, 16, 16, p32, 8, 8, 0, 0, 0, None) == 2
+    # the fused withgradient calls reject aliased fields before touching the chain
     assert lib.fo_chain_withgradient_sid(p, p, p32, p32, m, m, 1, p, p, p, 0, None) == 1
     assert lib.fo_chain_withgradient_sid(p, p32, p32, p48, m, m, 1, p, p, p, 0, None) == 1
     assert "alias" in lib.fo_last_error().decode()
