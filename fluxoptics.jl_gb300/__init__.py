@@ -15,7 +15,9 @@ from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierM
                          ScalarSource, TeaDOE, TeaReflector, backpropagate, backpropagate_, function_to_array,
                          get_components, get_data, get_source, isbuffered, istrainable, propagate, propagate_,
                          reverse, spatial_vectors, trainable)
-from .fields import ScalarField, coupling_efficiency, intensity, normalize_power_, power
+from .fields import (ScalarField, coupling_efficiency, dot, get_lambdas, get_lambdas_collection, get_tilts,
+                     get_tilts_collection, intensity, is_on_axis, normalize_power_, offset_tilts_, phase, power,
+                     set_field_data, set_field_ds_, set_field_tilts)
 from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
 from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, gaussian, hermite_gaussian,
                     hermite_gaussian_groups)
@@ -31,7 +33,9 @@ __all__ = [
     "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "adjoint", "backpropagate", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
-    "istrainable", "trainable", "build_library", "coupling_efficiency", "function_to_array", "gaussian",
+    "istrainable", "trainable", "build_library", "coupling_efficiency", "dot", "function_to_array", "get_lambdas", "get_lambdas_collection", "get_tilts",
+    "get_tilts_collection", "is_on_axis", "offset_tilts_", "phase", "set_field_data", "set_field_ds_",
+    "set_field_tilts", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
     "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "tv_denoise_", "update_",
     "withgradient",

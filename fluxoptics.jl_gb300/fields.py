@@ -104,6 +104,79 @@ class ScalarField:
     def is_on_axis(self):
         return not bool(np.any(self.tilts_per_field() != 0.0))
 
+    # -- accessors of the reference (src/Fields.jl:153-300) ----------------------
+    def get_lambdas(self):
+        """The wavelengths as given at construction."""
+        return self.lambdas
+
+    def get_lambdas_collection(self):
+        """One wavelength per field, in memory order."""
+        return self.lambdas_per_field()
+
+    def get_tilts(self):
+        return self.tilts
+
+    def get_tilts_collection(self):
+        """(batch, 2) array of (theta_x, theta_y) per field."""
+        return self.tilts_per_field()
+
+    def set_field_ds_(self, ds):
+        """In-place change of the sampling steps (src/Fields.jl:182-185)."""
+        self.ds = (float(ds[0]), float(ds[1]))
+        return self
+
+    def set_field_tilts(self, tilts):
+        """New field sharing the data with other tilts (src/Fields.jl:243-245)."""
+        return ScalarField(self.electric, self.ds, self.lambdas, tilts)
+
+    def offset_tilts_(self, tilts):
+        """Change the tilts to ``tilts`` and multiply the field by the linear phase
+        cis(2 pi / lambda ((sin tx0 - sin tx) x + (sin ty0 - sin ty) y)) that keeps the
+        physical field unchanged (src/Fields.jl:280-301)."""
+        new = ScalarField(self.electric[..., :1, :1], self.ds, self.lambdas, tilts)
+        t0, t1 = self.tilts_per_field(), new.tilts_per_field()
+        if np.array_equal(t0, t1):
+            return self
+        lam = self.lambdas_per_field()
+        x = (np.arange(self.nx) - (self.nx - 1) / 2.0) * self.ds[0]
+        y = (np.arange(self.ny) - (self.ny - 1) / 2.0) * self.ds[1]
+        ax = 2 * np.pi / lam * (np.sin(t0[:, 0]) - np.sin(t1[:, 0]))
+        ay = 2 * np.pi / lam * (np.sin(t0[:, 1]) - np.sin(t1[:, 1]))
+        ph = ax[:, None, None] * x[None, None, :] + ay[:, None, None] * y[None, :, None]
+        f = torch.polar(torch.ones(ph.shape, dtype=torch.float64), torch.as_tensor(ph)).to(torch.complex64)
+        self.electric.view(-1, self.ny, self.nx).mul_(f.to(self.electric.device))
+        self.tilts = new.tilts
+        return self
+
+    # -- arithmetic (src/Fields.jl:315-337, 392-400, 899-901) --------------------
+    def __add__(self, v):
+        return self.set_field_data(self.electric + v.electric)
+
+    def __sub__(self, v):
+        return self.set_field_data(self.electric - v.electric)
+
+    def __neg__(self):
+        return self.set_field_data(-self.electric)
+
+    def __mul__(self, a):
+        return self.set_field_data(self.electric * a)
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, a):
+        return self.set_field_data(self.electric / a)
+
+    def conj(self):
+        return self.set_field_data(self.electric.conj().resolve_conj())
+
+    def fill_(self, v):
+        """Fill with a number, or copy an array of the field's shape in (src/Fields.jl:392-400)."""
+        if isinstance(v, (int, float, complex)):
+            self.electric.fill_(v)
+        else:
+            self.electric.copy_(torch.as_tensor(np.asarray(v) if not isinstance(v, torch.Tensor) else v))
+        return self
+
 
 def power(u: ScalarField):
     """sum |u|^2 dx dy per field (src/Fields.jl:843-846)."""
@@ -130,3 +203,51 @@ def coupling_efficiency(u: ScalarField, v: ScalarField):
     num = (a.conj() * b).sum(-1).abs() ** 2
     den = (a.abs() ** 2).sum(-1) * (b.abs() ** 2).sum(-1)
     return num / den
+
+
+def phase(u):
+    """angle(u) of a field or an array (src/Fields.jl:667-673)."""
+    return torch.angle(u.electric) if isinstance(u, ScalarField) else torch.angle(torch.as_tensor(u))
+
+
+def dot(u: ScalarField, v: ScalarField):
+    """<u, v> = sum conj(u) v per field, without dx dy (src/Fields.jl:810-815)."""
+    a = u.electric.reshape(-1, u.ny * u.nx)
+    b = v.electric.reshape(-1, v.ny * v.nx)
+    return (a.conj() * b).sum(-1)
+
+
+def get_lambdas(u: ScalarField):
+    return u.get_lambdas()
+
+
+def get_lambdas_collection(u: ScalarField):
+    return u.get_lambdas_collection()
+
+
+def get_tilts(u: ScalarField):
+    return u.get_tilts()
+
+
+def get_tilts_collection(u: ScalarField):
+    return u.get_tilts_collection()
+
+
+def set_field_data(u: ScalarField, data):
+    return u.set_field_data(data)
+
+
+def set_field_ds_(u: ScalarField, ds):
+    return u.set_field_ds_(ds)
+
+
+def set_field_tilts(u: ScalarField, tilts):
+    return u.set_field_tilts(tilts)
+
+
+def offset_tilts_(u: ScalarField, tilts):
+    return u.offset_tilts_(tilts)
+
+
+def is_on_axis(u: ScalarField):
+    return u.is_on_axis()

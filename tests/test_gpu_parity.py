@@ -1584,3 +1584,48 @@ def test_padcrop_operator_backward_direction_and_errors(fo, orc):
         (fo.ScalarSource(up) | fo.adjoint(op) | fo.ASProp(up, 100.0))()  # crops before any pad
     with pytest.raises(ValueError):
         fo.PadCropOperator(u, (40, 64))  # does not fit
+
+
+def test_field_helpers(fo, orc):
+    """ScalarField accessors, offset_tilts_, arithmetic, phase and dot (src/Fields.jl)."""
+    rng = np.random.default_rng(81)
+    n = 32
+    u0 = rand_field(rng, (2, 3, n, n))  # Julia (n, n, 3, 2)
+    lams = np.array([0.64, 0.538, 0.455])
+    u = fo.ScalarField(u0, (0.5, 0.25), lams)
+    assert fo.get_lambdas(u) is lams
+    assert np.array_equal(fo.get_lambdas_collection(u), np.tile(lams, 2))
+    assert fo.is_on_axis(u) and fo.get_tilts(u) == (0.0, 0.0)
+    ut = fo.set_field_tilts(u, (0.01, np.array([0.0, -0.02, 0.03])))
+    assert not fo.is_on_axis(ut) and ut.electric is u.electric
+    tc = fo.get_tilts_collection(ut)
+    assert np.allclose(tc[:, 0], 0.01) and np.allclose(tc[:, 1], np.tile([0.0, -0.02, 0.03], 2))
+    fo.set_field_ds_(ut, (1.0, 2.0))
+    assert ut.ds == (1.0, 2.0) and u.ds == (0.5, 0.25)
+    # offset_tilts_: the carrier moves into the envelope, and back
+    v = u.copy()
+    fo.offset_tilts_(v, (0.01, -0.02))
+    x = (np.arange(n) - (n - 1) / 2) * 0.5
+    y = (np.arange(n) - (n - 1) / 2) * 0.25
+    k = 2 * np.pi / np.tile(lams, 2)
+    ref = u0.reshape(6, n, n) * np.exp(-1j * k[:, None, None] * (np.sin(0.01) * x[None, None, :]
+                                                                  + np.sin(-0.02) * y[None, :, None]))
+    assert orc.rel_l2(npy(v.electric).reshape(6, n, n), ref) < 1e-6
+    assert np.allclose(v.tilts_per_field(), [[0.01, -0.02]] * 6)
+    fo.offset_tilts_(v, (0.0, 0.0))
+    assert orc.rel_l2(npy(v.electric), u0) < 1e-6 and fo.is_on_axis(v)
+    # arithmetic, conj, fill_
+    w = fo.ScalarField(rand_field(rng, (2, 3, n, n)), (0.5, 0.25), lams)
+    assert torch.equal((u + w).electric, u.electric + w.electric)
+    assert torch.equal((u - w).electric, u.electric - w.electric)
+    assert torch.equal((-u).electric, -u.electric)
+    assert torch.equal((2.0 * u).electric, (u * 2.0).electric)
+    assert torch.equal((u / 4.0).electric, u.electric / 4.0)
+    assert np.array_equal(npy(u.conj().electric), np.conj(npy(u.electric)))
+    f = u.copy().fill_(1.5 - 0.5j)
+    assert torch.all(f.electric == complex(1.5, -0.5))
+    # phase and dot (no dx dy factor)
+    assert np.allclose(npy(fo.phase(u)), np.angle(npy(u.electric)), atol=1e-6)
+    d = npy(fo.dot(u, w))
+    ref = np.sum(np.conj(npy(u.electric)) * npy(w.electric), axis=(-2, -1)).reshape(-1)
+    assert np.max(np.abs(d - ref) / np.abs(ref)) < 1e-5
