@@ -18,7 +18,8 @@ from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierM
 from .fields import (ScalarField, coupling_efficiency, dot, get_lambdas, get_lambdas_collection, get_tilts,
                      get_tilts_collection, intensity, is_on_axis, normalize_power_, offset_tilts_, phase, power,
                      set_field_data, set_field_ds_, set_field_tilts)
-from .metrics import DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference, withgradient
+from .metrics import (DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference,
+                      backpropagate_metric, compute_metric, withgradient)
 from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, gaussian, hermite_gaussian,
                     hermite_gaussian_groups)
 from .optimisers import (ClampProx, Descent, Fista, IstaProx, Momentum, Nesterov, NoDescent, PointwiseProx,
@@ -32,7 +33,7 @@ __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
     "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
-    "TeaReflector", "adjoint", "backpropagate", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
+    "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
     "istrainable", "trainable", "build_library", "coupling_efficiency", "dot", "function_to_array", "get_lambdas", "get_lambdas_collection", "get_tilts",
     "get_tilts_collection", "is_on_axis", "offset_tilts_", "phase", "set_field_data", "set_field_ds_",
     "set_field_tilts", "gaussian",

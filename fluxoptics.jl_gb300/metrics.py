@@ -153,6 +153,17 @@ class PowerCoupling(_Overlap):
     power = 1
 
 
+def compute_metric(metric, u: ScalarField):
+    """The metric's values on u (metrics/Metrics.jl: compute_metric, the callable form)."""
+    return metric(u)
+
+
+def backpropagate_metric(metric, u: ScalarField, dc=None):
+    """The metric's pull-back: the gradient with respect to u of sum(dc * c)
+    (metrics/Metrics.jl: backpropagate_metric), as a new field."""
+    return metric.backpropagate(u, dc)
+
+
 def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     """Loss sum(dc * c) (dc = 1 by default) and the gradients of every trainable
     component, through the hand-written adjoint (the GPU counterpart of

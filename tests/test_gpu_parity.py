@@ -1629,3 +1629,19 @@ def test_field_helpers(fo, orc):
     d = npy(fo.dot(u, w))
     ref = np.sum(np.conj(npy(u.electric)) * npy(w.electric), axis=(-2, -1)).reshape(-1)
     assert np.max(np.abs(d - ref) / np.abs(ref)) < 1e-5
+
+
+def test_metric_free_functions(fo, orc):
+    """compute_metric / backpropagate_metric (metrics/Metrics.jl) equal the callable
+    form and the pull-back, for SquaredFieldDifference and DotProduct."""
+    rng = np.random.default_rng(82)
+    u0, v0 = rand_field(rng, (3, 32, 32)), rand_field(rng, (3, 32, 32))
+    u = fo.ScalarField(u0, (1.0, 1.0), 0.64)
+    v = fo.ScalarField(v0, (1.0, 1.0), 0.64)
+    m = fo.SquaredFieldDifference(v)
+    assert np.allclose(npy(fo.compute_metric(m, u)), orc.sfd_value(u0, v0), rtol=1e-5)
+    w = torch.tensor([1.0, 2.0, 0.5], device="cuda")
+    du = fo.backpropagate_metric(m, u, w)
+    assert orc.rel_l2(npy(du.electric), orc.sfd_backward(u0, v0, [1.0, 2.0, 0.5])) < 1e-6
+    d = fo.DotProduct(v)
+    assert torch.equal(fo.compute_metric(d, u).clone(), d(u).clone())
