@@ -10,10 +10,10 @@ from . import _capi
 from ._capi import FluxOpticsError
 from .build import build as build_library
 from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierOperator, FourierPhase,
-                         FourierWrapper, Forward, Mask, OpticalSystem, PadCropOperator, ParaxialProp, Phase,
+                         FourierWrapper, Forward, Mask, OpticalSequence, OpticalSystem, PadCropOperator, ParaxialProp, Phase,
                          RSProp, adjoint, crop, pad,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate, backpropagate_, function_to_array,
-                         get_components, get_data, get_source, isbuffered, istrainable, propagate, propagate_,
+                         get_components, get_data, get_sequence, get_source, isbuffered, istrainable, propagate, propagate_,
                          reverse, spatial_vectors, trainable)
 from .fields import (ScalarField, coupling_efficiency, dot, get_lambdas, get_lambdas_collection, get_tilts,
                      get_tilts_collection, intensity, is_on_axis, normalize_power_, offset_tilts_, phase, power,
@@ -31,9 +31,9 @@ load_library = _capi.load
 
 __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
-    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
+    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSequence", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
-    "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_source", "isbuffered",
+    "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_sequence", "get_source", "isbuffered",
     "istrainable", "trainable", "build_library", "coupling_efficiency", "dot", "function_to_array", "get_lambdas", "get_lambdas_collection", "get_tilts",
     "get_tilts_collection", "is_on_axis", "offset_tilts_", "phase", "set_field_data", "set_field_ds_",
     "set_field_tilts", "gaussian",

@@ -752,10 +752,53 @@ class FourierOperator(Component):
                 lib.fo_prop_destroy(h)
 
 
+class OpticalSequence(Component):
+    """Components applied as one (system/optical_sequence.jl:54-137): in order for the
+    Forward direction and in reverse order for the Backward direction, each with that
+    direction.  Inside an OpticalSystem the sequence is expanded that way before the
+    components are fused, so it costs nothing over listing its components."""
+
+    def __init__(self, *components):
+        self.components = list(components)
+        self.trainable = any(getattr(c, "trainable", False) for c in self.components)
+        self._systems = {}
+
+    def get_sequence(self):
+        return tuple(self.components)
+
+    def expanded(self, direction=Forward):
+        seq = self.components if int(direction) == int(Forward) else list(reversed(self.components))
+        out = []
+        for c in seq:
+            out.extend(c.expanded(direction) if isinstance(c, OpticalSequence) else [c])
+        return out
+
+    def __len__(self):
+        return len(self.expanded())
+
+    def propagate_(self, u, direction=Forward):
+        s = self._systems.get(int(direction))
+        if s is None:
+            s = OpticalSystem(None, [self], direction=direction)
+            self._systems[int(direction)] = s
+        return s.forward(u)
+
+    def backpropagate_(self, dv, direction=Forward):
+        for c in reversed(self.expanded(direction)):
+            c.backpropagate_(dv, direction)
+        return dv
+
+
+def get_sequence(p):
+    """The components of a sequence (optical_sequence.jl: get_sequence)."""
+    return p.get_sequence()
+
+
 def FourierWrapper(u, *components):
     """FFT, the components on the spectrum, inverse FFT (fourier/fourier_wrapper.jl:1-42),
-    as a source-less system to pipe into another."""
-    return OpticalSystem(None, [FourierOperator(u, True), *components, FourierOperator(u, False)])
+    as an OpticalSequence (reversed, with each part's Backward form, in the Backward
+    direction)."""
+    return OpticalSequence(FourierOperator(u, True), *components, FourierOperator(u, False))
 
 
 class FieldProbe(Component):
@@ -990,6 +1033,14 @@ class OpticalSystem:
     def get_components(self):
         return list(self.components)
 
+    def leaf_components(self):
+        """The components with every OpticalSequence expanded for the system's direction:
+        the order in which they are applied."""
+        out = []
+        for c in self.components:
+            out.extend(c.expanded(self.direction) if isinstance(c, OpticalSequence) else [c])
+        return out
+
     # -- planning ---------------------------------------------------------------
     def merged_components(self, u: ScalarField):
         """The components after the reference's merge rules (system/merge_rules.jl:1-80),
@@ -1006,7 +1057,7 @@ class OpticalSystem:
             return cache[key]
         out = []
         depth = 0  # inside a padded span the components live on another grid: not merged here
-        for c in self.components:
+        for c in self.leaf_components():
             if isinstance(c, PadCropOperator):
                 depth += 1 if c.pads(self.direction) else -1
                 out.append(c)
@@ -1042,7 +1093,7 @@ class OpticalSystem:
 
     def segments(self, u: ScalarField):
         """Split the components into fused chains and single components."""
-        comps = self.merged_components(u) if self.merge_components else self.components
+        comps = self.merged_components(u) if self.merge_components else self.leaf_components()
         segs = []
         i, n = 0, len(comps)
         fuse = self.merge_components
@@ -1393,8 +1444,9 @@ def backpropagate(dv, p, direction=Forward):
 def trainable(p):
     """The trainable arrays of a component, {name: tensor} ({} when static); of a
     system, {component: {name: tensor}} over its source and components."""
-    if isinstance(p, OpticalSystem):
-        parts = ([p.source] if p.source is not None else []) + list(p.components)
+    if isinstance(p, (OpticalSystem, OpticalSequence)):
+        leaves = p.leaf_components() if isinstance(p, OpticalSystem) else p.expanded()
+        parts = ([p.source] if getattr(p, "source", None) is not None else []) + leaves
         return {c: c.params() for c in parts if c.params()}
     return p.params()
 

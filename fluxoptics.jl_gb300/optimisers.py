@@ -255,7 +255,7 @@ def setup(rules, model_or_default=None, model=None):
     if not isinstance(rules, dict):
         default, rules = rules, {}
     st = OptState()
-    comps = list(model.components)
+    comps = model.leaf_components()
     if model.source is not None:
         comps = [model.source] + comps
     for c in comps:

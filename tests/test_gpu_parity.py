@@ -376,6 +376,45 @@ def test_fourier_operator_and_wrapper(fo, orc):
     assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
 
 
+def test_fourier_wrapper_backward_direction(fo, orc):
+    """A sequence runs in reverse in the Backward direction, each part with its Backward
+    form (optical_sequence.jl:54-70): FourierWrapper(u, Phase) in a Backward system is
+    IFFT(cis(-phi) FFT(u)), with the phase gradient of that order.  Also get_sequence,
+    a standalone sequence in both directions, and trainable(system) through it."""
+    rng = np.random.default_rng(46)
+    n = 64
+    lams = [0.64, 0.538]
+    v0 = rand_field(rng, (2, n, n))
+    target = f32(rng.uniform(0, 2, (n, n)))
+    phi = f32(rng.uniform(0, 6, (n, n)))
+    uu = fo.ScalarField(v0, (0.5, 0.5), lams)
+    ph = fo.Phase(uu, phi, trainable=True)
+    fw = fo.FourierWrapper(uu, ph)
+    assert len(fo.get_sequence(fw)) == 3 and fo.get_sequence(fw)[1] is ph
+    system = fo.OpticalSystem(fo.ScalarSource(uu), [fw], direction=fo.Backward)
+    assert list(fo.trainable(system)) == [ph]
+    X = np.fft.fft2(v0)
+    out = np.fft.ifft2(orc.phase_forward(X, phi, orc.BACKWARD))
+    assert orc.rel_l2(npy(system()["out"].electric), out) < 1e-6
+    metric = fo.SquaredIntensityDifference((uu, target))
+    loss, grads = fo.withgradient(metric, system)
+    c_ref, _ = orc.sid_value(out, target)
+    assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+    dY = np.fft.fft2(orc.sid_backward(out, target)) / (n * n)  # adjoint of the inverse transform
+    _, gphi = orc.phase_backward(dY, phi, X, orc.BACKWARD)
+    assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+    # standalone: Forward and Backward, and the sequence's adjoint
+    seq = fo.OpticalSequence(fo.ASProp(uu, 100.0), fo.Phase(uu, phi))
+    a = fo.propagate(uu, seq, fo.Forward)
+    assert orc.rel_l2(npy(a.electric), orc.phase_forward(orc.asprop(v0, 0.5, 0.5, lams, 100.0), phi)) < FIELD_TOL
+    b = fo.propagate(uu, seq, fo.Backward)
+    ref_b = orc.asprop(orc.phase_forward(v0, phi, orc.BACKWARD), 0.5, 0.5, lams, 100.0, orc.BACKWARD)
+    assert orc.rel_l2(npy(b.electric), ref_b) < FIELD_TOL
+    g = fo.backpropagate(uu, seq, fo.Forward)
+    ref_g = orc.asprop(orc.phase_forward(v0, phi, orc.BACKWARD), 0.5, 0.5, lams, 100.0, orc.BACKWARD)
+    assert orc.rel_l2(npy(g.electric), ref_g) < FIELD_TOL
+
+
 @pytest.mark.parametrize("selective", [True, False])
 def test_dot_product_power_coupling(fo, orc, selective):
     """DotProduct and PowerCoupling (values and pull-backs) against the oracle, and
