@@ -1200,12 +1200,13 @@ struct RowShape {
   }
 };
 
-// Whether pass launches carry the programmatic-dependent-launch attribute (FO_PDL=1 enables).
-bool pdl_enabled();
+// Whether a pass over field_bytes of fields is launched with the programmatic-dependent-
+// launch attribute (small passes; FO_PDL=1 / 0 force it for all).
+bool pdl_for(long long field_bytes);
 
 template <typename... KArgs, typename... Args>
-inline cudaError_t launch_pass(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                               Args&&... args) {
+inline cudaError_t launch_pass(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                               cudaStream_t s, Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -1215,7 +1216,7 @@ inline cudaError_t launch_pass(void (*kernel)(KArgs...), dim3 grid, dim3 block, 
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
@@ -1232,6 +1233,7 @@ template <int N, int E, int LANES>
 cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_t s, int staging) {
   using SH = RowShape<N, E, LANES>;
   dim3 grid((a.batch + a.fields_per_cta - 1) / a.fields_per_cta, (a.nrows + LANES - 1) / LANES);
+  const bool pdl = pdl_for((long long)a.batch * a.nrows * N * (long long)sizeof(float2));
   const bool grad = a.mod_bwd && a.grad != nullptr && a.mod_kind != MOD_NONE;
   const bool sid = a.sid_partials != nullptr;  // GK 3 (no staging)
   const bool pf = staging == 1;
@@ -1242,10 +1244,10 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
   do {                                                                                            \
     if (full) {                                                                                   \
       e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV, true>, smem);                            \
-      if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, true>, grid, dim3(SH::threads), smem, s, a, tw); \
+      if (e == cudaSuccess) e = launch_pass(pdl, row_pass_kernel<N, E, LANES, GK, PFV, true>, grid, dim3(SH::threads), smem, s, a, tw); \
     } else {                                                                                      \
       e = set_smem(row_pass_kernel<N, E, LANES, GK, PFV, false>, smem);                           \
-      if (e == cudaSuccess) e = launch_pass(row_pass_kernel<N, E, LANES, GK, PFV, false>, grid, dim3(SH::threads), smem, s, a, tw); \
+      if (e == cudaSuccess) e = launch_pass(pdl, row_pass_kernel<N, E, LANES, GK, PFV, false>, grid, dim3(SH::threads), smem, s, a, tw); \
     }                                                                                             \
   } while (0)
   if (a.sfd_rows) {
@@ -1254,11 +1256,11 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
     if (full) {
       e = set_smem(row_pass_kernel<N, E, LANES, 5, false, true>, smem5);
       if (e == cudaSuccess)
-        e = launch_pass(row_pass_kernel<N, E, LANES, 5, false, true>, grid, dim3(SH::threads), smem5, s, a, tw);
+        e = launch_pass(pdl, row_pass_kernel<N, E, LANES, 5, false, true>, grid, dim3(SH::threads), smem5, s, a, tw);
     } else {
       e = set_smem(row_pass_kernel<N, E, LANES, 5, false, false>, smem5);
       if (e == cudaSuccess)
-        e = launch_pass(row_pass_kernel<N, E, LANES, 5, false, false>, grid, dim3(SH::threads), smem5, s, a, tw);
+        e = launch_pass(pdl, row_pass_kernel<N, E, LANES, 5, false, false>, grid, dim3(SH::threads), smem5, s, a, tw);
     }
   } else if (sid && a.seed_dst) {
     FO_ROW_GO(4, false);
@@ -1268,11 +1270,11 @@ cudaError_t row_launch_shape(const RowPassArgs& a, const float2* tw, cudaStream_
     if (full) {
       e = set_smem(row_pass_kernel<N, E, LANES, 0, false, true, true>, smem);
       if (e == cudaSuccess)
-        e = launch_pass(row_pass_kernel<N, E, LANES, 0, false, true, true>, grid, dim3(SH::threads), smem, s, a, tw);
+        e = launch_pass(pdl, row_pass_kernel<N, E, LANES, 0, false, true, true>, grid, dim3(SH::threads), smem, s, a, tw);
     } else {
       e = set_smem(row_pass_kernel<N, E, LANES, 0, false, false, true>, smem);
       if (e == cudaSuccess)
-        e = launch_pass(row_pass_kernel<N, E, LANES, 0, false, false, true>, grid, dim3(SH::threads), smem, s, a, tw);
+        e = launch_pass(pdl, row_pass_kernel<N, E, LANES, 0, false, false, true>, grid, dim3(SH::threads), smem, s, a, tw);
     }
   } else if (!grad) {
     if (pf) FO_ROW_GO(0, true); else FO_ROW_GO(0, false);
@@ -1298,6 +1300,7 @@ template <int N, int E, int W, int P>
 cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_t s, bool pf) {
   constexpr int threads = (W / (P == 2 ? 2 : 1)) * (N / E);
   dim3 grid(a.n_items, (a.ncols + W - 1) / W);
+  const bool pdl = pdl_for((long long)a.batch * a.ncols * N * (long long)sizeof(float2));
   const bool full = a.y_in == N && a.y_out == N && a.ncols % W == 0;
   cudaError_t e;
 #define FO_COL_GO(PFV, HSV)                                                                     \
@@ -1305,13 +1308,13 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     constexpr size_t smem = col_smem<N, W>(PFV, HSV);                                           \
     if constexpr (P == 2) {                                                                     \
       e = set_smem(col_pass2_kernel<N, E, W, PFV, HSV>, smem);                                  \
-      if (e == cudaSuccess) e = launch_pass(col_pass2_kernel<N, E, W, PFV, HSV>, grid, dim3(threads), smem, s, a, tw); \
+      if (e == cudaSuccess) e = launch_pass(pdl, col_pass2_kernel<N, E, W, PFV, HSV>, grid, dim3(threads), smem, s, a, tw); \
     } else if (full) {                                                                          \
       e = set_smem(col_pass_kernel<N, E, W, PFV, HSV, true>, smem);                             \
-      if (e == cudaSuccess) e = launch_pass(col_pass_kernel<N, E, W, PFV, HSV, true>, grid, dim3(threads), smem, s, a, tw); \
+      if (e == cudaSuccess) e = launch_pass(pdl, col_pass_kernel<N, E, W, PFV, HSV, true>, grid, dim3(threads), smem, s, a, tw); \
     } else {                                                                                    \
       e = set_smem(col_pass_kernel<N, E, W, PFV, HSV, false>, smem);                            \
-      if (e == cudaSuccess) e = launch_pass(col_pass_kernel<N, E, W, PFV, HSV, false>, grid, dim3(threads), smem, s, a, tw); \
+      if (e == cudaSuccess) e = launch_pass(pdl, col_pass_kernel<N, E, W, PFV, HSV, false>, grid, dim3(threads), smem, s, a, tw); \
     }                                                                                           \
   } while (0)
   if constexpr (P == 4 || P == 6) {
@@ -1329,7 +1332,7 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     if (!a.tmap_buf || !a.tmap_h) return cudaErrorInvalidValue;
     if (a.units) grid = dim3(a.persistent ? std::min(a.persistent, a.n_units) : a.n_units, 1);
     if (e == cudaSuccess)
-      e = launch_pass(col_tma_kernel<N, E, W, TWR>, grid, dim3(threads), smem_t, s, a, tw,
+      e = launch_pass(pdl, col_tma_kernel<N, E, W, TWR>, grid, dim3(threads), smem_t, s, a, tw,
                       *reinterpret_cast<const CUtensorMap*>(a.tmap_buf),
                       *reinterpret_cast<const CUtensorMap*>(a.tmap_h));
   } else if constexpr (P == 0) {
@@ -1339,10 +1342,10 @@ cudaError_t col_launch_shape(const ColPassArgs& a, const float2* tw, cudaStream_
     (void)pf;
     if constexpr (smem_hs <= kMaxSmemPerCta) {
       e = set_smem(col_lane_kernel<N, E, W, true>, smem_hs);
-      if (e == cudaSuccess) e = launch_pass(col_lane_kernel<N, E, W, true>, grid, dim3(threads), smem_hs, s, a, tw);
+      if (e == cudaSuccess) e = launch_pass(pdl, col_lane_kernel<N, E, W, true>, grid, dim3(threads), smem_hs, s, a, tw);
     } else {
       e = set_smem(col_lane_kernel<N, E, W, false>, smem_nohs);
-      if (e == cudaSuccess) e = launch_pass(col_lane_kernel<N, E, W, false>, grid, dim3(threads), smem_nohs, s, a, tw);
+      if (e == cudaSuccess) e = launch_pass(pdl, col_lane_kernel<N, E, W, false>, grid, dim3(threads), smem_nohs, s, a, tw);
     }
   } else if (pf) {
     if constexpr (col_smem<N, W>(true, true) <= kMaxSmemPerCta) FO_COL_GO(true, true);

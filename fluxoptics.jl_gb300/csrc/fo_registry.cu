@@ -61,16 +61,20 @@ constexpr size_t kMaxSmem = 227 * 1024;
 
 bool fft_size_supported(int n) { return table_for(n, true).n > 0; }
 
-// Off by default: with the whole iteration captured as one graph, programmatic
-// edges between the passes measured slower (16.8 vs 15.4 ms for 2048^2 x 48 fields,
-// three propagations forward and back) and only the launch-bound BPM march
-// gained (about 2 %).  FO_PDL=1 turns it on.
-bool pdl_enabled() {
-  static const bool on = [] {
+// Programmatic dependent launch lets a pass start while the previous one drains; every
+// pass kernel waits for its predecessor (griddepcontrol.wait) before touching memory.
+// It pays for small passes, whose launch latency it hides (a 512^2 RSProp chain on
+// 1024^2 grids: 62.1 vs 58.5 k propagations/s), and costs large ones (2048^2 x 48
+// fields: 12.17 vs 10.52 ms per iteration).  So it is used for passes over at most
+// kPdlMaxBytes of fields; FO_PDL=1 / FO_PDL=0 force it on / off for every pass.
+constexpr long long kPdlMaxBytes = 32LL << 20;
+
+bool pdl_for(long long field_bytes) {
+  static const int mode = [] {
     const char* v = getenv("FO_PDL");
-    return v && v[0] == '1';
+    return !v || !*v ? -1 : (v[0] == '1' ? 1 : 0);
   }();
-  return on;
+  return mode < 0 ? field_bytes <= kPdlMaxBytes : mode == 1;
 }
 
 int row_variant_count(int N) { return table_for(N, true).n; }
