@@ -17,7 +17,7 @@ from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierM
                          reverse, spatial_vectors, trainable)
 from .fields import (ScalarField, coupling_efficiency, dot, get_lambdas, get_lambdas_collection, get_tilts,
                      get_tilts_collection, intensity, is_on_axis, normalize_power_, offset_tilts_, phase, power,
-                     set_field_data, set_field_ds_, set_field_tilts)
+                     select_lambdas, select_tilts, set_field_data, set_field_ds_, set_field_tilts)
 from .metrics import (DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference,
                       backpropagate_metric, compute_metric, withgradient)
 from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, gaussian, hermite_gaussian,
@@ -35,7 +35,7 @@ __all__ = [
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_sequence", "get_source", "isbuffered",
     "istrainable", "trainable", "build_library", "coupling_efficiency", "dot", "function_to_array", "get_lambdas", "get_lambdas_collection", "get_tilts",
-    "get_tilts_collection", "is_on_axis", "offset_tilts_", "phase", "set_field_data", "set_field_ds_",
+    "get_tilts_collection", "is_on_axis", "offset_tilts_", "phase", "select_lambdas", "select_tilts", "set_field_data", "set_field_ds_",
     "set_field_tilts", "gaussian",
     "hermite_gaussian", "hermite_gaussian_groups", "intensity", "load_library", "make_rules",
     "normalize_power_", "power", "propagate", "propagate_", "reverse", "setup", "spatial_vectors", "tv_denoise_", "update_",

@@ -120,6 +120,17 @@ class ScalarField:
         """(batch, 2) array of (theta_x, theta_y) per field."""
         return self.tilts_per_field()
 
+    def select_lambdas(self):
+        """A function of is_collection giving the per-field wavelengths or the
+        wavelengths as given (src/Fields.jl:161-166)."""
+        return lambda is_collection: self.get_lambdas_collection() if is_collection else self.get_lambdas()
+
+    def select_tilts(self):
+        """(select_x, select_y): each a function of is_collection giving the per-field
+        tilt angles or the angles as given (src/Fields.jl:176-180)."""
+        tc = self.get_tilts_collection()
+        return tuple((lambda is_collection, k=k: tc[:, k] if is_collection else self.tilts[k]) for k in range(2))
+
     def set_field_ds_(self, ds):
         """In-place change of the sampling steps (src/Fields.jl:182-185)."""
         self.ds = (float(ds[0]), float(ds[1]))
@@ -231,6 +242,14 @@ def get_tilts(u: ScalarField):
 
 def get_tilts_collection(u: ScalarField):
     return u.get_tilts_collection()
+
+
+def select_lambdas(u: ScalarField):
+    return u.select_lambdas()
+
+
+def select_tilts(u: ScalarField):
+    return u.select_tilts()
 
 
 def set_field_data(u: ScalarField, data):

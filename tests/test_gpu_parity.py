@@ -1639,6 +1639,10 @@ def test_field_helpers(fo, orc):
     assert not fo.is_on_axis(ut) and ut.electric is u.electric
     tc = fo.get_tilts_collection(ut)
     assert np.allclose(tc[:, 0], 0.01) and np.allclose(tc[:, 1], np.tile([0.0, -0.02, 0.03], 2))
+    sel = fo.select_lambdas(u)
+    assert sel(False) is lams and np.array_equal(sel(True), np.tile(lams, 2))
+    sx, sy = fo.select_tilts(ut)
+    assert sx(False) == 0.01 and np.allclose(sy(True), np.tile([0.0, -0.02, 0.03], 2))
     fo.set_field_ds_(ut, (1.0, 2.0))
     assert ut.ds == (1.0, 2.0) and u.ds == (0.5, 0.25)
     # offset_tilts_: the carrier moves into the envelope, and back
