@@ -20,7 +20,8 @@ from .fields import (ScalarField, coupling_efficiency, dot, get_lambdas, get_lam
                      select_lambdas, select_tilts, set_field_data, set_field_ds_, set_field_tilts)
 from .metrics import (DotProduct, PowerCoupling, SquaredFieldDifference, SquaredIntensityDifference,
                       backpropagate_metric, compute_metric, withgradient)
-from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, gaussian, hermite_gaussian,
+from .modes import (Gaussian, Gaussian1D, HermiteGaussian, HermiteGaussian1D, LaguerreGaussian, gaussian,
+                    hermite_gaussian,
                     hermite_gaussian_groups)
 from .optimisers import (ClampProx, Descent, Fista, IstaProx, Momentum, Nesterov, NoDescent, PointwiseProx,
                          PositiveProx, ProxRule,
@@ -31,7 +32,7 @@ load_library = _capi.load
 
 __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
-    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSequence", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
+    "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "LaguerreGaussian", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSequence", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_sequence", "get_source", "isbuffered",
     "istrainable", "trainable", "build_library", "coupling_efficiency", "dot", "function_to_array", "get_lambdas", "get_lambdas_collection", "get_tilts",

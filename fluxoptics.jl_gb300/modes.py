@@ -1,11 +1,12 @@
-"""Host-side input generators: Gaussian and Hermite-Gauss modes, at the waist or
-propagated to a distance z (src/modes/gaussian_modes.jl:1-478).
+"""Host-side input generators: Gaussian, Hermite-Gauss and Laguerre-Gauss modes, at the
+waist or propagated to a distance z (src/modes/gaussian_modes.jl).
 
 The mode objects mirror the reference's constructors by their positional arguments:
 
     Gaussian(w0) | Gaussian(w0x, w0y) | Gaussian(w0, lam, z) | Gaussian(w0x, w0y, lam, z)
     HermiteGaussian(w0, m, n) | HermiteGaussian(w0x, w0y, m, n)
     HermiteGaussian(w0, m, n, lam, z) | HermiteGaussian(w0x, w0y, m, n, lam, z)
+    LaguerreGaussian(w0, p, l; kind) | LaguerreGaussian(w0, p, l, lam, z; kind)
 
 and are evaluated on grid vectors: ``mode(x, y)`` returns the (ny, nx) complex128 array
 whose element [j, i] is the mode at (x[i], y[j]) -- the memory layout of the reference's
@@ -171,6 +172,70 @@ class HermiteGaussian(_Mode2D):
         fx = mx.hermite(x) * np.exp(mx.g.exp_arg(x))
         fy = my.hermite(y) * np.exp(my.g.exp_arg(y))
         return c * (fy[:, None] * fx[None, :])
+
+
+def _laguerre(p, l, x):
+    """Generalised Laguerre polynomial L_p^l(x) by its three-term recurrence."""
+    x = np.asarray(x)
+    if p == 0:
+        return np.ones_like(x)
+    a, b = np.ones_like(x), 1.0 + l - x
+    for k in range(2, p + 1):
+        a, b = b, ((2 * k + l - 1 - x) * b - (k + l - 1) * a) / k
+    return b
+
+
+class LaguerreGaussian(_Mode2D):
+    """LG_{p,l} (gaussian_modes.jl:480-640): LaguerreGaussian(w0, p, l) at the waist or
+    LaguerreGaussian(w0, p, l, lam, z) propagated, with the azimuthal factor
+    exp(i l phi) (kind "vortex"), sqrt(2) cos(l phi) ("even") or sqrt(2) sin(l phi)
+    ("odd")."""
+
+    def __init__(self, *args, constant_phase=True, kind="vortex"):
+        if len(args) == 3:
+            w0, p, l = args
+            lam = z = None
+        elif len(args) == 5:
+            w0, p, l, lam, z = args
+        else:
+            raise TypeError("LaguerreGaussian takes (w0, p, l) or (w0, p, l, lam, z)")
+        if int(p) != p or p < 0 or int(l) != l:
+            raise ValueError("p must be a non-negative integer and l an integer")
+        kind = str(kind).lstrip(":")
+        if kind not in ("vortex", "even", "odd"):
+            raise ValueError("kind must be vortex, even or odd")
+        self.w0, self.p, self.l, self.kind = float(w0), int(p), int(l), kind
+        al = abs(self.l)
+        norm = math.sqrt(2.0 * math.factorial(self.p) / (math.pi * math.factorial(self.p + al))) / self.w0
+        self.propagated = lam is not None
+        if not self.propagated:
+            self.C = complex(norm)
+            return
+        lam, z = float(lam), float(z)
+        zr = math.pi * self.w0 ** 2 / lam
+        q0, qz = complex(0.0, -zr), complex(z, -zr)
+        k = 2.0 * math.pi / lam
+        self.wz = self.w0 * math.sqrt(1.0 + (z / zr) ** 2)
+        self.eikz = cmath.exp(1j * k * z) if constant_phase else 1.0 + 0j
+        self.e_arg = 1j * k / (2.0 * qz)
+        self.C = norm * (q0 / qz) * (-qz.conjugate() / qz) ** (self.p + al / 2.0)
+
+    def _angular(self, x, y):
+        phi = np.arctan2(y[:, None], x[None, :])
+        if self.kind == "vortex":
+            return np.exp(1j * self.l * phi)
+        return math.sqrt(2.0) * (np.cos(self.l * phi) if self.kind == "even" else np.sin(self.l * phi))
+
+    def _eval(self, x, y):
+        al = abs(self.l)
+        r2 = y[:, None] ** 2 + x[None, :] ** 2
+        if not self.propagated:
+            s = r2 / self.w0 ** 2
+            v = self.C * (math.sqrt(2.0) * np.sqrt(s)) ** al * _laguerre(self.p, al, 2.0 * s) * np.exp(-s)
+            return v * self._angular(x, y)
+        rl = (math.sqrt(2.0) * np.sqrt(r2) / self.wz) ** al
+        v = self.C * rl * _laguerre(self.p, al, 2.0 * r2 / self.wz ** 2) * np.exp(self.e_arg * r2)
+        return v * self._angular(x, y) * self.eikz
 
 
 def gaussian(w0, x, y):

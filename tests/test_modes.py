@@ -115,3 +115,31 @@ def test_constructor_forms(fo):
         fo.HermiteGaussian(10.0, -1, 0)
     with pytest.raises(ValueError):
         fo.Gaussian(10.0)(grid(8, 1.0), grid(8, 1.0), out=np.zeros((4, 4), np.complex128))
+
+
+def test_laguerre_gaussian_docstring(fo):
+    # gaussian_modes.jl:516-541
+    n, d = 65, 2.0
+    x = y = grid(n, d)
+    f00 = fo.LaguerreGaussian(10.0, 0, 0)(x, y)
+    f01 = fo.LaguerreGaussian(10.0, 0, 1)(x, y)
+    assert np.isclose(np.sum(np.abs(f00) ** 2) * d * d, 1.0)
+    assert abs(f01[n // 2, n // 2]) < 1e-10
+    even = fo.LaguerreGaussian(10.0, 0, 2, kind="even")(x, y)
+    assert np.all(even.imag == 0)
+    # LG00 is the Gaussian; LG modes are orthonormal
+    assert np.max(np.abs(f00 - fo.Gaussian(10.0)(x, y))) < 1e-15
+    modes = [fo.LaguerreGaussian(10.0, p, l)(x, y) for p, l in [(0, 0), (0, 1), (1, 0), (1, -2), (2, 3)]]
+    G = np.array([[np.sum(np.conj(a) * b) * d * d for b in modes] for a in modes])
+    assert np.max(np.abs(G - np.eye(len(modes)))) < 1e-8
+    # even and odd are the real combinations of the +l and -l vortices
+    vp, vm = fo.LaguerreGaussian(10.0, 1, 2)(x, y), fo.LaguerreGaussian(10.0, 1, -2)(x, y)
+    assert np.allclose(fo.LaguerreGaussian(10.0, 1, 2, kind="odd")(x, y), (vp - vm) / (np.sqrt(2) * 1j), atol=1e-14)
+
+
+@pytest.mark.parametrize("p,l", [(0, 1), (1, -2), (2, 1)])
+def test_propagated_laguerre_gaussian_matches_the_angular_spectrum(fo, p, l):
+    N, d, lam, w0, z = 512, 1.0, 1.064, 40.0, 1500.0
+    x = y = grid(N, d)
+    v = orc.asprop(fo.LaguerreGaussian(w0, p, l)(x, y), d, d, lam, z)
+    assert orc.rel_l2(v, fo.LaguerreGaussian(w0, p, l, lam, z)(x, y)) < 2e-4
