@@ -9,7 +9,7 @@ fails loudly when the library cannot be loaded.
 from . import _capi
 from ._capi import FluxOpticsError
 from .build import build as build_library
-from .components import (AS_BPM, ASProp, ASPropZ, Backward, FieldProbe, FourierMask, FourierOperator, FourierPhase,
+from .components import (AS_BPM, ASProp, ASPropZ, Backward, Component, FieldProbe, FourierMask, FourierOperator, FourierPhase,
                          FourierWrapper, Forward, Mask, OpticalSequence, OpticalSystem, PadCropOperator, ParaxialProp, Phase,
                          RSProp, adjoint, crop, pad,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate, backpropagate_, function_to_array,
@@ -31,7 +31,7 @@ from .ragged import RaggedBatch
 load_library = _capi.load
 
 __all__ = [
-    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
+    "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Component", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
     "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "LaguerreGaussian", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSequence", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
     "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_sequence", "get_source", "isbuffered",

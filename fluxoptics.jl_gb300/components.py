@@ -66,7 +66,13 @@ def function_to_array(f, ns, ds, isfourier=False):
 
 
 class Component:
-    """Base of all pipe components."""
+    """Base of all pipe components.  OpticalSystem drives any component through the
+    protocol of the reference's AbstractCustomComponent (OpticalComponents.jl:751-816):
+    ``propagate_(u, d)`` in place and its adjoint ``backpropagate_(dv, d)``; a trainable
+    component also gives ``params()`` ({name: tensor}), ``propagate_and_save_(u, saved,
+    d)`` (``saved`` from ``get_saved_buffer(u)`` when it defines one),
+    ``get_gradient_buffer()`` and ``backpropagate_with_gradient_(dv, saved, grad, d)``,
+    which returns (dv, {name: grad})."""
 
     trainable = False
     buffered = False
@@ -1247,13 +1253,15 @@ class OpticalSystem:
                 seg.forward(u, tape, probes)
             else:
                 c = seg
-                if tape is not None and c.trainable and isinstance(c, _Modulator):
-                    sv = c.get_saved_buffer(u)
-                    c.propagate_and_save_(u, sv, d)
-                    tape.append((c, sv))
-                elif tape is not None and c.trainable and isinstance(c, AS_BPM):
+                if tape is not None and c.trainable and isinstance(c, AS_BPM):
                     c.propagate_and_save_(u, None, d)
                     tape.append((c, None))
+                elif tape is not None and c.trainable and hasattr(c, "propagate_and_save_"):
+                    # the component protocol (OpticalComponents.jl:751-816): a trainable
+                    # component saves what its adjoint needs into its saved buffer
+                    sv = c.get_saved_buffer(u) if hasattr(c, "get_saved_buffer") else None
+                    c.propagate_and_save_(u, sv, d)
+                    tape.append((c, sv))
                 elif isinstance(c, FieldProbe):
                     if probes is not None:
                         probes[c] = u.copy()
@@ -1391,12 +1399,12 @@ class OpticalSystem:
                     g = c.get_gradient_buffer()
                     _, gd = c.backpropagate_with_gradient_(du, saved, g, d)
                     grads[c] = gd
-                elif _is_prop(c) or _is_mod(c) or isinstance(c, (ASPropZ, _FourierModulator, FourierOperator)):
-                    c.backpropagate_(du, d)
                 elif isinstance(c, AS_BPM):
                     c.backpropagate_with_gradient_(du, None, None, d)
                 elif isinstance(c, FieldProbe):
                     pass
+                elif type(c).backpropagate_ is not Component.backpropagate_:
+                    c.backpropagate_(du, d)
                 else:
                     raise NotImplementedError(f"no adjoint for {type(c).__name__}")
             first = False

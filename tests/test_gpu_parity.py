@@ -1688,3 +1688,70 @@ def test_metric_free_functions(fo, orc):
     assert orc.rel_l2(npy(du.electric), orc.sfd_backward(u0, v0, [1.0, 2.0, 0.5])) < 1e-6
     d = fo.DotProduct(v)
     assert torch.equal(fo.compute_metric(d, u).clone(), d(u).clone())
+
+
+def test_user_component_protocol(fo, orc):
+    """A component written by a user against the component protocol (the reference's
+    AbstractCustomComponent, OpticalComponents.jl:751-816) runs inside a system between
+    fused chains, trainable and static: output, loss and both gradients against the
+    oracle."""
+
+    class Amplitude(fo.Component):
+        def __init__(self, a, trainable=False):
+            self.a = torch.tensor(a, dtype=torch.float32, device="cuda")
+            self.trainable = trainable
+
+        def params(self):
+            return {"a": self.a} if self.trainable else {}
+
+        def propagate_(self, u, direction=fo.Forward):
+            u.electric.mul_(self.a)
+            return u
+
+        def backpropagate_(self, dv, direction=fo.Forward):
+            dv.electric.mul_(self.a)
+            return dv
+
+        def get_saved_buffer(self, u):
+            return torch.empty_like(u.electric)
+
+        def propagate_and_save_(self, u, saved, direction=fo.Forward):
+            saved.copy_(u.electric)
+            return self.propagate_(u, direction)
+
+        def get_gradient_buffer(self):
+            return torch.empty_like(self.a)
+
+        def backpropagate_with_gradient_(self, dv, saved, grad, direction=fo.Forward):
+            grad.copy_((dv.electric.conj() * saved).real.reshape(-1, *self.a.shape).sum(0))
+            return self.backpropagate_(dv, direction), {"a": grad}
+
+    rng = np.random.default_rng(83)
+    n, lams, ds = 64, np.array([0.64, 0.455]), (1.0, 1.0)
+    x, y = orc.spatial_vectors((n, n), ds)
+    u0 = c64(np.stack([orc.gaussian(8.0, x, y)] * 2) * (1 + 0.1 * rng.standard_normal((2, n, n))))
+    phi = f32(rng.uniform(0, 6, (n, n)))
+    a = f32(rng.uniform(0.5, 1.5, (n, n)))
+    target = f32(np.abs(orc.gaussian(10.0, x, y)) ** 2)
+    u = fo.ScalarField(u0, ds, lams)
+    for trainable in (True, False):
+        ph = fo.Phase(u, phi, trainable=True)
+        amp = Amplitude(a, trainable)
+        system = fo.ScalarSource(u) | ph | fo.ASProp(u, 300.0) | amp | fo.ASProp(u, 200.0)
+        metric = fo.SquaredIntensityDifference((u, target))
+        loss, grads = fo.withgradient(metric, system)
+        a1 = orc.asprop(orc.phase_forward(u0, phi), 1.0, 1.0, lams, 300.0)
+        out = orc.asprop(a1 * a, 1.0, 1.0, lams, 200.0)
+        assert orc.rel_l2(npy(system()["out"].electric), out) < FIELD_TOL
+        c_ref, _ = orc.sid_value(out, target)
+        assert abs(float(loss) - c_ref.sum()) / c_ref.sum() < 1e-4
+        dv = orc.asprop(orc.sid_backward(out, target), 1.0, 1.0, lams, 200.0, orc.BACKWARD)
+        ga = np.sum(np.real(np.conj(dv) * a1), axis=0)
+        dv = orc.asprop(dv * a, 1.0, 1.0, lams, 300.0, orc.BACKWARD)
+        _, gphi = orc.phase_backward(dv, phi, u0)
+        assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+        if trainable:
+            assert orc.rel_l2(npy(grads[amp]["a"]), ga) < GRAD_TOL
+            assert list(fo.trainable(system)) == [ph, amp]
+        else:
+            assert amp not in grads
