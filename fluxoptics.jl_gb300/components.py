@@ -877,7 +877,7 @@ def _padded_size(u_tmp):
 
 
 class PadCropOperator(Component):
-    """Reversible padding of a field into a larger grid (pad_crop_operators.jl:224-356).
+    """Reversible padding of a field into a larger grid (pad_crop_operators.jl:122-356).
 
     ``PadCropOperator(u, u_tmp; offset, pad_val)`` pads fields of u's grid to the grid of
     ``u_tmp`` (a ScalarField, an array of shape (..., py, px), or (px, py)) with u at the
