@@ -11,7 +11,7 @@ from ._capi import FluxOpticsError
 from .build import build as build_library
 from .components import (AS_BPM, ASProp, ASPropZ, Backward, Component, FieldProbe, FourierMask, FourierOperator, FourierPhase,
                          FourierWrapper, Forward, Mask, OpticalSequence, OpticalSystem, PadCropOperator, ParaxialProp, Phase,
-                         RSProp, adjoint, crop, pad,
+                         RSProp, TiltAnchor, adjoint, crop, pad,
                          ScalarSource, TeaDOE, TeaReflector, backpropagate, backpropagate_, function_to_array,
                          get_components, get_data, get_sequence, get_source, isbuffered, istrainable, propagate, propagate_,
                          reverse, spatial_vectors, trainable)
@@ -34,7 +34,7 @@ __all__ = [
     "ASProp", "ASPropZ", "AS_BPM", "Backward", "ClampProx", "Component", "Descent", "DotProduct", "FieldProbe", "Fista", "FluxOpticsError", "FourierMask", "FourierOperator", "FourierPhase", "FourierWrapper",
     "Forward", "Gaussian", "Gaussian1D", "HermiteGaussian", "HermiteGaussian1D", "LaguerreGaussian", "IstaProx", "Mask", "Momentum", "Nesterov", "NoDescent", "OpticalSequence", "OpticalSystem", "PadCropOperator", "ParaxialProp", "Phase", "PointwiseProx", "PositiveProx", "PowerCoupling", "ProxRule",
     "RSProp", "RaggedBatch", "ScalarField", "ScalarSource", "SquaredFieldDifference", "SquaredIntensityDifference", "TVProx", "TeaDOE",
-    "TeaReflector", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_sequence", "get_source", "isbuffered",
+    "TeaReflector", "TiltAnchor", "adjoint", "backpropagate", "backpropagate_metric", "compute_metric", "crop", "pad", "backpropagate_", "get_components", "get_data", "get_sequence", "get_source", "isbuffered",
     "istrainable", "trainable", "build_library", "coupling_efficiency", "dot", "function_to_array", "get_lambdas", "get_lambdas_collection", "get_tilts",
     "get_tilts_collection", "is_on_axis", "offset_tilts_", "phase", "select_lambdas", "select_tilts", "set_field_data", "set_field_ds_",
     "set_field_tilts", "gaussian",

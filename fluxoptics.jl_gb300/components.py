@@ -758,6 +758,31 @@ class FourierOperator(Component):
                 lib.fo_prop_destroy(h)
 
 
+class TiltAnchor(Component):
+    """Resets the field's tilts to the ones of the template field it was built from,
+    moving the difference of the carriers into the envelope with offset_tilts_
+    (utilities/tilt_anchor.jl:1-84).  In a system its pull-back restores the tilts the
+    field had on entry (the exact adjoint of the offset, as the reference's trainable
+    form computes it); the standalone ``backpropagate_`` offsets to the anchor's tilts
+    like the reference's static form.  It has no trainable parameters."""
+
+    def __init__(self, u, trainable=False, buffered=False):
+        tc = u.tilts_per_field()
+        shape = u.julia_batch_shape
+        self.tilts = tuple(tc[:, k].reshape(shape, order="F") if shape else float(tc[0, k]) for k in range(2))
+        self.trainable = bool(trainable)
+        self.buffered = bool(buffered)
+
+    def params(self):
+        return {}
+
+    def propagate_(self, u, direction=Forward):
+        return u.offset_tilts_(self.tilts)
+
+    def backpropagate_(self, dv, direction=Forward):
+        return dv.offset_tilts_(self.tilts)
+
+
 class OpticalSequence(Component):
     """Components applied as one (system/optical_sequence.jl:54-137): in order for the
     Forward direction and in reverse order for the Backward direction, each with that
@@ -1253,7 +1278,12 @@ class OpticalSystem:
                 seg.forward(u, tape, probes)
             else:
                 c = seg
-                if tape is not None and c.trainable and isinstance(c, AS_BPM):
+                if isinstance(c, TiltAnchor):
+                    entry = u.tilts
+                    c.propagate_(u, d)
+                    if tape is not None:
+                        tape.append((c, entry))
+                elif tape is not None and c.trainable and isinstance(c, AS_BPM):
                     c.propagate_and_save_(u, None, d)
                     tape.append((c, None))
                 elif tape is not None and c.trainable and hasattr(c, "propagate_and_save_"):
@@ -1395,6 +1425,8 @@ class OpticalSystem:
                 c = seg
                 if isinstance(c, _PaddedSpan):
                     grads.update(c.backward(du, saved))
+                elif isinstance(c, TiltAnchor):
+                    du.offset_tilts_(saved)  # back to the tilts the field had on entry
                 elif c.trainable and hasattr(c, "backpropagate_with_gradient_"):
                     g = c.get_gradient_buffer()
                     _, gd = c.backpropagate_with_gradient_(du, saved, g, d)

@@ -149,13 +149,17 @@ class ScalarField:
         if np.array_equal(t0, t1):
             return self
         lam = self.lambdas_per_field()
-        x = (np.arange(self.nx) - (self.nx - 1) / 2.0) * self.ds[0]
-        y = (np.arange(self.ny) - (self.ny - 1) / 2.0) * self.ds[1]
-        ax = 2 * np.pi / lam * (np.sin(t0[:, 0]) - np.sin(t1[:, 0]))
-        ay = 2 * np.pi / lam * (np.sin(t0[:, 1]) - np.sin(t1[:, 1]))
-        ph = ax[:, None, None] * x[None, None, :] + ay[:, None, None] * y[None, :, None]
-        f = torch.polar(torch.ones(ph.shape, dtype=torch.float64), torch.as_tensor(ph)).to(torch.complex64)
-        self.electric.view(-1, self.ny, self.nx).mul_(f.to(self.electric.device))
+        dev = self.electric.device
+        ax = torch.as_tensor(2 * np.pi / lam * (np.sin(t0[:, 0]) - np.sin(t1[:, 0])), device=dev)
+        ay = torch.as_tensor(2 * np.pi / lam * (np.sin(t0[:, 1]) - np.sin(t1[:, 1])), device=dev)
+        x = (torch.arange(self.nx, dtype=torch.float64, device=dev) - (self.nx - 1) / 2.0) * self.ds[0]
+        y = (torch.arange(self.ny, dtype=torch.float64, device=dev) - (self.ny - 1) / 2.0) * self.ds[1]
+        # the phase is separable: one factor along x and one along y per field, formed in
+        # float64 and rounded once each
+        fx = torch.polar(torch.ones_like(x)[None, :].expand(len(lam), -1), ax[:, None] * x[None, :])
+        fy = torch.polar(torch.ones_like(y)[None, :].expand(len(lam), -1), ay[:, None] * y[None, :])
+        v = self.electric.view(-1, self.ny, self.nx)
+        v.mul_(fx.to(torch.complex64)[:, None, :]).mul_(fy.to(torch.complex64)[:, :, None])
         self.tilts = new.tilts
         return self
 

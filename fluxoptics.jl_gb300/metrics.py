@@ -200,6 +200,7 @@ def withgradient(metric, system: OpticalSystem, x=None, dc=None):
     else:
         system.forward(u, tape, src=src)
         c = metric(u)
+    du.tilts = u.tilts  # the adjoint sweep starts at the output's tilts (a TiltAnchor may have changed them)
     if isinstance(metric, SquaredIntensityDifference) and dc is None:
         grads = system.backward(du, tape, seed=(metric, u))
         return c.sum(), with_source(grads)
