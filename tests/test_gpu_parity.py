@@ -1789,3 +1789,40 @@ def test_tilt_anchor(fo, orc):
     dv = orc.asprop(dv, 1.0, 1.0, lams, 200.0, orc.BACKWARD, tilts=th)
     _, gphi = orc.phase_backward(dv, phi, a1)
     assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+
+def test_padded_span_with_rsprop_mask_and_sfd(fo, orc):
+    """A padded span holding an RSProp (which pads again inside its own passes), a
+    trainable Mask on the padded grid and an ASProp, with SquaredFieldDifference and
+    per-field weights: values, input-side phase gradient and mask gradient against the
+    oracle."""
+    rng = np.random.default_rng(85)
+    n, npad, lams, ds = 40, 64, np.array([1.064, 0.8]), (1.0, 1.0)
+    u0 = rand_field(rng, (2, n, n))
+    v0 = rand_field(rng, (2, n, n))
+    phi = f32(rng.uniform(0, 6, (n, n)))
+    m = c64(rng.uniform(0.5, 1.0, (npad, npad)) * np.exp(1j * rng.uniform(0, 6, (npad, npad))))
+    w = np.array([0.5, 2.0])
+    u = fo.ScalarField(u0, ds, lams)
+    up = fo.ScalarField(np.zeros((2, npad, npad), np.complex64), ds, lams)
+    op = fo.PadCropOperator(u, up, offset=(10, 6))
+    ph = fo.Phase(u, phi, trainable=True)
+    mk = fo.Mask(up, m, trainable=True)
+    system = fo.ScalarSource(u) | ph | op | fo.RSProp(up, 150.0) | mk | fo.ASProp(up, 120.0) | fo.adjoint(op)
+    metric = fo.SquaredFieldDifference(fo.ScalarField(v0, ds, lams))
+    loss, grads = fo.withgradient(metric, system, dc=torch.tensor(w, device="cuda"))
+    a1 = orc.phase_forward(u0, phi)
+    b0 = orc.pad(a1, (npad, npad), (10, 6))
+    b1 = orc.rsprop(b0, 1.0, 1.0, lams, 150.0)
+    b2 = orc.asprop(orc.mask_forward(b1, m), 1.0, 1.0, lams, 120.0)
+    out = orc.crop(b2, (n, n), (10, 6))
+    c_ref = orc.sfd_value(out, v0)
+    assert abs(float(loss) - np.sum(w * c_ref)) / np.sum(w * c_ref) < 1e-4
+    dv = orc.pad(orc.sfd_backward(out, v0, w), (npad, npad), (10, 6))
+    dv = orc.asprop(dv, 1.0, 1.0, lams, 120.0, orc.BACKWARD)
+    dv, gm = orc.mask_backward(dv, m, b1)
+    dv = orc.rsprop(dv, 1.0, 1.0, lams, 150.0, orc.BACKWARD)
+    dv = orc.crop(dv, (n, n), (10, 6))
+    _, gphi = orc.phase_backward(dv, phi, u0)
+    assert orc.rel_l2(npy(grads[mk]["m"]), gm) < GRAD_TOL
+    assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
