@@ -53,6 +53,9 @@ class ScalarField:
     array broadcast the same way (src/Fields.jl:34-38, :130-141)."""
 
     def __init__(self, data, ds, lambdas, tilts=None):
+        if isinstance(data, tuple) and data and all(isinstance(n, (int, np.integer)) for n in data):
+            # ScalarField(nd::NTuple, ds, lambdas; tilts): zeros of the Julia size nd (src/Fields.jl:143-148)
+            data = torch.zeros(tuple(int(n) for n in reversed(data)), dtype=torch.complex64)
         self.electric = _as_device_field(data)
         if self.electric.dim() < 2:
             raise ValueError("a field needs two spatial dims")
@@ -80,6 +83,15 @@ class ScalarField:
     def size(self):
         """Size in Julia order (nx, ny, trailing...)."""
         return (self.nx, self.ny) + self.julia_batch_shape
+
+    def ndims(self, spatial=False):
+        """Number of dimensions, or of spatial ones (src/Fields.jl:360-362)."""
+        return 2 if spatial else self.electric.dim()
+
+    def copyto_(self, v):
+        """Copy another field's data in (src/Fields.jl:433-436)."""
+        self.electric.copy_(v.electric)
+        return self
 
     def lambdas_per_field(self):
         return per_field(self.lambdas, self.julia_batch_shape)

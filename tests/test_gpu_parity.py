@@ -1657,6 +1657,12 @@ def test_field_helpers(fo, orc):
     assert np.allclose(v.tilts_per_field(), [[0.01, -0.02]] * 6)
     fo.offset_tilts_(v, (0.0, 0.0))
     assert orc.rel_l2(npy(v.electric), u0) < 1e-6 and fo.is_on_axis(v)
+    # construction from a Julia size, ndims, copyto_
+    z = fo.ScalarField((24, 16, 3), (1.0, 1.0), lams)
+    assert z.size() == (24, 16, 3) and tuple(z.electric.shape) == (3, 16, 24) and not torch.any(z.electric != 0)
+    assert z.ndims() == 3 and z.ndims(True) == 2
+    z2 = fo.ScalarField((24, 16, 3), (1.0, 1.0), lams).fill_(2.0)
+    assert torch.equal(z.copyto_(z2).electric, z2.electric)
     # arithmetic, conj, fill_
     w = fo.ScalarField(rand_field(rng, (2, 3, n, n)), (0.5, 0.25), lams)
     assert torch.equal((u + w).electric, u.electric + w.electric)
