@@ -130,3 +130,49 @@ def test_bad_arguments_are_rejected(capi):
     assert "v must not alias" in lib.fo_last_error().decode()
     assert lib.fo_copy(None, None, 16, None) == 1
     assert lib.fo_copy(None, None, 0, None) == 0  # nothing to copy
+
+
+def _header_decls():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_shim_test", os.path.join(os.path.dirname(__file__),
+                                                                              "test_julia_shim.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.header_decls()
+
+
+def _is_c_pointer(ct, handles):
+    return ct.endswith("*") or ct in handles or ct.endswith("_fn")
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every ctypes binding of the Python mirror has the header's argument count and,
+    argument by argument, the same kind (pointer, int, long long, double), so a call
+    through ctypes passes what the C function reads."""
+    import ctypes as C
+    from __graft_entry__ import load_package
+    capi = load_package()._capi
+    decls, handles = _header_decls()
+    scalar = {"int": C.c_int, "long long": C.c_longlong, "double": C.c_double, "size_t": C.c_size_t,
+              "unsigned": C.c_uint, "unsigned int": C.c_uint}
+    pointee = {"double*": C.c_double, "const double*": C.c_double, "int*": C.c_int, "const int*": C.c_int,
+               "float*": C.c_float, "const float*": C.c_float}
+    for name, (res, args) in capi.SIGNATURES.items():
+        assert name in decls, f"{name} is bound but not declared"
+        cret, cargs = decls[name]
+        assert len(args) == len(cargs), f"{name}: ctypes has {len(args)} arguments, the header {len(cargs)}"
+        for k, (ct, pt) in enumerate(zip(cargs, args)):
+            is_ptr_type = (pt in (C.c_void_p, C.c_char_p)
+                           or (isinstance(pt, type) and issubclass(pt, C._Pointer))  # POINTER(T)
+                           or bool(getattr(pt, "_flags_", 0) & C._FUNCFLAG_CDECL))  # a CFUNCTYPE
+            if _is_c_pointer(ct, handles):
+                assert is_ptr_type, f"{name} argument {k + 1}: header {ct!r}, ctypes {pt}"
+                if ct in pointee and pt is not C.c_void_p:
+                    assert pt._type_ is pointee[ct], f"{name} argument {k + 1}: header {ct!r}, ctypes {pt}"
+            else:
+                assert ct in scalar, f"{name} argument {k + 1}: unexpected header type {ct!r}"
+                assert pt is scalar[ct], f"{name} argument {k + 1}: header {ct!r}, ctypes {pt}"
+        if cret == "const char*":
+            assert res is C.c_char_p, name
+        else:
+            assert res is C.c_int, f"{name} returns {cret}"
