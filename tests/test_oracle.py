@@ -529,3 +529,17 @@ def test_filtered_kernel_is_conjugated_for_negative_z(orc):
         hp = orc.as_kernel_general(8, 8, 0.5, 0.5, 0.8, 30.0, 1.0, False, theta, False, filt)
         hm = orc.as_kernel_general(8, 8, 0.5, 0.5, 0.8, -30.0, 1.0, False, theta, False, filt)
         assert np.allclose(hm, np.conj(hp))
+
+
+# --- pad / crop (utilities/pad_crop_operators.jl:1-120; test/optical_components_test.jl:171-189) ---
+def test_pad_crop_restatement():
+    u = np.ones((32, 32), dtype=np.complex128)
+    p = orc.pad(u, (64, 64))
+    assert p.shape == (64, 64) and p[16, 16] == 1.0 and p[40, 40] == 0.0
+    assert np.array_equal(orc.crop(p, (32, 32)), u)
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((2, 5, 7)) + 1j * rng.standard_normal((2, 5, 7))
+    q = orc.pad(a, (11, 9), offset=(3, 2), pad_val=0.5)
+    assert q.shape == (2, 9, 11)
+    assert np.array_equal(q[:, 2:7, 3:10], a) and np.all(q[:, :2] == 0.5) and np.all(q[:, :, :3] == 0.5)
+    assert np.array_equal(orc.crop(q, (7, 5), offset=(3, 2)), a)
