@@ -1832,3 +1832,28 @@ def test_padded_span_with_rsprop_mask_and_sfd(fo, orc):
     _, gphi = orc.phase_backward(dv, phi, u0)
     assert orc.rel_l2(npy(grads[mk]["m"]), gm) < GRAD_TOL
     assert orc.rel_l2(npy(grads[ph]["phi"]), gphi) < GRAD_TOL
+
+
+@pytest.mark.parametrize("track", [False, True])
+def test_tilted_propagation_identities(fo, orc, track):
+    """The GPU's tilted ASProp against its own on-axis ASProp through the physical
+    identities of the tilted kernels: an envelope on a carrier of whole frequency bins
+    propagates as the physical field (without track_tilts), or as the physical field
+    followed along its walk-off z sin(theta) (with track_tilts)."""
+    N, d, lam = 64, 1.0, 1.0
+    x = (np.arange(N) - (N - 1) / 2) * d
+    u = orc.gaussian(6.0, x, x) * np.exp(1j * 0.02 * (x[None, :] ** 2 - 0.5 * x[:, None] ** 2))
+    f0 = np.array([3 / (N * d), -2 / (N * d)])
+    th = tuple(np.arcsin(f0 * lam))
+    carrier = np.exp(2j * np.pi * (f0[0] * x[None, :] + f0[1] * x[:, None]))
+    z = 64.0 if track else 40.0
+    uf = fo.ScalarField(u.astype(np.complex64), (d, d), lam)
+    ef = fo.ScalarField((u / carrier).astype(np.complex64), (d, d), lam, tilts=th)
+    out_u = npy(fo.propagate(uf, fo.ASProp(uf, z)).electric)
+    out_e = npy(fo.propagate(ef, fo.ASProp(ef, z, track_tilts=track)).electric)
+    if track:
+        ref = np.roll(out_u, shift=(2, -3), axis=(0, 1))
+        got = out_e * carrier * np.exp(2j * np.pi * (f0[0] * 3 + f0[1] * -2))
+    else:
+        ref, got = out_u, out_e * carrier
+    assert orc.rel_l2(got, ref) < FIELD_TOL

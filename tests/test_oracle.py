@@ -543,3 +543,33 @@ def test_pad_crop_restatement():
     assert q.shape == (2, 9, 11)
     assert np.array_equal(q[:, 2:7, 3:10], a) and np.all(q[:, :2] == 0.5) and np.all(q[:, :, :3] == 0.5)
     assert np.array_equal(orc.crop(q, (7, 5), offset=(3, 2)), a)
+
+
+# --- tilted kernels against the on-axis one (angular_spectrum.jl:27-76) ----------------------
+# A field u carried as the envelope e = u exp(-i 2 pi f0.r) with f0 = sin(theta)/lambda on the
+# frequency grid: the tilted kernel H(f + f0) propagates e exactly as the on-axis kernel
+# propagates u (for a band-limited u, whose spectrum does not wrap at Nyquist); with
+# track_tilts the envelope also follows the beam's walk-off, e'(r) = u'(r + z sin(theta)) x
+# exp(-i 2 pi f0.(r + z sin(theta))).  Both pin the tilted kernels physically.
+def _tilt_case():
+    N, d, lam = 64, 1.0, 1.0
+    x = (np.arange(N) - (N - 1) / 2) * d
+    u = orc.gaussian(6.0, x, x) * np.exp(1j * 0.02 * (x[None, :] ** 2 - 0.5 * x[:, None] ** 2))
+    f0 = np.array([3 / (N * d), -2 / (N * d)])
+    carrier = np.exp(2j * np.pi * (f0[0] * x[None, :] + f0[1] * x[:, None]))
+    return N, d, lam, u, f0, tuple(np.arcsin(f0 * lam)), carrier
+
+
+def test_tilted_kernel_propagates_the_envelope():
+    N, d, lam, u, f0, th, carrier = _tilt_case()
+    v = orc.asprop(u / carrier, d, d, lam, 40.0, tilts=th) * carrier
+    assert orc.rel_l2(v, orc.asprop(u, d, d, lam, 40.0)) < 1e-12
+
+
+def test_tracked_tilts_follow_the_walk_off():
+    N, d, lam, u, f0, th, carrier = _tilt_case()
+    z = 64.0  # z sin(theta) = (3, -2) pixels
+    e = orc.asprop(u / carrier, d, d, lam, z, tilts=th, track_tilts=True)
+    ref = np.roll(orc.asprop(u, d, d, lam, z), shift=(2, -3), axis=(0, 1))  # u'(r + (3, -2))
+    ph = np.exp(2j * np.pi * (f0[0] * 3 + f0[1] * -2))
+    assert orc.rel_l2(e * carrier * ph, ref) < 1e-12
