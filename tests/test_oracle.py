@@ -573,3 +573,18 @@ def test_tracked_tilts_follow_the_walk_off():
     ref = np.roll(orc.asprop(u, d, d, lam, z), shift=(2, -3), axis=(0, 1))  # u'(r + (3, -2))
     ph = np.exp(2j * np.pi * (f0[0] * 3 + f0[1] * -2))
     assert orc.rel_l2(e * carrier * ph, ref) < 1e-12
+
+
+# --- RSProp against ASProp (rayleigh_sommerfeld.jl:1-12 against angular_spectrum.jl:1-12) -----
+# The RS impulse response is the inverse Fourier transform of the AS transfer function, so
+# for a band-limited field the two propagators, each restated independently (one from a
+# sampled impulse response, one from the analytic transfer function), agree; AS runs on a
+# window padded so that its circular convolution is the linear one.
+@pytest.mark.parametrize("n,lam,w0,z", [(256, 1.064, 12.0, 400.0), (256, 1.064, 12.0, 1500.0),
+                                        (200, 0.8, 10.0, 600.0)])
+def test_rs_and_as_agree_on_band_limited_fields(n, lam, w0, z):
+    x = (np.arange(n) - (n - 1) / 2)
+    u = orc.gaussian(w0, x, x)
+    h = n // 2
+    a = orc.asprop(np.pad(u, ((h, h), (h, h))), 1.0, 1.0, lam, z)[h:h + n, h:h + n]
+    assert orc.rel_l2(orc.rsprop(u, 1.0, 1.0, lam, z), a) < 1e-11
