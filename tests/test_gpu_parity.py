@@ -1857,3 +1857,20 @@ def test_tilted_propagation_identities(fo, orc, track):
     else:
         ref, got = out_u, out_e * carrier
     assert orc.rel_l2(got, ref) < FIELD_TOL
+
+
+def test_rsprop_equals_padded_asprop_on_band_limited_fields(fo, orc):
+    """The GPU's RSProp against its own ASProp run inside a PadCropOperator span on a
+    window of twice the size: the RS impulse response is the inverse transform of the AS
+    transfer function, so for a band-limited field the two agree (the oracle's
+    restatements agree to 1e-13)."""
+    n, lam, z = 256, 0.8, 600.0  # the padded window (512) must be a power of two for ASProp
+    x = (np.arange(n) - (n - 1) / 2)
+    lams = [lam, 1.064]
+    u0 = np.stack([orc.gaussian(10.0, x, x), orc.gaussian(14.0, x - 5, x + 3)]).astype(np.complex64)
+    u = fo.ScalarField(u0, (1.0, 1.0), lams)
+    up = fo.ScalarField(np.zeros((2, 2 * n, 2 * n), np.complex64), (1.0, 1.0), lams)
+    op = fo.PadCropOperator(u, up, offset=(n // 2, n // 2))
+    rs = npy(fo.propagate(u, fo.RSProp(u, z)).electric)
+    as_ = npy((fo.ScalarSource(u) | op | fo.ASProp(up, z) | fo.adjoint(op))()["out"].electric)
+    assert orc.rel_l2(rs, as_) < FIELD_TOL
