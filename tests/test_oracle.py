@@ -588,3 +588,19 @@ def test_rs_and_as_agree_on_band_limited_fields(n, lam, w0, z):
     h = n // 2
     a = orc.asprop(np.pad(u, ((h, h), (h, h))), 1.0, 1.0, lam, z)[h:h + n, h:h + n]
     assert orc.rel_l2(orc.rsprop(u, 1.0, 1.0, lam, z), a) < 1e-11
+
+
+# --- AS_BPM with a uniform index perturbation (bpm.jl:3-6, 235-260) -----------------------------
+# A uniform dn = c commutes with every step of the march, so the split-step result is one
+# ASProp over the thickness times cis(2 pi c L / (lambda cos(theta_x) cos(theta_y))): this
+# pins the dn phase scale kdz / lambda, the slice count and the half steps.
+@pytest.mark.parametrize("tilts", [None, (0.02, -0.03)])
+def test_bpm_uniform_dn_is_a_constant_phase(tilts):
+    n, lam, n0, L, ns, c = 64, 1.064, 1.5, 100.0, 20, 3e-3
+    x = (np.arange(n) - (n - 1) / 2)
+    u = orc.gaussian(8.0, x, x)
+    v, _ = orc.bpm_forward(u, 1.0, 1.0, lam, L, n0, np.full((ns, n, n), c), tilts=tilts)
+    th = (0.0, 0.0) if tilts is None else tilts
+    w = orc.asprop(u, 1.0, 1.0, lam, L, orc.FORWARD, n0, tilts=tilts)
+    w = w * np.exp(2j * np.pi * c * L / (lam * np.cos(th[0]) * np.cos(th[1])))
+    assert orc.rel_l2(v, w) < 1e-12
