@@ -130,3 +130,21 @@ def test_tilt_anchor_stores_the_template_tilts(fo):
     assert np.allclose(anc.tilts[1][:, 0], [0.0, 0.02, -0.03]) and np.allclose(anc.tilts[1][:, 1], [0.0, 0.02, -0.03])
     single = fo.TiltAnchor(Grid(16, 16, tilts=(0.005, -0.002)))
     assert single.tilts == (0.005, -0.002)
+
+
+def test_per_field_broadcast_follows_parse_val(fo):
+    """Per-field wavelengths / tilts (src/Fields.jl:18-38): the value array keeps its own
+    shape on the trailing dims (copyto! into a (1, 1, size(val)...) array) and broadcasts
+    against the field; fields are listed in column-major order of the trailing dims."""
+    from fluxoptics_gb300.fields import per_field
+    assert np.array_equal(per_field(0.64, (3, 2)), np.full(6, 0.64))
+    assert np.array_equal(per_field([1.0, 2.0, 3.0], (3, 2)), [1, 2, 3, 1, 2, 3])
+    v = np.array([[1.0, 4.0], [2.0, 5.0], [3.0, 6.0]])  # Julia (3, 2): v[i, j] for field (i, j)
+    assert np.array_equal(per_field(v, (3, 2)), [1, 2, 3, 4, 5, 6])
+    assert np.array_equal(per_field([7.0], (3, 2)), np.full(6, 7.0))
+    assert np.array_equal(per_field(np.array([[1.0, 2.0]]), (3, 2)), [1, 1, 1, 2, 2, 2])  # (1, 2) over d4
+    assert np.array_equal(per_field([0.5], ()), [0.5])
+    with pytest.raises(ValueError):
+        per_field([1.0, 2.0], ())
+    with pytest.raises(ValueError):
+        per_field([1.0, 2.0], (3,))
